@@ -1,0 +1,586 @@
+/*
+ * gwr_oracle.c -- TEST INFRASTRUCTURE ONLY: the CPU oracle for the GWRBasic
+ * hot path.  Every function restates the reference line range it cites
+ * (paths inside libgwmodel).  Build with -ffp-contract=off so that distances
+ * and weights round exactly as the reference's expressions do.
+ */
+#include "gwr_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../libgwmodel_gb300/csrc/gw_arith.h"
+
+#define X_(pb, i, k) ((pb)->x[(size_t)(i) + (size_t)(k) * (size_t)(pb)->n])
+#define U_(pb, i) ((pb)->coords[(size_t)(i)])
+#define V_(pb, i) ((pb)->coords[(size_t)(i) + (size_t)(pb)->n])
+
+static int orc_threads(const orc_problem* pb)
+{
+    return pb->threads > 0 ? pb->threads : 1;
+}
+
+static int orc_thread_id(void)
+{
+#ifdef _OPENMP
+    return omp_get_thread_num();
+#else
+    return 0;
+#endif
+}
+
+/* ---------------------------------------------------------------- distance */
+
+/* CRSDistance::SpGcdist (CRSDistance.cpp:15-69) with libm, line for line. */
+double orc_gcdist_libm(double lon1, double lon2, double lat1, double lat2)
+{
+    double F, G, L, sinG2, cosG2, sinF2, cosF2, sinL2, cosL2, S, C;
+    double w, R, a, f, D, H1, H2;
+    double lat1R, lat2R, lon1R, lon2R, DE2RA;
+    DE2RA = M_PI / 180;
+    a = 6378.137;
+    f = 1.0 / 298.257223563;
+    if (fabs(lat1 - lat2) < GW_DOUBLE_EPS)
+    {
+        if (fabs(lon1 - lon2) < GW_DOUBLE_EPS)
+            return 0.0;
+        else if (fabs((fabs(lon1) + fabs(lon2)) - 360.0) < GW_DOUBLE_EPS)
+            return 0.0;
+    }
+    lat1R = lat1 * DE2RA;
+    lat2R = lat2 * DE2RA;
+    lon1R = lon1 * DE2RA;
+    lon2R = lon2 * DE2RA;
+    F = (lat1R + lat2R) / 2.0;
+    G = (lat1R - lat2R) / 2.0;
+    L = (lon1R - lon2R) / 2.0;
+    sinG2 = pow(sin(G), 2);
+    cosG2 = pow(cos(G), 2);
+    sinF2 = pow(sin(F), 2);
+    cosF2 = pow(cos(F), 2);
+    sinL2 = pow(sin(L), 2);
+    cosL2 = pow(cos(L), 2);
+    S = sinG2 * cosL2 + cosF2 * sinL2;
+    C = cosG2 * cosL2 + sinF2 * sinL2;
+    w = atan(sqrt(S / C));
+    R = sqrt(S * C) / w;
+    D = 2 * w * a;
+    H1 = (3 * R - 1) / (2 * C);
+    H2 = (3 * R + 1) / (2 * S);
+    return D * (1 + f * H1 * sinF2 * cosG2 - f * H2 * cosF2 * sinG2);
+}
+
+/* The same formula evaluated with the engine's portable sin/cos/atan. */
+double orc_gcdist_portable(double lon1, double lon2, double lat1, double lat2)
+{
+    const double DE2RA = M_PI / 180;
+    return gw_gc_dist(lon1, lon2, lat1, lat2, lon1 * DE2RA, lon2 * DE2RA, lat1 * DE2RA, lat2 * DE2RA);
+}
+
+/* CRSDistance::distance(focus) (CRSDistance.cpp:122-131) with focus points ==
+ * data points; planar EuclideanDistance (CRSDistance.h:95-99) or
+ * SpatialDistance (CRSDistance.cpp:71-81: SpGcdist(data lon, focus lon,
+ * data lat, focus lat)). */
+void orc_distance_row(const orc_problem* pb, int focus, double* out)
+{
+    const double uf = U_(pb, focus), vf = V_(pb, focus);
+    for (int j = 0; j < pb->n; j++)
+    {
+        if (!pb->geographic)
+            out[j] = gw_planar_dist(U_(pb, j), V_(pb, j), uf, vf);
+        else if (pb->gc_mode == ORC_GC_PORTABLE)
+            out[j] = orc_gcdist_portable(U_(pb, j), uf, V_(pb, j), vf);
+        else
+            out[j] = orc_gcdist_libm(U_(pb, j), uf, V_(pb, j), vf);
+    }
+}
+
+/* CRSDistance::maxDistance (CRSDistance.cpp:133-143). */
+double orc_max_distance(const orc_problem* pb)
+{
+    const int n = pb->n, T = orc_threads(pb);
+    double maxD = 0.0;
+    double* buf = (double*)malloc(sizeof(double) * (size_t)n * (size_t)T);
+#pragma omp parallel for num_threads(T) schedule(dynamic, 16) reduction(max : maxD)
+    for (int i = 0; i < n; i++)
+    {
+        double* d = buf + (size_t)n * (size_t)orc_thread_id();
+        orc_distance_row(pb, i, d);
+        double m = d[0];
+        for (int j = 1; j < n; j++)
+            if (d[j] > m) m = d[j];
+        maxD = m > maxD ? m : maxD;
+    }
+    free(buf);
+    return maxD;
+}
+
+/* ------------------------------------------------------------------ weight */
+
+static int cmp_double(const void* a, const void* b)
+{
+    double x = *(const double*)a, y = *(const double*)b;
+    return (x > y) - (x < y);
+}
+
+/* fixbw of the adaptive branch, BandwidthWeight.cpp:40-53. */
+int orc_adaptive_threshold(const double* dist, int n, double bw, double* fixbw)
+{
+    double dn = bw / n;
+    if (dn < 1)
+    {
+        double b0 = floor(bw), bx = bw - b0;
+        long long i0 = (long long)(int)b0 - 1, i1 = (long long)(int)b0;
+        if (i0 < 0 || i1 >= n) return -1; /* Armadillo bounds error */
+        double* s = (double*)malloc(sizeof(double) * (size_t)n);
+        memcpy(s, dist, sizeof(double) * (size_t)n);
+        qsort(s, (size_t)n, sizeof(double), cmp_double);
+        double d0 = s[i0], d1 = s[i1];
+        *fixbw = d0 + (d1 - d0) * bx;
+        free(s);
+    }
+    else
+    {
+        double m = dist[0];
+        for (int j = 1; j < n; j++)
+            if (dist[j] > m) m = dist[j];
+        *fixbw = dn * m;
+    }
+    return 0;
+}
+
+/* BandwidthWeight::weight (BandwidthWeight.cpp:35-61). */
+int orc_weight(const double* dist, int n, double bw, int adaptive, int kernel, double* w)
+{
+    double b = bw;
+    if (adaptive && orc_adaptive_threshold(dist, n, bw, &b) != 0) return -1;
+    for (int j = 0; j < n; j++)
+        w[j] = gw_kernel_weight(kernel, dist[j], b);
+    return 0;
+}
+
+/* ------------------------------------------------------------ local solve */
+
+/* inv_sympd: Cholesky A = L L^T (dpotrf), then A^-1 = L^-T L^-1 (dpotri).
+ * Fails like dpotrf when a leading minor is not positive. */
+int orc_inv_sympd(double* a, int p)
+{
+    /* factor in place, lower triangle, column-major a[i + j*p] */
+    for (int j = 0; j < p; j++)
+    {
+        double s = a[j + j * p];
+        for (int k = 0; k < j; k++)
+            s -= a[j + k * p] * a[j + k * p];
+        if (!(s > 0.0)) return -1;
+        double ljj = sqrt(s);
+        a[j + j * p] = ljj;
+        for (int i = j + 1; i < p; i++)
+        {
+            double t = a[i + j * p];
+            for (int k = 0; k < j; k++)
+                t -= a[i + k * p] * a[j + k * p];
+            a[i + j * p] = t / ljj;
+        }
+    }
+    /* invert L in place (lower) */
+    for (int j = 0; j < p; j++)
+    {
+        a[j + j * p] = 1.0 / a[j + j * p];
+        for (int i = j + 1; i < p; i++)
+        {
+            double t = 0.0;
+            for (int k = j; k < i; k++)
+                t -= a[i + k * p] * a[k + j * p];
+            a[i + j * p] = t / a[i + i * p];
+        }
+    }
+    /* A^-1 = L^-T L^-1, fill both triangles */
+    for (int j = 0; j < p; j++)
+        for (int i = j; i < p; i++)
+        {
+            double t = 0.0;
+            for (int k = i; k < p; k++)
+                t += a[k + i * p] * a[k + j * p];
+            a[i + j * p] = t; /* lower part now holds (i >= j) */
+        }
+    for (int j = 0; j < p; j++)
+        for (int i = 0; i < j; i++)
+            a[i + j * p] = a[j + i * p];
+    return 0;
+}
+
+/* Per-thread scratch for one local regression. */
+typedef struct
+{
+    double *d, *w, *xtw, *ci, *si, *a, *b, *beta;
+} orc_ws;
+
+static void ws_alloc(orc_ws* ws, int n, int p, int need_c)
+{
+    ws->d = (double*)malloc(sizeof(double) * (size_t)n);
+    ws->w = (double*)malloc(sizeof(double) * (size_t)n);
+    ws->xtw = (double*)malloc(sizeof(double) * (size_t)n * (size_t)p);
+    ws->ci = need_c ? (double*)malloc(sizeof(double) * (size_t)n * (size_t)p) : NULL;
+    ws->si = need_c ? (double*)malloc(sizeof(double) * (size_t)n) : NULL;
+    ws->a = (double*)malloc(sizeof(double) * (size_t)p * (size_t)p);
+    ws->b = (double*)malloc(sizeof(double) * (size_t)p);
+    ws->beta = (double*)malloc(sizeof(double) * (size_t)p);
+}
+
+static void ws_free(orc_ws* ws)
+{
+    free(ws->d); free(ws->w); free(ws->xtw); free(ws->ci); free(ws->si);
+    free(ws->a); free(ws->b); free(ws->beta);
+}
+
+/* xtw = trans(x.each_col() % w) (p x n, column-major: xtw[k + j*p]);
+ * xtwx = xtw * x; xtwy = xtw * y; then inv_sympd and beta = inv * xtwy
+ * (GWRBasic.cpp:500-508).  Returns -1 when not SPD. */
+static int local_solve(const orc_problem* pb, const double* x, int p, orc_ws* ws)
+{
+    const int n = pb->n;
+    for (int j = 0; j < n; j++)
+        for (int k = 0; k < p; k++)
+            ws->xtw[k + (size_t)j * p] = x[(size_t)j + (size_t)k * n] * ws->w[j];
+    for (int c = 0; c < p; c++)
+        for (int r = 0; r < p; r++)
+        {
+            double s = 0.0;
+            for (int j = 0; j < n; j++)
+                s += ws->xtw[r + (size_t)j * p] * x[(size_t)j + (size_t)c * n];
+            ws->a[r + c * p] = s;
+        }
+    for (int r = 0; r < p; r++)
+    {
+        double s = 0.0;
+        for (int j = 0; j < n; j++)
+            s += ws->xtw[r + (size_t)j * p] * pb->y[j];
+        ws->b[r] = s;
+    }
+    if (orc_inv_sympd(ws->a, p) != 0) return -1;
+    for (int r = 0; r < p; r++)
+    {
+        double s = 0.0;
+        for (int c = 0; c < p; c++)
+            s += ws->a[r + c * p] * ws->b[c];
+        ws->beta[r] = s;
+    }
+    return 0;
+}
+
+/* ci = inv * xtw (p x n); si = x.row(i) * ci (1 x n) (GWRBasic.cpp:509-510). */
+static void hat_row(const orc_problem* pb, const double* x, int p, int i, orc_ws* ws)
+{
+    const int n = pb->n;
+    for (int j = 0; j < n; j++)
+        for (int r = 0; r < p; r++)
+        {
+            double s = 0.0;
+            for (int c = 0; c < p; c++)
+                s += ws->a[r + c * p] * ws->xtw[c + (size_t)j * p];
+            ws->ci[r + (size_t)j * p] = s;
+        }
+    for (int j = 0; j < n; j++)
+    {
+        double s = 0.0;
+        for (int r = 0; r < p; r++)
+            s += x[(size_t)i + (size_t)r * n] * ws->ci[r + (size_t)j * p];
+        ws->si[j] = s;
+    }
+}
+
+/* GWRBase::RSS and AICc (GWRBase.h:41-94): betas is n x p. */
+static double rss_of(const orc_problem* pb, const double* x, int p, const double* betas)
+{
+    const int n = pb->n;
+    double ss = 0.0;
+    for (int i = 0; i < n; i++)
+    {
+        double fit = 0.0;
+        for (int k = 0; k < p; k++)
+            fit += betas[(size_t)i + (size_t)k * n] * x[(size_t)i + (size_t)k * n];
+        double r = pb->y[i] - fit;
+        ss += r * r;
+    }
+    return ss;
+}
+
+static double aicc_of(double n, double rss, double trS)
+{
+    return n * log(rss / n) + n * log(2 * M_PI) + n * ((n + trS) / (n - 2 - trS));
+}
+
+/* ---------------------------------------------------------------- criteria */
+
+typedef struct
+{
+    double sum0, sum1; /* AIC: trS, trStS;  CV: sum of squares */
+    int ok;
+} crit_part;
+
+static crit_part criterion_rows_impl(const orc_problem* pb, double bw, int adaptive, int kernel,
+                                     int criterion, int row0, int row1, double* betas)
+{
+    const int n = pb->n, p = pb->p, T = orc_threads(pb);
+    const int need_c = criterion == ORC_AIC;
+    orc_ws* ws = (orc_ws*)malloc(sizeof(orc_ws) * (size_t)T);
+    for (int t = 0; t < T; t++) ws_alloc(&ws[t], n, p, need_c);
+    double s0 = 0.0, s1 = 0.0;
+    int ok = 1;
+#pragma omp parallel for num_threads(T) schedule(dynamic, 1) reduction(+ : s0, s1) reduction(&& : ok)
+    for (int i = row0; i < row1; i++)
+    {
+        orc_ws* w = &ws[orc_thread_id()];
+        orc_distance_row(pb, i, w->d);
+        if (orc_weight(w->d, n, bw, adaptive, kernel, w->w) != 0) { ok = 0; continue; }
+        if (criterion == ORC_CV) w->w[i] = 0.0; /* GWRBasic.cpp:455 */
+        if (local_solve(pb, pb->x, p, w) != 0) { ok = 0; continue; }
+        if (criterion == ORC_CV)
+        {
+            /* res = y(i) - x.row(i) * beta (GWRBasic.cpp:462-467) */
+            double yhat = 0.0;
+            for (int k = 0; k < p; k++) yhat += X_(pb, i, k) * w->beta[k];
+            double res = pb->y[i] - yhat;
+            if (isfinite(res)) s0 += res * res;
+            else ok = 0;
+        }
+        else
+        {
+            if (betas)
+                for (int k = 0; k < p; k++) betas[(size_t)i + (size_t)k * n] = w->beta[k];
+            hat_row(pb, pb->x, p, i, w);
+            double ss = 0.0;
+            for (int j = 0; j < n; j++) ss += w->si[j] * w->si[j];
+            s0 += w->si[i]; /* shat(0) += si(0, i) */
+            s1 += ss;       /* shat(1) += det(si * si.t()) */
+        }
+    }
+    for (int t = 0; t < T; t++) ws_free(&ws[t]);
+    free(ws);
+    crit_part r = {s0, s1, ok};
+    return r;
+}
+
+/* bandwidthSizeCriterionCVOmp / AICOmp (GWRBasic.cpp:440-535). */
+double orc_criterion(const orc_problem* pb, double bw, int adaptive, int kernel, int criterion,
+                     double* shat_out)
+{
+    const int n = pb->n, p = pb->p;
+    double* betas = criterion == ORC_AIC ? (double*)calloc((size_t)n * (size_t)p, sizeof(double)) : NULL;
+    crit_part r = criterion_rows_impl(pb, bw, adaptive, kernel, criterion, 0, n, betas);
+    double value = DBL_MAX;
+    if (r.ok)
+    {
+        if (criterion == ORC_CV)
+            value = isfinite(r.sum0) ? r.sum0 : DBL_MAX;
+        else
+        {
+            double v = aicc_of((double)n, rss_of(pb, pb->x, p, betas), r.sum0);
+            value = isfinite(v) ? v : DBL_MAX;
+            if (shat_out) { shat_out[0] = r.sum0; shat_out[1] = r.sum1; }
+        }
+    }
+    free(betas);
+    return value;
+}
+
+double orc_criterion_rows(const orc_problem* pb, double bw, int adaptive, int kernel, int criterion,
+                          int row0, int row1)
+{
+    crit_part r = criterion_rows_impl(pb, bw, adaptive, kernel, criterion, row0, row1, NULL);
+    return r.ok ? r.sum0 : DBL_MAX;
+}
+
+/* indepVarsSelectionCriterionOmp (GWRBasic.cpp:537-580): the AICc of the
+ * model on columns cols with every weight equal to one. */
+double orc_indep_vars_criterion(const orc_problem* pb, const int* cols, int ncols)
+{
+    const int n = pb->n, T = orc_threads(pb);
+    double* x = (double*)malloc(sizeof(double) * (size_t)n * (size_t)ncols);
+    for (int k = 0; k < ncols; k++)
+        memcpy(x + (size_t)k * n, pb->x + (size_t)cols[k] * n, sizeof(double) * (size_t)n);
+    double* betas = (double*)calloc((size_t)n * (size_t)ncols, sizeof(double));
+    orc_ws* ws = (orc_ws*)malloc(sizeof(orc_ws) * (size_t)T);
+    for (int t = 0; t < T; t++) ws_alloc(&ws[t], n, ncols, 1);
+    double s0 = 0.0;
+    int ok = 1;
+#pragma omp parallel for num_threads(T) schedule(dynamic, 4) reduction(+ : s0) reduction(&& : ok)
+    for (int i = 0; i < n; i++)
+    {
+        orc_ws* w = &ws[orc_thread_id()];
+        for (int j = 0; j < n; j++) w->w[j] = 1.0;
+        if (local_solve(pb, x, ncols, w) != 0) { ok = 0; continue; }
+        for (int k = 0; k < ncols; k++) betas[(size_t)i + (size_t)k * n] = w->beta[k];
+        hat_row(pb, x, ncols, i, w);
+        s0 += w->si[i];
+    }
+    double value = DBL_MAX;
+    if (ok) value = aicc_of((double)n, rss_of(pb, x, ncols, betas), s0);
+    for (int t = 0; t < T; t++) ws_free(&ws[t]);
+    free(ws);
+    free(betas);
+    free(x);
+    return value;
+}
+
+/* ---------------------------------------------------------------- final fit */
+
+/* fitOmp (GWRBasic.cpp:386-438). */
+int orc_fit_core(const orc_problem* pb, double bw, int adaptive, int kernel, int store_s,
+                 double* betas, double* betas_se, double* shat, double* qdiag, double* S)
+{
+    const int n = pb->n, p = pb->p, T = orc_threads(pb);
+    orc_ws* ws = (orc_ws*)malloc(sizeof(orc_ws) * (size_t)T);
+    double* qall = (double*)calloc((size_t)n * (size_t)T, sizeof(double));
+    for (int t = 0; t < T; t++) ws_alloc(&ws[t], n, p, 1);
+    const size_t srows = store_s ? (size_t)n : 1;
+    double s0 = 0.0, s1 = 0.0;
+    int ok = 1;
+#pragma omp parallel for num_threads(T) schedule(dynamic, 1) reduction(+ : s0, s1) reduction(&& : ok)
+    for (int i = 0; i < n; i++)
+    {
+        const int t = orc_thread_id();
+        orc_ws* w = &ws[t];
+        orc_distance_row(pb, i, w->d);
+        if (orc_weight(w->d, n, bw, adaptive, kernel, w->w) != 0) { ok = 0; continue; }
+        if (local_solve(pb, pb->x, p, w) != 0) { ok = 0; continue; }
+        for (int k = 0; k < p; k++) betas[(size_t)i + (size_t)k * n] = w->beta[k];
+        hat_row(pb, pb->x, p, i, w);
+        /* betasSE.col(i) = sum(ci % ci, 1) */
+        for (int r = 0; r < p; r++)
+        {
+            double s = 0.0;
+            for (int j = 0; j < n; j++) s += w->ci[r + (size_t)j * p] * w->ci[r + (size_t)j * p];
+            betas_se[(size_t)i + (size_t)r * n] = s;
+        }
+        double ss = 0.0;
+        for (int j = 0; j < n; j++) ss += w->si[j] * w->si[j];
+        s0 += w->si[i];
+        s1 += ss;
+        /* p = -si.t(); p(i) += 1; qDiag += p % p */
+        double* q = qall + (size_t)n * (size_t)t;
+        for (int j = 0; j < n; j++)
+        {
+            double v = -w->si[j];
+            if (j == i) v += 1.0;
+            q[j] += v * v;
+        }
+        const size_t row = store_s ? (size_t)i : 0;
+        if (store_s || i == n - 1)
+            for (int j = 0; j < n; j++) S[row + (size_t)j * srows] = w->si[j];
+    }
+    for (int j = 0; j < n; j++)
+    {
+        double s = 0.0;
+        for (int t = 0; t < T; t++) s += qall[(size_t)n * (size_t)t + (size_t)j];
+        qdiag[j] = s;
+    }
+    shat[0] = s0;
+    shat[1] = s1;
+    for (int t = 0; t < T; t++) ws_free(&ws[t]);
+    free(ws);
+    free(qall);
+    return ok ? 0 : -1;
+}
+
+/* ------------------------------------------------------------ golden search */
+
+typedef struct
+{
+    double* bw;
+    double* f;
+    int n, cap;
+} crit_map;
+
+/* mBandwidthCriterion[x] = f (std::map insert-or-assign). */
+static void map_put(crit_map* m, double x, double f)
+{
+    for (int i = 0; i < m->n; i++)
+        if (m->bw[i] == x) { m->f[i] = f; return; }
+    if (m->n < m->cap) { m->bw[m->n] = x; m->f[m->n] = f; m->n++; }
+}
+
+/* BandwidthSelector::optimize (BandwidthSelector.cpp:6-81). */
+int orc_golden(const orc_problem* pb, double bw0, int adaptive, int kernel, int criterion,
+               double lower, double upper, double* bw_out, double* list_bw, double* list_f, int cap)
+{
+    crit_map m = {list_bw, list_f, 0, cap};
+    double xU = upper, xL = lower;
+    const double eps = 1e-4;
+    const double R = (sqrt(5) - 1) / 2;
+    int iter = 0;
+    double d = R * (xU - xL);
+    double x1 = adaptive ? floor(xL + d) : (xL + d);
+    double x2 = adaptive ? round(xU - d) : (xU - d);
+    double f1 = orc_criterion(pb, x1, adaptive, kernel, criterion, NULL);
+    double f2 = orc_criterion(pb, x2, adaptive, kernel, criterion, NULL);
+    if (f1 == DBL_MAX && f2 == DBL_MAX) return -1; /* "Invalid initial values." */
+    if (f1 < DBL_MAX) map_put(&m, x1, f1);
+    if (f2 < DBL_MAX) map_put(&m, x2, f2);
+    double d1 = f2 - f1;
+    double xopt = f1 < f2 ? x1 : x2;
+    double ea = 100;
+    while ((fabs(d) > eps) && (fabs(d1) > eps) && iter < ea)
+    {
+        d = R * d;
+        if (f1 < f2)
+        {
+            xL = x2;
+            x2 = x1;
+            x1 = adaptive ? round(xL + d) : (xL + d);
+            f2 = f1;
+            f1 = orc_criterion(pb, x1, adaptive, kernel, criterion, NULL);
+            if (f1 < DBL_MAX) map_put(&m, x1, f1);
+        }
+        else
+        {
+            xU = x1;
+            x1 = x2;
+            x2 = adaptive ? floor(xU - d) : (xU - d);
+            f1 = f2;
+            f2 = orc_criterion(pb, x2, adaptive, kernel, criterion, NULL);
+            if (f2 < DBL_MAX) map_put(&m, x2, f2);
+        }
+        iter = iter + 1;
+        xopt = (f1 < f2) ? x1 : x2;
+        d1 = f2 - f1;
+    }
+    (void)bw0;
+    *bw_out = xopt;
+    /* bandwidthCriterion(): sorted by bandwidth (BandwidthSelector.cpp:83-95) */
+    for (int i = 1; i < m.n; i++)
+        for (int j = i; j > 0 && m.bw[j - 1] > m.bw[j]; j--)
+        {
+            double tb = m.bw[j], tf = m.f[j];
+            m.bw[j] = m.bw[j - 1]; m.f[j] = m.f[j - 1];
+            m.bw[j - 1] = tb; m.f[j - 1] = tf;
+        }
+    return m.n;
+}
+
+/* -------------------------------------------------------------- diagnostic */
+
+/* GWRBasic::CalcDiagnostic (GWRBasic.cpp:21-34). */
+void orc_diagnostic(const orc_problem* pb, const double* betas, const double* shat, double* out)
+{
+    const int n_ = pb->n;
+    double rss = rss_of(pb, pb->x, pb->p, betas);
+    double n = (double)n_;
+    double AIC = n * log(rss / n) + n * log(2 * M_PI) + n + shat[0];
+    double AICc = n * log(rss / n) + n * log(2 * M_PI) + n * ((n + shat[0]) / (n - 2 - shat[0]));
+    double edf = n - 2 * shat[0] + shat[1];
+    double enp = 2 * shat[0] - shat[1];
+    double mean = 0.0;
+    for (int i = 0; i < n_; i++) mean += pb->y[i];
+    mean /= n;
+    double yss = 0.0;
+    for (int i = 0; i < n_; i++) yss += (pb->y[i] - mean) * (pb->y[i] - mean);
+    double r2 = 1 - rss / yss;
+    double r2_adj = 1 - (1 - r2) * (n - 1) / (edf - 1);
+    out[0] = rss; out[1] = AIC; out[2] = AICc; out[3] = enp; out[4] = edf; out[5] = r2; out[6] = r2_adj;
+}

@@ -1,0 +1,95 @@
+/*
+ * gwr_oracle.h -- TEST INFRASTRUCTURE ONLY.
+ *
+ * CPU restatement of libgwmodel's GWRBasic hot path (GWRBasic::fit with
+ * golden-section bandwidth selection), used by tests/, by the smoke check
+ * and by bench.py's CPU-baseline leg as the parity checker.  Nothing in the
+ * product library links or calls it.
+ *
+ * Pinned against the known answers of the reference's own tests
+ * (test/testGWRBasic.cpp:40-137, 186-240) on the londonhp100 fixture; see
+ * tests/test_oracle_golden.py.
+ *
+ * Matrices are column-major (Armadillo layout): element (i, k) of an
+ * n x p matrix is at [i + k*n].
+ */
+#ifndef GWR_ORACLE_H
+#define GWR_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORC_AIC 0 /* GWRBasic::BandwidthSelectionCriterionType::AIC */
+#define ORC_CV 1  /* GWRBasic::BandwidthSelectionCriterionType::CV */
+
+#define ORC_GC_LIBM 0     /* great-circle with the platform libm, as the reference */
+#define ORC_GC_PORTABLE 1 /* great-circle with the engine's portable sin/cos/atan */
+
+typedef struct orc_problem
+{
+    int n, p;
+    const double* x;      /* n x p */
+    const double* y;      /* n */
+    const double* coords; /* n x 2: column 0 = x or longitude, column 1 = y or latitude */
+    int geographic;       /* CRSDistance(isGeographic) */
+    int gc_mode;          /* ORC_GC_LIBM or ORC_GC_PORTABLE */
+    int threads;          /* OpenMP threads (mOmpThreadNum) */
+} orc_problem;
+
+/* CRSDistance::SpGcdist with libm (CRSDistance.cpp:15-69). */
+double orc_gcdist_libm(double lon1, double lon2, double lat1, double lat2);
+/* The same formula with the engine's portable arithmetic. */
+double orc_gcdist_portable(double lon1, double lon2, double lat1, double lat2);
+
+/* CRSDistance::distance(focus) for focus points == data points (CRSDistance.cpp:122-131). */
+void orc_distance_row(const orc_problem* pb, int focus, double* out);
+/* CRSDistance::maxDistance (CRSDistance.cpp:133-143). */
+double orc_max_distance(const orc_problem* pb);
+
+/* BandwidthWeight::weight (BandwidthWeight.cpp:35-61).  Returns 0, or -1 when
+ * the adaptive bandwidth indexes outside the sorted distances. */
+int orc_weight(const double* dist, int n, double bw, int adaptive, int kernel, double* w);
+
+/* Adaptive threshold alone: the fixbw of BandwidthWeight.cpp:40-53. */
+int orc_adaptive_threshold(const double* dist, int n, double bw, double* fixbw);
+
+/* bandwidthSizeCriterion{AIC,CV}Omp (GWRBasic.cpp:440-535).  Returns the
+ * criterion, DBL_MAX when a local system is not SPD or the value is not
+ * finite.  shat_out (may be NULL) receives (trS, trStS) for AIC. */
+double orc_criterion(const orc_problem* pb, double bw, int adaptive, int kernel, int criterion,
+                     double* shat_out);
+
+/* The same criterion restricted to rows [row0, row1) and summed: the timed
+ * CPU-baseline sample.  Returns the partial sum of s_ii (AIC) or the CV sum. */
+double orc_criterion_rows(const orc_problem* pb, double bw, int adaptive, int kernel, int criterion,
+                          int row0, int row1);
+
+/* indepVarsSelectionCriterionOmp (GWRBasic.cpp:537-580): AICc with w == 1 on
+ * the columns cols[0..ncols). */
+double orc_indep_vars_criterion(const orc_problem* pb, const int* cols, int ncols);
+
+/* fitOmp (GWRBasic.cpp:386-438).  betas and betas_se are n x p; shat has 2
+ * entries; qdiag n; S is n x n when store_s, else 1 x n (the last row).
+ * Returns 0, or -1 when a local system is not SPD. */
+int orc_fit_core(const orc_problem* pb, double bw, int adaptive, int kernel, int store_s,
+                 double* betas, double* betas_se, double* shat, double* qdiag, double* S);
+
+/* BandwidthSelector::optimize (BandwidthSelector.cpp:6-81) over orc_criterion.
+ * Writes the chosen bandwidth; list_bw/list_f (capacity cap) receive the
+ * (bandwidth, criterion) pairs sorted by bandwidth (:83-95).  Returns the
+ * number of pairs, or -1 for "Invalid initial values." */
+int orc_golden(const orc_problem* pb, double bw0, int adaptive, int kernel, int criterion,
+               double lower, double upper, double* bw_out, double* list_bw, double* list_f, int cap);
+
+/* GWRBasic::CalcDiagnostic (GWRBasic.cpp:21-34): out = RSS, AIC, AICc, ENP,
+ * EDF, R2, R2adj. */
+void orc_diagnostic(const orc_problem* pb, const double* betas, const double* shat, double* out);
+
+/* Local Cholesky inverse of an SPD p x p matrix in place (inv_sympd); 0 or -1. */
+int orc_inv_sympd(double* a, int p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GWR_ORACLE_H */
