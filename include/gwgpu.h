@@ -1,0 +1,164 @@
+/*
+ * gwgpu.h -- plain C ABI of the GB300 GWRBasic engine (libgwgpu.so).
+ *
+ * Two layers, both over plain pointers and sizes:
+ *
+ *  1. gwgpu_gwr_*  -- the gwm::GWRBasic surface (include/gwmodelpp/GWRBasic.h:29
+ *     in libgwmodel) as a C handle: the same setters, fit() and getters.
+ *     This is what a non-C++ caller binds (ctypes, cgo, JNI, N-API).
+ *  2. gwgpu_engine_* -- the engine primitives behind it: one criterion
+ *     evaluation, the final fit, maxDistance, adaptive thresholds.  They
+ *     replace bandwidthSizeCriterion{AIC,CV}Cuda (GWRBasic.cpp:709-836),
+ *     fitCuda (GWRBasic.cpp:585-663), CRSDistance::maxDistance
+ *     (CRSDistance.cpp:133-143) and BandwidthWeight::weight's adaptive
+ *     threshold (BandwidthWeight.cpp:40-53).
+ *
+ * The binary drop-in for libgwmodelcuda (IGWRBasicGpuTask and its three
+ * extern "C" factories) is declared in IGWRBasicGpuTask.h.
+ *
+ * Matrices are column-major doubles (Armadillo layout: (i, j) at i + j*rows).
+ * Every function returns GWGPU_OK or an error code; gwgpu_last_error() gives
+ * the message of the calling thread's last failure.  No function resets the
+ * device.
+ */
+#ifndef GWGPU_H
+#define GWGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GWGPU_OK 0
+#define GWGPU_ERR_INVALID 1     /* bad argument or state */
+#define GWGPU_ERR_CUDA 2        /* CUDA runtime error (no device reset is done) */
+#define GWGPU_ERR_NOT_SPD 3     /* a local X^T W X is not positive definite */
+#define GWGPU_ERR_RUNTIME 4     /* other std::runtime_error (e.g. "Invalid initial values.") */
+#define GWGPU_ERR_RANGE 5       /* adaptive bandwidth below one neighbour */
+
+/* BandwidthWeight::KernelFunctionType (BandwidthWeight.h:46-53) */
+#define GWGPU_GAUSSIAN 0
+#define GWGPU_EXPONENTIAL 1
+#define GWGPU_BISQUARE 2
+#define GWGPU_TRICUBE 3
+#define GWGPU_BOXCAR 4
+
+/* GWRBasic::BandwidthSelectionCriterionType (GWRBasic.h:41-45) */
+#define GWGPU_AIC 0
+#define GWGPU_CV 1
+
+/* ParallelType (IParallelizable.h:15-20); every value runs on the GPU */
+#define GWGPU_SERIAL 1
+#define GWGPU_OPENMP 2
+#define GWGPU_CUDA 4
+
+/* numeric form */
+#define GWGPU_FP64 0
+#define GWGPU_MIXED 1
+
+/* Status (Status.h:10-14) */
+#define GWGPU_STATUS_SUCCESS 0
+#define GWGPU_STATUS_TERMINATED 1
+
+int gwgpu_version(void);
+const char* gwgpu_last_error(void);
+int gwgpu_device_count(int* count);
+
+/* ---------------------------------------------------------------- telegram */
+
+/* ITelegram (Logger.h:31-83) as C callbacks; any member may be NULL. */
+typedef struct gwgpu_telegram {
+    void* user;
+    void (*print)(void* user, const char* message, int level, const char* fun_name, const char* file_name);
+    void (*progress)(void* user, size_t current, size_t total, const char* fun_name, const char* file_name);
+    void (*progress_percent)(void* user, double percent, const char* fun_name, const char* file_name);
+    int (*stop)(void* user);
+} gwgpu_telegram;
+
+/* ------------------------------------------------------- GWRBasic surface */
+
+typedef struct gwgpu_gwr gwgpu_gwr;
+
+int gwgpu_gwr_create(gwgpu_gwr** out);
+void gwgpu_gwr_destroy(gwgpu_gwr* g);
+
+int gwgpu_gwr_set_coords(gwgpu_gwr* g, int n, const double* coords /* n x 2 */);
+int gwgpu_gwr_set_dependent_variable(gwgpu_gwr* g, int n, const double* y);
+int gwgpu_gwr_set_independent_variables(gwgpu_gwr* g, int n, int p, const double* x /* n x p */);
+/* SpatialWeight(BandwidthWeight(bandwidth, adaptive, kernel), CRSDistance(geographic)) */
+int gwgpu_gwr_set_spatial_weight(gwgpu_gwr* g, double bandwidth, int adaptive, int kernel, int geographic);
+int gwgpu_gwr_set_is_autoselect_bandwidth(gwgpu_gwr* g, int on);
+int gwgpu_gwr_set_bandwidth_selection_criterion(gwgpu_gwr* g, int criterion);
+int gwgpu_gwr_set_golden_upper_bounds(gwgpu_gwr* g, double value);
+int gwgpu_gwr_set_golden_lower_bounds(gwgpu_gwr* g, double value);
+int gwgpu_gwr_set_has_hat_matrix(gwgpu_gwr* g, int on);
+int gwgpu_gwr_set_has_intercept(gwgpu_gwr* g, int on);
+int gwgpu_gwr_set_is_autoselect_indep_vars(gwgpu_gwr* g, int on);
+int gwgpu_gwr_set_indep_var_selection_threshold(gwgpu_gwr* g, double threshold);
+int gwgpu_gwr_set_parallel_type(gwgpu_gwr* g, int type);
+int gwgpu_gwr_set_omp_thread_num(gwgpu_gwr* g, int threads);
+int gwgpu_gwr_set_gpu_id(gwgpu_gwr* g, int gpu);
+int gwgpu_gwr_set_group_size(gwgpu_gwr* g, size_t size);
+int gwgpu_gwr_set_precision(gwgpu_gwr* g, int precision);
+/* The telegram struct is copied; callbacks must outlive the handle. */
+int gwgpu_gwr_set_telegram(gwgpu_gwr* g, const gwgpu_telegram* t);
+
+/* GWRBasic::fit().  GWGPU_OK also when cancelled: check gwgpu_gwr_status. */
+int gwgpu_gwr_fit(gwgpu_gwr* g);
+int gwgpu_gwr_status(gwgpu_gwr* g);
+
+/* Shapes after fit (p shrinks when variables were selected). */
+int gwgpu_gwr_shape(gwgpu_gwr* g, int* n, int* p, int* s_rows);
+int gwgpu_gwr_betas(gwgpu_gwr* g, double* out /* n x p */);
+int gwgpu_gwr_betas_se(gwgpu_gwr* g, double* out /* n x p */);
+int gwgpu_gwr_shat(gwgpu_gwr* g, double* out /* 2: tr(S), tr(S^T S) */);
+int gwgpu_gwr_qdiag(gwgpu_gwr* g, double* out /* n */);
+int gwgpu_gwr_s(gwgpu_gwr* g, double* out /* s_rows x n */);
+/* RSS, AIC, AICc, ENP, EDF, RSquare, RSquareAdjust */
+int gwgpu_gwr_diagnostic(gwgpu_gwr* g, double* out /* 7 */);
+int gwgpu_gwr_bandwidth(gwgpu_gwr* g, double* bandwidth);
+/* bandwidthSelectionCriterionList(): count first (out may be NULL), sorted by bandwidth */
+int gwgpu_gwr_bandwidth_criterion_list(gwgpu_gwr* g, int* count, double* bw, double* value);
+/* selectedVariables() */
+int gwgpu_gwr_selected_vars(gwgpu_gwr* g, int* count, int* vars);
+/* indepVarsSelectionCriterionList(): entry i has lens[i] variables starting at vars[offset]. */
+int gwgpu_gwr_var_criterion_list(gwgpu_gwr* g, int* count, int* total_vars, int* lens, int* vars, double* value);
+
+/* --------------------------------------------------------- engine layer */
+
+typedef struct gwgpu_engine gwgpu_engine;
+
+typedef struct gwgpu_stats {
+    int criterion_evals;
+    int contract_launches;
+    double contract_ms;
+    double contract_flops;
+    double contract_bytes;
+    int select_launches;
+    double select_ms;
+} gwgpu_stats;
+
+int gwgpu_engine_create(int device, gwgpu_engine** out);
+void gwgpu_engine_destroy(gwgpu_engine* e);
+int gwgpu_engine_set_data(gwgpu_engine* e, int n, int p, const double* x, const double* y, const double* coords,
+                          int geographic);
+int gwgpu_engine_set_precision(gwgpu_engine* e, int precision);
+/* One bandwidth criterion (DBL_MAX when a local system is not SPD). */
+int gwgpu_engine_criterion(gwgpu_engine* e, double bandwidth, int adaptive, int kernel, int criterion,
+                           double* value);
+/* AICc with every weight one on the given columns (variable selection). */
+int gwgpu_engine_global_criterion(gwgpu_engine* e, int ncols, const int* cols, double* value);
+/* fitCuda outputs before GWRBasic::fit's sigma scaling of betasSE. */
+int gwgpu_engine_fit(gwgpu_engine* e, double bandwidth, int adaptive, int kernel, int store_s, double* betas,
+                     double* betas_se, double* shat, double* qdiag, double* s);
+int gwgpu_engine_max_distance(gwgpu_engine* e, double* out);
+int gwgpu_engine_thresholds(gwgpu_engine* e, double bandwidth, int adaptive, double* out /* n */);
+int gwgpu_engine_enable_stats(gwgpu_engine* e, int on);
+int gwgpu_engine_get_stats(gwgpu_engine* e, gwgpu_stats* out);
+int gwgpu_engine_reset_stats(gwgpu_engine* e);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GWGPU_H */

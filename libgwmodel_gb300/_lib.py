@@ -1,0 +1,135 @@
+"""ctypes binding of libgwgpu.so (include/gwgpu.h).
+
+The library is built in-tree by ``libgwmodel_gb300.build``.  There is no
+fallback: if the library cannot be loaded, or a call needs a GPU that is not
+there, the call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgwgpu.so")
+
+OK, ERR_INVALID, ERR_CUDA, ERR_NOT_SPD, ERR_RUNTIME, ERR_RANGE = range(6)
+
+_lock = threading.Lock()
+_lib = None
+
+
+class GwgpuError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[gwgpu error {code}] {message}")
+        self.code = code
+
+
+class Telegram(ctypes.Structure):
+    PRINT = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p)
+    PROGRESS = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_char_p,
+                                ctypes.c_char_p)
+    PERCENT = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_double, ctypes.c_char_p, ctypes.c_char_p)
+    STOP = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p)
+    _fields_ = [("user", ctypes.c_void_p), ("print", PRINT), ("progress", PROGRESS),
+                ("progress_percent", PERCENT), ("stop", STOP)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("criterion_evals", ctypes.c_int), ("contract_launches", ctypes.c_int),
+                ("contract_ms", ctypes.c_double), ("contract_flops", ctypes.c_double),
+                ("contract_bytes", ctypes.c_double), ("select_launches", ctypes.c_int),
+                ("select_ms", ctypes.c_double)]
+
+
+# (name, restype, argtypes) of every function declared in include/gwgpu.h
+_vp, _ip, _dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)
+_i, _d, _sz = ctypes.c_int, ctypes.c_double, ctypes.c_size_t
+SIGNATURES = [
+    ("gwgpu_version", _i, []),
+    ("gwgpu_last_error", ctypes.c_char_p, []),
+    ("gwgpu_device_count", _i, [_ip]),
+    ("gwgpu_gwr_create", _i, [ctypes.POINTER(_vp)]),
+    ("gwgpu_gwr_destroy", None, [_vp]),
+    ("gwgpu_gwr_set_coords", _i, [_vp, _i, _dp]),
+    ("gwgpu_gwr_set_dependent_variable", _i, [_vp, _i, _dp]),
+    ("gwgpu_gwr_set_independent_variables", _i, [_vp, _i, _i, _dp]),
+    ("gwgpu_gwr_set_spatial_weight", _i, [_vp, _d, _i, _i, _i]),
+    ("gwgpu_gwr_set_is_autoselect_bandwidth", _i, [_vp, _i]),
+    ("gwgpu_gwr_set_bandwidth_selection_criterion", _i, [_vp, _i]),
+    ("gwgpu_gwr_set_golden_upper_bounds", _i, [_vp, _d]),
+    ("gwgpu_gwr_set_golden_lower_bounds", _i, [_vp, _d]),
+    ("gwgpu_gwr_set_has_hat_matrix", _i, [_vp, _i]),
+    ("gwgpu_gwr_set_has_intercept", _i, [_vp, _i]),
+    ("gwgpu_gwr_set_is_autoselect_indep_vars", _i, [_vp, _i]),
+    ("gwgpu_gwr_set_indep_var_selection_threshold", _i, [_vp, _d]),
+    ("gwgpu_gwr_set_parallel_type", _i, [_vp, _i]),
+    ("gwgpu_gwr_set_omp_thread_num", _i, [_vp, _i]),
+    ("gwgpu_gwr_set_gpu_id", _i, [_vp, _i]),
+    ("gwgpu_gwr_set_group_size", _i, [_vp, _sz]),
+    ("gwgpu_gwr_set_precision", _i, [_vp, _i]),
+    ("gwgpu_gwr_set_telegram", _i, [_vp, ctypes.POINTER(Telegram)]),
+    ("gwgpu_gwr_fit", _i, [_vp]),
+    ("gwgpu_gwr_status", _i, [_vp]),
+    ("gwgpu_gwr_shape", _i, [_vp, _ip, _ip, _ip]),
+    ("gwgpu_gwr_betas", _i, [_vp, _dp]),
+    ("gwgpu_gwr_betas_se", _i, [_vp, _dp]),
+    ("gwgpu_gwr_shat", _i, [_vp, _dp]),
+    ("gwgpu_gwr_qdiag", _i, [_vp, _dp]),
+    ("gwgpu_gwr_s", _i, [_vp, _dp]),
+    ("gwgpu_gwr_diagnostic", _i, [_vp, _dp]),
+    ("gwgpu_gwr_bandwidth", _i, [_vp, _dp]),
+    ("gwgpu_gwr_bandwidth_criterion_list", _i, [_vp, _ip, _dp, _dp]),
+    ("gwgpu_gwr_selected_vars", _i, [_vp, _ip, _ip]),
+    ("gwgpu_gwr_var_criterion_list", _i, [_vp, _ip, _ip, _ip, _ip, _dp]),
+    ("gwgpu_engine_create", _i, [_i, ctypes.POINTER(_vp)]),
+    ("gwgpu_engine_destroy", None, [_vp]),
+    ("gwgpu_engine_set_data", _i, [_vp, _i, _i, _dp, _dp, _dp, _i]),
+    ("gwgpu_engine_set_precision", _i, [_vp, _i]),
+    ("gwgpu_engine_criterion", _i, [_vp, _d, _i, _i, _i, _dp]),
+    ("gwgpu_engine_global_criterion", _i, [_vp, _i, _ip, _dp]),
+    ("gwgpu_engine_fit", _i, [_vp, _d, _i, _i, _i, _dp, _dp, _dp, _dp, _dp]),
+    ("gwgpu_engine_max_distance", _i, [_vp, _dp]),
+    ("gwgpu_engine_thresholds", _i, [_vp, _d, _i, _dp]),
+    ("gwgpu_engine_enable_stats", _i, [_vp, _i]),
+    ("gwgpu_engine_get_stats", _i, [_vp, ctypes.POINTER(Stats)]),
+    ("gwgpu_engine_reset_stats", _i, [_vp]),
+]
+
+# The drop-in factories of include/IGWRBasicGpuTask.h.
+TASK_SIGNATURES = [
+    ("GWRBasicGpuTaskFit_Create", _vp, [_i, _i, _i]),
+    ("GWRBasicGpuTaskPredict_Create", _vp, [_i, _i, _i, _i]),
+    ("GWRBasicGpuTask_Del", None, [_vp]),
+]
+
+
+def lib():
+    """Load libgwgpu.so, building it first when it is missing."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                from . import build
+                build.build()
+            L = ctypes.CDLL(LIB_PATH)
+            for name, res, args in SIGNATURES + TASK_SIGNATURES:
+                f = getattr(L, name)
+                f.restype = res
+                f.argtypes = args
+            _lib = L
+    return _lib
+
+
+def check(rc: int):
+    if rc != OK:
+        raise GwgpuError(rc, lib().gwgpu_last_error().decode(errors="replace"))
+    return rc
+
+
+def dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def iptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))

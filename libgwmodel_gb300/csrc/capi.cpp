@@ -1,0 +1,480 @@
+// capi.cpp -- extern "C" layer of include/gwgpu.h over gwm::GWRBasic and the engine.
+#include "../../include/gwgpu.h"
+
+#include <cfloat>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+
+#include "../../include/gwmodel_gb300/GWRBasic.h"
+#include "engine.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* msg)
+{
+    g_last_error = msg ? msg : "";
+    return code;
+}
+
+template <class F>
+int guarded(F&& f)
+{
+    try {
+        f();
+        return GWGPU_OK;
+    } catch (const gwgpu::NotSPDError& e) {
+        return fail(GWGPU_ERR_NOT_SPD, e.what());
+    } catch (const gwgpu::CudaError& e) {
+        return fail(GWGPU_ERR_CUDA, e.what());
+    } catch (const std::out_of_range& e) {
+        return fail(GWGPU_ERR_RANGE, e.what());
+    } catch (const std::invalid_argument& e) {
+        return fail(GWGPU_ERR_INVALID, e.what());
+    } catch (const std::logic_error& e) {
+        return fail(GWGPU_ERR_INVALID, e.what());
+    } catch (const std::bad_alloc&) {
+        return fail(GWGPU_ERR_RUNTIME, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(GWGPU_ERR_RUNTIME, e.what());
+    }
+}
+
+// ITelegram over the C callbacks.
+class CTelegram : public gwm::ITelegram {
+public:
+    explicit CTelegram(const gwgpu_telegram& t) : t_(t) {}
+    void print(std::string message, LogLevel level, std::string fun, std::string file) override
+    {
+        if (t_.print) t_.print(t_.user, message.c_str(), (int)level, fun.c_str(), file.c_str());
+    }
+    void progress(std::size_t current, std::size_t total, std::string fun, std::string file) override
+    {
+        if (t_.progress) t_.progress(t_.user, current, total, fun.c_str(), file.c_str());
+    }
+    void progress(double percent, std::string fun, std::string file) override
+    {
+        if (t_.progress_percent) t_.progress_percent(t_.user, percent, fun.c_str(), file.c_str());
+    }
+    bool stop() override { return t_.stop ? t_.stop(t_.user) != 0 : false; }
+
+private:
+    gwgpu_telegram t_;
+};
+
+}  // namespace
+
+struct gwgpu_gwr {
+    gwm::GWRBasic alg;
+    double bandwidth = 0.0;
+    bool adaptive = true;
+    int kernel = GWGPU_GAUSSIAN;
+    bool geographic = false;
+};
+
+struct gwgpu_engine {
+    explicit gwgpu_engine(int device) : eng(device) {}
+    gwgpu::Engine eng;
+};
+
+extern "C" {
+
+int gwgpu_version(void) { return 10000; }
+
+const char* gwgpu_last_error(void) { return g_last_error.c_str(); }
+
+int gwgpu_device_count(int* count)
+{
+    if (!count) return fail(GWGPU_ERR_INVALID, "null pointer");
+    cudaError_t e = cudaGetDeviceCount(count);
+    if (e != cudaSuccess) {
+        *count = 0;
+        return fail(GWGPU_ERR_CUDA, cudaGetErrorString(e));
+    }
+    return GWGPU_OK;
+}
+
+// ------------------------------------------------------------------- gwr
+
+int gwgpu_gwr_create(gwgpu_gwr** out)
+{
+    if (!out) return fail(GWGPU_ERR_INVALID, "null pointer");
+    return guarded([&] { *out = new gwgpu_gwr(); });
+}
+
+void gwgpu_gwr_destroy(gwgpu_gwr* g) { delete g; }
+
+#define GWR_CHECK(g) \
+    if (!(g)) return fail(GWGPU_ERR_INVALID, "null handle")
+
+int gwgpu_gwr_set_coords(gwgpu_gwr* g, int n, const double* coords)
+{
+    GWR_CHECK(g);
+    if (n < 0 || (!coords && n)) return fail(GWGPU_ERR_INVALID, "bad coords");
+    return guarded([&] { g->alg.setCoords(gwm::mat(n, 2, coords)); });
+}
+
+int gwgpu_gwr_set_dependent_variable(gwgpu_gwr* g, int n, const double* y)
+{
+    GWR_CHECK(g);
+    if (n < 0 || (!y && n)) return fail(GWGPU_ERR_INVALID, "bad y");
+    return guarded([&] { g->alg.setDependentVariable(gwm::vec(n, 1, y)); });
+}
+
+int gwgpu_gwr_set_independent_variables(gwgpu_gwr* g, int n, int p, const double* x)
+{
+    GWR_CHECK(g);
+    if (n < 0 || p < 0 || (!x && n && p)) return fail(GWGPU_ERR_INVALID, "bad x");
+    return guarded([&] { g->alg.setIndependentVariables(gwm::mat(n, p, x)); });
+}
+
+int gwgpu_gwr_set_spatial_weight(gwgpu_gwr* g, double bandwidth, int adaptive, int kernel, int geographic)
+{
+    GWR_CHECK(g);
+    if (kernel < 0 || kernel > 4) return fail(GWGPU_ERR_INVALID, "unknown kernel");
+    gwm::BandwidthWeight w(bandwidth, adaptive != 0, (gwm::BandwidthWeight::KernelFunctionType)kernel);
+    gwm::CRSDistance d(geographic != 0);
+    g->alg.setSpatialWeight(gwm::SpatialWeight(&w, &d));
+    return GWGPU_OK;
+}
+
+int gwgpu_gwr_set_is_autoselect_bandwidth(gwgpu_gwr* g, int on)
+{
+    GWR_CHECK(g);
+    g->alg.setIsAutoselectBandwidth(on != 0);
+    return GWGPU_OK;
+}
+
+int gwgpu_gwr_set_bandwidth_selection_criterion(gwgpu_gwr* g, int criterion)
+{
+    GWR_CHECK(g);
+    if (criterion != GWGPU_AIC && criterion != GWGPU_CV) return fail(GWGPU_ERR_INVALID, "unknown criterion");
+    g->alg.setBandwidthSelectionCriterion((gwm::GWRBasic::BandwidthSelectionCriterionType)criterion);
+    return GWGPU_OK;
+}
+
+int gwgpu_gwr_set_golden_upper_bounds(gwgpu_gwr* g, double value)
+{
+    GWR_CHECK(g);
+    g->alg.setGoldenUpperBounds(value);
+    return GWGPU_OK;
+}
+
+int gwgpu_gwr_set_golden_lower_bounds(gwgpu_gwr* g, double value)
+{
+    GWR_CHECK(g);
+    g->alg.setGoldenLowerBounds(value);
+    return GWGPU_OK;
+}
+
+int gwgpu_gwr_set_has_hat_matrix(gwgpu_gwr* g, int on)
+{
+    GWR_CHECK(g);
+    g->alg.setHasHatMatrix(on != 0);
+    return GWGPU_OK;
+}
+
+int gwgpu_gwr_set_has_intercept(gwgpu_gwr* g, int on)
+{
+    GWR_CHECK(g);
+    g->alg.setHasIntercept(on != 0);
+    return GWGPU_OK;
+}
+
+int gwgpu_gwr_set_is_autoselect_indep_vars(gwgpu_gwr* g, int on)
+{
+    GWR_CHECK(g);
+    g->alg.setIsAutoselectIndepVars(on != 0);
+    return GWGPU_OK;
+}
+
+int gwgpu_gwr_set_indep_var_selection_threshold(gwgpu_gwr* g, double threshold)
+{
+    GWR_CHECK(g);
+    g->alg.setIndepVarSelectionThreshold(threshold);
+    return GWGPU_OK;
+}
+
+int gwgpu_gwr_set_parallel_type(gwgpu_gwr* g, int type)
+{
+    GWR_CHECK(g);
+    g->alg.setParallelType((gwm::ParallelType)type);
+    return GWGPU_OK;
+}
+
+int gwgpu_gwr_set_omp_thread_num(gwgpu_gwr* g, int threads)
+{
+    GWR_CHECK(g);
+    g->alg.setOmpThreadNum(threads);
+    return GWGPU_OK;
+}
+
+int gwgpu_gwr_set_gpu_id(gwgpu_gwr* g, int gpu)
+{
+    GWR_CHECK(g);
+    g->alg.setGPUId(gpu);
+    return GWGPU_OK;
+}
+
+int gwgpu_gwr_set_group_size(gwgpu_gwr* g, size_t size)
+{
+    GWR_CHECK(g);
+    g->alg.setGroupSize(size);
+    return GWGPU_OK;
+}
+
+int gwgpu_gwr_set_precision(gwgpu_gwr* g, int precision)
+{
+    GWR_CHECK(g);
+    if (precision != GWGPU_FP64 && precision != GWGPU_MIXED) return fail(GWGPU_ERR_INVALID, "unknown precision");
+    g->alg.setPrecision((gwm::Precision)precision);
+    return GWGPU_OK;
+}
+
+int gwgpu_gwr_set_telegram(gwgpu_gwr* g, const gwgpu_telegram* t)
+{
+    GWR_CHECK(g);
+    return guarded([&] {
+        if (t)
+            g->alg.setTelegram(std::unique_ptr<gwm::ITelegram>(new CTelegram(*t)));
+        else
+            g->alg.setTelegram(std::unique_ptr<gwm::ITelegram>(new gwm::Logger()));
+    });
+}
+
+int gwgpu_gwr_fit(gwgpu_gwr* g)
+{
+    GWR_CHECK(g);
+    return guarded([&] { g->alg.fit(); });
+}
+
+int gwgpu_gwr_status(gwgpu_gwr* g)
+{
+    if (!g) return -1;
+    return (int)g->alg.status();
+}
+
+int gwgpu_gwr_shape(gwgpu_gwr* g, int* n, int* p, int* s_rows)
+{
+    GWR_CHECK(g);
+    if (n) *n = (int)g->alg.betas().n_rows;
+    if (p) *p = (int)g->alg.betas().n_cols;
+    if (s_rows) *s_rows = (int)g->alg.s().n_rows;
+    return GWGPU_OK;
+}
+
+static int copy_out(const gwm::mat& m, double* out)
+{
+    if (!out) return fail(GWGPU_ERR_INVALID, "null output");
+    if (m.n_elem()) std::memcpy(out, m.memptr(), sizeof(double) * m.n_elem());
+    return GWGPU_OK;
+}
+
+int gwgpu_gwr_betas(gwgpu_gwr* g, double* out)
+{
+    GWR_CHECK(g);
+    return copy_out(g->alg.betas(), out);
+}
+
+int gwgpu_gwr_betas_se(gwgpu_gwr* g, double* out)
+{
+    GWR_CHECK(g);
+    return copy_out(g->alg.betasSE(), out);
+}
+
+int gwgpu_gwr_shat(gwgpu_gwr* g, double* out)
+{
+    GWR_CHECK(g);
+    return copy_out(g->alg.sHat(), out);
+}
+
+int gwgpu_gwr_qdiag(gwgpu_gwr* g, double* out)
+{
+    GWR_CHECK(g);
+    return copy_out(g->alg.qDiag(), out);
+}
+
+int gwgpu_gwr_s(gwgpu_gwr* g, double* out)
+{
+    GWR_CHECK(g);
+    return copy_out(g->alg.s(), out);
+}
+
+int gwgpu_gwr_diagnostic(gwgpu_gwr* g, double* out)
+{
+    GWR_CHECK(g);
+    if (!out) return fail(GWGPU_ERR_INVALID, "null output");
+    gwm::RegressionDiagnostic d = g->alg.diagnostic();
+    out[0] = d.RSS;
+    out[1] = d.AIC;
+    out[2] = d.AICc;
+    out[3] = d.ENP;
+    out[4] = d.EDF;
+    out[5] = d.RSquare;
+    out[6] = d.RSquareAdjust;
+    return GWGPU_OK;
+}
+
+int gwgpu_gwr_bandwidth(gwgpu_gwr* g, double* bandwidth)
+{
+    GWR_CHECK(g);
+    if (!bandwidth) return fail(GWGPU_ERR_INVALID, "null output");
+    *bandwidth = g->alg.spatialWeight().weight()->bandwidth();
+    return GWGPU_OK;
+}
+
+int gwgpu_gwr_bandwidth_criterion_list(gwgpu_gwr* g, int* count, double* bw, double* value)
+{
+    GWR_CHECK(g);
+    const auto& l = g->alg.bandwidthSelectionCriterionList();
+    if (count) *count = (int)l.size();
+    for (size_t i = 0; i < l.size(); i++) {
+        if (bw) bw[i] = l[i].first;
+        if (value) value[i] = l[i].second;
+    }
+    return GWGPU_OK;
+}
+
+int gwgpu_gwr_selected_vars(gwgpu_gwr* g, int* count, int* vars)
+{
+    GWR_CHECK(g);
+    auto v = g->alg.selectedVariables();
+    if (count) *count = (int)v.size();
+    if (vars)
+        for (size_t i = 0; i < v.size(); i++) vars[i] = (int)v[i];
+    return GWGPU_OK;
+}
+
+int gwgpu_gwr_var_criterion_list(gwgpu_gwr* g, int* count, int* total_vars, int* lens, int* vars, double* value)
+{
+    GWR_CHECK(g);
+    const auto& l = g->alg.indepVarsSelectionCriterionList();
+    if (count) *count = (int)l.size();
+    int off = 0;
+    for (size_t i = 0; i < l.size(); i++) {
+        if (lens) lens[i] = (int)l[i].first.size();
+        if (value) value[i] = l[i].second;
+        for (size_t k = 0; k < l[i].first.size(); k++) {
+            if (vars) vars[off] = (int)l[i].first[k];
+            off++;
+        }
+    }
+    if (total_vars) *total_vars = off;
+    return GWGPU_OK;
+}
+
+// ---------------------------------------------------------------- engine
+
+int gwgpu_engine_create(int device, gwgpu_engine** out)
+{
+    if (!out) return fail(GWGPU_ERR_INVALID, "null pointer");
+    *out = nullptr;
+    return guarded([&] { *out = new gwgpu_engine(device); });
+}
+
+void gwgpu_engine_destroy(gwgpu_engine* e) { delete e; }
+
+#define ENG_CHECK(e) \
+    if (!(e)) return fail(GWGPU_ERR_INVALID, "null handle")
+
+int gwgpu_engine_set_data(gwgpu_engine* e, int n, int p, const double* x, const double* y, const double* coords,
+                          int geographic)
+{
+    ENG_CHECK(e);
+    if (!x || !y || !coords) return fail(GWGPU_ERR_INVALID, "null input");
+    return guarded([&] { e->eng.setData(n, p, x, y, coords, geographic != 0); });
+}
+
+int gwgpu_engine_set_precision(gwgpu_engine* e, int precision)
+{
+    ENG_CHECK(e);
+    if (precision != GWGPU_FP64 && precision != GWGPU_MIXED) return fail(GWGPU_ERR_INVALID, "unknown precision");
+    e->eng.setPrecision(precision);
+    return GWGPU_OK;
+}
+
+int gwgpu_engine_criterion(gwgpu_engine* e, double bandwidth, int adaptive, int kernel, int criterion, double* value)
+{
+    ENG_CHECK(e);
+    if (!value) return fail(GWGPU_ERR_INVALID, "null output");
+    if (kernel < 0 || kernel > 4) return fail(GWGPU_ERR_INVALID, "unknown kernel");
+    return guarded([&] { *value = e->eng.criterion(bandwidth, adaptive != 0, kernel, criterion); });
+}
+
+int gwgpu_engine_global_criterion(gwgpu_engine* e, int ncols, const int* cols, double* value)
+{
+    ENG_CHECK(e);
+    if (!value || !cols) return fail(GWGPU_ERR_INVALID, "null pointer");
+    return guarded([&] { *value = e->eng.globalCriterion(std::vector<int>(cols, cols + ncols)); });
+}
+
+int gwgpu_engine_fit(gwgpu_engine* e, double bandwidth, int adaptive, int kernel, int store_s, double* betas,
+                     double* betas_se, double* shat, double* qdiag, double* s)
+{
+    ENG_CHECK(e);
+    if (kernel < 0 || kernel > 4) return fail(GWGPU_ERR_INVALID, "unknown kernel");
+    return guarded([&] {
+        gwgpu::FitOutput o;
+        e->eng.fit(bandwidth, adaptive != 0, kernel, store_s != 0, o);
+        if (betas) std::memcpy(betas, o.betas.data(), sizeof(double) * o.betas.size());
+        if (betas_se) std::memcpy(betas_se, o.betasSE.data(), sizeof(double) * o.betasSE.size());
+        if (shat) {
+            shat[0] = o.shat[0];
+            shat[1] = o.shat[1];
+        }
+        if (qdiag) std::memcpy(qdiag, o.qdiag.data(), sizeof(double) * o.qdiag.size());
+        if (s) std::memcpy(s, o.S.data(), sizeof(double) * o.S.size());
+    });
+}
+
+int gwgpu_engine_max_distance(gwgpu_engine* e, double* out)
+{
+    ENG_CHECK(e);
+    if (!out) return fail(GWGPU_ERR_INVALID, "null output");
+    return guarded([&] { *out = e->eng.maxDistance(); });
+}
+
+int gwgpu_engine_thresholds(gwgpu_engine* e, double bandwidth, int adaptive, double* out)
+{
+    ENG_CHECK(e);
+    if (!out) return fail(GWGPU_ERR_INVALID, "null output");
+    return guarded([&] {
+        std::vector<double> t;
+        e->eng.thresholds(bandwidth, adaptive != 0, t);
+        std::memcpy(out, t.data(), sizeof(double) * t.size());
+    });
+}
+
+int gwgpu_engine_enable_stats(gwgpu_engine* e, int on)
+{
+    ENG_CHECK(e);
+    e->eng.enableStats(on != 0);
+    return GWGPU_OK;
+}
+
+int gwgpu_engine_get_stats(gwgpu_engine* e, gwgpu_stats* out)
+{
+    ENG_CHECK(e);
+    if (!out) return fail(GWGPU_ERR_INVALID, "null output");
+    const gwgpu::EngineStats& s = e->eng.stats();
+    out->criterion_evals = s.criterion_evals;
+    out->contract_launches = s.contract_launches;
+    out->contract_ms = s.contract_ms;
+    out->contract_flops = s.contract_flops;
+    out->contract_bytes = s.contract_bytes;
+    out->select_launches = s.select_launches;
+    out->select_ms = s.select_ms;
+    return GWGPU_OK;
+}
+
+int gwgpu_engine_reset_stats(gwgpu_engine* e)
+{
+    ENG_CHECK(e);
+    e->eng.stats() = gwgpu::EngineStats{};
+    return GWGPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,430 @@
+// engine.cpp -- host side of the device-resident GWR engine.
+#include "engine.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+#include "gw_kernels.h"
+
+namespace gwgpu {
+
+void check(cudaError_t e, const char* what)
+{
+    if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+namespace {
+
+uint64_t spread_bits(uint32_t x)
+{
+    uint64_t v = x;
+    v = (v | (v << 16)) & 0x0000FFFF0000FFFFull;
+    v = (v | (v << 8)) & 0x00FF00FF00FF00FFull;
+    v = (v | (v << 4)) & 0x0F0F0F0F0F0F0F0Full;
+    v = (v | (v << 2)) & 0x3333333333333333ull;
+    v = (v | (v << 1)) & 0x5555555555555555ull;
+    return v;
+}
+
+// GWRBase::AICc (GWRBase.h:90-94) from RSS and tr(S).
+double aicc(double n, double rss, double trS)
+{
+    return n * std::log(rss / n) + n * std::log(2 * M_PI) + n * ((n + trS) / (n - 2 - trS));
+}
+
+}  // namespace
+
+Engine::Engine(int device) : device_(device)
+{
+    check(cudaSetDevice(device), "cudaSetDevice");
+    cudaDeviceProp prop;
+    check(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
+    num_sms_ = prop.multiProcessorCount;
+    check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    check(cudaMallocHost(&host_sums_, 8 * sizeof(double)), "cudaMallocHost");
+}
+
+Engine::~Engine()
+{
+    if (stream_) cudaStreamSynchronize(stream_);
+    if (host_sums_) cudaFreeHost(host_sums_);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+void Engine::synchronize() { check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize"); }
+
+DevPoints Engine::points() const
+{
+    DevPoints P;
+    P.n = n_;
+    P.u = u_.get();
+    P.v = v_.get();
+    P.uR = uR_.get();
+    P.vR = vR_.get();
+    return P;
+}
+
+void Engine::setData(int n, int p, const double* x, const double* y, const double* coords, bool geographic)
+{
+    if (n < 2) throw std::invalid_argument("GWRBasic needs at least two data points");
+    if (p < 1 || p > kMaxP) throw std::invalid_argument("number of independent variables must be in [1, 32]");
+    check(cudaSetDevice(device_), "cudaSetDevice");
+    n_ = n;
+    p_ = p;
+    mm_ = p * (p + 1) / 2;
+    m_ = mm_ + p;
+    geographic_ = geographic;
+    thr_valid_ = false;
+    gall_valid_ = false;
+
+    // Morton order of the coordinates
+    double umin = coords[0], umax = coords[0], vmin = coords[n], vmax = coords[n];
+    for (int i = 0; i < n; i++) {
+        umin = std::min(umin, coords[i]);
+        umax = std::max(umax, coords[i]);
+        vmin = std::min(vmin, coords[n + i]);
+        vmax = std::max(vmax, coords[n + i]);
+    }
+    const double su = umax > umin ? 2147483647.0 / (umax - umin) : 0.0;
+    const double sv = vmax > vmin ? 2147483647.0 / (vmax - vmin) : 0.0;
+    std::vector<std::pair<uint64_t, int>> keyed(n);
+    for (int i = 0; i < n; i++) {
+        double fu = (coords[i] - umin) * su, fv = (coords[n + i] - vmin) * sv;
+        uint32_t qu = std::isfinite(fu) ? (uint32_t)std::min(std::max(fu, 0.0), 2147483647.0) : 0u;
+        uint32_t qv = std::isfinite(fv) ? (uint32_t)std::min(std::max(fv, 0.0), 2147483647.0) : 0u;
+        keyed[i] = {spread_bits(qu) | (spread_bits(qv) << 1), i};
+    }
+    std::sort(keyed.begin(), keyed.end());
+    perm_.resize(n);
+    for (int s = 0; s < n; s++) perm_[s] = keyed[s].second;
+
+    std::vector<double> hu(n), hv(n), huR, hvR, hx((size_t)n * p), hy(n);
+    const double DE2RA = M_PI / 180;
+    if (geographic) {
+        huR.resize(n);
+        hvR.resize(n);
+    }
+    for (int s = 0; s < n; s++) {
+        int i = perm_[s];
+        hu[s] = coords[i];
+        hv[s] = coords[n + i];
+        if (geographic) {
+            huR[s] = hu[s] * DE2RA;
+            hvR[s] = hv[s] * DE2RA;
+        }
+        for (int k = 0; k < p; k++) hx[(size_t)s * p + k] = x[(size_t)i + (size_t)k * n];
+        hy[s] = y[i];
+    }
+    const int ntiles = (n + kTile - 1) / kTile;
+    std::vector<TileBox> ht(ntiles);
+    for (int t = 0; t < ntiles; t++) {
+        TileBox b{hu[t * kTile], hu[t * kTile], hv[t * kTile], hv[t * kTile]};
+        for (int s = t * kTile; s < std::min(n, (t + 1) * kTile); s++) {
+            b.ulo = std::min(b.ulo, hu[s]);
+            b.uhi = std::max(b.uhi, hu[s]);
+            b.vlo = std::min(b.vlo, hv[s]);
+            b.vhi = std::max(b.vhi, hv[s]);
+        }
+        ht[t] = b;
+    }
+    if (geographic) {
+        dhi_ = 20300.0;  // above half the WGS-84 meridian circumference with the flattening term
+    } else {
+        double du = umax - umin, dv = vmax - vmin;
+        dhi_ = std::sqrt(du * du + dv * dv) * (1.0 + 1e-9);
+        if (!(dhi_ > 0.0) || !std::isfinite(dhi_)) dhi_ = 1.0;
+    }
+    dlo_ = std::ldexp(dhi_, -24);
+
+    u_.alloc(n);
+    v_.alloc(n);
+    if (geographic) {
+        uR_.alloc(n);
+        vR_.alloc(n);
+    } else {
+        uR_.release();
+        vR_.release();
+    }
+    x_.alloc((size_t)n * p);
+    y_.alloc(n);
+    z_.alloc((size_t)n * m_);
+    g_.alloc((size_t)n * m_);
+    thr_.alloc(n);
+    sel0_.alloc(n);
+    sel1_.alloc(n);
+    beta_.alloc((size_t)n * p);
+    sii_.alloc(n);
+    resid_.alloc(n);
+    partials_.alloc(4096 * 4);
+    sums_.alloc(8);
+    tiles_.alloc(ntiles);
+    key_.alloc(1);
+    check(cudaMemcpyAsync(u_.get(), hu.data(), sizeof(double) * n, cudaMemcpyHostToDevice, stream_), "H2D u");
+    check(cudaMemcpyAsync(v_.get(), hv.data(), sizeof(double) * n, cudaMemcpyHostToDevice, stream_), "H2D v");
+    if (geographic) {
+        check(cudaMemcpyAsync(uR_.get(), huR.data(), sizeof(double) * n, cudaMemcpyHostToDevice, stream_), "H2D");
+        check(cudaMemcpyAsync(vR_.get(), hvR.data(), sizeof(double) * n, cudaMemcpyHostToDevice, stream_), "H2D");
+    }
+    check(cudaMemcpyAsync(x_.get(), hx.data(), sizeof(double) * hx.size(), cudaMemcpyHostToDevice, stream_),
+          "H2D x");
+    check(cudaMemcpyAsync(y_.get(), hy.data(), sizeof(double) * n, cudaMemcpyHostToDevice, stream_), "H2D y");
+    check(cudaMemcpyAsync(tiles_.get(), ht.data(), sizeof(TileBox) * ntiles, cudaMemcpyHostToDevice, stream_),
+          "H2D tiles");
+    check(launch_build_z(n, p, x_.get(), y_.get(), z_.get(), stream_), "build_z");
+    synchronize();
+}
+
+void Engine::computeThresholds(double bw, bool adaptive)
+{
+    if (!adaptive) return;
+    if (thr_valid_ && thr_bw_ == bw) return;
+    const DevPoints P = points();
+    const double dn = bw / n_;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (stats_on_) {
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, stream_);
+    }
+    if (dn < 1) {
+        // d0 = vdist(int(b0) - 1), d1 = vdist(int(b0)) (BandwidthWeight.cpp:46-48)
+        const double b0 = std::floor(bw), bx = bw - b0;
+        const long long r0 = (long long)(int)b0;
+        if (r0 < 1 || r0 >= n_) throw std::out_of_range("Mat::operator(): index out of bounds");
+        check(launch_select(P, geographic_, (unsigned)r0, dlo_, dhi_, sel0_.get(), num_sms_, stream_), "select");
+        const double* d1 = nullptr;
+        if (bx != 0.0) {
+            check(launch_select(P, geographic_, (unsigned)(r0 + 1), dlo_, dhi_, sel1_.get(), num_sms_, stream_),
+                  "select");
+            d1 = sel1_.get();
+        }
+        check(launch_threshold_combine(n_, bw, sel0_.get(), d1, thr_.get(), stream_), "threshold");
+    } else {
+        // fixbw = dn * max(dist) (BandwidthWeight.cpp:50-53)
+        check(launch_select(P, geographic_, (unsigned)n_, dlo_, dhi_, sel0_.get(), num_sms_, stream_), "select");
+        check(launch_threshold_combine(n_, bw, sel0_.get(), nullptr, thr_.get(), stream_), "threshold");
+    }
+    if (stats_on_) {
+        cudaEventRecord(e1, stream_);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        stats_.select_ms += ms;
+        stats_.select_launches += 1;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    thr_valid_ = true;
+    thr_bw_ = bw;
+}
+
+void Engine::contract(const double* Z, int mcols, double* G, int ldg, double bw, bool adaptive, int kernel,
+                      bool exclude_self, int wpow)
+{
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (stats_on_) {
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, stream_);
+    }
+    check(launch_contract64(points(), geographic_, tiles_.get(), Z, m_, mcols, G, ldg, thrPtr(adaptive), bw, kernel,
+                            exclude_self, wpow, true, stream_),
+          "contract64");
+    if (stats_on_) {
+        cudaEventRecord(e1, stream_);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        stats_.contract_ms += ms;
+        stats_.contract_launches += 1;
+        // useful pairs: dense kernels touch every pair; adaptive compact kernels
+        // have b-1 neighbours with d < r_i per row (ties aside)
+        double pairs = (double)n_ * n_;
+        if (adaptive && kernel >= GW_KERNEL_BISQUARE) pairs = (double)n_ * std::max(0.0, std::min(bw, (double)n_) - 1);
+        stats_.contract_flops += 2.0 * mcols * pairs;
+        stats_.contract_bytes += 8.0 * ((double)n_ * m_ + (double)n_ * mcols) + 16.0 * n_;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+}
+
+void Engine::solve(int mode, double bw, bool adaptive, int kernel, double out[4])
+{
+    SolveArgs a{};
+    a.n = n_;
+    a.p = p_;
+    a.mode = mode;
+    a.kernel = kernel;
+    a.G = g_.get();
+    a.ldg = m_;
+    a.G2 = g2_.get();
+    a.ldg2 = mm_;
+    a.X = x_.get();
+    a.y = y_.get();
+    a.thr = thrPtr(adaptive);
+    a.bw = bw;
+    a.beta = beta_.get();
+    a.sii = sii_.get();
+    a.resid = resid_.get();
+    a.v = vvec_.get();
+    a.bse = bse_.get();
+    a.partials = partials_.get();
+    int nb = 0;
+    check(launch_solve(a, &nb, stream_), "solve");
+    check(launch_reduce_partials(partials_.get(), nb, sums_.get(), stream_), "reduce");
+    check(cudaMemcpyAsync(host_sums_, sums_.get(), 4 * sizeof(double), cudaMemcpyDeviceToHost, stream_), "D2H sums");
+    synchronize();
+    for (int q = 0; q < 4; q++) out[q] = host_sums_[q];
+}
+
+double Engine::criterion(double bw, bool adaptive, int kernel, int crit)
+{
+    if (n_ == 0) throw std::logic_error("no data");
+    check(cudaSetDevice(device_), "cudaSetDevice");
+    computeThresholds(bw, adaptive);
+    contract(z_.get(), m_, g_.get(), m_, bw, adaptive, kernel, crit == kCV, 1);
+    double s[4];
+    solve(crit == kCV ? kSolveCV : kSolveAIC, bw, adaptive, kernel, s);
+    if (stats_on_) stats_.criterion_evals++;
+    if (s[3] > 0.0) return DBL_MAX;
+    if (crit == kCV) return std::isfinite(s[1]) ? s[1] : DBL_MAX;
+    double v = aicc((double)n_, s[1], s[0]);
+    return std::isfinite(v) ? v : DBL_MAX;
+}
+
+void Engine::fit(double bw, bool adaptive, int kernel, bool storeS, FitOutput& out)
+{
+    if (n_ == 0) throw std::logic_error("no data");
+    check(cudaSetDevice(device_), "cudaSetDevice");
+    const int n = n_, p = p_;
+    g2_.alloc((size_t)n * mm_);
+    vvec_.alloc((size_t)n * p);
+    bse_.alloc((size_t)n * p);
+    qdiag_.alloc(n);
+    computeThresholds(bw, adaptive);
+    contract(z_.get(), m_, g_.get(), m_, bw, adaptive, kernel, false, 1);
+    contract(z_.get(), mm_, g2_.get(), mm_, bw, adaptive, kernel, false, 2);
+    double s[4];
+    solve(kSolveFit, bw, adaptive, kernel, s);
+    if (s[3] > 0.0) throw NotSPDError("inv_sympd(): matrix is singular or not positive definite");
+    // S: n x n when stored (isStoreS, GWRBasic.h:708), else only the last
+    // location's row, which is what S.row(0) holds after the reference's loop
+    int last_sorted = 0;
+    for (int sidx = 0; sidx < n; sidx++)
+        if (perm_[sidx] == n - 1) last_sorted = sidx;
+    S_.alloc(storeS ? (size_t)n * n : (size_t)n);
+    check(cudaMemsetAsync(S_.get(), 0, sizeof(double) * S_.size(), stream_), "memset S");
+    check(launch_hat_pass(points(), geographic_, tiles_.get(), x_.get(), p, vvec_.get(), thrPtr(adaptive), bw, kernel,
+                          true, qdiag_.get(), storeS ? S_.get() : nullptr, storeS ? -1 : last_sorted,
+                          storeS ? nullptr : S_.get(), stream_),
+          "hat pass");
+    std::vector<double> hb((size_t)n * p), hse((size_t)n * p), hq(n), hsii(n), hres(n);
+    check(cudaMemcpyAsync(hb.data(), beta_.get(), sizeof(double) * hb.size(), cudaMemcpyDeviceToHost, stream_), "D2H");
+    check(cudaMemcpyAsync(hse.data(), bse_.get(), sizeof(double) * hse.size(), cudaMemcpyDeviceToHost, stream_), "D2H");
+    check(cudaMemcpyAsync(hq.data(), qdiag_.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, stream_), "D2H");
+    std::vector<double> hS(S_.size());
+    check(cudaMemcpyAsync(hS.data(), S_.get(), sizeof(double) * hS.size(), cudaMemcpyDeviceToHost, stream_), "D2H S");
+    synchronize();
+    out.betas.assign((size_t)n * p, 0.0);
+    out.betasSE.assign((size_t)n * p, 0.0);
+    out.qdiag.assign(n, 0.0);
+    for (int sidx = 0; sidx < n; sidx++) {
+        const int i = perm_[sidx];
+        for (int k = 0; k < p; k++) {
+            out.betas[(size_t)i + (size_t)k * n] = hb[(size_t)sidx * p + k];
+            out.betasSE[(size_t)i + (size_t)k * n] = hse[(size_t)sidx * p + k];
+        }
+        out.qdiag[i] = hq[sidx];
+    }
+    if (storeS) {
+        out.sRows = n;
+        out.S.assign((size_t)n * n, 0.0);
+        for (int a = 0; a < n; a++)
+            for (int b = 0; b < n; b++) out.S[(size_t)perm_[a] + (size_t)perm_[b] * n] = hS[(size_t)a * n + b];
+    } else {
+        out.sRows = 1;
+        out.S.assign(n, 0.0);
+        for (int b = 0; b < n; b++) out.S[perm_[b]] = hS[b];
+    }
+    out.shat[0] = s[0];
+    out.shat[1] = s[2];
+    out.rss = s[1];
+}
+
+double Engine::globalCriterion(const std::vector<int>& cols)
+{
+    if (n_ == 0) throw std::logic_error("no data");
+    const int q = (int)cols.size();
+    if (q < 1 || q > kMaxP) throw std::invalid_argument("column subset size out of range");
+    check(cudaSetDevice(device_), "cudaSetDevice");
+    if (!gall_valid_) {
+        const int nb = 256;
+        gall_.alloc(m_);
+        gall_part_.alloc((size_t)nb * m_);
+        check(launch_column_sums(n_, m_, z_.get(), gall_part_.get(), nb, gall_.get(), stream_), "column sums");
+        gall_valid_ = true;
+    }
+    ColumnSet cs{};
+    cs.count = q;
+    for (int a = 0; a < q; a++) {
+        if (cols[a] < 0 || cols[a] >= p_) throw std::invalid_argument("column index out of range");
+        cs.cols[a] = cols[a];
+    }
+    xsub_.alloc((size_t)n_ * kMaxP);
+    gsub_.alloc((size_t)kMaxP * (kMaxP + 3) / 2 + kMaxP);
+    check(launch_gather_subset(n_, p_, cs, x_.get(), gall_.get(), xsub_.get(), gsub_.get(), stream_), "gather");
+    SolveArgs a{};
+    a.n = n_;
+    a.p = q;
+    a.mode = kSolveAIC;
+    a.kernel = GW_KERNEL_GAUSSIAN;  // w_ii = exp(0) = 1
+    a.G = gsub_.get();
+    a.ldg = 0;                      // every location solves the same X^T X
+    a.X = xsub_.get();
+    a.y = y_.get();
+    a.thr = nullptr;
+    a.bw = 1.0;
+    a.beta = beta_.get();
+    a.sii = sii_.get();
+    a.resid = resid_.get();
+    a.partials = partials_.get();
+    int nb = 0;
+    check(launch_solve(a, &nb, stream_), "solve");
+    check(launch_reduce_partials(partials_.get(), nb, sums_.get(), stream_), "reduce");
+    check(cudaMemcpyAsync(host_sums_, sums_.get(), 4 * sizeof(double), cudaMemcpyDeviceToHost, stream_), "D2H sums");
+    synchronize();
+    if (host_sums_[3] > 0.0) return DBL_MAX;
+    double v = aicc((double)n_, host_sums_[1], host_sums_[0]);
+    return std::isfinite(v) ? v : DBL_MAX;
+}
+
+double Engine::maxDistance()
+{
+    check(cudaSetDevice(device_), "cudaSetDevice");
+    check(cudaMemsetAsync(key_.get(), 0, sizeof(unsigned long long), stream_), "memset");
+    check(launch_max_distance(points(), geographic_, key_.get(), num_sms_, stream_), "maxdist");
+    unsigned long long k = 0;
+    check(cudaMemcpyAsync(&k, key_.get(), sizeof(k), cudaMemcpyDeviceToHost, stream_), "D2H");
+    synchronize();
+    uint64_t b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+    double d;
+    std::memcpy(&d, &b, 8);
+    return d;
+}
+
+void Engine::thresholds(double bw, bool adaptive, std::vector<double>& out)
+{
+    check(cudaSetDevice(device_), "cudaSetDevice");
+    out.assign(n_, bw);
+    if (!adaptive) return;
+    computeThresholds(bw, adaptive);
+    std::vector<double> h(n_);
+    check(cudaMemcpyAsync(h.data(), thr_.get(), sizeof(double) * n_, cudaMemcpyDeviceToHost, stream_), "D2H");
+    synchronize();
+    for (int s = 0; s < n_; s++) out[perm_[s]] = h[s];
+}
+
+}  // namespace gwgpu

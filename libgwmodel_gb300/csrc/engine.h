@@ -1,0 +1,153 @@
+// engine.h -- the device-resident GWR engine behind the C ABI and the
+// gwm::GWRBasic facade.  One engine owns one dataset on one GPU and one
+// stream; it is not re-entrant (serialize calls per engine).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <functional>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "gw_common.cuh"
+
+namespace gwgpu {
+
+enum Precision { kFP64 = 0, kMixed = 1 };
+enum Criterion { kAIC = 0, kCV = 1 };
+
+struct CudaError : std::runtime_error {
+    explicit CudaError(const std::string& s) : std::runtime_error(s) {}
+};
+
+// A local X^T W X that is not symmetric positive definite; mirrors the
+// std::runtime_error of inv_sympd / "Cuda failed to get the inverse of matrix".
+struct NotSPDError : std::runtime_error {
+    explicit NotSPDError(const std::string& s) : std::runtime_error(s) {}
+};
+
+void check(cudaError_t e, const char* what);
+
+template <class T>
+class DevBuf {
+public:
+    DevBuf() = default;
+    ~DevBuf() { release(); }
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    void alloc(size_t count)
+    {
+        if (count == count_ && ptr_) return;
+        release();
+        if (count) check(cudaMalloc(&ptr_, count * sizeof(T)), "cudaMalloc");
+        count_ = count;
+    }
+    void release()
+    {
+        if (ptr_) cudaFree(ptr_);
+        ptr_ = nullptr;
+        count_ = 0;
+    }
+    T* get() const { return ptr_; }
+    size_t size() const { return count_; }
+
+private:
+    T* ptr_ = nullptr;
+    size_t count_ = 0;
+};
+
+// Timing of the contraction launches, filled when stats are enabled.
+struct EngineStats {
+    int contract_launches = 0;
+    double contract_ms = 0.0;      // sum of event-timed contraction launches
+    double contract_flops = 0.0;   // algorithmic 2 * m * P, P = nonzero weight pairs
+    double contract_bytes = 0.0;   // algorithmic Z + G + coordinate bytes
+    int select_launches = 0;
+    double select_ms = 0.0;
+    double solve_ms = 0.0;
+    int criterion_evals = 0;
+};
+
+struct FitOutput {
+    std::vector<double> betas;     // n x p column-major (original order)
+    std::vector<double> betasSE;   // n x p, before the sigma scaling of GWRBasic::fit
+    std::vector<double> qdiag;     // n
+    std::vector<double> S;         // sRows x n column-major
+    int sRows = 0;
+    double shat[2] = {0.0, 0.0};
+    double rss = 0.0;
+};
+
+class Engine {
+public:
+    explicit Engine(int device);
+    ~Engine();
+    Engine(const Engine&) = delete;
+    Engine& operator=(const Engine&) = delete;
+
+    // Copies X (n x p column-major), y and coords (n x 2 column-major) to the
+    // device in Morton order.
+    void setData(int n, int p, const double* x, const double* y, const double* coords, bool geographic);
+    void setPrecision(int precision) { precision_ = precision; }
+    int precision() const { return precision_; }
+
+    int n() const { return n_; }
+    int p() const { return p_; }
+
+    // bandwidthSizeCriterion{AIC,CV}: DBL_MAX when a local system is not SPD
+    // or the value is not finite (GWRBasic.cpp:440-535).  shat receives
+    // (trS, trStS-unused) for AIC.
+    double criterion(double bw, bool adaptive, int kernel, int crit);
+    // fitOmp outputs (GWRBasic.cpp:386-438); throws NotSPDError.
+    void fit(double bw, bool adaptive, int kernel, bool storeS, FitOutput& out);
+    // CRSDistance::maxDistance.
+    double maxDistance();
+    // indepVarsSelectionCriterion (GWRBasic.cpp:309-346): AICc of the model
+    // on the given columns with every weight equal to one; DBL_MAX on failure.
+    double globalCriterion(const std::vector<int>& cols);
+    // Per-row adaptive thresholds (fixbw) in original order, for tests.
+    void thresholds(double bw, bool adaptive, std::vector<double>& out);
+
+    void enableStats(bool on) { stats_on_ = on; }
+    EngineStats& stats() { return stats_; }
+    cudaStream_t stream() const { return stream_; }
+    void synchronize();
+
+private:
+    void computeThresholds(double bw, bool adaptive);
+    const double* thrPtr(bool adaptive) const { return adaptive ? thr_.get() : nullptr; }
+    void contract(const double* Z, int mcols, double* G, int ldg, double bw, bool adaptive, int kernel,
+                  bool exclude_self, int wpow);
+    void solve(int mode, double bw, bool adaptive, int kernel, double out[4]);
+    DevPoints points() const;
+
+    int device_ = 0;
+    int num_sms_ = 0;
+    cudaStream_t stream_ = nullptr;
+    int n_ = 0, p_ = 0, m_ = 0, mm_ = 0;
+    bool geographic_ = false;
+    int precision_ = kFP64;
+    double dlo_ = 0.0, dhi_ = 0.0;
+    std::vector<int> perm_;  // sorted position -> original index
+
+    DevBuf<double> u_, v_, uR_, vR_, x_, y_, z_, g_, g2_;
+    DevBuf<double> thr_, sel0_, sel1_;
+    DevBuf<double> beta_, sii_, resid_, vvec_, bse_, qdiag_, S_;
+    DevBuf<double> partials_, sums_;
+    DevBuf<double> gall_, gall_part_, gsub_, xsub_;
+    bool gall_valid_ = false;
+    DevBuf<TileBox> tiles_;
+    DevBuf<unsigned long long> key_;
+    double* host_sums_ = nullptr;  // pinned
+
+    bool thr_valid_ = false;
+    double thr_bw_ = 0.0;
+
+    bool stats_on_ = false;
+    EngineStats stats_;
+};
+
+}  // namespace gwgpu

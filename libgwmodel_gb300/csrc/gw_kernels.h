@@ -1,0 +1,87 @@
+// gw_kernels.h -- host-side launch wrappers of the GWR kernels.
+#pragma once
+
+#include <cstddef>
+#include <cuda_runtime.h>
+
+#include "gw_common.cuh"
+
+namespace gwgpu {
+
+// Solve modes of launch_solve.
+enum SolveMode { kSolveAIC = 0, kSolveCV = 1, kSolveFit = 2 };
+
+// Per-row k-th smallest distance (1-based rank).  [dlo, dhi] is the expected
+// range of positive distances; it only shapes the first histogram.
+cudaError_t launch_select(const DevPoints& P, bool geographic, unsigned rank, double dlo, double dhi,
+                          double* out, int num_sms, cudaStream_t stream);
+size_t select_smem_bytes();
+
+// thr = fixbw of BandwidthWeight.cpp:40-53 from order statistics d0 (rank
+// floor(bw), or the row maximum when bw >= n) and d1 (rank floor(bw)+1, may
+// be null when bw is integral).
+cudaError_t launch_threshold_combine(int n, double bw, const double* d0, const double* d1, double* thr,
+                                     cudaStream_t stream);
+
+// Z[j, :] = (upper triangle of x_j x_j^T packed by rows, x_j * y_j); X row-major n x p.
+cudaError_t launch_build_z(int n, int p, const double* X, const double* y, double* Z, cudaStream_t stream);
+
+// G[i, c] = sum_j w_ij^wpow Z[j, c] for c < mcols, with w_ij = K(d_ij, r_i)
+// (r_i = thr[i], or bw when thr is null); exclude_self zeroes w_ii (CV).
+// FP64 SIMT, the weight matrix is produced tile by tile and never stored.
+cudaError_t launch_contract64(const DevPoints& P, bool geographic, const TileBox* tiles, const double* Z, int ldz,
+                              int mcols, double* G, int ldg, const double* thr, double bw, int kernel,
+                              bool exclude_self, int wpow, bool skip_tiles, cudaStream_t stream);
+
+// Warp-per-location Cholesky solve of A_i beta_i = b_i and the per-location
+// criterion terms; partial sums per block in partials[block*4 + {0..3}] =
+// (sum s_ii, sum residual^2, sum ||s_i||^2, failures).  Returns the number
+// of partial blocks through nblocks.
+struct SolveArgs {
+    int n, p, mode, kernel;
+    const double* G;   // n x m (A packed upper, then b)
+    int ldg;
+    const double* G2;  // n x p(p+1)/2 (X^T W^2 X packed upper), fit only
+    int ldg2;
+    const double* X;   // n x p row-major
+    const double* y;
+    const double* thr; // per-row threshold or null
+    double bw;
+    double* beta;      // n x p row-major
+    double* sii;       // n
+    double* resid;     // n
+    double* v;         // n x p: A_i^{-1} x_i (fit)
+    double* bse;       // n x p: diag(A^-1 Q A^-1) (fit)
+    double* partials;
+};
+cudaError_t launch_solve(const SolveArgs& a, int* nblocks, cudaStream_t stream);
+
+// Sums nblocks x 4 partials into out[4] in a fixed order.
+cudaError_t launch_reduce_partials(const double* partials, int nblocks, double* out, cudaStream_t stream);
+
+// qdiag[j] = sum_i (delta_ij - s_ij)^2 with s_ij = w_ij v_i . x_j, w_ij =
+// K(d_ij, r_i); also writes S (n x n row-major, sorted order) when S != null
+// and row row_target of S into s_row (length n) when s_row != null.
+cudaError_t launch_hat_pass(const DevPoints& P, bool geographic, const TileBox* tiles, const double* X, int p,
+                            const double* v, const double* thr, double bw, int kernel, bool skip_tiles,
+                            double* qdiag, double* S, int row_target, double* s_row, cudaStream_t stream);
+
+// Column subset of X for the w == 1 criterion of variable selection.
+struct ColumnSet {
+    int count;
+    int cols[kMaxP];
+};
+
+// out[c] = sum_j Z[j, c] (n x m row-major) with nb fixed partial blocks (part: nb x m).
+cudaError_t launch_column_sums(int n, int m, const double* Z, double* part, int nb, double* out, cudaStream_t stream);
+
+// Xs = X[:, cols] (n x q row-major) and gsub = the packed X^T X / X^T y of the
+// subset taken from the full column sums gall.
+cudaError_t launch_gather_subset(int n, int p, const ColumnSet& cs, const double* X, const double* gall, double* Xs,
+                                 double* gsub, cudaStream_t stream);
+
+// Maximum pairwise distance (CRSDistance::maxDistance), as an ordered key in *key_out.
+cudaError_t launch_max_distance(const DevPoints& P, bool geographic, unsigned long long* key_out, int num_sms,
+                                cudaStream_t stream);
+
+}  // namespace gwgpu

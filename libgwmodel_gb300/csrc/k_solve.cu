@@ -1,0 +1,423 @@
+// k_solve.cu -- per-location solves and the passes around the contraction.
+//
+//  * k_build_z      Z[j, :] = packed x_j x_j^T, x_j y_j (the contraction's B operand)
+//  * k_solve        one warp per location: Cholesky of A_i = X^T W_i X (in
+//                   place of inv_sympd, GWRBasic.cpp:507), beta_i, s_ii = w_ii
+//                   x_i^T A_i^-1 x_i, the residual, and for the final fit
+//                   v_i = A_i^-1 x_i, diag(A^-1 Q A^-1) (betasSE) and
+//                   ||s_i||^2 = v_i^T Q_i v_i with Q_i = X^T W_i^2 X
+//                   (GWRBasic.cpp:409-415); block partial sums of the criterion
+//  * k_reduce       fixed-order sum of the block partials
+//  * k_hat          qDiag_j = sum_i (delta_ij - s_ij)^2 and the rows of S
+//                   (GWRBasic.cpp:416-419) without materialising C_i
+//  * k_maxdist      CRSDistance::maxDistance (CRSDistance.cpp:133-143)
+#include "gw_common.cuh"
+#include "gw_kernels.h"
+
+namespace gwgpu {
+
+namespace {
+
+constexpr int SV_WARPS = 4;
+constexpr unsigned FULL = 0xffffffffu;
+
+__device__ __forceinline__ int packed_index(int a, int b, int p)
+{
+    // a <= b, upper triangle packed by rows
+    return a * p - (a * (a - 1)) / 2 + (b - a);
+}
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(FULL, v, off);
+    return v;
+}
+
+__global__ void k_build_z(int n, int p, const double* __restrict__ X, const double* __restrict__ y,
+                          double* __restrict__ Z)
+{
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int mm = p * (p + 1) / 2, m = mm + p;
+    const double* x = X + (size_t)j * p;
+    double* z = Z + (size_t)j * m;
+    int e = 0;
+    for (int a = 0; a < p; a++)
+        for (int b = a; b < p; b++) z[e++] = x[a] * x[b];
+    for (int a = 0; a < p; a++) z[mm + a] = x[a] * y[j];
+}
+
+// Forward substitution L z = rhs (lane r holds rhs_r; returns z_r).
+__device__ __forceinline__ double fwd_solve(const double* L, int ld, int p, int lane, double rhs)
+{
+    double v = rhs;
+    for (int j = 0; j < p; j++) {
+        double zj = __shfl_sync(FULL, v, j) / L[j * ld + j];
+        if (lane == j) v = zj;
+        else if (lane > j && lane < p) v -= L[lane * ld + j] * zj;
+    }
+    return v;
+}
+
+// Backward substitution L^T x = rhs.
+__device__ __forceinline__ double bwd_solve(const double* L, int ld, int p, int lane, double rhs)
+{
+    double v = rhs;
+    for (int j = p - 1; j >= 0; j--) {
+        double xj = __shfl_sync(FULL, v, j) / L[j * ld + j];
+        if (lane == j) v = xj;
+        else if (lane < j) v -= L[j * ld + lane] * xj;
+    }
+    return v;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(SV_WARPS * 32) k_solve(SolveArgs a)
+{
+    extern __shared__ double smem[];
+    const int p = a.p, ld = p + 1, mm = p * (p + 1) / 2;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int per_warp = (MODE == kSolveFit) ? 3 * p * ld + p : p * ld + p;
+    double* L = smem + warp * per_warp;
+    double* Ainv = L + p * ld;
+    double* Q = Ainv + p * ld;
+    double* vsh = (MODE == kSolveFit) ? Q + p * ld : L + p * ld;
+    __shared__ double part[SV_WARPS][4];
+
+    double acc_s = 0.0, acc_r = 0.0, acc_t = 0.0, acc_f = 0.0;
+    for (int row = blockIdx.x * SV_WARPS + warp; row < a.n; row += gridDim.x * SV_WARPS) {
+        const double* g = a.G + (size_t)row * a.ldg;
+        if (lane < p)
+            for (int c = 0; c <= lane; c++) L[lane * ld + c] = g[packed_index(c, lane, p)];
+        const double bvec = lane < p ? g[mm + lane] : 0.0;
+        const double xr = lane < p ? a.X[(size_t)row * p + lane] : 0.0;
+        __syncwarp();
+        // Cholesky-Crout, lane r owns row r
+        bool fail = false;
+        for (int j = 0; j < p; j++) {
+            double t = 0.0;
+            if (lane >= j && lane < p) {
+                t = L[lane * ld + j];
+                for (int k = 0; k < j; k++) t -= L[lane * ld + k] * L[j * ld + k];
+            }
+            double tjj = __shfl_sync(FULL, t, j);
+            if (!(tjj > 0.0)) { fail = true; break; }
+            double ljj = sqrt(tjj);
+            __syncwarp();
+            if (lane == j) L[j * ld + j] = ljj;
+            else if (lane > j && lane < p) L[lane * ld + j] = t / ljj;
+            __syncwarp();
+        }
+        if (fail) {
+            if (lane < p) a.beta[(size_t)row * p + lane] = __longlong_as_double(0x7ff8000000000000ll);
+            if (lane == 0) {
+                acc_f += 1.0;
+                a.resid[row] = __longlong_as_double(0x7ff8000000000000ll);
+                a.sii[row] = 0.0;
+            }
+            __syncwarp();
+            continue;
+        }
+        const double z = fwd_solve(L, ld, p, lane, bvec);
+        const double beta = bwd_solve(L, ld, p, lane, z);
+        if (lane < p) a.beta[(size_t)row * p + lane] = beta;
+        const double yhat = warp_sum(lane < p ? xr * beta : 0.0);
+        const double res = a.y[row] - yhat;
+        double sii = 0.0;
+        if (MODE != kSolveCV) {
+            const double u = fwd_solve(L, ld, p, lane, xr);
+            const double uu = warp_sum(lane < p ? u * u : 0.0);
+            const double rr = a.thr ? a.thr[row] : a.bw;
+            sii = gw_kernel_weight(a.kernel, 0.0, rr) * uu;
+            if (MODE == kSolveFit) {
+                const double v = bwd_solve(L, ld, p, lane, u);
+                if (lane < p) {
+                    a.v[(size_t)row * p + lane] = v;
+                    vsh[lane] = v;
+                }
+                // explicit inverse, column by column
+                for (int k = 0; k < p; k++) {
+                    double e = fwd_solve(L, ld, p, lane, lane == k ? 1.0 : 0.0);
+                    e = bwd_solve(L, ld, p, lane, e);
+                    if (lane < p) Ainv[lane * ld + k] = e;
+                }
+                const double* g2 = a.G2 + (size_t)row * a.ldg2;
+                if (lane < p)
+                    for (int c = 0; c < p; c++)
+                        Q[lane * ld + c] = g2[lane <= c ? packed_index(lane, c, p) : packed_index(c, lane, p)];
+                __syncwarp();
+                double se = 0.0, qv = 0.0;
+                if (lane < p) {
+                    for (int b = 0; b < p; b++) {
+                        double tb = 0.0;
+                        for (int q = 0; q < p; q++) tb += Ainv[lane * ld + q] * Q[q * ld + b];
+                        se += tb * Ainv[b * ld + lane];
+                        qv += Q[lane * ld + b] * vsh[b];
+                    }
+                    a.bse[(size_t)row * p + lane] = se;
+                }
+                const double sts = warp_sum(lane < p ? vsh[lane] * qv : 0.0);
+                if (lane == 0) acc_t += sts;
+            }
+        }
+        if (lane == 0) {
+            a.sii[row] = sii;
+            a.resid[row] = res;
+            acc_s += sii;
+            acc_r += res * res;
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        part[warp][0] = acc_s;
+        part[warp][1] = acc_r;
+        part[warp][2] = acc_t;
+        part[warp][3] = acc_f;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double s = 0.0;
+        for (int w = 0; w < SV_WARPS; w++) s += part[w][threadIdx.x];
+        a.partials[blockIdx.x * 4 + threadIdx.x] = s;
+    }
+}
+
+__global__ void k_reduce(const double* __restrict__ partials, int nblocks, double* __restrict__ out)
+{
+    __shared__ double sh[256][4];
+    double s[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int b = threadIdx.x; b < nblocks; b += 256)
+        for (int q = 0; q < 4; q++) s[q] += partials[b * 4 + q];
+    for (int q = 0; q < 4; q++) sh[threadIdx.x][q] = s[q];
+    __syncthreads();
+    for (int stride = 128; stride > 0; stride >>= 1) {
+        if (threadIdx.x < stride)
+            for (int q = 0; q < 4; q++) sh[threadIdx.x][q] += sh[threadIdx.x + stride][q];
+        __syncthreads();
+    }
+    if (threadIdx.x < 4) out[threadIdx.x] = sh[0][threadIdx.x];
+}
+
+constexpr int HAT_THREADS = 128;
+constexpr int HAT_TILE = kTile;
+
+template <bool GEO>
+__global__ void __launch_bounds__(HAT_THREADS)
+    k_hat(DevPoints P, const TileBox* __restrict__ tiles, const double* __restrict__ X, int p,
+          const double* __restrict__ v, const double* __restrict__ thr, double bw, int kernel, int skip,
+          double* __restrict__ qdiag, double* __restrict__ S, int row_target, double* __restrict__ s_row)
+{
+    extern __shared__ double hsm[];
+    double* sX = hsm;                          // HAT_THREADS x p (x_j of this block)
+    double* sV = sX + HAT_THREADS * p;         // HAT_TILE x p   (v_i of the staged rows)
+    __shared__ double su[HAT_TILE], sv[HAT_TILE], suR[HAT_TILE], svR[HAT_TILE], sr[HAT_TILE];
+    __shared__ TileBox sblock;
+    const int n = P.n, t = threadIdx.x;
+    const int j0 = blockIdx.x * HAT_THREADS, j = j0 + t;
+    for (int e = t; e < HAT_THREADS * p; e += HAT_THREADS) {
+        int jj = j0 + e / p;
+        sX[e] = jj < n ? X[(size_t)j0 * p + e] : 0.0;
+    }
+    if (t == 0) {
+        TileBox b = tiles[j0 / HAT_TILE];
+        int last = min(j0 + HAT_THREADS, n) - 1;
+        for (int q = j0 / HAT_TILE + 1; q <= last / HAT_TILE; q++) {
+            TileBox c = tiles[q];
+            b.ulo = fmin(b.ulo, c.ulo); b.uhi = fmax(b.uhi, c.uhi);
+            b.vlo = fmin(b.vlo, c.vlo); b.vhi = fmax(b.vhi, c.vhi);
+        }
+        sblock = b;
+    }
+    __syncthreads();
+    double du = 0.0, dv = 0.0, duR = 0.0, dvR = 0.0;
+    if (j < n) {
+        du = P.u[j]; dv = P.v[j];
+        if (GEO) { duR = P.uR[j]; dvR = P.vR[j]; }
+    }
+    const bool can_skip = skip && !GEO && kernel >= GW_KERNEL_BISQUARE;
+    double acc = 0.0;
+    const int ntiles = (n + HAT_TILE - 1) / HAT_TILE;
+    for (int tile = 0; tile < ntiles; tile++) {
+        const int i0 = tile * HAT_TILE;
+        if (can_skip) {
+            double rmax = -1.0;
+            for (int q = 0; q < HAT_TILE && i0 + q < n; q++) rmax = fmax(rmax, thr ? thr[i0 + q] : bw);
+            if (rmax > 0.0 && box_lower_bound(sblock, tiles[tile]) * (1.0 - 1e-14) >= rmax) continue;
+        }
+        if (t < HAT_TILE) {
+            int i = i0 + t;
+            bool ok = i < n;
+            su[t] = ok ? P.u[i] : 0.0;
+            sv[t] = ok ? P.v[i] : 0.0;
+            suR[t] = (GEO && ok) ? P.uR[i] : 0.0;
+            svR[t] = (GEO && ok) ? P.vR[i] : 0.0;
+            sr[t] = ok ? (thr ? thr[i] : bw) : 0.0;
+        }
+        for (int e = t; e < HAT_TILE * p; e += HAT_THREADS) {
+            int i = i0 + e / p;
+            sV[e] = i < n ? v[(size_t)i0 * p + e] : 0.0;
+        }
+        __syncthreads();
+        if (j < n) {
+            const int iend = min(HAT_TILE, n - i0);
+            for (int q = 0; q < iend; q++) {
+                double d;
+                if constexpr (GEO)
+                    d = gw_gc_dist(du, su[q], dv, sv[q], duR, suR[q], dvR, svR[q]);
+                else
+                    d = gw_planar_dist(du, dv, su[q], sv[q]);
+                double w = gw_kernel_weight(kernel, d, sr[q]);
+                double dot = 0.0;
+                for (int r = 0; r < p; r++) dot += sV[q * p + r] * sX[t * p + r];
+                double s = w * dot;
+                double e = (i0 + q == j) ? 1.0 - s : -s;
+                acc += e * e;
+                if (S) S[(size_t)(i0 + q) * n + j] = s;
+                if (i0 + q == row_target) s_row[j] = s;
+            }
+        }
+        __syncthreads();
+    }
+    if (j < n) qdiag[j] = acc;
+}
+
+template <bool GEO>
+__global__ void k_maxdist(DevPoints P, unsigned long long* __restrict__ key)
+{
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (blockDim.x / 32);
+    double best = 0.0;
+    for (int i = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); i < P.n; i += warps) {
+        const double fu = P.u[i], fv = P.v[i];
+        const double fuR = GEO ? P.uR[i] : 0.0, fvR = GEO ? P.vR[i] : 0.0;
+        for (int j = lane; j < P.n; j += 32) {
+            double d = pair_dist<GEO>(P, j, fu, fv, fuR, fvR);
+            best = fmax(best, d);
+        }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) best = fmax(best, __shfl_xor_sync(FULL, best, off));
+    if (lane == 0) atomicMax(key, (unsigned long long)dkey(best));
+}
+
+__global__ void k_colsum_partial(int n, int m, const double* __restrict__ Z, double* __restrict__ part)
+{
+    const int chunk = (n + gridDim.x - 1) / gridDim.x;
+    const int r0 = blockIdx.x * chunk, r1 = min(n, r0 + chunk);
+    for (int c = threadIdx.x; c < m; c += blockDim.x) {
+        double s = 0.0;
+        for (int r = r0; r < r1; r++) s += Z[(size_t)r * m + c];
+        part[(size_t)blockIdx.x * m + c] = s;
+    }
+}
+
+__global__ void k_colsum_final(int nb, int m, const double* __restrict__ part, double* __restrict__ out)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m) return;
+    double s = 0.0;
+    for (int b = 0; b < nb; b++) s += part[(size_t)b * m + c];
+    out[c] = s;
+}
+
+__global__ void k_gather_subset(int n, int p, ColumnSet cs, const double* __restrict__ X,
+                                const double* __restrict__ gall, double* __restrict__ Xs, double* __restrict__ gsub)
+{
+    const int q = cs.count;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        for (int a = 0; a < q; a++) Xs[(size_t)i * q + a] = X[(size_t)i * p + cs.cols[a]];
+    if (i == 0) {
+        const int mm = p * (p + 1) / 2, mmq = q * (q + 1) / 2;
+        int e = 0;
+        for (int a = 0; a < q; a++)
+            for (int b = a; b < q; b++) {
+                int ca = min(cs.cols[a], cs.cols[b]), cb = max(cs.cols[a], cs.cols[b]);
+                gsub[e++] = gall[packed_index(ca, cb, p)];
+            }
+        for (int a = 0; a < q; a++) gsub[mmq + a] = gall[mm + cs.cols[a]];
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_column_sums(int n, int m, const double* Z, double* part, int nb, double* out, cudaStream_t stream)
+{
+    k_colsum_partial<<<nb, 128, 0, stream>>>(n, m, Z, part);
+    k_colsum_final<<<(m + 127) / 128, 128, 0, stream>>>(nb, m, part, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_subset(int n, int p, const ColumnSet& cs, const double* X, const double* gall, double* Xs,
+                                 double* gsub, cudaStream_t stream)
+{
+    k_gather_subset<<<(n + 127) / 128, 128, 0, stream>>>(n, p, cs, X, gall, Xs, gsub);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build_z(int n, int p, const double* X, const double* y, double* Z, cudaStream_t stream)
+{
+    k_build_z<<<(n + 127) / 128, 128, 0, stream>>>(n, p, X, y, Z);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_solve(const SolveArgs& a, int* nblocks, cudaStream_t stream)
+{
+    if (a.p < 1 || a.p > kMaxP) return cudaErrorInvalidValue;
+    int grid = (a.n + SV_WARPS - 1) / SV_WARPS;
+    if (grid > 4096) grid = 4096;
+    const int ld = a.p + 1;
+    size_t per_warp = (a.mode == kSolveFit) ? 3 * a.p * ld + a.p : a.p * ld + a.p;
+    size_t smem = per_warp * SV_WARPS * sizeof(double);
+    *nblocks = grid;
+    switch (a.mode) {
+    case kSolveAIC:
+        cudaFuncSetAttribute(k_solve<kSolveAIC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_solve<kSolveAIC><<<grid, SV_WARPS * 32, smem, stream>>>(a);
+        break;
+    case kSolveCV:
+        cudaFuncSetAttribute(k_solve<kSolveCV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_solve<kSolveCV><<<grid, SV_WARPS * 32, smem, stream>>>(a);
+        break;
+    default:
+        cudaFuncSetAttribute(k_solve<kSolveFit>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_solve<kSolveFit><<<grid, SV_WARPS * 32, smem, stream>>>(a);
+        break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_partials(const double* partials, int nblocks, double* out, cudaStream_t stream)
+{
+    k_reduce<<<1, 256, 0, stream>>>(partials, nblocks, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_hat_pass(const DevPoints& P, bool geographic, const TileBox* tiles, const double* X, int p,
+                            const double* v, const double* thr, double bw, int kernel, bool skip_tiles,
+                            double* qdiag, double* S, int row_target, double* s_row, cudaStream_t stream)
+{
+    int grid = (P.n + HAT_THREADS - 1) / HAT_THREADS;
+    size_t smem = (size_t)(HAT_THREADS + HAT_TILE) * p * sizeof(double);
+    if (geographic)
+        k_hat<true><<<grid, HAT_THREADS, smem, stream>>>(P, tiles, X, p, v, thr, bw, kernel, skip_tiles ? 1 : 0,
+                                                         qdiag, S, row_target, s_row);
+    else
+        k_hat<false><<<grid, HAT_THREADS, smem, stream>>>(P, tiles, X, p, v, thr, bw, kernel, skip_tiles ? 1 : 0,
+                                                          qdiag, S, row_target, s_row);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_max_distance(const DevPoints& P, bool geographic, unsigned long long* key_out, int num_sms,
+                                cudaStream_t stream)
+{
+    int grid = num_sms * 8;
+    if (geographic)
+        k_maxdist<true><<<grid, 256, 0, stream>>>(P, key_out);
+    else
+        k_maxdist<false><<<grid, 256, 0, stream>>>(P, key_out);
+    return cudaGetLastError();
+}
+
+}  // namespace gwgpu
