@@ -157,6 +157,10 @@ int gwgpu_engine_thresholds(gwgpu_engine* e, double bandwidth, int adaptive, dou
 int gwgpu_engine_enable_stats(gwgpu_engine* e, int on);
 int gwgpu_engine_get_stats(gwgpu_engine* e, gwgpu_stats* out);
 int gwgpu_engine_reset_stats(gwgpu_engine* e);
+/* Tensor-core self-test: D[128 x N] = A[128 x 32] B[N x 32]^T through the same
+ * tcgen05 descriptors, swizzled layouts and TMEM reads as the mixed-precision
+ * contraction (TF32 inputs, FP32 output; N a multiple of 16 up to 256). */
+int gwgpu_engine_tc_selftest(gwgpu_engine* e, int N, const float* A, const float* B, float* D);
 
 #ifdef __cplusplus
 }

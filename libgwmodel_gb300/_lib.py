@@ -94,6 +94,8 @@ SIGNATURES = [
     ("gwgpu_engine_enable_stats", _i, [_vp, _i]),
     ("gwgpu_engine_get_stats", _i, [_vp, ctypes.POINTER(Stats)]),
     ("gwgpu_engine_reset_stats", _i, [_vp]),
+    ("gwgpu_engine_tc_selftest", _i, [_vp, _i, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                      ctypes.POINTER(ctypes.c_float)]),
 ]
 
 # The drop-in factories of include/IGWRBasicGpuTask.h.

@@ -477,4 +477,12 @@ int gwgpu_engine_reset_stats(gwgpu_engine* e)
     return GWGPU_OK;
 }
 
+int gwgpu_engine_tc_selftest(gwgpu_engine* e, int N, const float* A, const float* B, float* D)
+{
+    ENG_CHECK(e);
+    if (!A || !B || !D) return fail(GWGPU_ERR_INVALID, "null pointer");
+    if (N < 16 || N > 256 || N % 16) return fail(GWGPU_ERR_INVALID, "N must be a multiple of 16 in [16, 256]");
+    return guarded([&] { e->eng.tcSelftest(N, A, B, D); });
+}
+
 }  // extern "C"

@@ -79,6 +79,7 @@ void Engine::setData(int n, int p, const double* x, const double* y, const doubl
     geographic_ = geographic;
     thr_valid_ = false;
     gall_valid_ = false;
+    mixed_ready_ = false;
 
     // Morton order of the coordinates
     double umin = coords[0], umax = coords[0], vmin = coords[n], vmax = coords[n];
@@ -175,6 +176,211 @@ void Engine::setData(int n, int p, const double* x, const double* y, const doubl
           "H2D tiles");
     check(launch_build_z(n, p, x_.get(), y_.get(), z_.get(), stream_), "build_z");
     synchronize();
+    hx_ = std::move(hx);
+    hy_ = std::move(hy);
+    hu_ = std::move(hu);
+    hv_ = std::move(hv);
+}
+
+// Mixed-precision operands: X and y centred (when a constant column is the
+// intercept) and scaled, Z~ split into TF32 hi/lo swizzled tile images, FP32
+// hi/lo coordinates, 32-point tile boxes.
+void Engine::ensureMixed()
+{
+    if (mixed_ready_) return;
+    const int n = n_, p = p_;
+    if (m_ > 256) throw std::invalid_argument("mixed precision supports at most 21 columns of X");
+    intercept_col_ = -1;
+    for (int k = 0; k < p && intercept_col_ < 0; k++) {
+        const double c0 = hx_[k];
+        bool constant = c0 != 0.0;
+        for (int s = 1; s < n && constant; s++) constant = hx_[(size_t)s * p + k] == c0;
+        if (constant) intercept_col_ = k;
+    }
+    mu_.assign(p, 0.0);
+    sc_.assign(p, 1.0);
+    for (int k = 0; k < p; k++) {
+        if (k == intercept_col_) {
+            sc_[k] = hx_[k];
+            continue;
+        }
+        double mean = 0.0;
+        if (intercept_col_ >= 0) {
+            for (int s = 0; s < n; s++) mean += hx_[(size_t)s * p + k];
+            mean /= n;
+        }
+        double ss = 0.0;
+        for (int s = 0; s < n; s++) {
+            double d = hx_[(size_t)s * p + k] - mean;
+            ss += d * d;
+        }
+        double sd = std::sqrt(ss / n);
+        mu_[k] = mean;
+        sc_[k] = (sd > 0.0 && std::isfinite(sd)) ? sd : 1.0;
+    }
+    mu_y_ = 0.0;
+    if (intercept_col_ >= 0) {
+        for (int s = 0; s < n; s++) mu_y_ += hy_[s];
+        mu_y_ /= n;
+    }
+    double ssy = 0.0;
+    for (int s = 0; s < n; s++) ssy += (hy_[s] - mu_y_) * (hy_[s] - mu_y_);
+    s_y_ = std::sqrt(ssy / n);
+    if (!(s_y_ > 0.0) || !std::isfinite(s_y_)) s_y_ = 1.0;
+
+    std::vector<double> xs((size_t)n * p), ys(n);
+    for (int s = 0; s < n; s++) {
+        for (int k = 0; k < p; k++) xs[(size_t)s * p + k] = (hx_[(size_t)s * p + k] - mu_[k]) / sc_[k];
+        ys[s] = (hy_[s] - mu_y_) / s_y_;
+    }
+    std::vector<double> tinv(p), tvec(p, 0.0);
+    for (int k = 0; k < p; k++) tinv[k] = 1.0 / sc_[k];
+    if (intercept_col_ >= 0) {
+        const double c = sc_[intercept_col_];
+        for (int k = 0; k < p; k++) tvec[k] = (k == intercept_col_) ? 1.0 / c : -mu_[k] / (c * sc_[k]);
+    }
+
+    npad_ = (m_ + 31) / 32 * 32;
+    ntiles32_ = (n + 31) / 32;
+    xs_.alloc((size_t)n * p);
+    ys_.alloc(n);
+    zs_.alloc((size_t)n * m_);
+    zimg_.alloc((size_t)ntiles32_ * 2 * npad_ * 128);
+    acc_.alloc((size_t)n * npad_);
+    thr32_.alloc(n);
+    err_.alloc(1);
+    tinv_.alloc(p);
+    tvec_.alloc(p);
+    boxes32_.alloc(ntiles32_);
+
+    std::vector<TileBox> bx(ntiles32_);
+    for (int t = 0; t < ntiles32_; t++) {
+        TileBox b{hu_[t * 32], hu_[t * 32], hv_[t * 32], hv_[t * 32]};
+        for (int s = t * 32; s < std::min(n, (t + 1) * 32); s++) {
+            b.ulo = std::min(b.ulo, hu_[s]);
+            b.uhi = std::max(b.uhi, hu_[s]);
+            b.vlo = std::min(b.vlo, hv_[s]);
+            b.vhi = std::max(b.vhi, hv_[s]);
+        }
+        bx[t] = b;
+    }
+    std::vector<float4> pts;
+    auto split = [](double v, float& hi, float& lo) {
+        hi = (float)v;
+        lo = (float)(v - (double)hi);
+    };
+    if (!geographic_) {
+        double uc = 0.0, vc = 0.0;
+        for (int s = 0; s < n; s++) {
+            uc += hu_[s];
+            vc += hv_[s];
+        }
+        uc /= n;
+        vc /= n;
+        pts.resize(n);
+        for (int s = 0; s < n; s++) {
+            float a, b, c, d;
+            split(hu_[s] - uc, a, b);
+            split(hv_[s] - vc, c, d);
+            pts[s] = make_float4(a, b, c, d);
+        }
+    } else {
+        pts.resize((size_t)3 * n);
+        const double DE2RA = M_PI / 180;
+        for (int s = 0; s < n; s++) {
+            const double lat = hv_[s] * DE2RA, lon = hu_[s] * DE2RA;
+            const double px = std::cos(lat) * std::cos(lon), py = std::cos(lat) * std::sin(lon), pz = std::sin(lat);
+            float xh, xl, yh, yl, zh, zl, lh, ll;
+            split(px, xh, xl);
+            split(py, yh, yl);
+            split(pz, zh, zl);
+            split(hv_[s], lh, ll);
+            pts[3 * (size_t)s] = make_float4(xh, yh, zh, lh);
+            pts[3 * (size_t)s + 1] = make_float4(xl, yl, zl, ll);
+            pts[3 * (size_t)s + 2] = make_float4((float)std::sin(lat / 2), (float)std::cos(lat / 2), 0.f, 0.f);
+        }
+    }
+    pts32_.alloc(pts.size());
+    check(cudaMemcpyAsync(pts32_.get(), pts.data(), sizeof(float4) * pts.size(), cudaMemcpyHostToDevice, stream_),
+          "H2D pts32");
+    check(cudaMemcpyAsync(boxes32_.get(), bx.data(), sizeof(TileBox) * bx.size(), cudaMemcpyHostToDevice, stream_),
+          "H2D boxes");
+    check(cudaMemcpyAsync(xs_.get(), xs.data(), sizeof(double) * xs.size(), cudaMemcpyHostToDevice, stream_),
+          "H2D xs");
+    check(cudaMemcpyAsync(ys_.get(), ys.data(), sizeof(double) * n, cudaMemcpyHostToDevice, stream_), "H2D ys");
+    check(cudaMemcpyAsync(tinv_.get(), tinv.data(), sizeof(double) * p, cudaMemcpyHostToDevice, stream_), "H2D");
+    check(cudaMemcpyAsync(tvec_.get(), tvec.data(), sizeof(double) * p, cudaMemcpyHostToDevice, stream_), "H2D");
+    check(cudaMemsetAsync(err_.get(), 0, sizeof(int), stream_), "memset err");
+    check(launch_build_z(n, p, xs_.get(), ys_.get(), zs_.get(), stream_), "build_z");
+    check(launch_build_zimg(n, m_, npad_, zs_.get(), m_, zimg_.get(), stream_), "build_zimg");
+    synchronize();
+    mixed_ready_ = true;
+}
+
+void Engine::contractMixed(double* G, int ldg, int mcols, double bw, bool adaptive, int kernel, bool exclude_self,
+                           int wpow)
+{
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (adaptive) check(launch_to_float(n_, thr_.get(), thr32_.get(), stream_), "thr32");
+    if (stats_on_) {
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, stream_);
+    }
+    TcArgs a{};
+    a.n = n_;
+    a.mcols = mcols;
+    a.npad = npad_;
+    a.ntiles = ntiles32_;
+    a.pts = pts32_.get();
+    a.boxes = boxes32_.get();
+    a.zimg = zimg_.get();
+    a.thr = adaptive ? thr32_.get() : nullptr;
+    a.bw = (float)bw;
+    a.kernel = kernel;
+    a.exclude_self = exclude_self ? 1 : 0;
+    a.skip = 1;
+    a.flush_tiles = 32;
+    a.wpow = wpow;
+    a.acc = acc_.get();
+    a.G = G;
+    a.ldg = ldg;
+    a.err = err_.get();
+    check(launch_contract_tc(a, geographic_, stream_), "contract_tc");
+    if (stats_on_) {
+        cudaEventRecord(e1, stream_);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        stats_.contract_ms += ms;
+        stats_.contract_launches += 1;
+        double pairs = (double)n_ * n_;
+        if (adaptive && kernel >= GW_KERNEL_BISQUARE) pairs = (double)n_ * std::max(0.0, std::min(bw, (double)n_) - 1);
+        stats_.contract_flops += 2.0 * mcols * pairs;
+        stats_.contract_bytes += 2.0 * npad_ * 128.0 * ntiles32_ * 2 + 8.0 * n_ * mcols + 16.0 * n_;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+}
+
+void Engine::tcSelftest(int N, const float* A, const float* B, float* D)
+{
+    check(cudaSetDevice(device_), "cudaSetDevice");
+    DevBuf<float> dA, dB, dD;
+    DevBuf<int> derr;
+    dA.alloc(128 * 32);
+    dB.alloc((size_t)N * 32);
+    dD.alloc((size_t)128 * N);
+    derr.alloc(1);
+    check(cudaMemcpyAsync(dA.get(), A, sizeof(float) * 128 * 32, cudaMemcpyHostToDevice, stream_), "H2D");
+    check(cudaMemcpyAsync(dB.get(), B, sizeof(float) * N * 32, cudaMemcpyHostToDevice, stream_), "H2D");
+    check(cudaMemsetAsync(derr.get(), 0, sizeof(int), stream_), "memset");
+    check(launch_tc_selftest(dA.get(), dB.get(), dD.get(), N, derr.get(), stream_), "tc selftest");
+    int err = 0;
+    check(cudaMemcpyAsync(D, dD.get(), sizeof(float) * 128 * N, cudaMemcpyDeviceToHost, stream_), "D2H");
+    check(cudaMemcpyAsync(&err, derr.get(), sizeof(int), cudaMemcpyDeviceToHost, stream_), "D2H");
+    synchronize();
+    if (err) throw CudaError("tensor-core self-test: a bounded wait timed out");
 }
 
 void Engine::computeThresholds(double bw, bool adaptive)
@@ -262,8 +468,9 @@ void Engine::solve(int mode, double bw, bool adaptive, int kernel, double out[4]
     a.ldg = m_;
     a.G2 = g2_.get();
     a.ldg2 = mm_;
-    a.X = x_.get();
-    a.y = y_.get();
+    const bool mixed = precision_ == kMixed;
+    a.X = mixed ? xs_.get() : x_.get();
+    a.y = mixed ? ys_.get() : y_.get();
     a.thr = thrPtr(adaptive);
     a.bw = bw;
     a.beta = beta_.get();
@@ -272,20 +479,34 @@ void Engine::solve(int mode, double bw, bool adaptive, int kernel, double out[4]
     a.v = vvec_.get();
     a.bse = bse_.get();
     a.partials = partials_.get();
+    a.tinv = mixed ? tinv_.get() : nullptr;
+    a.tvec = (mixed && intercept_col_ >= 0) ? tvec_.get() : nullptr;
+    a.tcol = mixed ? intercept_col_ : -1;
     int nb = 0;
     check(launch_solve(a, &nb, stream_), "solve");
     check(launch_reduce_partials(partials_.get(), nb, sums_.get(), stream_), "reduce");
     check(cudaMemcpyAsync(host_sums_, sums_.get(), 4 * sizeof(double), cudaMemcpyDeviceToHost, stream_), "D2H sums");
+    if (mixed) check(cudaMemcpyAsync(host_sums_ + 4, err_.get(), sizeof(int), cudaMemcpyDeviceToHost, stream_), "D2H");
     synchronize();
     for (int q = 0; q < 4; q++) out[q] = host_sums_[q];
+    if (mixed) {
+        int err = 0;
+        std::memcpy(&err, host_sums_ + 4, sizeof(int));
+        if (err) throw CudaError("tensor-core contraction: a bounded wait timed out");
+        out[1] *= s_y_ * s_y_;  // RSS / CV in the units of y
+    }
 }
 
 double Engine::criterion(double bw, bool adaptive, int kernel, int crit)
 {
     if (n_ == 0) throw std::logic_error("no data");
     check(cudaSetDevice(device_), "cudaSetDevice");
+    if (precision_ == kMixed) ensureMixed();
     computeThresholds(bw, adaptive);
-    contract(z_.get(), m_, g_.get(), m_, bw, adaptive, kernel, crit == kCV, 1);
+    if (precision_ == kMixed)
+        contractMixed(g_.get(), m_, m_, bw, adaptive, kernel, crit == kCV, 1);
+    else
+        contract(z_.get(), m_, g_.get(), m_, bw, adaptive, kernel, crit == kCV, 1);
     double s[4];
     solve(crit == kCV ? kSolveCV : kSolveAIC, bw, adaptive, kernel, s);
     if (stats_on_) stats_.criterion_evals++;
@@ -304,9 +525,16 @@ void Engine::fit(double bw, bool adaptive, int kernel, bool storeS, FitOutput& o
     vvec_.alloc((size_t)n * p);
     bse_.alloc((size_t)n * p);
     qdiag_.alloc(n);
+    const bool mixed = precision_ == kMixed;
+    if (mixed) ensureMixed();
     computeThresholds(bw, adaptive);
-    contract(z_.get(), m_, g_.get(), m_, bw, adaptive, kernel, false, 1);
-    contract(z_.get(), mm_, g2_.get(), mm_, bw, adaptive, kernel, false, 2);
+    if (mixed) {
+        contractMixed(g_.get(), m_, m_, bw, adaptive, kernel, false, 1);
+        contractMixed(g2_.get(), mm_, mm_, bw, adaptive, kernel, false, 2);
+    } else {
+        contract(z_.get(), m_, g_.get(), m_, bw, adaptive, kernel, false, 1);
+        contract(z_.get(), mm_, g2_.get(), mm_, bw, adaptive, kernel, false, 2);
+    }
     double s[4];
     solve(kSolveFit, bw, adaptive, kernel, s);
     if (s[3] > 0.0) throw NotSPDError("inv_sympd(): matrix is singular or not positive definite");
@@ -317,7 +545,8 @@ void Engine::fit(double bw, bool adaptive, int kernel, bool storeS, FitOutput& o
         if (perm_[sidx] == n - 1) last_sorted = sidx;
     S_.alloc(storeS ? (size_t)n * n : (size_t)n);
     check(cudaMemsetAsync(S_.get(), 0, sizeof(double) * S_.size(), stream_), "memset S");
-    check(launch_hat_pass(points(), geographic_, tiles_.get(), x_.get(), p, vvec_.get(), thrPtr(adaptive), bw, kernel,
+    check(launch_hat_pass(points(), geographic_, tiles_.get(), mixed ? xs_.get() : x_.get(), p, vvec_.get(),
+                          thrPtr(adaptive), bw, kernel,
                           true, qdiag_.get(), storeS ? S_.get() : nullptr, storeS ? -1 : last_sorted,
                           storeS ? nullptr : S_.get(), stream_),
           "hat pass");
@@ -331,6 +560,22 @@ void Engine::fit(double bw, bool adaptive, int kernel, bool storeS, FitOutput& o
     out.betas.assign((size_t)n * p, 0.0);
     out.betasSE.assign((size_t)n * p, 0.0);
     out.qdiag.assign(n, 0.0);
+    if (mixed) {
+        // beta_k = s_y beta~_k / s_k; the intercept absorbs the centring
+        for (int sidx = 0; sidx < n; sidx++) {
+            double* b = &hb[(size_t)sidx * p];
+            double shift = 0.0;
+            for (int k = 0; k < p; k++) {
+                if (k == intercept_col_) continue;
+                b[k] = s_y_ * b[k] / sc_[k];
+                shift += b[k] * mu_[k];
+            }
+            if (intercept_col_ >= 0) {
+                const int c = intercept_col_;
+                b[c] = (mu_y_ + s_y_ * b[c] - shift) / sc_[c];
+            }
+        }
+    }
     for (int sidx = 0; sidx < n; sidx++) {
         const int i = perm_[sidx];
         for (int k = 0; k < p; k++) {

@@ -116,7 +116,13 @@ public:
     cudaStream_t stream() const { return stream_; }
     void synchronize();
 
+    // tcgen05 self-test: D[128 x N] = A[128 x 32] B[N x 32]^T (host arrays).
+    void tcSelftest(int N, const float* A, const float* B, float* D);
+
 private:
+    void ensureMixed();
+    void contractMixed(double* G, int ldg, int mcols, double bw, bool adaptive, int kernel, bool exclude_self,
+                       int wpow);
     void computeThresholds(double bw, bool adaptive);
     const double* thrPtr(bool adaptive) const { return adaptive ? thr_.get() : nullptr; }
     void contract(const double* Z, int mcols, double* G, int ldg, double bw, bool adaptive, int kernel,
@@ -132,6 +138,7 @@ private:
     int precision_ = kFP64;
     double dlo_ = 0.0, dhi_ = 0.0;
     std::vector<int> perm_;  // sorted position -> original index
+    std::vector<double> hx_, hy_, hu_, hv_;  // host copies in sorted order
 
     DevBuf<double> u_, v_, uR_, vR_, x_, y_, z_, g_, g2_;
     DevBuf<double> thr_, sel0_, sel1_;
@@ -140,6 +147,20 @@ private:
     DevBuf<double> gall_, gall_part_, gsub_, xsub_;
     bool gall_valid_ = false;
     DevBuf<TileBox> tiles_;
+
+    // mixed-precision state (built on first use): X~ = (X - mu) / s, y~ likewise
+    bool mixed_ready_ = false;
+    int npad_ = 0, ntiles32_ = 0, intercept_col_ = -1;
+    std::vector<double> mu_, sc_;  // per column mean (0 if not centred) and scale
+    double mu_y_ = 0.0, s_y_ = 1.0;
+    DevBuf<double> xs_, ys_, zs_;
+    DevBuf<unsigned char> zimg_;
+    DevBuf<float4> pts32_;
+    DevBuf<TileBox> boxes32_;
+    DevBuf<float2> acc_;
+    DevBuf<float> thr32_;
+    DevBuf<int> err_;
+    DevBuf<double> tinv_, tvec_;   // transform of the fit's covariance diagonal
     DevBuf<unsigned long long> key_;
     double* host_sums_ = nullptr;  // pinned
 

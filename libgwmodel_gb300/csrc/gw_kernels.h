@@ -23,6 +23,9 @@ size_t select_smem_bytes();
 cudaError_t launch_threshold_combine(int n, double bw, const double* d0, const double* d1, double* thr,
                                      cudaStream_t stream);
 
+// out[i] = (float)in[i].
+cudaError_t launch_to_float(int n, const double* in, float* out, cudaStream_t stream);
+
 // Z[j, :] = (upper triangle of x_j x_j^T packed by rows, x_j * y_j); X row-major n x p.
 cudaError_t launch_build_z(int n, int p, const double* X, const double* y, double* Z, cudaStream_t stream);
 
@@ -51,8 +54,13 @@ struct SolveArgs {
     double* sii;       // n
     double* resid;     // n
     double* v;         // n x p: A_i^{-1} x_i (fit)
-    double* bse;       // n x p: diag(A^-1 Q A^-1) (fit)
+    double* bse;       // n x p: diag(T A^-1 Q A^-1 T^T) (fit)
     double* partials;
+    // Optional linear map T of the coefficients (fit): T = diag(tinv) except
+    // row tcol = tvec (the intercept row after centring).  Null: identity.
+    const double* tinv;
+    const double* tvec;
+    int tcol;
 };
 cudaError_t launch_solve(const SolveArgs& a, int* nblocks, cudaStream_t stream);
 
@@ -79,6 +87,27 @@ cudaError_t launch_column_sums(int n, int m, const double* Z, double* part, int 
 // subset taken from the full column sums gall.
 cudaError_t launch_gather_subset(int n, int p, const ColumnSet& cs, const double* X, const double* gall, double* Xs,
                                  double* gsub, cudaStream_t stream);
+
+// Mixed-precision W.Z contraction on tcgen05 (k_contract_tc.cu).
+struct TcArgs {
+    int n, mcols, npad, ntiles;   // ntiles: 32-point tiles
+    const float4* pts;            // planar: {u_hi, u_lo, v_hi, v_lo}; geographic: 3 float4 per point
+    const TileBox* boxes;         // bounds of each 32-point tile
+    const unsigned char* zimg;    // per tile: [hi | lo] swizzled images, npad x 128 bytes each
+    const float* thr;             // per-row threshold, or null for the fixed bandwidth bw
+    float bw;
+    int kernel, exclude_self, skip, flush_tiles, wpow;
+    float2* acc;                  // n x npad double-float accumulators
+    double* G;                    // n x ldg FP64 output (first mcols columns)
+    int ldg;
+    int* err;                     // set to 1 if a bounded wait timed out
+};
+size_t contract_tc_smem_bytes(int npad);
+cudaError_t launch_contract_tc(const TcArgs& a, bool geographic, cudaStream_t stream);
+cudaError_t launch_build_zimg(int n, int mcols, int npad, const double* Z, int ldz, unsigned char* img,
+                              cudaStream_t stream);
+// D[128 x N] = A[128 x 32] B[N x 32]^T through tcgen05 (device pointers).
+cudaError_t launch_tc_selftest(const float* A, const float* B, float* D, int N, int* err, cudaStream_t stream);
 
 // Maximum pairwise distance (CRSDistance::maxDistance), as an ordered key in *key_out.
 cudaError_t launch_max_distance(const DevPoints& P, bool geographic, unsigned long long* key_out, int num_sms,

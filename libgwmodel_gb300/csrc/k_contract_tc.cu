@@ -1,0 +1,437 @@
+// k_contract_tc.cu -- mixed-precision W.Z contraction on the tcgen05 tensor cores.
+//
+// G[i, :] = sum_j w_ij Z~[j, :] for a block of 128 focus rows per CTA:
+//  * producer: 256 threads compute the 128 x 32 weight tile of each stage in
+//    FP32 from the coordinates (planar or WGS-84 great-circle), split every
+//    weight into TF32 hi + lo and store both in the 128-byte-swizzled K-major
+//    layout the tensor core reads;
+//  * the matching Z~ tile (scaled/centred products, split hi + lo, stored in
+//    global memory already in the swizzled image) arrives by one 1-D TMA bulk
+//    copy on an mbarrier;
+//  * one thread issues 3 x 4 tcgen05.mma.kind::tf32 (hi.hi + hi.lo + lo.hi,
+//    K = 8 each) into a 128 x N FP32 accumulator in TMEM and commits to an
+//    mbarrier; two stages double-buffer producer and tensor core;
+//  * every flush_tiles stages the accumulator is read back with tcgen05.ld
+//    and added into double-float (hi, lo) accumulators in global memory, so
+//    FP32 rounding never sums more than a chunk of points.
+// Compactly supported kernels skip data tiles farther than the block's
+// largest threshold (planar boxes).  Waits are bounded and report through err.
+#include "gw_common.cuh"
+#include "gw_kernels.h"
+#include "tc05.cuh"
+
+namespace gwgpu {
+
+namespace {
+
+using namespace tc05;
+
+constexpr int TC_THREADS = 256;
+constexpr int TC_M = 128;
+constexpr int TC_BK = 32;  // points per stage (128 bytes of TF32 per row)
+constexpr uint32_t TC_A_BYTES = TC_M * 128;  // one split part of the weight tile
+constexpr uint32_t TC_WAIT = 1u << 22;
+
+struct Smem {
+    uint64_t bar_b[2];
+    uint64_t bar_mma[2];
+    uint32_t tmem_base;
+    int abort;
+};
+
+__device__ __forceinline__ float sin_poly(float x)
+{
+    // Taylor series to x^13, |x| <= pi/2
+    float z = x * x;
+    float p = -1.6059043836821614e-10f;        // -1/13!
+    p = fmaf(p, z, 2.505210838544172e-08f);    //  1/11!
+    p = fmaf(p, z, -2.7557319223985893e-06f);  // -1/9!
+    p = fmaf(p, z, 1.984126984126984e-04f);    //  1/7!
+    p = fmaf(p, z, -8.333333333333333e-03f);   // -1/5!  (sign alternates: x - x^3/6 + ...)
+    p = fmaf(p, z, 1.6666666666666666e-01f);   //  1/3!
+    return x - x * z * p;
+}
+
+// FP32 great-circle distance (km) of the reference's Lambert formula with the
+// haversine term taken from the 3-D chord of hi/lo unit vectors.
+__device__ __forceinline__ float geo_dist32(const float4& fa, const float4& fb, const float4& fc, const float4& pa,
+                                            const float4& pb, const float4& pc)
+{
+    const float dx = (pa.x - fa.x) + (pb.x - fb.x);
+    const float dy = (pa.y - fa.y) + (pb.y - fb.y);
+    const float dz = (pa.z - fa.z) + (pb.z - fb.z);
+    const float S = 0.25f * fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    if (!(S > 0.0f)) return 0.0f;
+    const float C = fmaxf(1.0f - S, 0.0f);
+    const float sq = sqrtf(S), cq = sqrtf(C);
+    const float w = atan2f(sq, cq);
+    const float R = sq * cq / w;
+    const float dlat = (pa.w - fa.w) + (pb.w - fb.w);            // degrees
+    const float G = dlat * 8.7266462599716478846e-3f;            // (pi/180)/2
+    const float sG = sin_poly(G);
+    const float sG2 = sG * sG, cG2 = 1.0f - sG2;
+    const float sF = pc.x * fc.y + pc.y * fc.x;                  // sin((lat_a+lat_b)/2)
+    const float cF = pc.y * fc.y - pc.x * fc.x;
+    const float sF2 = sF * sF, cF2 = cF * cF;
+    const float H1 = (3.0f * R - 1.0f) / (2.0f * C);
+    const float H2 = (3.0f * R + 1.0f) / (2.0f * S);
+    const float f = 1.0f / 298.257223563f;
+    return 2.0f * 6378.137f * w * (1.0f + f * H1 * sF2 * cG2 - f * H2 * cF2 * sG2);
+}
+
+__device__ __forceinline__ float weight32(int kernel, float d2, float r, float inv_r2)
+{
+    switch (kernel) {
+    case GW_KERNEL_GAUSSIAN:
+        return __expf(-0.5f * d2 * inv_r2);
+    case GW_KERNEL_EXPONENTIAL:
+        return __expf(-sqrtf(d2) / r);
+    case GW_KERNEL_BISQUARE: {
+        float t = 1.0f - d2 * inv_r2;
+        return d2 < r * r ? t * t : 0.0f;
+    }
+    case GW_KERNEL_TRICUBE: {
+        float q = sqrtf(d2) / r;
+        float t = 1.0f - q * q * q;
+        return d2 < r * r ? t * t * t : 0.0f;
+    }
+    default:
+        return d2 < r * r ? 1.0f : 0.0f;
+    }
+}
+
+// Double-float accumulate: (hi, lo) += v.
+__device__ __forceinline__ float2 df_add(float2 a, float v)
+{
+    float s = a.x + v;
+    float bp = s - a.x;
+    float e = (a.x - (s - bp)) + (v - bp);
+    float lo = a.y + e;
+    float hi = s + lo;
+    return make_float2(hi, lo - (hi - s));
+}
+
+template <bool GEO>
+__global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
+{
+    extern __shared__ unsigned char smem_dyn[];
+    __shared__ Smem ctl;
+    // 1024-byte aligned stage buffers: [A_hi A_lo B_hi B_lo] x 2
+    const uint32_t base_u32 = smem_u32(smem_dyn);
+    const uint32_t pad = (1024u - (base_u32 & 1023u)) & 1023u;
+    unsigned char* stage0 = smem_dyn + pad;
+    const uint32_t b_bytes = (uint32_t)a.npad * 128u;
+    const uint32_t stage_bytes = 2u * TC_A_BYTES + 2u * b_bytes;
+
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const int r = t & (TC_M - 1), half = t >> 7;
+    const int row0 = blockIdx.x * TC_M;
+    const int i = row0 + r;
+    const bool row_ok = i < a.n;
+
+    if (warp == 0) {
+        tmem_alloc(&ctl.tmem_base, 256);
+        tmem_relinquish();
+    }
+    if (t == 0) {
+        for (int s = 0; s < 2; s++) {
+            mbar_init(&ctl.bar_b[s], 1);
+            mbar_init(&ctl.bar_mma[s], 1);
+        }
+        ctl.abort = 0;
+        fence_mbar_init();
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = ctl.tmem_base;
+
+    // focus point
+    float4 fa = make_float4(0.f, 0.f, 0.f, 0.f), fb = fa, fc = fa;
+    if (row_ok) {
+        if (GEO) {
+            fa = a.pts[3 * (size_t)i];
+            fb = a.pts[3 * (size_t)i + 1];
+            fc = a.pts[3 * (size_t)i + 2];
+        } else {
+            fa = a.pts[i];
+        }
+    }
+    const float rr = row_ok ? (a.thr ? a.thr[i] : a.bw) : 1.0f;
+    const float inv_r2 = 1.0f / (rr * rr);
+
+    // block box and largest threshold for tile skipping
+    __shared__ float red[TC_THREADS / 32];
+    __shared__ TileBox fbox;
+    float rmax = row_ok ? rr : 0.0f;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, off));
+    if (lane == 0) red[warp] = rmax;
+    if (t == 0) {
+        TileBox b = a.boxes[row0 / TC_BK];
+        int last = min(row0 + TC_M, a.n) - 1;
+        for (int q = row0 / TC_BK + 1; q <= last / TC_BK; q++) {
+            TileBox c = a.boxes[q];
+            b.ulo = fmin(b.ulo, c.ulo); b.uhi = fmax(b.uhi, c.uhi);
+            b.vlo = fmin(b.vlo, c.vlo); b.vhi = fmax(b.vhi, c.vhi);
+        }
+        fbox = b;
+    }
+    __syncthreads();
+    rmax = red[0];
+    for (int q = 1; q < TC_THREADS / 32; q++) rmax = fmaxf(rmax, red[q]);
+    const bool can_skip = a.skip && !GEO && a.kernel >= GW_KERNEL_BISQUARE && rmax > 0.0f;
+    const double rmax_d = (double)rmax * (1.0 + 1e-5);
+
+    const uint32_t idesc = idesc_tf32(TC_M, a.npad);
+    int issued = 0;        // stages issued so far (non-skipped tiles)
+    int in_chunk = 0;      // stages accumulated in TMEM since the last flush
+    bool first_flush = true;
+    bool aborted = false;
+
+    auto flush = [&](int last_stage) {
+        // wait for the last MMA group, read TMEM, accumulate in double-float
+        const int s = last_stage & 1;
+        const uint32_t par = (uint32_t)((last_stage >> 1) & 1);
+        if (!mbar_wait(&ctl.bar_mma[s], par, TC_WAIT)) atomicExch(&ctl.abort, 1);
+        fence_after_sync();
+        const int quad = warp & 3, colhalf = warp >> 2;
+        const int lrow = quad * 32 + lane;
+        const int grow = row0 + lrow;
+        const int ncol_half = a.npad / 2;
+        for (int c0 = colhalf * ncol_half; c0 < (colhalf + 1) * ncol_half; c0 += 16) {
+            uint32_t v[16];
+            tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0, v);
+            tmem_wait_ld();
+            if (grow < a.n) {
+                float2* acc = a.acc + (size_t)grow * a.npad + c0;
+#pragma unroll
+                for (int q = 0; q < 16; q++) {
+                    float x = __uint_as_float(v[q]);
+                    acc[q] = first_flush ? make_float2(x, 0.0f) : df_add(acc[q], x);
+                }
+            }
+        }
+        fence_before_sync();
+        __syncthreads();
+        first_flush = false;
+        in_chunk = 0;
+    };
+
+    for (int tile = 0; tile < a.ntiles && !aborted; tile++) {
+        if (can_skip) {
+            const double lb = box_lower_bound(fbox, a.boxes[tile]);
+            if (lb * (1.0 - 1e-12) >= rmax_d) continue;  // uniform over the CTA
+        }
+        const int s = issued & 1;
+        unsigned char* st = stage0 + (size_t)s * stage_bytes;
+        unsigned char* A_hi = st;
+        unsigned char* A_lo = st + TC_A_BYTES;
+        unsigned char* B_hi = st + 2 * TC_A_BYTES;
+        if (issued >= 2 && in_chunk >= 2) {
+            // the MMAs that read this stage two issues ago must be done
+            const uint32_t par = (uint32_t)(((issued >> 1) - 1) & 1);
+            if (!mbar_wait(&ctl.bar_mma[s], par, TC_WAIT)) atomicExch(&ctl.abort, 1);
+        }
+        if (t == 0) {
+            mbar_arrive_expect_tx(&ctl.bar_b[s], 2u * b_bytes);
+            bulk_g2s(B_hi, a.zimg + (size_t)tile * 2u * b_bytes, 2u * b_bytes, &ctl.bar_b[s]);
+        }
+        // weight tile: thread (r, half) fills points [16*half, 16*half + 16) of row r
+        const int jbase = tile * TC_BK + half * 16;
+#pragma unroll
+        for (int q4 = 0; q4 < 4; q4++) {
+            float hi[4], lo[4];
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int j = jbase + q4 * 4 + e;
+                float w = 0.0f;
+                if (row_ok && j < a.n) {
+                    float d2;
+                    if (GEO) {
+                        float d = geo_dist32(fa, fb, fc, a.pts[3 * (size_t)j], a.pts[3 * (size_t)j + 1],
+                                             a.pts[3 * (size_t)j + 2]);
+                        d2 = d * d;
+                    } else {
+                        const float4 p = a.pts[j];
+                        const float dx = (p.x - fa.x) + (p.y - fa.y);
+                        const float dy = (p.z - fa.z) + (p.w - fa.w);
+                        d2 = fmaf(dx, dx, dy * dy);
+                    }
+                    w = weight32(a.kernel, d2, rr, inv_r2);
+                    if (a.exclude_self && i == j) w = 0.0f;
+                    if (a.wpow == 2) w = w * w;
+                }
+                hi[e] = to_tf32(w);
+                lo[e] = to_tf32(w - hi[e]);
+            }
+            const uint32_t off = sw128_offset((uint32_t)r, (uint32_t)(half * 16 + q4 * 4));
+            *reinterpret_cast<float4*>(A_hi + off) = make_float4(hi[0], hi[1], hi[2], hi[3]);
+            *reinterpret_cast<float4*>(A_lo + off) = make_float4(lo[0], lo[1], lo[2], lo[3]);
+        }
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (ctl.abort) {
+            aborted = true;
+            break;
+        }
+        if (t == 0) {
+            if (!mbar_wait(&ctl.bar_b[s], (uint32_t)((issued >> 1) & 1), TC_WAIT)) {
+                atomicExch(&ctl.abort, 1);
+            } else {
+                fence_after_sync();
+                const uint64_t ahi = sw128_kmajor_desc(smem_u32(A_hi));
+                const uint64_t alo = sw128_kmajor_desc(smem_u32(A_lo));
+                const uint64_t bhi = sw128_kmajor_desc(smem_u32(B_hi));
+                const uint64_t blo = sw128_kmajor_desc(smem_u32(B_hi + b_bytes));
+#pragma unroll
+                for (int kk = 0; kk < 4; kk++) {
+                    const uint64_t dk = (uint64_t)(kk * 2);  // 32 bytes = 8 TF32 along K
+                    mma_tf32(tmem, ahi + dk, bhi + dk, idesc, (in_chunk > 0 || kk > 0) ? 1u : 0u);
+                    mma_tf32(tmem, ahi + dk, blo + dk, idesc, 1u);
+                    mma_tf32(tmem, alo + dk, bhi + dk, idesc, 1u);
+                }
+                mma_commit(&ctl.bar_mma[s]);
+            }
+        }
+        issued++;
+        in_chunk++;
+        if (in_chunk >= a.flush_tiles) flush(issued - 1);
+    }
+    if (!aborted && in_chunk > 0) flush(issued - 1);
+    __syncthreads();
+    aborted = aborted || ctl.abort;
+    // epilogue: double-float -> FP64 rows (only columns of Z)
+    if (!aborted) {
+        for (int e = t; e < TC_M * a.mcols; e += TC_THREADS) {
+            const int lr = e / a.mcols, c = e - lr * a.mcols;
+            const int grow = row0 + lr;
+            if (grow >= a.n) continue;
+            double v = 0.0;
+            if (!first_flush) {
+                const float2 x = a.acc[(size_t)grow * a.npad + c];
+                v = (double)x.x + (double)x.y;
+            }
+            a.G[(size_t)grow * a.ldg + c] = v;
+        }
+    } else if (t == 0) {
+        atomicExch(a.err, 1);
+        // leave no MMA in flight before TMEM is freed
+        if (issued > 0) {
+            const int ls = issued - 1;
+            mbar_wait(&ctl.bar_mma[ls & 1], (uint32_t)((ls >> 1) & 1), TC_WAIT);
+        }
+    }
+    fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, 256);
+}
+
+// D[128 x N] = A[128 x 32] * B[N x 32]^T through the same layouts (TF32 in, FP32 out).
+__global__ void __launch_bounds__(128, 1) k_tc_selftest(const float* A, const float* B, float* D, int N, int* err)
+{
+    extern __shared__ unsigned char smem_dyn[];
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tmem_base;
+    const uint32_t base_u32 = smem_u32(smem_dyn);
+    const uint32_t pad = (1024u - (base_u32 & 1023u)) & 1023u;
+    unsigned char* sA = smem_dyn + pad;
+    unsigned char* sB = sA + TC_A_BYTES;
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    if (warp == 0) {
+        tmem_alloc(&tmem_base, 256);
+        tmem_relinquish();
+    }
+    if (t == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    for (int k = 0; k < 32; k++) *reinterpret_cast<float*>(sA + sw128_offset(t, k)) = to_tf32(A[t * 32 + k]);
+    for (int e = t; e < N * 32; e += 128) {
+        int row = e / 32, k = e % 32;
+        *reinterpret_cast<float*>(sB + sw128_offset(row, k)) = to_tf32(B[row * 32 + k]);
+    }
+    fence_proxy_async_smem();
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = tmem_base;
+    if (t == 0) {
+        const uint64_t ad = sw128_kmajor_desc(smem_u32(sA)), bd = sw128_kmajor_desc(smem_u32(sB));
+        for (int kk = 0; kk < 4; kk++)
+            mma_tf32(tmem, ad + (uint64_t)(kk * 2), bd + (uint64_t)(kk * 2), idesc_tf32(128, N), kk > 0 ? 1u : 0u);
+        mma_commit(&bar);
+    }
+    bool ok = mbar_wait(&bar, 0, TC_WAIT);
+    fence_after_sync();
+    if (ok) {
+        for (int c0 = 0; c0 < N; c0 += 16) {
+            uint32_t v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+            tmem_wait_ld();
+            for (int q = 0; q < 16; q++) D[(warp * 32 + lane) * N + c0 + q] = __uint_as_float(v[q]);
+        }
+    } else {
+        atomicExch(err, 1);
+    }
+    fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, 256);
+}
+
+// Swizzled Z~ tile images: per 32-point tile, [hi: npad x 128 B][lo: npad x 128 B].
+__global__ void k_build_zimg(int n, int mcols, int npad, const double* __restrict__ Z, int ldz,
+                             unsigned char* __restrict__ img)
+{
+    const size_t tile = blockIdx.x;
+    const uint32_t b_bytes = (uint32_t)npad * 128u;
+    unsigned char* base = img + tile * 2u * b_bytes;
+    for (int e = threadIdx.x; e < npad * TC_BK; e += blockDim.x) {
+        const int c = e / TC_BK, k = e - c * TC_BK;
+        const int j = (int)tile * TC_BK + k;
+        const double z = (j < n && c < mcols) ? Z[(size_t)j * ldz + c] : 0.0;
+        const float hi = to_tf32((float)z);
+        const float lo = to_tf32((float)(z - (double)hi));
+        const uint32_t off = sw128_offset((uint32_t)c, (uint32_t)k);
+        *reinterpret_cast<float*>(base + off) = hi;
+        *reinterpret_cast<float*>(base + b_bytes + off) = lo;
+    }
+}
+
+}  // namespace
+
+size_t contract_tc_smem_bytes(int npad) { return 1024 + 2 * (2 * (size_t)TC_A_BYTES + 2 * (size_t)npad * 128); }
+
+cudaError_t launch_contract_tc(const TcArgs& a, bool geographic, cudaStream_t stream)
+{
+    if (a.npad % 32 != 0 || a.npad < 32 || a.npad > 256 || a.mcols > a.npad) return cudaErrorInvalidValue;
+    const size_t smem = contract_tc_smem_bytes(a.npad);
+    const int grid = (a.n + TC_M - 1) / TC_M;
+    if (geographic) {
+        cudaFuncSetAttribute(k_contract_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_contract_tc<true><<<grid, TC_THREADS, smem, stream>>>(a);
+    } else {
+        cudaFuncSetAttribute(k_contract_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_contract_tc<false><<<grid, TC_THREADS, smem, stream>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build_zimg(int n, int mcols, int npad, const double* Z, int ldz, unsigned char* img,
+                              cudaStream_t stream)
+{
+    const int ntiles = (n + TC_BK - 1) / TC_BK;
+    k_build_zimg<<<ntiles, 256, 0, stream>>>(n, mcols, npad, Z, ldz, img);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tc_selftest(const float* A, const float* B, float* D, int N, int* err, cudaStream_t stream)
+{
+    if (N % 16 != 0 || N < 16 || N > 256) return cudaErrorInvalidValue;
+    const size_t smem = 1024 + TC_A_BYTES + (size_t)N * 128;
+    cudaFuncSetAttribute(k_tc_selftest, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_tc_selftest<<<1, 128, smem, stream>>>(A, B, D, N, err);
+    return cudaGetLastError();
+}
+
+}  // namespace gwgpu

@@ -245,7 +245,19 @@ __global__ void k_threshold_combine(int n, double bw, const double* __restrict__
     }
 }
 
+__global__ void k_to_float(int n, const double* __restrict__ in, float* __restrict__ out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (float)in[i];
+}
+
 }  // namespace
+
+cudaError_t launch_to_float(int n, const double* in, float* out, cudaStream_t stream)
+{
+    k_to_float<<<(n + 255) / 256, 256, 0, stream>>>(n, in, out);
+    return cudaGetLastError();
+}
 
 size_t select_smem_bytes() { return sizeof(SelShared); }
 

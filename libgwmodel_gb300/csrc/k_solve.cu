@@ -78,11 +78,13 @@ __global__ void __launch_bounds__(SV_WARPS * 32) k_solve(SolveArgs a)
     extern __shared__ double smem[];
     const int p = a.p, ld = p + 1, mm = p * (p + 1) / 2;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int per_warp = (MODE == kSolveFit) ? 3 * p * ld + p : p * ld + p;
+    const int per_warp = (MODE == kSolveFit) ? 4 * p * ld + 2 * p : p * ld + p;
     double* L = smem + warp * per_warp;
     double* Ainv = L + p * ld;
     double* Q = Ainv + p * ld;
-    double* vsh = (MODE == kSolveFit) ? Q + p * ld : L + p * ld;
+    double* T = Q + p * ld;
+    double* vsh = (MODE == kSolveFit) ? T + p * ld : L + p * ld;
+    double* tsh = vsh + p;
     __shared__ double part[SV_WARPS][4];
 
     double acc_s = 0.0, acc_r = 0.0, acc_t = 0.0, acc_f = 0.0;
@@ -146,17 +148,29 @@ __global__ void __launch_bounds__(SV_WARPS * 32) k_solve(SolveArgs a)
                 if (lane < p)
                     for (int c = 0; c < p; c++)
                         Q[lane * ld + c] = g2[lane <= c ? packed_index(lane, c, p) : packed_index(c, lane, p)];
+                if (lane < p) tsh[lane] = a.tvec ? a.tvec[lane] : 0.0;
                 __syncwarp();
-                double se = 0.0, qv = 0.0;
-                if (lane < p) {
+                // T = A^-1 Q (row per lane), then row `lane` of M = T A^-1
+                double qv = 0.0;
+                if (lane < p)
                     for (int b = 0; b < p; b++) {
                         double tb = 0.0;
                         for (int q = 0; q < p; q++) tb += Ainv[lane * ld + q] * Q[q * ld + b];
-                        se += tb * Ainv[b * ld + lane];
+                        T[lane * ld + b] = tb;
                         qv += Q[lane * ld + b] * vsh[b];
                     }
-                    a.bse[(size_t)row * p + lane] = se;
-                }
+                __syncwarp();
+                double mdiag = 0.0, mt = 0.0;
+                if (lane < p)
+                    for (int l = 0; l < p; l++) {
+                        double m = 0.0;
+                        for (int b = 0; b < p; b++) m += T[lane * ld + b] * Ainv[b * ld + l];
+                        if (l == lane) mdiag = m;
+                        mt += m * tsh[l];
+                    }
+                const double ti = (a.tinv && lane < p) ? a.tinv[lane] : 1.0;
+                const double tmt = warp_sum(lane < p ? tsh[lane] * mt : 0.0);
+                if (lane < p) a.bse[(size_t)row * p + lane] = (a.tvec && lane == a.tcol) ? tmt : ti * ti * mdiag;
                 const double sts = warp_sum(lane < p ? vsh[lane] * qv : 0.0);
                 if (lane == 0) acc_t += sts;
             }
@@ -368,7 +382,7 @@ cudaError_t launch_solve(const SolveArgs& a, int* nblocks, cudaStream_t stream)
     int grid = (a.n + SV_WARPS - 1) / SV_WARPS;
     if (grid > 4096) grid = 4096;
     const int ld = a.p + 1;
-    size_t per_warp = (a.mode == kSolveFit) ? 3 * a.p * ld + a.p : a.p * ld + a.p;
+    size_t per_warp = (a.mode == kSolveFit) ? 4 * a.p * ld + 2 * a.p : a.p * ld + a.p;
     size_t smem = per_warp * SV_WARPS * sizeof(double);
     *nblocks = grid;
     switch (a.mode) {

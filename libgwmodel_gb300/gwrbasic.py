@@ -410,6 +410,17 @@ class Engine:
     def reset_stats(self):
         check(lib().gwgpu_engine_reset_stats(self._h))
 
+    def tc_selftest(self, A, B):
+        """D = A B^T on the tensor cores (A: 128 x 32, B: N x 32, float32)."""
+        A = np.ascontiguousarray(A, dtype=np.float32)
+        B = np.ascontiguousarray(B, dtype=np.float32)
+        N = B.shape[0]
+        D = np.zeros((128, N), dtype=np.float32)
+        fp = ctypes.POINTER(ctypes.c_float)
+        check(lib().gwgpu_engine_tc_selftest(self._h, N, A.ctypes.data_as(fp), B.ctypes.data_as(fp),
+                                             D.ctypes.data_as(fp)))
+        return D
+
 
 __all__ = ["GWRBasic", "CRSDistance", "BandwidthWeight", "SpatialWeight", "RegressionDiagnostic", "Logger",
            "ParallelType", "Status", "Precision", "LogLevel", "Engine", "GwgpuError"]
