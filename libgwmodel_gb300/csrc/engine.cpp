@@ -29,6 +29,42 @@ uint64_t spread_bits(uint32_t x)
     return v;
 }
 
+// Geographic bounds of consecutive tiles of `size` points (sorted order).
+std::vector<TileCap> make_caps(const std::vector<double>& lon, const std::vector<double>& lat, int size)
+{
+    const int n = (int)lon.size(), nt = (n + size - 1) / size;
+    const double DE2RA = M_PI / 180;
+    std::vector<TileCap> caps(nt);
+    for (int t = 0; t < nt; t++) {
+        const int s0 = t * size, s1 = std::min(n, s0 + size);
+        double sx = 0, sy = 0, sz = 0;
+        std::vector<double> P((size_t)3 * (s1 - s0));
+        for (int s = s0; s < s1; s++) {
+            const double la = lat[s] * DE2RA, lo = lon[s] * DE2RA;
+            double* q = &P[(size_t)3 * (s - s0)];
+            q[0] = std::cos(la) * std::cos(lo);
+            q[1] = std::cos(la) * std::sin(lo);
+            q[2] = std::sin(la);
+            sx += q[0];
+            sy += q[1];
+            sz += q[2];
+        }
+        double nrm = std::sqrt(sx * sx + sy * sy + sz * sz);
+        TileCap c{1.0, 0.0, 0.0, 2.0};  // degenerate tile: no bound
+        if (nrm > 1e-12) {
+            c = TileCap{sx / nrm, sy / nrm, sz / nrm, 0.0};
+            for (int s = s0; s < s1; s++) {
+                const double* q = &P[(size_t)3 * (s - s0)];
+                const double dx = q[0] - c.cx, dy = q[1] - c.cy, dz = q[2] - c.cz;
+                c.rho = std::max(c.rho, std::sqrt(dx * dx + dy * dy + dz * dz));
+            }
+            c.rho = c.rho * (1.0 + 1e-12) + 1e-15;
+        }
+        caps[t] = c;
+    }
+    return caps;
+}
+
 // GWRBase::AICc (GWRBase.h:90-94) from RSS and tr(S).
 double aicc(double n, double rss, double trS)
 {
@@ -174,6 +210,15 @@ void Engine::setData(int n, int p, const double* x, const double* y, const doubl
     check(cudaMemcpyAsync(y_.get(), hy.data(), sizeof(double) * n, cudaMemcpyHostToDevice, stream_), "H2D y");
     check(cudaMemcpyAsync(tiles_.get(), ht.data(), sizeof(TileBox) * ntiles, cudaMemcpyHostToDevice, stream_),
           "H2D tiles");
+    if (geographic) {
+        std::vector<TileCap> hc = make_caps(hu, hv, kTile);
+        caps_.alloc(hc.size());
+        check(cudaMemcpyAsync(caps_.get(), hc.data(), sizeof(TileCap) * hc.size(), cudaMemcpyHostToDevice, stream_),
+              "H2D caps");
+        synchronize();
+    } else {
+        caps_.release();
+    }
     check(launch_build_z(n, p, x_.get(), y_.get(), z_.get(), stream_), "build_z");
     synchronize();
     hx_ = std::move(hx);
@@ -300,6 +345,17 @@ void Engine::ensureMixed()
             pts[3 * (size_t)s + 2] = make_float4((float)std::sin(lat / 2), (float)std::cos(lat / 2), 0.f, 0.f);
         }
     }
+    if (geographic_) {
+        std::vector<TileCap> c32 = make_caps(hu_, hv_, 32);
+        caps32_.alloc(c32.size());
+        check(cudaMemcpyAsync(caps32_.get(), c32.data(), sizeof(TileCap) * c32.size(), cudaMemcpyHostToDevice,
+                              stream_),
+              "H2D caps32");
+        synchronize();
+    } else {
+        caps32_.release();
+    }
+    rvec_.alloc((size_t)n * p);
     pts32_.alloc(pts.size());
     check(cudaMemcpyAsync(pts32_.get(), pts.data(), sizeof(float4) * pts.size(), cudaMemcpyHostToDevice, stream_),
           "H2D pts32");
@@ -334,6 +390,7 @@ void Engine::contractMixed(double* G, int ldg, int mcols, double bw, bool adapti
     a.ntiles = ntiles32_;
     a.pts = pts32_.get();
     a.boxes = boxes32_.get();
+    a.caps = caps32_.get();
     a.zimg = zimg_.get();
     a.thr = adaptive ? thr32_.get() : nullptr;
     a.bw = (float)bw;
@@ -436,8 +493,8 @@ void Engine::contract(const double* Z, int mcols, double* G, int ldg, double bw,
         cudaEventCreate(&e1);
         cudaEventRecord(e0, stream_);
     }
-    check(launch_contract64(points(), geographic_, tiles_.get(), Z, m_, mcols, G, ldg, thrPtr(adaptive), bw, kernel,
-                            exclude_self, wpow, true, stream_),
+    check(launch_contract64(points(), geographic_, tiles_.get(), caps_.get(), Z, m_, mcols, G, ldg, thrPtr(adaptive),
+                            bw, kernel, exclude_self, wpow, true, stream_),
           "contract64");
     if (stats_on_) {
         cudaEventRecord(e1, stream_);
@@ -482,6 +539,7 @@ void Engine::solve(int mode, double bw, bool adaptive, int kernel, double out[4]
     a.tinv = mixed ? tinv_.get() : nullptr;
     a.tvec = (mixed && intercept_col_ >= 0) ? tvec_.get() : nullptr;
     a.tcol = mixed ? intercept_col_ : -1;
+    a.rvec = rvec_.get();
     int nb = 0;
     check(launch_solve(a, &nb, stream_), "solve");
     check(launch_reduce_partials(partials_.get(), nb, sums_.get(), stream_), "reduce");
@@ -497,6 +555,29 @@ void Engine::solve(int mode, double bw, bool adaptive, int kernel, double out[4]
     }
 }
 
+// One refinement step of every local solve (mixed path): residual of the
+// normal equations in FP64 over the contraction's weights, then beta += A~^-1 r.
+void Engine::refine(double bw, bool adaptive, int kernel, double out[4])
+{
+    RefineArgs r{};
+    r.n = n_;
+    r.p = p_;
+    r.ntiles = ntiles32_;
+    r.kernel = kernel;
+    r.skip = 1;
+    r.pts = pts32_.get();
+    r.boxes = boxes32_.get();
+    r.caps = caps32_.get();
+    r.X = xs_.get();
+    r.y = ys_.get();
+    r.beta = beta_.get();
+    r.thr = adaptive ? thr32_.get() : nullptr;
+    r.bw = (float)bw;
+    r.r = rvec_.get();
+    check(launch_refine_residual(r, geographic_, stream_), "refine residual");
+    solve(kSolveRefine, bw, adaptive, kernel, out);
+}
+
 double Engine::criterion(double bw, bool adaptive, int kernel, int crit)
 {
     if (n_ == 0) throw std::logic_error("no data");
@@ -509,6 +590,12 @@ double Engine::criterion(double bw, bool adaptive, int kernel, int crit)
         contract(z_.get(), m_, g_.get(), m_, bw, adaptive, kernel, crit == kCV, 1);
     double s[4];
     solve(crit == kCV ? kSolveCV : kSolveAIC, bw, adaptive, kernel, s);
+    if (precision_ == kMixed && refine_search_ && crit == kAIC && s[3] == 0.0) {
+        // refine beta (and so RSS); the CV criterion excludes w_ii and is not refined
+        double r[4];
+        for (int it = 0; it < refine_steps_; it++) refine(bw, adaptive, kernel, r);
+        if (refine_steps_ > 0) s[1] = r[1];
+    }
     if (stats_on_) stats_.criterion_evals++;
     if (s[3] > 0.0) return DBL_MAX;
     if (crit == kCV) return std::isfinite(s[1]) ? s[1] : DBL_MAX;
@@ -538,6 +625,11 @@ void Engine::fit(double bw, bool adaptive, int kernel, bool storeS, FitOutput& o
     double s[4];
     solve(kSolveFit, bw, adaptive, kernel, s);
     if (s[3] > 0.0) throw NotSPDError("inv_sympd(): matrix is singular or not positive definite");
+    if (mixed) {
+        double r[4];
+        for (int it = 0; it < refine_steps_; it++) refine(bw, adaptive, kernel, r);
+        if (refine_steps_ > 0) s[1] = r[1];
+    }
     // S: n x n when stored (isStoreS, GWRBasic.h:708), else only the last
     // location's row, which is what S.row(0) holds after the reference's loop
     int last_sorted = 0;
@@ -545,7 +637,8 @@ void Engine::fit(double bw, bool adaptive, int kernel, bool storeS, FitOutput& o
         if (perm_[sidx] == n - 1) last_sorted = sidx;
     S_.alloc(storeS ? (size_t)n * n : (size_t)n);
     check(cudaMemsetAsync(S_.get(), 0, sizeof(double) * S_.size(), stream_), "memset S");
-    check(launch_hat_pass(points(), geographic_, tiles_.get(), mixed ? xs_.get() : x_.get(), p, vvec_.get(),
+    check(launch_hat_pass(points(), geographic_, tiles_.get(), caps_.get(), mixed ? xs_.get() : x_.get(), p,
+                          vvec_.get(),
                           thrPtr(adaptive), bw, kernel,
                           true, qdiag_.get(), storeS ? S_.get() : nullptr, storeS ? -1 : last_sorted,
                           storeS ? nullptr : S_.get(), stream_),

@@ -92,6 +92,12 @@ public:
     // device in Morton order.
     void setData(int n, int p, const double* x, const double* y, const double* coords, bool geographic);
     void setPrecision(int precision) { precision_ = precision; }
+    // Refinement steps of the mixed final fit (and of each search criterion when refine_search).
+    void setRefinement(int steps, bool refine_search)
+    {
+        refine_steps_ = steps;
+        refine_search_ = refine_search;
+    }
     int precision() const { return precision_; }
 
     int n() const { return n_; }
@@ -128,6 +134,7 @@ private:
     void contract(const double* Z, int mcols, double* G, int ldg, double bw, bool adaptive, int kernel,
                   bool exclude_self, int wpow);
     void solve(int mode, double bw, bool adaptive, int kernel, double out[4]);
+    void refine(double bw, bool adaptive, int kernel, double out[4]);
     DevPoints points() const;
 
     int device_ = 0;
@@ -147,6 +154,9 @@ private:
     DevBuf<double> gall_, gall_part_, gsub_, xsub_;
     bool gall_valid_ = false;
     DevBuf<TileBox> tiles_;
+    DevBuf<TileCap> caps_;      // geographic bounds of the 16-point tiles
+    int refine_steps_ = 2;
+    bool refine_search_ = false;
 
     // mixed-precision state (built on first use): X~ = (X - mu) / s, y~ likewise
     bool mixed_ready_ = false;
@@ -157,6 +167,8 @@ private:
     DevBuf<unsigned char> zimg_;
     DevBuf<float4> pts32_;
     DevBuf<TileBox> boxes32_;
+    DevBuf<TileCap> caps32_;
+    DevBuf<double> rvec_;
     DevBuf<float2> acc_;
     DevBuf<float> thr32_;
     DevBuf<int> err_;

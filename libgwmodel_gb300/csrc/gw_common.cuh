@@ -28,6 +28,13 @@ struct TileBox {
     double ulo, uhi, vlo, vhi;
 };
 
+// Geographic tile bound: centre c of the tile's unit vectors (geodetic
+// latitude on the unit sphere, the sphere of the haversine term S of the
+// reference formula) and the largest 3-D chord rho from c to a member point.
+struct TileCap {
+    double cx, cy, cz, rho;
+};
+
 #if defined(__CUDACC__)
 // Distance from focus point f to data point d, CRSDistance::distance
 // (CRSDistance.cpp:122-131): planar EuclideanDistance(data - focus) or
@@ -62,6 +69,42 @@ __device__ __forceinline__ double box_lower_bound(const TileBox& a, const TileBo
     double dx = fmax(0.0, fmax(b.ulo - a.uhi, a.ulo - b.uhi));
     double dy = fmax(0.0, fmax(b.vlo - a.vhi, a.vlo - b.vhi));
     return sqrt(dx * dx + dy * dy);
+}
+// Lower bound (km) of the reference's ellipsoidal distance between any point
+// of cap a and any point of cap b; 0 when no bound is proven.
+//  * chord(P, Q) >= |ca - cb| - rho_a - rho_b (triangle inequality in R^3);
+//  * S = chord^2 / 4 = sin^2(w), w the half central angle;
+//  * D = 2 a w (1 + f (H1 sin^2F cos^2G - H2 cos^2F sin^2G)) with
+//    H2 cos^2F sin^2G <= (3R + 1) / 2 <= 2 (since cos^2F sin^2G <= S) and
+//    H1 >= -0.6 for w <= 1.2 rad, so D >= 2 a w (1 - 2.6 f) there.
+__device__ __forceinline__ double cap_lower_bound(const TileCap& a, const TileCap& b)
+{
+    const double dx = a.cx - b.cx, dy = a.cy - b.cy, dz = a.cz - b.cz;
+    const double cc = sqrt(dx * dx + dy * dy + dz * dz);
+    const double lo = cc - a.rho - b.rho;
+    if (!(lo > 0.0)) return 0.0;
+    if (cc + a.rho + b.rho >= 1.8640781719344526) return 0.0;  // 2 sin(1.2)
+    const double w = asin(0.5 * lo);
+    return 2.0 * 6378.137 * w * (1.0 - 2.6 / 298.257223563);
+}
+
+// Cap covering caps[first..last].
+__device__ __forceinline__ TileCap cap_union(const TileCap* caps, int first, int last)
+{
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    for (int q = first; q <= last; q++) {
+        sx += caps[q].cx;
+        sy += caps[q].cy;
+        sz += caps[q].cz;
+    }
+    const double nrm = sqrt(sx * sx + sy * sy + sz * sz);
+    TileCap u{sx / nrm, sy / nrm, sz / nrm, 0.0};
+    for (int q = first; q <= last; q++) {
+        const double dx = caps[q].cx - u.cx, dy = caps[q].cy - u.cy, dz = caps[q].cz - u.cz;
+        u.rho = fmax(u.rho, sqrt(dx * dx + dy * dy + dz * dz) + caps[q].rho);
+    }
+    u.rho = u.rho * (1.0 + 1e-12) + 1e-15;
+    return u;
 }
 #endif  // __CUDACC__
 

@@ -9,7 +9,7 @@
 namespace gwgpu {
 
 // Solve modes of launch_solve.
-enum SolveMode { kSolveAIC = 0, kSolveCV = 1, kSolveFit = 2 };
+enum SolveMode { kSolveAIC = 0, kSolveCV = 1, kSolveFit = 2, kSolveRefine = 3 };
 
 // Per-row k-th smallest distance (1-based rank).  [dlo, dhi] is the expected
 // range of positive distances; it only shapes the first histogram.
@@ -32,9 +32,10 @@ cudaError_t launch_build_z(int n, int p, const double* X, const double* y, doubl
 // G[i, c] = sum_j w_ij^wpow Z[j, c] for c < mcols, with w_ij = K(d_ij, r_i)
 // (r_i = thr[i], or bw when thr is null); exclude_self zeroes w_ii (CV).
 // FP64 SIMT, the weight matrix is produced tile by tile and never stored.
-cudaError_t launch_contract64(const DevPoints& P, bool geographic, const TileBox* tiles, const double* Z, int ldz,
-                              int mcols, double* G, int ldg, const double* thr, double bw, int kernel,
-                              bool exclude_self, int wpow, bool skip_tiles, cudaStream_t stream);
+// caps: geographic tile bounds (16-point tiles), needed to skip geographic tiles.
+cudaError_t launch_contract64(const DevPoints& P, bool geographic, const TileBox* tiles, const TileCap* caps,
+                              const double* Z, int ldz, int mcols, double* G, int ldg, const double* thr, double bw,
+                              int kernel, bool exclude_self, int wpow, bool skip_tiles, cudaStream_t stream);
 
 // Warp-per-location Cholesky solve of A_i beta_i = b_i and the per-location
 // criterion terms; partial sums per block in partials[block*4 + {0..3}] =
@@ -61,6 +62,8 @@ struct SolveArgs {
     const double* tinv;
     const double* tvec;
     int tcol;
+    // Refine mode: beta += A^-1 rvec (n x p), then the residuals are recomputed.
+    const double* rvec;
 };
 cudaError_t launch_solve(const SolveArgs& a, int* nblocks, cudaStream_t stream);
 
@@ -70,7 +73,8 @@ cudaError_t launch_reduce_partials(const double* partials, int nblocks, double* 
 // qdiag[j] = sum_i (delta_ij - s_ij)^2 with s_ij = w_ij v_i . x_j, w_ij =
 // K(d_ij, r_i); also writes S (n x n row-major, sorted order) when S != null
 // and row row_target of S into s_row (length n) when s_row != null.
-cudaError_t launch_hat_pass(const DevPoints& P, bool geographic, const TileBox* tiles, const double* X, int p,
+cudaError_t launch_hat_pass(const DevPoints& P, bool geographic, const TileBox* tiles, const TileCap* caps,
+                            const double* X, int p,
                             const double* v, const double* thr, double bw, int kernel, bool skip_tiles,
                             double* qdiag, double* S, int row_target, double* s_row, cudaStream_t stream);
 
@@ -93,6 +97,7 @@ struct TcArgs {
     int n, mcols, npad, ntiles;   // ntiles: 32-point tiles
     const float4* pts;            // planar: {u_hi, u_lo, v_hi, v_lo}; geographic: 3 float4 per point
     const TileBox* boxes;         // bounds of each 32-point tile
+    const TileCap* caps;          // geographic bounds of each 32-point tile (null: no geographic skipping)
     const unsigned char* zimg;    // per tile: [hi | lo] swizzled images, npad x 128 bytes each
     const float* thr;             // per-row threshold, or null for the fixed bandwidth bw
     float bw;
@@ -108,6 +113,22 @@ cudaError_t launch_build_zimg(int n, int mcols, int npad, const double* Z, int l
                               cudaStream_t stream);
 // D[128 x N] = A[128 x 32] B[N x 32]^T through tcgen05 (device pointers).
 cudaError_t launch_tc_selftest(const float* A, const float* B, float* D, int N, int* err, cudaStream_t stream);
+
+// Refinement residual of the mixed path: r_i = X~^T W_i (y~ - X~ beta_i) in
+// FP64 arithmetic over the FP32 weights of the contraction (n x p output).
+struct RefineArgs {
+    int n, p, ntiles, kernel, skip;
+    const float4* pts;
+    const TileBox* boxes;
+    const TileCap* caps;
+    const double* X;      // n x p row-major (X~)
+    const double* y;      // y~
+    const double* beta;   // n x p
+    const float* thr;
+    float bw;
+    double* r;            // n x p
+};
+cudaError_t launch_refine_residual(const RefineArgs& a, bool geographic, cudaStream_t stream);
 
 // Maximum pairwise distance (CRSDistance::maxDistance), as an ordered key in *key_out.
 cudaError_t launch_max_distance(const DevPoints& P, bool geographic, unsigned long long* key_out, int num_sms,

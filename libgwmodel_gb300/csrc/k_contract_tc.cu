@@ -18,6 +18,7 @@
 // largest threshold (planar boxes).  Waits are bounded and report through err.
 #include "gw_common.cuh"
 #include "gw_kernels.h"
+#include "mixed_weight.cuh"
 #include "tc05.cuh"
 
 namespace gwgpu {
@@ -38,67 +39,6 @@ struct Smem {
     uint32_t tmem_base;
     int abort;
 };
-
-__device__ __forceinline__ float sin_poly(float x)
-{
-    // Taylor series to x^13, |x| <= pi/2
-    float z = x * x;
-    float p = -1.6059043836821614e-10f;        // -1/13!
-    p = fmaf(p, z, 2.505210838544172e-08f);    //  1/11!
-    p = fmaf(p, z, -2.7557319223985893e-06f);  // -1/9!
-    p = fmaf(p, z, 1.984126984126984e-04f);    //  1/7!
-    p = fmaf(p, z, -8.333333333333333e-03f);   // -1/5!  (sign alternates: x - x^3/6 + ...)
-    p = fmaf(p, z, 1.6666666666666666e-01f);   //  1/3!
-    return x - x * z * p;
-}
-
-// FP32 great-circle distance (km) of the reference's Lambert formula with the
-// haversine term taken from the 3-D chord of hi/lo unit vectors.
-__device__ __forceinline__ float geo_dist32(const float4& fa, const float4& fb, const float4& fc, const float4& pa,
-                                            const float4& pb, const float4& pc)
-{
-    const float dx = (pa.x - fa.x) + (pb.x - fb.x);
-    const float dy = (pa.y - fa.y) + (pb.y - fb.y);
-    const float dz = (pa.z - fa.z) + (pb.z - fb.z);
-    const float S = 0.25f * fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    if (!(S > 0.0f)) return 0.0f;
-    const float C = fmaxf(1.0f - S, 0.0f);
-    const float sq = sqrtf(S), cq = sqrtf(C);
-    const float w = atan2f(sq, cq);
-    const float R = sq * cq / w;
-    const float dlat = (pa.w - fa.w) + (pb.w - fb.w);            // degrees
-    const float G = dlat * 8.7266462599716478846e-3f;            // (pi/180)/2
-    const float sG = sin_poly(G);
-    const float sG2 = sG * sG, cG2 = 1.0f - sG2;
-    const float sF = pc.x * fc.y + pc.y * fc.x;                  // sin((lat_a+lat_b)/2)
-    const float cF = pc.y * fc.y - pc.x * fc.x;
-    const float sF2 = sF * sF, cF2 = cF * cF;
-    const float H1 = (3.0f * R - 1.0f) / (2.0f * C);
-    const float H2 = (3.0f * R + 1.0f) / (2.0f * S);
-    const float f = 1.0f / 298.257223563f;
-    return 2.0f * 6378.137f * w * (1.0f + f * H1 * sF2 * cG2 - f * H2 * cF2 * sG2);
-}
-
-__device__ __forceinline__ float weight32(int kernel, float d2, float r, float inv_r2)
-{
-    switch (kernel) {
-    case GW_KERNEL_GAUSSIAN:
-        return __expf(-0.5f * d2 * inv_r2);
-    case GW_KERNEL_EXPONENTIAL:
-        return __expf(-sqrtf(d2) / r);
-    case GW_KERNEL_BISQUARE: {
-        float t = 1.0f - d2 * inv_r2;
-        return d2 < r * r ? t * t : 0.0f;
-    }
-    case GW_KERNEL_TRICUBE: {
-        float q = sqrtf(d2) / r;
-        float t = 1.0f - q * q * q;
-        return d2 < r * r ? t * t * t : 0.0f;
-    }
-    default:
-        return d2 < r * r ? 1.0f : 0.0f;
-    }
-}
 
 // Double-float accumulate: (hi, lo) += v.
 __device__ __forceinline__ float2 df_add(float2 a, float v)
@@ -163,6 +103,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
     // block box and largest threshold for tile skipping
     __shared__ float red[TC_THREADS / 32];
     __shared__ TileBox fbox;
+    __shared__ TileCap fcap_s;
     float rmax = row_ok ? rr : 0.0f;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, off));
@@ -176,12 +117,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
             b.vlo = fmin(b.vlo, c.vlo); b.vhi = fmax(b.vhi, c.vhi);
         }
         fbox = b;
+        if (GEO && a.caps) fcap_s = cap_union(a.caps, row0 / TC_BK, last / TC_BK);
     }
     __syncthreads();
     rmax = red[0];
     for (int q = 1; q < TC_THREADS / 32; q++) rmax = fmaxf(rmax, red[q]);
-    const bool can_skip = a.skip && !GEO && a.kernel >= GW_KERNEL_BISQUARE && rmax > 0.0f;
-    const double rmax_d = (double)rmax * (1.0 + 1e-5);
+    const bool can_skip = a.skip && (!GEO || a.caps) && a.kernel >= GW_KERNEL_BISQUARE && rmax > 0.0f;
+    const double rmax_d = (double)rmax * (1.0 + 1e-4);
+    const TileCap fcap = fcap_s;
 
     const uint32_t idesc = idesc_tf32(TC_M, a.npad);
     int issued = 0;        // stages issued so far (non-skipped tiles)
@@ -220,7 +163,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
 
     for (int tile = 0; tile < a.ntiles && !aborted; tile++) {
         if (can_skip) {
-            const double lb = box_lower_bound(fbox, a.boxes[tile]);
+            const double lb = GEO ? cap_lower_bound(fcap, a.caps[tile]) : box_lower_bound(fbox, a.boxes[tile]);
             if (lb * (1.0 - 1e-12) >= rmax_d) continue;  // uniform over the CTA
         }
         const int s = issued & 1;
@@ -247,18 +190,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
                 const int j = jbase + q4 * 4 + e;
                 float w = 0.0f;
                 if (row_ok && j < a.n) {
-                    float d2;
-                    if (GEO) {
-                        float d = geo_dist32(fa, fb, fc, a.pts[3 * (size_t)j], a.pts[3 * (size_t)j + 1],
-                                             a.pts[3 * (size_t)j + 2]);
-                        d2 = d * d;
-                    } else {
-                        const float4 p = a.pts[j];
-                        const float dx = (p.x - fa.x) + (p.y - fa.y);
-                        const float dy = (p.z - fa.z) + (p.w - fa.w);
-                        d2 = fmaf(dx, dx, dy * dy);
-                    }
-                    w = weight32(a.kernel, d2, rr, inv_r2);
+                    w = mixed_weight<GEO>(a.pts, j, fa, fb, fc, a.kernel, rr, inv_r2);
                     if (a.exclude_self && i == j) w = 0.0f;
                     if (a.wpow == 2) w = w * w;
                 }

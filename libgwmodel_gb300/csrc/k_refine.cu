@@ -1,0 +1,138 @@
+// k_refine.cu -- iterative refinement of the mixed-precision local solves.
+//
+// The tensor-core contraction gives A~_i and b~_i to about 1e-6 relative; the
+// Cholesky solve of A~_i beta = b~_i inherits that error times cond(A_i).  One
+// refinement step computes the residual of the local normal equation directly
+// from the data,
+//     r_i = sum_j w_ij x~_j (y~_j - x~_j^T beta_i)        (FP64 arithmetic),
+// with the very FP32 weights the contraction used, and then solves
+// A~_i delta = r_i with the existing factor (k_solve's refine mode).  The
+// residual is small, so its FP64 evaluation is what carries the accuracy.
+// One thread owns one focus row; data tiles beyond the block's largest
+// threshold are skipped exactly as in the contraction.
+#include "gw_common.cuh"
+#include "gw_kernels.h"
+#include "mixed_weight.cuh"
+
+namespace gwgpu {
+
+namespace {
+
+constexpr int RF_THREADS = 128;
+constexpr int RF_TILE = 32;
+
+template <bool GEO, int PMAX>
+__global__ void __launch_bounds__(RF_THREADS) k_refine(RefineArgs a)
+{
+    extern __shared__ double rsm[];  // RF_TILE x (p + 1): x~_j then y~_j
+    __shared__ TileBox fbox;
+    __shared__ TileCap fcap_s;
+    __shared__ float red[RF_THREADS / 32];
+    const int p = a.p, pp = a.p + 1;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int row0 = blockIdx.x * RF_THREADS;
+    const int i = row0 + t;
+    const bool ok = i < a.n;
+
+    float4 fa = make_float4(0.f, 0.f, 0.f, 0.f), fb = fa, fc = fa;
+    if (ok) {
+        if (GEO) {
+            fa = a.pts[3 * (size_t)i];
+            fb = a.pts[3 * (size_t)i + 1];
+            fc = a.pts[3 * (size_t)i + 2];
+        } else {
+            fa = a.pts[i];
+        }
+    }
+    const float rr = ok ? (a.thr ? a.thr[i] : a.bw) : 1.0f;
+    const float inv_r2 = 1.0f / (rr * rr);
+    double beta[PMAX], r[PMAX];
+#pragma unroll
+    for (int k = 0; k < PMAX; k++) {
+        beta[k] = (ok && k < p) ? a.beta[(size_t)i * p + k] : 0.0;
+        r[k] = 0.0;
+    }
+    float rmax = ok ? rr : 0.0f;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, off));
+    if (lane == 0) red[warp] = rmax;
+    if (t == 0) {
+        const int last = min(row0 + RF_THREADS, a.n) - 1;
+        TileBox b = a.boxes[row0 / RF_TILE];
+        for (int q = row0 / RF_TILE + 1; q <= last / RF_TILE; q++) {
+            TileBox c = a.boxes[q];
+            b.ulo = fmin(b.ulo, c.ulo); b.uhi = fmax(b.uhi, c.uhi);
+            b.vlo = fmin(b.vlo, c.vlo); b.vhi = fmax(b.vhi, c.vhi);
+        }
+        fbox = b;
+        if (GEO && a.caps) fcap_s = cap_union(a.caps, row0 / RF_TILE, last / RF_TILE);
+    }
+    __syncthreads();
+    rmax = red[0];
+    for (int q = 1; q < RF_THREADS / 32; q++) rmax = fmaxf(rmax, red[q]);
+    const bool can_skip = a.skip && (!GEO || a.caps) && a.kernel >= GW_KERNEL_BISQUARE && rmax > 0.0f;
+    const double rmax_d = (double)rmax * (1.0 + 1e-4);
+    const TileCap fcap = fcap_s;
+
+    for (int tile = 0; tile < a.ntiles; tile++) {
+        if (can_skip) {
+            const double lb = GEO ? cap_lower_bound(fcap, a.caps[tile]) : box_lower_bound(fbox, a.boxes[tile]);
+            if (lb * (1.0 - 1e-12) >= rmax_d) continue;
+        }
+        const int j0 = tile * RF_TILE;
+        for (int e = t; e < RF_TILE * pp; e += RF_THREADS) {
+            const int q = e / pp, c = e - q * pp;
+            const int j = j0 + q;
+            rsm[e] = (j < a.n) ? (c < p ? a.X[(size_t)j * p + c] : a.y[j]) : 0.0;
+        }
+        __syncthreads();
+        if (ok) {
+            const int qend = min(RF_TILE, a.n - j0);
+            for (int q = 0; q < qend; q++) {
+                const float w = mixed_weight<GEO>(a.pts, j0 + q, fa, fb, fc, a.kernel, rr, inv_r2);
+                if (w == 0.0f) continue;
+                const double* xj = rsm + q * pp;
+                double e = xj[p];
+#pragma unroll
+                for (int k = 0; k < PMAX; k++)
+                    if (k < p) e -= xj[k] * beta[k];
+                const double we = (double)w * e;
+#pragma unroll
+                for (int k = 0; k < PMAX; k++)
+                    if (k < p) r[k] += we * xj[k];
+            }
+        }
+        __syncthreads();
+    }
+    if (ok)
+        for (int k = 0; k < p; k++) a.r[(size_t)i * p + k] = r[k];
+}
+
+template <bool GEO, int PMAX>
+cudaError_t launch_pm(const RefineArgs& a, cudaStream_t s)
+{
+    const int grid = (a.n + RF_THREADS - 1) / RF_THREADS;
+    const size_t smem = (size_t)RF_TILE * (a.p + 1) * sizeof(double);
+    k_refine<GEO, PMAX><<<grid, RF_THREADS, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <bool GEO>
+cudaError_t launch_geo(const RefineArgs& a, cudaStream_t s)
+{
+    if (a.p <= 4) return launch_pm<GEO, 4>(a, s);
+    if (a.p <= 8) return launch_pm<GEO, 8>(a, s);
+    if (a.p <= 12) return launch_pm<GEO, 12>(a, s);
+    if (a.p <= 16) return launch_pm<GEO, 16>(a, s);
+    if (a.p <= 21) return launch_pm<GEO, 21>(a, s);
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+cudaError_t launch_refine_residual(const RefineArgs& a, bool geographic, cudaStream_t stream)
+{
+    return geographic ? launch_geo<true>(a, stream) : launch_geo<false>(a, stream);
+}
+
+}  // namespace gwgpu

@@ -121,13 +121,21 @@ __global__ void __launch_bounds__(SV_WARPS * 32) k_solve(SolveArgs a)
             __syncwarp();
             continue;
         }
-        const double z = fwd_solve(L, ld, p, lane, bvec);
-        const double beta = bwd_solve(L, ld, p, lane, z);
+        double beta;
+        if (MODE == kSolveRefine) {
+            const double rv = lane < p ? a.rvec[(size_t)row * p + lane] : 0.0;
+            const double delta = bwd_solve(L, ld, p, lane, fwd_solve(L, ld, p, lane, rv));
+            beta = (lane < p ? a.beta[(size_t)row * p + lane] : 0.0) + delta;
+        } else {
+            beta = bwd_solve(L, ld, p, lane, fwd_solve(L, ld, p, lane, bvec));
+        }
         if (lane < p) a.beta[(size_t)row * p + lane] = beta;
         const double yhat = warp_sum(lane < p ? xr * beta : 0.0);
         const double res = a.y[row] - yhat;
         double sii = 0.0;
-        if (MODE != kSolveCV) {
+        if (MODE == kSolveRefine) {
+            sii = a.sii[row];
+        } else if (MODE != kSolveCV) {
             const double u = fwd_solve(L, ld, p, lane, xr);
             const double uu = warp_sum(lane < p ? u * u : 0.0);
             const double rr = a.thr ? a.thr[row] : a.bw;
@@ -218,7 +226,8 @@ constexpr int HAT_TILE = kTile;
 
 template <bool GEO>
 __global__ void __launch_bounds__(HAT_THREADS)
-    k_hat(DevPoints P, const TileBox* __restrict__ tiles, const double* __restrict__ X, int p,
+    k_hat(DevPoints P, const TileBox* __restrict__ tiles, const TileCap* __restrict__ caps,
+          const double* __restrict__ X, int p,
           const double* __restrict__ v, const double* __restrict__ thr, double bw, int kernel, int skip,
           double* __restrict__ qdiag, double* __restrict__ S, int row_target, double* __restrict__ s_row)
 {
@@ -227,6 +236,7 @@ __global__ void __launch_bounds__(HAT_THREADS)
     double* sV = sX + HAT_THREADS * p;         // HAT_TILE x p   (v_i of the staged rows)
     __shared__ double su[HAT_TILE], sv[HAT_TILE], suR[HAT_TILE], svR[HAT_TILE], sr[HAT_TILE];
     __shared__ TileBox sblock;
+    __shared__ TileCap scap;
     const int n = P.n, t = threadIdx.x;
     const int j0 = blockIdx.x * HAT_THREADS, j = j0 + t;
     for (int e = t; e < HAT_THREADS * p; e += HAT_THREADS) {
@@ -242,6 +252,7 @@ __global__ void __launch_bounds__(HAT_THREADS)
             b.vlo = fmin(b.vlo, c.vlo); b.vhi = fmax(b.vhi, c.vhi);
         }
         sblock = b;
+        if (GEO && caps) scap = cap_union(caps, j0 / HAT_TILE, last / HAT_TILE);
     }
     __syncthreads();
     double du = 0.0, dv = 0.0, duR = 0.0, dvR = 0.0;
@@ -249,7 +260,7 @@ __global__ void __launch_bounds__(HAT_THREADS)
         du = P.u[j]; dv = P.v[j];
         if (GEO) { duR = P.uR[j]; dvR = P.vR[j]; }
     }
-    const bool can_skip = skip && !GEO && kernel >= GW_KERNEL_BISQUARE;
+    const bool can_skip = skip && (!GEO || caps) && kernel >= GW_KERNEL_BISQUARE;
     double acc = 0.0;
     const int ntiles = (n + HAT_TILE - 1) / HAT_TILE;
     for (int tile = 0; tile < ntiles; tile++) {
@@ -257,7 +268,8 @@ __global__ void __launch_bounds__(HAT_THREADS)
         if (can_skip) {
             double rmax = -1.0;
             for (int q = 0; q < HAT_TILE && i0 + q < n; q++) rmax = fmax(rmax, thr ? thr[i0 + q] : bw);
-            if (rmax > 0.0 && box_lower_bound(sblock, tiles[tile]) * (1.0 - 1e-14) >= rmax) continue;
+            const double lb = GEO ? cap_lower_bound(scap, caps[tile]) * (1.0 - 1e-9) : box_lower_bound(sblock, tiles[tile]);
+            if (rmax > 0.0 && lb * (1.0 - 1e-14) >= rmax) continue;
         }
         if (t < HAT_TILE) {
             int i = i0 + t;
@@ -394,6 +406,10 @@ cudaError_t launch_solve(const SolveArgs& a, int* nblocks, cudaStream_t stream)
         cudaFuncSetAttribute(k_solve<kSolveCV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_solve<kSolveCV><<<grid, SV_WARPS * 32, smem, stream>>>(a);
         break;
+    case kSolveRefine:
+        cudaFuncSetAttribute(k_solve<kSolveRefine>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_solve<kSolveRefine><<<grid, SV_WARPS * 32, smem, stream>>>(a);
+        break;
     default:
         cudaFuncSetAttribute(k_solve<kSolveFit>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_solve<kSolveFit><<<grid, SV_WARPS * 32, smem, stream>>>(a);
@@ -408,17 +424,18 @@ cudaError_t launch_reduce_partials(const double* partials, int nblocks, double* 
     return cudaGetLastError();
 }
 
-cudaError_t launch_hat_pass(const DevPoints& P, bool geographic, const TileBox* tiles, const double* X, int p,
+cudaError_t launch_hat_pass(const DevPoints& P, bool geographic, const TileBox* tiles, const TileCap* caps,
+                            const double* X, int p,
                             const double* v, const double* thr, double bw, int kernel, bool skip_tiles,
                             double* qdiag, double* S, int row_target, double* s_row, cudaStream_t stream)
 {
     int grid = (P.n + HAT_THREADS - 1) / HAT_THREADS;
     size_t smem = (size_t)(HAT_THREADS + HAT_TILE) * p * sizeof(double);
     if (geographic)
-        k_hat<true><<<grid, HAT_THREADS, smem, stream>>>(P, tiles, X, p, v, thr, bw, kernel, skip_tiles ? 1 : 0,
+        k_hat<true><<<grid, HAT_THREADS, smem, stream>>>(P, tiles, caps, X, p, v, thr, bw, kernel, skip_tiles ? 1 : 0,
                                                          qdiag, S, row_target, s_row);
     else
-        k_hat<false><<<grid, HAT_THREADS, smem, stream>>>(P, tiles, X, p, v, thr, bw, kernel, skip_tiles ? 1 : 0,
+        k_hat<false><<<grid, HAT_THREADS, smem, stream>>>(P, tiles, caps, X, p, v, thr, bw, kernel, skip_tiles ? 1 : 0,
                                                           qdiag, S, row_target, s_row);
     return cudaGetLastError();
 }
