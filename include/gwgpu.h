@@ -137,6 +137,7 @@ typedef struct gwgpu_stats {
     double contract_bytes;
     int select_launches;
     double select_ms;
+    long long kernel_launches;  /* every kernel the engine launched */
 } gwgpu_stats;
 
 int gwgpu_engine_create(int device, gwgpu_engine** out);
@@ -153,6 +154,16 @@ int gwgpu_engine_global_criterion(gwgpu_engine* e, int ncols, const int* cols, d
 int gwgpu_engine_fit(gwgpu_engine* e, double bandwidth, int adaptive, int kernel, int store_s, double* betas,
                      double* betas_se, double* shat, double* qdiag, double* s);
 int gwgpu_engine_max_distance(gwgpu_engine* e, double* out);
+/* BandwidthSelector::optimize (BandwidthSelector.cpp:6-81) on the resident
+ * data: writes the chosen bandwidth and up to cap (bandwidth, criterion)
+ * pairs sorted by bandwidth; *count receives their number. */
+int gwgpu_engine_golden(gwgpu_engine* e, int adaptive, int kernel, int criterion, double lower, double upper,
+                        double* bandwidth, int* count, double* list_bw, double* list_value, int cap);
+/* Drop the dataset's cached order statistics and distance histograms. */
+int gwgpu_engine_clear_cache(gwgpu_engine* e);
+/* CUDA events on the engine's stream, slots 0..7: device-side timing. */
+int gwgpu_engine_event_record(gwgpu_engine* e, int slot);
+int gwgpu_engine_event_elapsed(gwgpu_engine* e, int first, int second, float* ms);
 int gwgpu_engine_thresholds(gwgpu_engine* e, double bandwidth, int adaptive, double* out /* n */);
 int gwgpu_engine_enable_stats(gwgpu_engine* e, int on);
 int gwgpu_engine_get_stats(gwgpu_engine* e, gwgpu_stats* out);

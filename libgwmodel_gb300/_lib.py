@@ -39,7 +39,7 @@ class Stats(ctypes.Structure):
     _fields_ = [("criterion_evals", ctypes.c_int), ("contract_launches", ctypes.c_int),
                 ("contract_ms", ctypes.c_double), ("contract_flops", ctypes.c_double),
                 ("contract_bytes", ctypes.c_double), ("select_launches", ctypes.c_int),
-                ("select_ms", ctypes.c_double)]
+                ("select_ms", ctypes.c_double), ("kernel_launches", ctypes.c_longlong)]
 
 
 # (name, restype, argtypes) of every function declared in include/gwgpu.h
@@ -90,6 +90,10 @@ SIGNATURES = [
     ("gwgpu_engine_global_criterion", _i, [_vp, _i, _ip, _dp]),
     ("gwgpu_engine_fit", _i, [_vp, _d, _i, _i, _i, _dp, _dp, _dp, _dp, _dp]),
     ("gwgpu_engine_max_distance", _i, [_vp, _dp]),
+    ("gwgpu_engine_golden", _i, [_vp, _i, _i, _i, _d, _d, _dp, _ip, _dp, _dp, _i]),
+    ("gwgpu_engine_clear_cache", _i, [_vp]),
+    ("gwgpu_engine_event_record", _i, [_vp, _i]),
+    ("gwgpu_engine_event_elapsed", _i, [_vp, _i, _i, ctypes.POINTER(ctypes.c_float)]),
     ("gwgpu_engine_thresholds", _i, [_vp, _d, _i, _dp]),
     ("gwgpu_engine_enable_stats", _i, [_vp, _i]),
     ("gwgpu_engine_get_stats", _i, [_vp, ctypes.POINTER(Stats)]),

@@ -3,6 +3,7 @@
 
 #include <cfloat>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <new>
 #include <string>
@@ -437,6 +438,46 @@ int gwgpu_engine_max_distance(gwgpu_engine* e, double* out)
     return guarded([&] { *out = e->eng.maxDistance(); });
 }
 
+int gwgpu_engine_golden(gwgpu_engine* e, int adaptive, int kernel, int criterion, double lower, double upper,
+                        double* bandwidth, int* count, double* list_bw, double* list_value, int cap)
+{
+    ENG_CHECK(e);
+    if (!bandwidth) return fail(GWGPU_ERR_INVALID, "null output");
+    if (kernel < 0 || kernel > 4) return fail(GWGPU_ERR_INVALID, "unknown kernel");
+    return guarded([&] {
+        std::map<double, double> rec;
+        *bandwidth = e->eng.golden(adaptive != 0, kernel, criterion, lower, upper, rec);
+        int k = 0;
+        for (auto& kv : rec) {
+            if (k < cap) {
+                if (list_bw) list_bw[k] = kv.first;
+                if (list_value) list_value[k] = kv.second;
+            }
+            k++;
+        }
+        if (count) *count = k;
+    });
+}
+
+int gwgpu_engine_clear_cache(gwgpu_engine* e)
+{
+    ENG_CHECK(e);
+    return guarded([&] { e->eng.clearCaches(); });
+}
+
+int gwgpu_engine_event_record(gwgpu_engine* e, int slot)
+{
+    ENG_CHECK(e);
+    return guarded([&] { e->eng.recordEvent(slot); });
+}
+
+int gwgpu_engine_event_elapsed(gwgpu_engine* e, int first, int second, float* ms)
+{
+    ENG_CHECK(e);
+    if (!ms) return fail(GWGPU_ERR_INVALID, "null output");
+    return guarded([&] { *ms = e->eng.elapsedMs(first, second); });
+}
+
 int gwgpu_engine_thresholds(gwgpu_engine* e, double bandwidth, int adaptive, double* out)
 {
     ENG_CHECK(e);
@@ -467,6 +508,7 @@ int gwgpu_engine_get_stats(gwgpu_engine* e, gwgpu_stats* out)
     out->contract_bytes = s.contract_bytes;
     out->select_launches = s.select_launches;
     out->select_ms = s.select_ms;
+    out->kernel_launches = s.kernel_launches;
     return GWGPU_OK;
 }
 

@@ -8,6 +8,7 @@
 #include <numeric>
 
 #include "gw_kernels.h"
+#include "golden.h"
 
 namespace gwgpu {
 
@@ -86,6 +87,8 @@ Engine::Engine(int device) : device_(device)
 Engine::~Engine()
 {
     if (stream_) cudaStreamSynchronize(stream_);
+    for (auto& e : events_)
+        if (e) cudaEventDestroy(e);
     if (host_sums_) cudaFreeHost(host_sums_);
     if (stream_) cudaStreamDestroy(stream_);
 }
@@ -225,79 +228,21 @@ void Engine::setData(int n, int p, const double* x, const double* y, const doubl
     hy_ = std::move(hy);
     hu_ = std::move(hu);
     hv_ = std::move(hv);
+    ranks_.clear();
+    hist_.release();
+    hist_tried_ = false;
+    hist_valid_ = false;
+    buildProxy();
 }
 
-// Mixed-precision operands: X and y centred (when a constant column is the
-// intercept) and scaled, Z~ split into TF32 hi/lo swizzled tile images, FP32
-// hi/lo coordinates, 32-point tile boxes.
-void Engine::ensureMixed()
+
+// FP32 proxy coordinates and 32-point tile bounds shared by the select and the
+// mixed path.
+void Engine::buildProxy()
 {
-    if (mixed_ready_) return;
     const int n = n_, p = p_;
-    if (m_ > 256) throw std::invalid_argument("mixed precision supports at most 21 columns of X");
-    intercept_col_ = -1;
-    for (int k = 0; k < p && intercept_col_ < 0; k++) {
-        const double c0 = hx_[k];
-        bool constant = c0 != 0.0;
-        for (int s = 1; s < n && constant; s++) constant = hx_[(size_t)s * p + k] == c0;
-        if (constant) intercept_col_ = k;
-    }
-    mu_.assign(p, 0.0);
-    sc_.assign(p, 1.0);
-    for (int k = 0; k < p; k++) {
-        if (k == intercept_col_) {
-            sc_[k] = hx_[k];
-            continue;
-        }
-        double mean = 0.0;
-        if (intercept_col_ >= 0) {
-            for (int s = 0; s < n; s++) mean += hx_[(size_t)s * p + k];
-            mean /= n;
-        }
-        double ss = 0.0;
-        for (int s = 0; s < n; s++) {
-            double d = hx_[(size_t)s * p + k] - mean;
-            ss += d * d;
-        }
-        double sd = std::sqrt(ss / n);
-        mu_[k] = mean;
-        sc_[k] = (sd > 0.0 && std::isfinite(sd)) ? sd : 1.0;
-    }
-    mu_y_ = 0.0;
-    if (intercept_col_ >= 0) {
-        for (int s = 0; s < n; s++) mu_y_ += hy_[s];
-        mu_y_ /= n;
-    }
-    double ssy = 0.0;
-    for (int s = 0; s < n; s++) ssy += (hy_[s] - mu_y_) * (hy_[s] - mu_y_);
-    s_y_ = std::sqrt(ssy / n);
-    if (!(s_y_ > 0.0) || !std::isfinite(s_y_)) s_y_ = 1.0;
-
-    std::vector<double> xs((size_t)n * p), ys(n);
-    for (int s = 0; s < n; s++) {
-        for (int k = 0; k < p; k++) xs[(size_t)s * p + k] = (hx_[(size_t)s * p + k] - mu_[k]) / sc_[k];
-        ys[s] = (hy_[s] - mu_y_) / s_y_;
-    }
-    std::vector<double> tinv(p), tvec(p, 0.0);
-    for (int k = 0; k < p; k++) tinv[k] = 1.0 / sc_[k];
-    if (intercept_col_ >= 0) {
-        const double c = sc_[intercept_col_];
-        for (int k = 0; k < p; k++) tvec[k] = (k == intercept_col_) ? 1.0 / c : -mu_[k] / (c * sc_[k]);
-    }
-
-    npad_ = (m_ + 31) / 32 * 32;
     ntiles32_ = (n + 31) / 32;
-    xs_.alloc((size_t)n * p);
-    ys_.alloc(n);
-    zs_.alloc((size_t)n * m_);
-    zimg_.alloc((size_t)ntiles32_ * 2 * npad_ * 128);
-    acc_.alloc((size_t)n * npad_);
-    thr32_.alloc(n);
-    err_.alloc(1);
-    tinv_.alloc(p);
-    tvec_.alloc(p);
     boxes32_.alloc(ntiles32_);
-
     std::vector<TileBox> bx(ntiles32_);
     for (int t = 0; t < ntiles32_; t++) {
         TileBox b{hu_[t * 32], hu_[t * 32], hv_[t * 32], hv_[t * 32]};
@@ -361,6 +306,131 @@ void Engine::ensureMixed()
           "H2D pts32");
     check(cudaMemcpyAsync(boxes32_.get(), bx.data(), sizeof(TileBox) * bx.size(), cudaMemcpyHostToDevice, stream_),
           "H2D boxes");
+    // FP32 tile bounds of 32- and 16-point tiles (rounded outward, with an
+    // absolute slack of a few ulp of the largest relative coordinate)
+    auto make_tb = [&](int size) {
+        const int nt = (n + size - 1) / size;
+        std::vector<float4> tb(nt);
+        if (!geographic_) {
+            double uc = 0.0, vc = 0.0, maxabs = 0.0;
+            for (int s = 0; s < n; s++) {
+                uc += hu_[s];
+                vc += hv_[s];
+            }
+            uc /= n;
+            vc /= n;
+            for (int s = 0; s < n; s++) maxabs = std::max(maxabs, std::max(std::fabs(hu_[s] - uc), std::fabs(hv_[s] - vc)));
+            const double slack = std::ldexp(maxabs, -20);
+            for (int t = 0; t < nt; t++) {
+                double ulo = hu_[t * size], uhi = ulo, vlo = hv_[t * size], vhi = vlo;
+                for (int s = t * size; s < std::min(n, (t + 1) * size); s++) {
+                    ulo = std::min(ulo, hu_[s]);
+                    uhi = std::max(uhi, hu_[s]);
+                    vlo = std::min(vlo, hv_[s]);
+                    vhi = std::max(vhi, hv_[s]);
+                }
+                tb[t] = make_float4(nextafterf((float)(ulo - uc - slack), -INFINITY),
+                                    nextafterf((float)(uhi - uc + slack), INFINITY),
+                                    nextafterf((float)(vlo - vc - slack), -INFINITY),
+                                    nextafterf((float)(vhi - vc + slack), INFINITY));
+            }
+        } else {
+            std::vector<TileCap> cp = make_caps(hu_, hv_, size);
+            for (int t = 0; t < nt; t++)
+                tb[t] = make_float4((float)cp[t].cx, (float)cp[t].cy, (float)cp[t].cz,
+                                    nextafterf((float)cp[t].rho, INFINITY) * (1.0f + 1e-6f) + 1e-7f);
+        }
+        return tb;
+    };
+    std::vector<float4> tb = make_tb(32), t16 = make_tb(16);
+    if (!geographic_) {
+        sel_eps_ = std::ldexp(1.0, -18);
+        sel_delta_ = std::ldexp(dhi_, -36);
+    } else {
+        sel_eps_ = std::ldexp(1.0, -12);
+        sel_delta_ = 1e-6;
+    }
+    tbsel_.alloc(tb.size());
+    check(cudaMemcpyAsync(tbsel_.get(), tb.data(), sizeof(float4) * tb.size(), cudaMemcpyHostToDevice, stream_),
+          "H2D tile bounds");
+    tb16_.alloc(t16.size());
+    check(cudaMemcpyAsync(tb16_.get(), t16.data(), sizeof(float4) * t16.size(), cudaMemcpyHostToDevice, stream_),
+          "H2D tile bounds");
+    tile_thr16_.alloc(t16.size());
+    sel_err_.alloc(1);
+    check(cudaMemsetAsync(sel_err_.get(), 0, sizeof(int), stream_), "memset");
+    synchronize();
+}
+
+// Mixed-precision operands: X and y centred (when a constant column is the
+// intercept) and scaled, Z~ split into TF32 hi/lo swizzled tile images, FP32
+// hi/lo coordinates, 32-point tile boxes.
+void Engine::ensureMixed()
+{
+    if (mixed_ready_) return;
+    const int n = n_, p = p_;
+    if (m_ > 256) throw std::invalid_argument("mixed precision supports at most 21 columns of X");
+    intercept_col_ = -1;
+    for (int k = 0; k < p && intercept_col_ < 0; k++) {
+        const double c0 = hx_[k];
+        bool constant = c0 != 0.0;
+        for (int s = 1; s < n && constant; s++) constant = hx_[(size_t)s * p + k] == c0;
+        if (constant) intercept_col_ = k;
+    }
+    mu_.assign(p, 0.0);
+    sc_.assign(p, 1.0);
+    for (int k = 0; k < p; k++) {
+        if (k == intercept_col_) {
+            sc_[k] = hx_[k];
+            continue;
+        }
+        double mean = 0.0;
+        if (intercept_col_ >= 0) {
+            for (int s = 0; s < n; s++) mean += hx_[(size_t)s * p + k];
+            mean /= n;
+        }
+        double ss = 0.0;
+        for (int s = 0; s < n; s++) {
+            double d = hx_[(size_t)s * p + k] - mean;
+            ss += d * d;
+        }
+        double sd = std::sqrt(ss / n);
+        mu_[k] = mean;
+        sc_[k] = (sd > 0.0 && std::isfinite(sd)) ? sd : 1.0;
+    }
+    mu_y_ = 0.0;
+    if (intercept_col_ >= 0) {
+        for (int s = 0; s < n; s++) mu_y_ += hy_[s];
+        mu_y_ /= n;
+    }
+    double ssy = 0.0;
+    for (int s = 0; s < n; s++) ssy += (hy_[s] - mu_y_) * (hy_[s] - mu_y_);
+    s_y_ = std::sqrt(ssy / n);
+    if (!(s_y_ > 0.0) || !std::isfinite(s_y_)) s_y_ = 1.0;
+
+    std::vector<double> xs((size_t)n * p), ys(n);
+    for (int s = 0; s < n; s++) {
+        for (int k = 0; k < p; k++) xs[(size_t)s * p + k] = (hx_[(size_t)s * p + k] - mu_[k]) / sc_[k];
+        ys[s] = (hy_[s] - mu_y_) / s_y_;
+    }
+    std::vector<double> tinv(p), tvec(p, 0.0);
+    for (int k = 0; k < p; k++) tinv[k] = 1.0 / sc_[k];
+    if (intercept_col_ >= 0) {
+        const double c = sc_[intercept_col_];
+        for (int k = 0; k < p; k++) tvec[k] = (k == intercept_col_) ? 1.0 / c : -mu_[k] / (c * sc_[k]);
+    }
+
+    npad_ = (m_ + 63) / 64 * 64;
+    xs_.alloc((size_t)n * p);
+    ys_.alloc(n);
+    zs_.alloc((size_t)n * m_);
+    zimg_.alloc((size_t)ntiles32_ * 2 * npad_ * 128);
+    acc_.alloc((size_t)n * npad_);
+    thr32_.alloc(n);
+    err_.alloc(1);
+    tinv_.alloc(p);
+    tvec_.alloc(p);
+
     check(cudaMemcpyAsync(xs_.get(), xs.data(), sizeof(double) * xs.size(), cudaMemcpyHostToDevice, stream_),
           "H2D xs");
     check(cudaMemcpyAsync(ys_.get(), ys.data(), sizeof(double) * n, cudaMemcpyHostToDevice, stream_), "H2D ys");
@@ -377,7 +447,10 @@ void Engine::contractMixed(double* G, int ldg, int mcols, double bw, bool adapti
                            int wpow)
 {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    if (adaptive) check(launch_to_float(n_, thr_.get(), thr32_.get(), stream_), "thr32");
+    if (adaptive) {
+        check(launch_to_float(n_, thr_.get(), thr32_.get(), stream_), "thr32");
+        stats_.kernel_launches += 1;
+    }
     if (stats_on_) {
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
@@ -389,8 +462,7 @@ void Engine::contractMixed(double* G, int ldg, int mcols, double bw, bool adapti
     a.npad = npad_;
     a.ntiles = ntiles32_;
     a.pts = pts32_.get();
-    a.boxes = boxes32_.get();
-    a.caps = caps32_.get();
+    a.tb = tbsel_.get();
     a.zimg = zimg_.get();
     a.thr = adaptive ? thr32_.get() : nullptr;
     a.bw = (float)bw;
@@ -404,6 +476,7 @@ void Engine::contractMixed(double* G, int ldg, int mcols, double bw, bool adapti
     a.ldg = ldg;
     a.err = err_.get();
     check(launch_contract_tc(a, geographic_, stream_), "contract_tc");
+    stats_.kernel_launches += 1;
     if (stats_on_) {
         cudaEventRecord(e1, stream_);
         cudaEventSynchronize(e1);
@@ -440,11 +513,53 @@ void Engine::tcSelftest(int N, const float* A, const float* B, float* D)
     if (err) throw CudaError("tensor-core self-test: a bounded wait timed out");
 }
 
+// Per-row order statistic of the given rank (1-based), computed once and kept
+// for the dataset.  The first select also stores every row's histogram of
+// proxy distances, so later ranks start from the right histogram bin.
+const double* Engine::orderStatistic(unsigned rank)
+{
+    const bool exact = precision_ == kFP64;
+    for (auto& e : ranks_)
+        if (e->exact == exact && e->rank == rank) return e->v.get();
+    if (ranks_.size() >= 64) ranks_.clear();
+    if (!hist_tried_) {
+        hist_tried_ = true;
+        const size_t bytes = (size_t)n_ * 4096 * sizeof(unsigned);
+        size_t free_b = 0, total_b = 0;
+        cudaMemGetInfo(&free_b, &total_b);
+        if (bytes < free_b / 4) hist_.alloc((size_t)n_ * 4096);
+        hist_valid_ = false;
+    }
+    std::unique_ptr<RankStat> r(new RankStat);
+    r->rank = rank;
+    r->exact = exact;
+    r->v.alloc(n_);
+    SelectArgs a{};
+    a.n = n_;
+    a.ntiles = ntiles32_;
+    a.P = points();
+    a.pts = pts32_.get();
+    a.tb = tbsel_.get();
+    a.hist_cache = hist_.get();
+    a.cache_valid = hist_valid_ ? 1 : 0;
+    a.rank = rank;
+    a.dlo = dlo_;
+    a.dhi = dhi_;
+    a.eps = sel_eps_;
+    a.delta = sel_delta_;
+    a.out = r->v.get();
+    a.err = sel_err_.get();
+    check(launch_select(a, geographic_, exact, num_sms_, stream_), "select");
+    stats_.kernel_launches += 1;
+    if (hist_.get()) hist_valid_ = true;
+    ranks_.push_back(std::move(r));
+    return ranks_.back()->v.get();
+}
+
 void Engine::computeThresholds(double bw, bool adaptive)
 {
     if (!adaptive) return;
-    if (thr_valid_ && thr_bw_ == bw) return;
-    const DevPoints P = points();
+    if (thr_valid_ && thr_bw_ == bw && thr_prec_ == precision_) return;
     const double dn = bw / n_;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (stats_on_) {
@@ -457,18 +572,15 @@ void Engine::computeThresholds(double bw, bool adaptive)
         const double b0 = std::floor(bw), bx = bw - b0;
         const long long r0 = (long long)(int)b0;
         if (r0 < 1 || r0 >= n_) throw std::out_of_range("Mat::operator(): index out of bounds");
-        check(launch_select(P, geographic_, (unsigned)r0, dlo_, dhi_, sel0_.get(), num_sms_, stream_), "select");
-        const double* d1 = nullptr;
-        if (bx != 0.0) {
-            check(launch_select(P, geographic_, (unsigned)(r0 + 1), dlo_, dhi_, sel1_.get(), num_sms_, stream_),
-                  "select");
-            d1 = sel1_.get();
-        }
-        check(launch_threshold_combine(n_, bw, sel0_.get(), d1, thr_.get(), stream_), "threshold");
+        const double* d0 = orderStatistic((unsigned)r0);
+        const double* d1 = bx != 0.0 ? orderStatistic((unsigned)(r0 + 1)) : nullptr;
+        check(launch_threshold_combine(n_, bw, d0, d1, thr_.get(), stream_), "threshold");
+    stats_.kernel_launches += 1;
     } else {
         // fixbw = dn * max(dist) (BandwidthWeight.cpp:50-53)
-        check(launch_select(P, geographic_, (unsigned)n_, dlo_, dhi_, sel0_.get(), num_sms_, stream_), "select");
-        check(launch_threshold_combine(n_, bw, sel0_.get(), nullptr, thr_.get(), stream_), "threshold");
+        const double* dmax = orderStatistic((unsigned)n_);
+        check(launch_threshold_combine(n_, bw, dmax, nullptr, thr_.get(), stream_), "threshold");
+    stats_.kernel_launches += 1;
     }
     if (stats_on_) {
         cudaEventRecord(e1, stream_);
@@ -482,6 +594,7 @@ void Engine::computeThresholds(double bw, bool adaptive)
     }
     thr_valid_ = true;
     thr_bw_ = bw;
+    thr_prec_ = precision_;
 }
 
 void Engine::contract(const double* Z, int mcols, double* G, int ldg, double bw, bool adaptive, int kernel,
@@ -493,9 +606,10 @@ void Engine::contract(const double* Z, int mcols, double* G, int ldg, double bw,
         cudaEventCreate(&e1);
         cudaEventRecord(e0, stream_);
     }
-    check(launch_contract64(points(), geographic_, tiles_.get(), caps_.get(), Z, m_, mcols, G, ldg, thrPtr(adaptive),
-                            bw, kernel, exclude_self, wpow, true, stream_),
+    check(launch_contract64(points(), geographic_, tb16_.get(), Z, m_, mcols, G, ldg, thrPtr(adaptive), bw, kernel,
+                            exclude_self, wpow, true, stream_),
           "contract64");
+    stats_.kernel_launches += 1;
     if (stats_on_) {
         cudaEventRecord(e1, stream_);
         cudaEventSynchronize(e1);
@@ -545,8 +659,14 @@ void Engine::solve(int mode, double bw, bool adaptive, int kernel, double out[4]
     check(launch_reduce_partials(partials_.get(), nb, sums_.get(), stream_), "reduce");
     check(cudaMemcpyAsync(host_sums_, sums_.get(), 4 * sizeof(double), cudaMemcpyDeviceToHost, stream_), "D2H sums");
     if (mixed) check(cudaMemcpyAsync(host_sums_ + 4, err_.get(), sizeof(int), cudaMemcpyDeviceToHost, stream_), "D2H");
+    check(cudaMemcpyAsync(host_sums_ + 5, sel_err_.get(), sizeof(int), cudaMemcpyDeviceToHost, stream_), "D2H");
     synchronize();
     for (int q = 0; q < 4; q++) out[q] = host_sums_[q];
+    {
+        int serr = 0;
+        std::memcpy(&serr, host_sums_ + 5, sizeof(int));
+        if (serr) throw CudaError("adaptive threshold select failed (code " + std::to_string(serr) + ")");
+    }
     if (mixed) {
         int err = 0;
         std::memcpy(&err, host_sums_ + 4, sizeof(int));
@@ -566,8 +686,7 @@ void Engine::refine(double bw, bool adaptive, int kernel, double out[4])
     r.kernel = kernel;
     r.skip = 1;
     r.pts = pts32_.get();
-    r.boxes = boxes32_.get();
-    r.caps = caps32_.get();
+    r.tb = tbsel_.get();
     r.X = xs_.get();
     r.y = ys_.get();
     r.beta = beta_.get();
@@ -575,6 +694,7 @@ void Engine::refine(double bw, bool adaptive, int kernel, double out[4])
     r.bw = (float)bw;
     r.r = rvec_.get();
     check(launch_refine_residual(r, geographic_, stream_), "refine residual");
+    stats_.kernel_launches += 1;
     solve(kSolveRefine, bw, adaptive, kernel, out);
 }
 
@@ -637,7 +757,9 @@ void Engine::fit(double bw, bool adaptive, int kernel, bool storeS, FitOutput& o
         if (perm_[sidx] == n - 1) last_sorted = sidx;
     S_.alloc(storeS ? (size_t)n * n : (size_t)n);
     check(cudaMemsetAsync(S_.get(), 0, sizeof(double) * S_.size(), stream_), "memset S");
-    check(launch_hat_pass(points(), geographic_, tiles_.get(), caps_.get(), mixed ? xs_.get() : x_.get(), p,
+    check(launch_tile_far_thr(n, kTile, geographic_, thrPtr(adaptive), bw, tile_thr16_.get(), stream_), "tile thr");
+    stats_.kernel_launches += 2;  // tile thresholds and the hat pass
+    check(launch_hat_pass(points(), geographic_, tb16_.get(), tile_thr16_.get(), mixed ? xs_.get() : x_.get(), p,
                           vvec_.get(),
                           thrPtr(adaptive), bw, kernel,
                           true, qdiag_.get(), storeS ? S_.get() : nullptr, storeS ? -1 : last_sorted,
@@ -690,6 +812,42 @@ void Engine::fit(double bw, bool adaptive, int kernel, bool storeS, FitOutput& o
     out.shat[0] = s[0];
     out.shat[1] = s[2];
     out.rss = s[1];
+}
+
+double Engine::golden(bool adaptive, int kernel, int crit, double lower, double upper,
+                      std::map<double, double>& record)
+{
+    double xopt = 0.0;
+    golden_section(
+        lower, upper, adaptive, [&](double b) { return criterion(b, adaptive, kernel, crit); }, [] { return true; },
+        xopt, record);
+    return xopt;
+}
+
+void Engine::clearCaches()
+{
+    ranks_.clear();
+    hist_valid_ = false;
+    thr_valid_ = false;
+    gall_valid_ = false;
+}
+
+void Engine::recordEvent(int slot)
+{
+    if (slot < 0 || slot >= 8) throw std::invalid_argument("event slot out of range");
+    check(cudaSetDevice(device_), "cudaSetDevice");
+    if (!events_[slot]) check(cudaEventCreate(&events_[slot]), "cudaEventCreate");
+    check(cudaEventRecord(events_[slot], stream_), "cudaEventRecord");
+}
+
+float Engine::elapsedMs(int a, int b)
+{
+    if (a < 0 || a >= 8 || b < 0 || b >= 8 || !events_[a] || !events_[b])
+        throw std::invalid_argument("event slot not recorded");
+    check(cudaEventSynchronize(events_[b]), "cudaEventSynchronize");
+    float ms = 0.f;
+    check(cudaEventElapsedTime(&ms, events_[a], events_[b]), "cudaEventElapsedTime");
+    return ms;
 }
 
 double Engine::globalCriterion(const std::vector<int>& cols)
@@ -760,8 +918,11 @@ void Engine::thresholds(double bw, bool adaptive, std::vector<double>& out)
     if (!adaptive) return;
     computeThresholds(bw, adaptive);
     std::vector<double> h(n_);
+    int serr = 0;
     check(cudaMemcpyAsync(h.data(), thr_.get(), sizeof(double) * n_, cudaMemcpyDeviceToHost, stream_), "D2H");
+    check(cudaMemcpyAsync(&serr, sel_err_.get(), sizeof(int), cudaMemcpyDeviceToHost, stream_), "D2H");
     synchronize();
+    if (serr) throw CudaError("adaptive threshold select failed (code " + std::to_string(serr) + ")");
     for (int s = 0; s < n_; s++) out[perm_[s]] = h[s];
 }
 

@@ -6,6 +6,8 @@
 #include <cstddef>
 #include <cstdint>
 #include <functional>
+#include <map>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -69,6 +71,7 @@ struct EngineStats {
     double select_ms = 0.0;
     double solve_ms = 0.0;
     int criterion_evals = 0;
+    long long kernel_launches = 0;  // kernels launched by the engine (always counted)
 };
 
 struct FitOutput {
@@ -111,6 +114,16 @@ public:
     void fit(double bw, bool adaptive, int kernel, bool storeS, FitOutput& out);
     // CRSDistance::maxDistance.
     double maxDistance();
+    // Golden-section bandwidth search on the device-resident data
+    // (BandwidthSelector::optimize); returns the chosen bandwidth and fills
+    // record with (bandwidth, criterion).
+    double golden(bool adaptive, int kernel, int crit, double lower, double upper, std::map<double, double>& record);
+    // Forget the per-dataset caches (order statistics, distance histograms,
+    // thresholds) so the next search recomputes everything.
+    void clearCaches();
+    // CUDA events on the engine stream (slots 0..7) for device timing.
+    void recordEvent(int slot);
+    float elapsedMs(int a, int b);
     // indepVarsSelectionCriterion (GWRBasic.cpp:309-346): AICc of the model
     // on the given columns with every weight equal to one; DBL_MAX on failure.
     double globalCriterion(const std::vector<int>& cols);
@@ -127,6 +140,7 @@ public:
 
 private:
     void ensureMixed();
+    void buildProxy();
     void contractMixed(double* G, int ldg, int mcols, double bw, bool adaptive, int kernel, bool exclude_self,
                        int wpow);
     void computeThresholds(double bw, bool adaptive);
@@ -149,6 +163,21 @@ private:
 
     DevBuf<double> u_, v_, uR_, vR_, x_, y_, z_, g_, g2_;
     DevBuf<double> thr_, sel0_, sel1_;
+    // order statistics already computed, by rank: brackets for new ranks
+    struct RankStat {
+        unsigned rank;
+        bool exact;
+        DevBuf<double> v;
+    };
+    std::vector<std::unique_ptr<RankStat>> ranks_;
+    DevBuf<unsigned> hist_;    // per-row histograms of proxy distances (n x 4096)
+    bool hist_tried_ = false, hist_valid_ = false;
+    const double* orderStatistic(unsigned rank);
+    DevBuf<float4> tbsel_;     // FP32 bounds of the 32-point tiles (select, mixed kernels)
+    DevBuf<float4> tb16_;      // FP32 bounds of the 16-point tiles (FP64 kernels)
+    DevBuf<float> tile_thr16_;
+    DevBuf<int> sel_err_;
+    double sel_eps_ = 0.0, sel_delta_ = 0.0;
     DevBuf<double> beta_, sii_, resid_, vvec_, bse_, qdiag_, S_;
     DevBuf<double> partials_, sums_;
     DevBuf<double> gall_, gall_part_, gsub_, xsub_;
@@ -178,9 +207,11 @@ private:
 
     bool thr_valid_ = false;
     double thr_bw_ = 0.0;
+    int thr_prec_ = -1;
 
     bool stats_on_ = false;
     EngineStats stats_;
+    cudaEvent_t events_[8] = {};
 };
 
 }  // namespace gwgpu

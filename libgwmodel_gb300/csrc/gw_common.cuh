@@ -106,6 +106,69 @@ __device__ __forceinline__ TileCap cap_union(const TileCap* caps, int first, int
     u.rho = u.rho * (1.0 + 1e-12) + 1e-15;
     return u;
 }
+// ---- FP32 tile tests (conservative, margins cover FP32 rounding) ----------
+// Tile bound as float4: planar box (ulo, uhi, vlo, vhi) relative to the
+// coordinate centroid, or geographic cap (cx, cy, cz, rho) on the unit sphere.
+
+// Union of tile bounds tb[first..last].
+template <bool GEO>
+__device__ __forceinline__ float4 tb_union(const float4* tb, int first, int last)
+{
+    if (!GEO) {
+        float4 b = tb[first];
+        for (int q = first + 1; q <= last; q++) {
+            const float4 c = tb[q];
+            b.x = fminf(b.x, c.x); b.y = fmaxf(b.y, c.y);
+            b.z = fminf(b.z, c.z); b.w = fmaxf(b.w, c.w);
+        }
+        return b;
+    }
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    for (int q = first; q <= last; q++) {
+        sx += tb[q].x;
+        sy += tb[q].y;
+        sz += tb[q].z;
+    }
+    const float nrm = sqrtf(sx * sx + sy * sy + sz * sz);
+    float4 u = make_float4(sx / nrm, sy / nrm, sz / nrm, 0.f);
+    for (int q = first; q <= last; q++) {
+        const float dx = tb[q].x - u.x, dy = tb[q].y - u.y, dz = tb[q].z - u.z;
+        u.w = fmaxf(u.w, sqrtf(dx * dx + dy * dy + dz * dz) + tb[q].w);
+    }
+    u.w = u.w * (1.0f + 1e-5f) + 1e-6f;
+    return u;
+}
+
+// Threshold of the far test for a largest bandwidth rmax (distance units):
+// planar: squared distance; geographic: 3-D chord.  Returns -1 when no tile
+// may be skipped.
+template <bool GEO>
+__device__ __forceinline__ float tb_far_threshold(double rmax)
+{
+    if (!(rmax > 0.0)) return -1.0f;
+    if (!GEO) return (float)(rmax * rmax * (1.0 + 1e-4));
+    const double w = rmax / (2.0 * 6378.137 * (1.0 - 2.6 / 298.257223563));
+    if (w >= 1.2) return -1.0f;
+    return (float)(2.0 * sin(w) * (1.0 + 1e-4));
+}
+
+// True when every pair between the focus bound fb and tile bound tb is at
+// least as far as the threshold (so every weight of a compact kernel is 0).
+template <bool GEO>
+__device__ __forceinline__ bool tb_far(const float4& fb, const float4& tb, float thr)
+{
+    if (thr < 0.0f) return false;
+    if (!GEO) {
+        const float dx = fmaxf(0.0f, fmaxf(tb.x - fb.y, fb.x - tb.y));
+        const float dy = fmaxf(0.0f, fmaxf(tb.z - fb.w, fb.z - tb.w));
+        return fmaf(dx, dx, dy * dy) * (1.0f - 1e-5f) >= thr;
+    }
+    const float dx = tb.x - fb.x, dy = tb.y - fb.y, dz = tb.z - fb.z;
+    const float cc = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+    const float lo = (cc - fb.w - tb.w) * (1.0f - 1e-5f) - 1e-7f;
+    const float hi = (cc + fb.w + tb.w) * (1.0f + 1e-5f) + 1e-7f;
+    return lo >= thr && hi < 1.8640781f;
+}
 #endif  // __CUDACC__
 
 }  // namespace gwgpu

@@ -11,10 +11,22 @@ namespace gwgpu {
 // Solve modes of launch_solve.
 enum SolveMode { kSolveAIC = 0, kSolveCV = 1, kSolveFit = 2, kSolveRefine = 3 };
 
-// Per-row k-th smallest distance (1-based rank).  [dlo, dhi] is the expected
-// range of positive distances; it only shapes the first histogram.
-cudaError_t launch_select(const DevPoints& P, bool geographic, unsigned rank, double dlo, double dhi,
-                          double* out, int num_sms, cudaStream_t stream);
+// Per-row k-th smallest distance (1-based rank), k_select.cu.
+struct SelectArgs {
+    int n, ntiles;                 // points, 32-point tiles
+    DevPoints P;                   // FP64 coordinates (exact formula)
+    const float4* pts;             // FP32 hi/lo proxy data (as the mixed path)
+    const float4* tb;              // per tile: planar box (ulo, uhi, vlo, vhi) or cap (cx, cy, cz, rho)
+    unsigned* hist_cache;          // n x 4096 proxy histograms of whole rows, or null
+    int cache_valid;               // 1: hist_cache holds every row's histogram
+    unsigned rank;
+    double dlo, dhi;               // expected range of positive distances (first histogram only)
+    double eps, delta;             // proxy band: d in [p (1 - eps) - delta, p (1 + eps) + delta]
+    double* out;
+    int* err;                      // 2: a row's select failed (value left NaN)
+};
+// exact: FP64 order statistics (bit-exact); otherwise the FP32 proxy's.
+cudaError_t launch_select(const SelectArgs& a, bool geographic, bool exact, int num_sms, cudaStream_t stream);
 size_t select_smem_bytes();
 
 // thr = fixbw of BandwidthWeight.cpp:40-53 from order statistics d0 (rank
@@ -32,10 +44,10 @@ cudaError_t launch_build_z(int n, int p, const double* X, const double* y, doubl
 // G[i, c] = sum_j w_ij^wpow Z[j, c] for c < mcols, with w_ij = K(d_ij, r_i)
 // (r_i = thr[i], or bw when thr is null); exclude_self zeroes w_ii (CV).
 // FP64 SIMT, the weight matrix is produced tile by tile and never stored.
-// caps: geographic tile bounds (16-point tiles), needed to skip geographic tiles.
-cudaError_t launch_contract64(const DevPoints& P, bool geographic, const TileBox* tiles, const TileCap* caps,
-                              const double* Z, int ldz, int mcols, double* G, int ldg, const double* thr, double bw,
-                              int kernel, bool exclude_self, int wpow, bool skip_tiles, cudaStream_t stream);
+// tb16: FP32 bounds of the 16-point tiles (planar box or geographic cap).
+cudaError_t launch_contract64(const DevPoints& P, bool geographic, const float4* tb16, const double* Z, int ldz,
+                              int mcols, double* G, int ldg, const double* thr, double bw, int kernel,
+                              bool exclude_self, int wpow, bool skip_tiles, cudaStream_t stream);
 
 // Warp-per-location Cholesky solve of A_i beta_i = b_i and the per-location
 // criterion terms; partial sums per block in partials[block*4 + {0..3}] =
@@ -73,7 +85,8 @@ cudaError_t launch_reduce_partials(const double* partials, int nblocks, double* 
 // qdiag[j] = sum_i (delta_ij - s_ij)^2 with s_ij = w_ij v_i . x_j, w_ij =
 // K(d_ij, r_i); also writes S (n x n row-major, sorted order) when S != null
 // and row row_target of S into s_row (length n) when s_row != null.
-cudaError_t launch_hat_pass(const DevPoints& P, bool geographic, const TileBox* tiles, const TileCap* caps,
+// tile_thr: far-test threshold of each 16-point tile's largest r_i (launch_tile_far_thr).
+cudaError_t launch_hat_pass(const DevPoints& P, bool geographic, const float4* tb16, const float* tile_thr,
                             const double* X, int p,
                             const double* v, const double* thr, double bw, int kernel, bool skip_tiles,
                             double* qdiag, double* S, int row_target, double* s_row, cudaStream_t stream);
@@ -96,8 +109,7 @@ cudaError_t launch_gather_subset(int n, int p, const ColumnSet& cs, const double
 struct TcArgs {
     int n, mcols, npad, ntiles;   // ntiles: 32-point tiles
     const float4* pts;            // planar: {u_hi, u_lo, v_hi, v_lo}; geographic: 3 float4 per point
-    const TileBox* boxes;         // bounds of each 32-point tile
-    const TileCap* caps;          // geographic bounds of each 32-point tile (null: no geographic skipping)
+    const float4* tb;             // FP32 bound of each 32-point tile (planar box or geographic cap)
     const unsigned char* zimg;    // per tile: [hi | lo] swizzled images, npad x 128 bytes each
     const float* thr;             // per-row threshold, or null for the fixed bandwidth bw
     float bw;
@@ -107,7 +119,7 @@ struct TcArgs {
     int ldg;
     int* err;                     // set to 1 if a bounded wait timed out
 };
-size_t contract_tc_smem_bytes(int npad);
+size_t contract_tc_smem_bytes(int npad, int ntiles);
 cudaError_t launch_contract_tc(const TcArgs& a, bool geographic, cudaStream_t stream);
 cudaError_t launch_build_zimg(int n, int mcols, int npad, const double* Z, int ldz, unsigned char* img,
                               cudaStream_t stream);
@@ -119,8 +131,7 @@ cudaError_t launch_tc_selftest(const float* A, const float* B, float* D, int N, 
 struct RefineArgs {
     int n, p, ntiles, kernel, skip;
     const float4* pts;
-    const TileBox* boxes;
-    const TileCap* caps;
+    const float4* tb;     // FP32 bound of each 32-point tile
     const double* X;      // n x p row-major (X~)
     const double* y;      // y~
     const double* beta;   // n x p
@@ -129,6 +140,10 @@ struct RefineArgs {
     double* r;            // n x p
 };
 cudaError_t launch_refine_residual(const RefineArgs& a, bool geographic, cudaStream_t stream);
+
+// tile_thr[t] = far-test threshold of the largest r_i (thr, or bw) over tile t of `tile` points.
+cudaError_t launch_tile_far_thr(int n, int tile, bool geographic, const double* thr, double bw, float* tile_thr,
+                                cudaStream_t stream);
 
 // Maximum pairwise distance (CRSDistance::maxDistance), as an ordered key in *key_out.
 cudaError_t launch_max_distance(const DevPoints& P, bool geographic, unsigned long long* key_out, int num_sms,

@@ -11,6 +11,7 @@
 #include <stdexcept>
 
 #include "engine.h"
+#include "golden.h"
 
 namespace gwm {
 
@@ -218,57 +219,15 @@ mat GWRBasic::fit()
         GW_LOG(LOG_INFO, infoBandwidthCriterion(bw0));
         // BandwidthSelector::optimize (BandwidthSelector.cpp:6-81)
         std::map<double, double> record;
-        BandwidthWeight w1 = bw0, w2 = bw0;
-        double xU = upper, xL = lower;
-        const double eps = 1e-4;
-        const double R = (std::sqrt(5) - 1) / 2;
-        int iter = 0;
-        double d = R * (xU - xL);
-        double x1 = adaptive ? std::floor(xL + d) : (xL + d);
-        double x2 = adaptive ? std::round(xU - d) : (xU - d);
-        w1.setBandwidth(x1);
-        w2.setBandwidth(x2);
-        double f1 = bandwidthCriterion(w1);
-        Status s1 = mStatus;
-        double f2 = bandwidthCriterion(w2);
-        Status s2 = mStatus;
-        bool chosen = false;
+        BandwidthWeight w = bw0;
         double xopt = 0.0;
-        if (s1 == Status::Success && s2 == Status::Success) {
-            if (f1 == DBL_MAX && f2 == DBL_MAX) throw std::runtime_error("Invalid initial values.");
-            if (f1 < DBL_MAX) record[x1] = f1;
-            if (f2 < DBL_MAX) record[x2] = f2;
-            double d1 = f2 - f1;
-            xopt = f1 < f2 ? x1 : x2;
-            const double ea = 100;
-            while (s1 == Status::Success && s2 == Status::Success && std::fabs(d) > eps && std::fabs(d1) > eps &&
-                   iter < ea) {
-                d = R * d;
-                if (f1 < f2) {
-                    xL = x2;
-                    x2 = x1;
-                    x1 = adaptive ? std::round(xL + d) : (xL + d);
-                    f2 = f1;
-                    w1.setBandwidth(x1);
-                    f1 = bandwidthCriterion(w1);
-                    s1 = mStatus;
-                    if (f1 < DBL_MAX) record[x1] = f1;
-                } else {
-                    xU = x1;
-                    x1 = x2;
-                    x2 = adaptive ? std::floor(xU - d) : (xU - d);
-                    f1 = f2;
-                    w2.setBandwidth(x2);
-                    f2 = bandwidthCriterion(w2);
-                    s2 = mStatus;
-                    if (f2 < DBL_MAX) record[x2] = f2;
-                }
-                iter = iter + 1;
-                xopt = (f1 < f2) ? x1 : x2;
-                d1 = f2 - f1;
-            }
-            chosen = s1 == Status::Success && s2 == Status::Success;
-        }
+        const bool chosen = gwgpu::golden_section(
+            lower, upper, adaptive,
+            [&](double b) {
+                w.setBandwidth(b);
+                return bandwidthCriterion(w);
+            },
+            [&] { return mStatus == Status::Success; }, xopt, record);
         if (chosen) {
             BandwidthWeight wopt;
             wopt.setKernel(bw0.kernel());

@@ -25,8 +25,7 @@ constexpr int CT_ROWS_PER_THREAD = CT_BM / 16;
 
 template <bool GEO, int NC>
 __global__ void __launch_bounds__(CT_THREADS)
-    k_contract64(DevPoints P, const TileBox* __restrict__ tiles, const TileCap* __restrict__ caps,
-                 const double* __restrict__ Z, int ldz, int mcols,
+    k_contract64(DevPoints P, const float4* __restrict__ tb16, const double* __restrict__ Z, int ldz, int mcols,
                  double* __restrict__ G, int ldg, const double* __restrict__ thr, double bw, int kernel,
                  int exclude_self, int wpow, int skip_tiles)
 {
@@ -35,8 +34,7 @@ __global__ void __launch_bounds__(CT_THREADS)
     __shared__ double sZ[CT_BK][NCOL];
     __shared__ double sfu[CT_BM], sfv[CT_BM], sfuR[CT_BM], sfvR[CT_BM], sthr[CT_BM];
     __shared__ double sred[CT_THREADS / 32];
-    __shared__ TileBox sblock;
-    __shared__ TileCap scap;
+    __shared__ float4 sbound;
 
     const int n = P.n;
     const int t = threadIdx.x, tx = t & 15, ty = t >> 4;
@@ -58,27 +56,15 @@ __global__ void __launch_bounds__(CT_THREADS)
         for (int off = 16; off > 0; off >>= 1) r = fmax(r, __shfl_xor_sync(0xffffffffu, r, off));
         if ((t & 31) == 0) sred[t >> 5] = r;
     }
-    if (t == 0) {
-        // the focus block is 4 consecutive data tiles
-        TileBox b = tiles[row0 / CT_BK];
-        int last = min(row0 + CT_BM, n) - 1;
-        for (int q = row0 / CT_BK + 1; q <= last / CT_BK; q++) {
-            TileBox c = tiles[q];
-            b.ulo = fmin(b.ulo, c.ulo); b.uhi = fmax(b.uhi, c.uhi);
-            b.vlo = fmin(b.vlo, c.vlo); b.vhi = fmax(b.vhi, c.vhi);
-        }
-        sblock = b;
-        if (GEO && caps) scap = cap_union(caps, row0 / CT_BK, last / CT_BK);
-    }
+    if (t == 0) sbound = tb_union<GEO>(tb16, row0 / CT_BK, (min(row0 + CT_BM, n) - 1) / CT_BK);
     __syncthreads();
     if (thr) {
         rmax = sred[0];
         for (int q = 1; q < CT_THREADS / 32; q++) rmax = fmax(rmax, sred[q]);
     }
     // a tile may be skipped only if every pair in it has d >= r_i, i.e. w = 0
-    const bool can_skip = skip_tiles && (!GEO || caps) && kernel >= GW_KERNEL_BISQUARE && rmax > 0.0;
-    const TileBox fb = sblock;
-    const TileCap fcap = scap;
+    const float4 fbound = sbound;
+    const float far_thr = (skip_tiles && kernel >= GW_KERNEL_BISQUARE) ? tb_far_threshold<GEO>(rmax) : -1.0f;
 
     double acc[CT_ROWS_PER_THREAD][NC];
 #pragma unroll
@@ -88,10 +74,7 @@ __global__ void __launch_bounds__(CT_THREADS)
 
     const int ntiles = (n + CT_BK - 1) / CT_BK;
     for (int tile = 0; tile < ntiles; tile++) {
-        if (can_skip) {
-            double lb = GEO ? cap_lower_bound(fcap, caps[tile]) * (1.0 - 1e-9) : box_lower_bound(fb, tiles[tile]);
-            if (lb * (1.0 - 1e-14) >= rmax) continue;  // uniform over the CTA
-        }
+        if (tb_far<GEO>(fbound, tb16[tile], far_thr)) continue;  // uniform over the CTA
         const int j0 = tile * CT_BK;
         // Z tile -> shared (zero padded)
         for (int e = t; e < CT_BK * NCOL; e += CT_THREADS) {
@@ -154,25 +137,25 @@ __global__ void __launch_bounds__(CT_THREADS)
 }
 
 template <bool GEO, int NC>
-cudaError_t launch_nc(const DevPoints& P, const TileBox* tiles, const TileCap* caps, const double* Z, int ldz,
+cudaError_t launch_nc(const DevPoints& P, const float4* tiles, const double* Z, int ldz,
                       int mcols, double* G, int ldg, const double* thr, double bw, int kernel, bool exclude_self,
                       int wpow, bool skip, cudaStream_t s)
 {
     int grid = (P.n + CT_BM - 1) / CT_BM;
-    k_contract64<GEO, NC><<<grid, CT_THREADS, 0, s>>>(P, tiles, caps, Z, ldz, mcols, G, ldg, thr, bw, kernel,
+    k_contract64<GEO, NC><<<grid, CT_THREADS, 0, s>>>(P, tiles, Z, ldz, mcols, G, ldg, thr, bw, kernel,
                                                      exclude_self ? 1 : 0, wpow, skip ? 1 : 0);
     return cudaGetLastError();
 }
 
 template <bool GEO>
-cudaError_t launch_geo(const DevPoints& P, const TileBox* tiles, const TileCap* caps, const double* Z, int ldz,
+cudaError_t launch_geo(const DevPoints& P, const float4* tiles, const double* Z, int ldz,
                        int mcols, double* G, int ldg, const double* thr, double bw, int kernel, bool exclude_self,
                        int wpow, bool skip, cudaStream_t s)
 {
     int nc = (mcols + 15) / 16;
 #define GW_NC_CASE(K) \
     case K:           \
-        return launch_nc<GEO, K>(P, tiles, caps, Z, ldz, mcols, G, ldg, thr, bw, kernel, exclude_self, wpow, skip, s);
+        return launch_nc<GEO, K>(P, tiles, Z, ldz, mcols, G, ldg, thr, bw, kernel, exclude_self, wpow, skip, s);
     switch (nc) {
         GW_NC_CASE(1) GW_NC_CASE(2) GW_NC_CASE(3) GW_NC_CASE(4) GW_NC_CASE(5) GW_NC_CASE(6) GW_NC_CASE(7)
         GW_NC_CASE(8) GW_NC_CASE(9) GW_NC_CASE(10) GW_NC_CASE(11) GW_NC_CASE(12) GW_NC_CASE(13)
@@ -184,15 +167,15 @@ cudaError_t launch_geo(const DevPoints& P, const TileBox* tiles, const TileCap* 
 
 }  // namespace
 
-cudaError_t launch_contract64(const DevPoints& P, bool geographic, const TileBox* tiles, const TileCap* caps,
-                              const double* Z, int ldz, int mcols, double* G, int ldg, const double* thr, double bw,
-                              int kernel, bool exclude_self, int wpow, bool skip_tiles, cudaStream_t stream)
+cudaError_t launch_contract64(const DevPoints& P, bool geographic, const float4* tb16, const double* Z, int ldz,
+                              int mcols, double* G, int ldg, const double* thr, double bw, int kernel,
+                              bool exclude_self, int wpow, bool skip_tiles, cudaStream_t stream)
 {
     if (mcols < 1 || mcols > 256) return cudaErrorInvalidValue;
     if (geographic)
-        return launch_geo<true>(P, tiles, caps, Z, ldz, mcols, G, ldg, thr, bw, kernel, exclude_self, wpow,
-                                skip_tiles, stream);
-    return launch_geo<false>(P, tiles, caps, Z, ldz, mcols, G, ldg, thr, bw, kernel, exclude_self, wpow, skip_tiles,
+        return launch_geo<true>(P, tb16, Z, ldz, mcols, G, ldg, thr, bw, kernel, exclude_self, wpow, skip_tiles,
+                                stream);
+    return launch_geo<false>(P, tb16, Z, ldz, mcols, G, ldg, thr, bw, kernel, exclude_self, wpow, skip_tiles,
                              stream);
 }
 

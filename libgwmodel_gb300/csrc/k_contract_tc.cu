@@ -27,7 +27,7 @@ namespace {
 
 using namespace tc05;
 
-constexpr int TC_THREADS = 256;
+constexpr int TC_THREADS = 512;
 constexpr int TC_M = 128;
 constexpr int TC_BK = 32;  // points per stage (128 bytes of TF32 per row)
 constexpr uint32_t TC_A_BYTES = TC_M * 128;  // one split part of the weight tile
@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
     const uint32_t stage_bytes = 2u * TC_A_BYTES + 2u * b_bytes;
 
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    const int r = t & (TC_M - 1), half = t >> 7;
+    const int r = t & (TC_M - 1), quarter = t >> 7;
     const int row0 = blockIdx.x * TC_M;
     const int i = row0 + r;
     const bool row_ok = i < a.n;
@@ -100,31 +100,32 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
     const float rr = row_ok ? (a.thr ? a.thr[i] : a.bw) : 1.0f;
     const float inv_r2 = 1.0f / (rr * rr);
 
-    // block box and largest threshold for tile skipping
+    // block bound and largest threshold for tile skipping
     __shared__ float red[TC_THREADS / 32];
-    __shared__ TileBox fbox;
-    __shared__ TileCap fcap_s;
+    __shared__ float4 fbound_s;
     float rmax = row_ok ? rr : 0.0f;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, off));
     if (lane == 0) red[warp] = rmax;
-    if (t == 0) {
-        TileBox b = a.boxes[row0 / TC_BK];
-        int last = min(row0 + TC_M, a.n) - 1;
-        for (int q = row0 / TC_BK + 1; q <= last / TC_BK; q++) {
-            TileBox c = a.boxes[q];
-            b.ulo = fmin(b.ulo, c.ulo); b.uhi = fmax(b.uhi, c.uhi);
-            b.vlo = fmin(b.vlo, c.vlo); b.vhi = fmax(b.vhi, c.vhi);
-        }
-        fbox = b;
-        if (GEO && a.caps) fcap_s = cap_union(a.caps, row0 / TC_BK, last / TC_BK);
-    }
+    if (t == 0) fbound_s = tb_union<GEO>(a.tb, row0 / TC_BK, (min(row0 + TC_M, a.n) - 1) / TC_BK);
     __syncthreads();
     rmax = red[0];
     for (int q = 1; q < TC_THREADS / 32; q++) rmax = fmaxf(rmax, red[q]);
-    const bool can_skip = a.skip && (!GEO || a.caps) && a.kernel >= GW_KERNEL_BISQUARE && rmax > 0.0f;
-    const double rmax_d = (double)rmax * (1.0 + 1e-4);
-    const TileCap fcap = fcap_s;
+    const float4 fbound = fbound_s;
+    const float far_thr =
+        (a.skip && a.kernel >= GW_KERNEL_BISQUARE) ? tb_far_threshold<GEO>((double)rmax) : -1.0f;
+    // tiles this CTA must visit, one bit per 32-point tile
+    uint32_t* tmask = reinterpret_cast<uint32_t*>(stage0 + 2 * (size_t)stage_bytes);
+    const int nwords = (a.ntiles + 31) / 32;
+    for (int wd = t; wd < nwords; wd += TC_THREADS) {
+        uint32_t bits = 0;
+        for (int b = 0; b < 32; b++) {
+            const int tile = wd * 32 + b;
+            if (tile < a.ntiles && !tb_far<GEO>(fbound, a.tb[tile], far_thr)) bits |= 1u << b;
+        }
+        tmask[wd] = bits;
+    }
+    __syncthreads();
 
     const uint32_t idesc = idesc_tf32(TC_M, a.npad);
     int issued = 0;        // stages issued so far (non-skipped tiles)
@@ -138,11 +139,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
         const uint32_t par = (uint32_t)((last_stage >> 1) & 1);
         if (!mbar_wait(&ctl.bar_mma[s], par, TC_WAIT)) atomicExch(&ctl.abort, 1);
         fence_after_sync();
-        const int quad = warp & 3, colhalf = warp >> 2;
+        const int quad = warp & 3, part = warp >> 2;
         const int lrow = quad * 32 + lane;
         const int grow = row0 + lrow;
-        const int ncol_half = a.npad / 2;
-        for (int c0 = colhalf * ncol_half; c0 < (colhalf + 1) * ncol_half; c0 += 16) {
+        const int ncol_part = a.npad / 4;
+        for (int c0 = part * ncol_part; c0 < (part + 1) * ncol_part; c0 += 16) {
             uint32_t v[16];
             tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0, v);
             tmem_wait_ld();
@@ -161,11 +162,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
         in_chunk = 0;
     };
 
-    for (int tile = 0; tile < a.ntiles && !aborted; tile++) {
-        if (can_skip) {
-            const double lb = GEO ? cap_lower_bound(fcap, a.caps[tile]) : box_lower_bound(fbox, a.boxes[tile]);
-            if (lb * (1.0 - 1e-12) >= rmax_d) continue;  // uniform over the CTA
-        }
+    int word = 0;
+    uint32_t bits = nwords > 0 ? tmask[0] : 0u;
+    while (!aborted) {
+        while (bits == 0 && ++word < nwords) bits = tmask[word];
+        if (bits == 0) break;
+        const int tile = word * 32 + (__ffs(bits) - 1);
+        bits &= bits - 1;
         const int s = issued & 1;
         unsigned char* st = stage0 + (size_t)s * stage_bytes;
         unsigned char* A_hi = st;
@@ -180,10 +183,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
             mbar_arrive_expect_tx(&ctl.bar_b[s], 2u * b_bytes);
             bulk_g2s(B_hi, a.zimg + (size_t)tile * 2u * b_bytes, 2u * b_bytes, &ctl.bar_b[s]);
         }
-        // weight tile: thread (r, half) fills points [16*half, 16*half + 16) of row r
-        const int jbase = tile * TC_BK + half * 16;
+        // weight tile: thread (r, quarter) fills points [8*quarter, 8*quarter + 8) of row r
+        const int jbase = tile * TC_BK + quarter * 8;
 #pragma unroll
-        for (int q4 = 0; q4 < 4; q4++) {
+        for (int q4 = 0; q4 < 2; q4++) {
             float hi[4], lo[4];
 #pragma unroll
             for (int e = 0; e < 4; e++) {
@@ -197,7 +200,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
                 hi[e] = to_tf32(w);
                 lo[e] = to_tf32(w - hi[e]);
             }
-            const uint32_t off = sw128_offset((uint32_t)r, (uint32_t)(half * 16 + q4 * 4));
+            const uint32_t off = sw128_offset((uint32_t)r, (uint32_t)(quarter * 8 + q4 * 4));
             *reinterpret_cast<float4*>(A_hi + off) = make_float4(hi[0], hi[1], hi[2], hi[3]);
             *reinterpret_cast<float4*>(A_lo + off) = make_float4(lo[0], lo[1], lo[2], lo[3]);
         }
@@ -332,12 +335,16 @@ __global__ void k_build_zimg(int n, int mcols, int npad, const double* __restric
 
 }  // namespace
 
-size_t contract_tc_smem_bytes(int npad) { return 1024 + 2 * (2 * (size_t)TC_A_BYTES + 2 * (size_t)npad * 128); }
+size_t contract_tc_smem_bytes(int npad, int ntiles)
+{
+    return 1024 + 2 * (2 * (size_t)TC_A_BYTES + 2 * (size_t)npad * 128) + 4 * (size_t)((ntiles + 31) / 32);
+}
 
 cudaError_t launch_contract_tc(const TcArgs& a, bool geographic, cudaStream_t stream)
 {
-    if (a.npad % 32 != 0 || a.npad < 32 || a.npad > 256 || a.mcols > a.npad) return cudaErrorInvalidValue;
-    const size_t smem = contract_tc_smem_bytes(a.npad);
+    if (a.npad % 64 != 0 || a.npad < 64 || a.npad > 256 || a.mcols > a.npad) return cudaErrorInvalidValue;
+    const size_t smem = contract_tc_smem_bytes(a.npad, a.ntiles);
+    if (smem > 227 * 1024) return cudaErrorInvalidValue;
     const int grid = (a.n + TC_M - 1) / TC_M;
     if (geographic) {
         cudaFuncSetAttribute(k_contract_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

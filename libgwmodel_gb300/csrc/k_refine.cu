@@ -25,8 +25,7 @@ template <bool GEO, int PMAX>
 __global__ void __launch_bounds__(RF_THREADS) k_refine(RefineArgs a)
 {
     extern __shared__ double rsm[];  // RF_TILE x (p + 1): x~_j then y~_j
-    __shared__ TileBox fbox;
-    __shared__ TileCap fcap_s;
+    __shared__ float4 fbound_s;
     __shared__ float red[RF_THREADS / 32];
     const int p = a.p, pp = a.p + 1;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -56,29 +55,16 @@ __global__ void __launch_bounds__(RF_THREADS) k_refine(RefineArgs a)
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, off));
     if (lane == 0) red[warp] = rmax;
-    if (t == 0) {
-        const int last = min(row0 + RF_THREADS, a.n) - 1;
-        TileBox b = a.boxes[row0 / RF_TILE];
-        for (int q = row0 / RF_TILE + 1; q <= last / RF_TILE; q++) {
-            TileBox c = a.boxes[q];
-            b.ulo = fmin(b.ulo, c.ulo); b.uhi = fmax(b.uhi, c.uhi);
-            b.vlo = fmin(b.vlo, c.vlo); b.vhi = fmax(b.vhi, c.vhi);
-        }
-        fbox = b;
-        if (GEO && a.caps) fcap_s = cap_union(a.caps, row0 / RF_TILE, last / RF_TILE);
-    }
+    if (t == 0) fbound_s = tb_union<GEO>(a.tb, row0 / RF_TILE, (min(row0 + RF_THREADS, a.n) - 1) / RF_TILE);
     __syncthreads();
     rmax = red[0];
     for (int q = 1; q < RF_THREADS / 32; q++) rmax = fmaxf(rmax, red[q]);
-    const bool can_skip = a.skip && (!GEO || a.caps) && a.kernel >= GW_KERNEL_BISQUARE && rmax > 0.0f;
-    const double rmax_d = (double)rmax * (1.0 + 1e-4);
-    const TileCap fcap = fcap_s;
+    const float4 fbound = fbound_s;
+    const float far_thr =
+        (a.skip && a.kernel >= GW_KERNEL_BISQUARE) ? tb_far_threshold<GEO>((double)rmax) : -1.0f;
 
     for (int tile = 0; tile < a.ntiles; tile++) {
-        if (can_skip) {
-            const double lb = GEO ? cap_lower_bound(fcap, a.caps[tile]) : box_lower_bound(fbox, a.boxes[tile]);
-            if (lb * (1.0 - 1e-12) >= rmax_d) continue;
-        }
+        if (tb_far<GEO>(fbound, a.tb[tile], far_thr)) continue;
         const int j0 = tile * RF_TILE;
         for (int e = t; e < RF_TILE * pp; e += RF_THREADS) {
             const int q = e / pp, c = e - q * pp;

@@ -1,41 +1,54 @@
 // k_select.cu -- adaptive bandwidth thresholds without sorting.
 //
 // The reference sorts every distance row to read the b-th smallest distance
-// (BandwidthWeight.cpp:40-53 with arma::sort; thrust::sort per row on the
-// GPU, BandwidthWeightKernel.cu:71-95).  Here one CTA owns one focus row and
-// finds the exact k-th order statistic of the row's FP64 distances with a
-// range-bucketed radix select on the IEEE bit pattern (a monotone key):
-//   pass 0  histogram of a coarse logarithmic bucket of every key (4096 bins),
-//   pass r  histogram of the next bits inside the chosen bucket,
-//   gather  once the chosen bucket holds <= 2048 keys, copy them to shared
-//           memory and bitonic-sort them there.
-// Distances are recomputed in every pass instead of stored, so the kernel
-// reads only the coordinates (16-32 B per point, L2 resident).  Integer keys
-// make the result bit-exact, ties included.
+// (BandwidthWeight.cpp:40-53 with arma::sort; thrust::sort per row on the GPU,
+// BandwidthWeightKernel.cu:71-95).  Here one CTA of 4 warps owns one focus row
+// and finds the k-th order statistic by a range-bucketed radix select:
+//
+//  * window [T_lo, T_hi]: order statistics of neighbouring ranks computed by
+//    earlier golden-section evaluations bracket the answer (0 and +inf when
+//    none), so most of the row is classified without looking at points;
+//  * tiles of 32 Morton-ordered points carry an FP32 bound (planar box or 3-D
+//    cap): a tile entirely below T_lo only adds its count, a tile entirely
+//    above T_hi is skipped, only straddling tiles are looked at point by point
+//    (one point per lane);
+//  * a point's FP32 proxy distance carries a proven error band; in the exact
+//    (FP64) mode only points whose band meets the window are evaluated with
+//    the reference's FP64 formula, so the result is bit-exact, ties included;
+//    the mixed mode selects on the proxy itself;
+//  * in-window values are histogrammed on their monotone 64-bit keys (4096
+//    bins) and gathered into shared memory; once the window holds <= 2048
+//    values they are bitonic-sorted there, otherwise the window narrows to
+//    the chosen bin and the pass repeats.
 #include "gw_common.cuh"
 #include "gw_kernels.h"
+#include "mixed_weight.cuh"
 
 namespace gwgpu {
 
 namespace {
 
-constexpr int SEL_THREADS = 256;
+constexpr int SEL_THREADS = 128;
+constexpr int SEL_WARPS = SEL_THREADS / 32;
 constexpr int SEL_BINS = 4096;
 constexpr int SEL_LOG_BINS = 12;
 constexpr int SEL_CAP = 2048;
 constexpr int SEL_BINS_PER_THREAD = SEL_BINS / SEL_THREADS;
+constexpr int SEL_MAX_PASSES = 10;
+constexpr int SEL_TILE = 32;
 
 struct SelShared {
     unsigned int hist[SEL_BINS];
     uint64_t cand[SEL_CAP];
-    unsigned int warp_tot[SEL_THREADS / 32];
+    unsigned int warp_tot[SEL_WARPS];
+    unsigned int below_w[SEL_WARPS];
     unsigned int chosen_bin, below, count, ncand;
 };
 
 struct Window {
     uint64_t base;  // bucket = (key - base) >> shift, clamped to [0, SEL_BINS)
     int shift;
-    uint64_t wlo, whi;  // keys outside [wlo, whi] are ignored
+    uint64_t wlo, whi;  // keys of the window ends (inclusive)
 };
 
 __device__ __forceinline__ unsigned bucket_of(const Window& w, uint64_t key)
@@ -56,32 +69,11 @@ __device__ __forceinline__ void bin_range(const Window& w, unsigned b, uint64_t&
     }
 }
 
-// Histogram of the keys of row (fu, fv) inside the window; warp-aggregated
-// shared-memory atomics because Morton-adjacent points share bins.
-template <bool GEO>
-__device__ void hist_pass(SelShared& sh, const DevPoints& P, const Window& w, double fu, double fv, double fuR,
-                          double fvR)
+__device__ __forceinline__ Window linear_window(uint64_t lo, uint64_t hi)
 {
-    for (int b = threadIdx.x; b < SEL_BINS; b += SEL_THREADS) sh.hist[b] = 0;
-    __syncthreads();
-    const int n = P.n;
-    for (int j0 = 0; j0 < n; j0 += SEL_THREADS) {
-        int j = j0 + threadIdx.x;
-        bool in = false;
-        unsigned bin = 0;
-        if (j < n) {
-            uint64_t key = dkey(pair_dist<GEO>(P, j, fu, fv, fuR, fvR));
-            in = key >= w.wlo && key <= w.whi;
-            if (in) bin = bucket_of(w, key);
-        }
-        unsigned act = __ballot_sync(0xffffffffu, in);
-        if (in) {
-            unsigned peers = __match_any_sync(act, bin);
-            int leader = __ffs(peers) - 1;
-            if ((int)(threadIdx.x & 31) == leader) atomicAdd(&sh.hist[bin], (unsigned)__popc(peers));
-        }
-    }
-    __syncthreads();
+    uint64_t span = hi - lo;
+    int bits = span ? 64 - __clzll((long long)span) : 0;
+    return Window{lo, bits > SEL_LOG_BINS ? bits - SEL_LOG_BINS : 0, lo, hi};
 }
 
 // Finds the bin where the cumulative count reaches krem (1-based).
@@ -98,17 +90,15 @@ __device__ void scan_pick(SelShared& sh, unsigned krem)
         if (lane >= off) incl += v;
     }
     if (lane == 31) sh.warp_tot[warp] = incl;
-    __syncthreads();
-    unsigned wpre = 0;
-    for (int q = 0; q < warp; q++) wpre += sh.warp_tot[q];
-    unsigned excl = wpre + incl - local;
     if (t == 0) {
-        // defaults if no bin reaches krem (cannot happen for a valid rank)
         sh.chosen_bin = SEL_BINS - 1;
         sh.below = 0;
         sh.count = 0;
     }
     __syncthreads();
+    unsigned wpre = 0;
+    for (int q = 0; q < warp; q++) wpre += sh.warp_tot[q];
+    const unsigned excl = wpre + incl - local;
     if (excl < krem && excl + local >= krem) {
         unsigned c = excl;
         for (int q = 0; q < SEL_BINS_PER_THREAD; q++) {
@@ -126,38 +116,7 @@ __device__ void scan_pick(SelShared& sh, unsigned krem)
     __syncthreads();
 }
 
-template <bool GEO>
-__device__ void gather_pass(SelShared& sh, const DevPoints& P, uint64_t lo, uint64_t hi, double fu, double fv,
-                            double fuR, double fvR)
-{
-    if (threadIdx.x == 0) sh.ncand = 0;
-    __syncthreads();
-    const int n = P.n;
-    for (int j0 = 0; j0 < n; j0 += SEL_THREADS) {
-        int j = j0 + threadIdx.x;
-        bool in = false;
-        uint64_t key = 0;
-        if (j < n) {
-            key = dkey(pair_dist<GEO>(P, j, fu, fv, fuR, fvR));
-            in = key >= lo && key <= hi;
-        }
-        unsigned act = __ballot_sync(0xffffffffu, in);
-        if (act) {
-            int lane = threadIdx.x & 31;
-            int leader = __ffs(act) - 1;
-            unsigned base = 0;
-            if (lane == leader) base = atomicAdd(&sh.ncand, (unsigned)__popc(act));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (in) {
-                unsigned slot = base + __popc(act & ((1u << lane) - 1u));
-                if (slot < SEL_CAP) sh.cand[slot] = key;
-            }
-        }
-    }
-    __syncthreads();
-}
-
-// Ascending bitonic sort of cand[0, len) padded with +inf keys to a power of two.
+// Ascending bitonic sort of cand[0, count) padded with +inf keys.
 __device__ void bitonic_sort(SelShared& sh, unsigned count)
 {
     unsigned len = 1;
@@ -181,49 +140,233 @@ __device__ void bitonic_sort(SelShared& sh, unsigned count)
     }
 }
 
+struct RowCtx {
+    double fu, fv, fuR, fvR;  // FP64 focus coordinates (exact formula)
+    float4 fa, fb, fc;        // FP32 proxy data of the focus point
+    float qx, qy, qz;         // planar: relative coordinates; geographic: unit vector
+};
+
+// Tile classification: -1 entirely below T_lo, +1 entirely above T_hi, 0 straddles.
+// Planar thresholds are squared distances, geographic ones 3-D chords.
 template <bool GEO>
-__global__ void __launch_bounds__(SEL_THREADS) k_select(DevPoints P, unsigned rank, uint64_t klo, int shift0,
-                                                        double* __restrict__ out)
+__device__ __forceinline__ int classify_tile(const float4& tb, const RowCtx& c, float below_thr, float above_thr)
+{
+    if (GEO) {
+        const float dx = tb.x - c.qx, dy = tb.y - c.qy, dz = tb.z - c.qz;
+        const float cc = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+        const float hi = (cc + tb.w) * (1.0f + 1e-5f) + 1e-7f;
+        const float lo = (cc - tb.w) * (1.0f - 1e-5f) - 1e-7f;
+        if (hi < below_thr) return -1;
+        if (lo > above_thr && hi < 1.8640781f) return 1;
+        return 0;
+    } else {
+        const float ex = fmaxf(0.0f, fmaxf(tb.x - c.qx, c.qx - tb.y));
+        const float ey = fmaxf(0.0f, fmaxf(tb.z - c.qy, c.qy - tb.w));
+        const float fx = fmaxf(c.qx - tb.x, tb.y - c.qx);
+        const float fy = fmaxf(c.qy - tb.z, tb.w - c.qy);
+        const float dmin2 = fmaf(ex, ex, ey * ey) * (1.0f - 1e-5f);
+        const float dmax2 = fmaf(fx, fx, fy * fy) * (1.0f + 1e-5f);
+        if (dmax2 < below_thr) return -1;
+        if (dmin2 > above_thr) return 1;
+        return 0;
+    }
+}
+
+// Runs passes over one row until the rank's value in [T_lo, T_hi] is found.
+// EXACT: values are the reference's FP64 distances (proxy band as a filter);
+// otherwise the FP32 proxies.  Returns false when the bracket does not hold
+// the rank or the pass limit is reached.  The first pass may store its
+// histogram (coarse log window over [0, +inf]) in cache_row.
+template <bool GEO, bool EXACT>
+__device__ bool select_row(SelShared& sh, const SelectArgs& a, const RowCtx& c, double T_lo, double T_hi, Window w,
+                           unsigned* cache_row, double& result)
+{
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int n = a.n;
+    const double INF = __longlong_as_double(0x7ff0000000000000ll);
+    for (int pass = 0; pass < SEL_MAX_PASSES; pass++) {
+        float below_thr, above_thr;
+        if (GEO) {
+            const double a2 = 2.0 * 6378.137;
+            const double f = 1.0 / 298.257223563;
+            const double wl = T_lo / (a2 * (1.0 + f));
+            below_thr = wl <= 0.0 ? -1.0f : (wl >= 1.5 ? 1e30f : (float)(2.0 * sin(wl) * (1.0 - 1e-6)));
+            const double wh = T_hi / (a2 * (1.0 - 2.6 * f));
+            above_thr = (wh >= 1.2) ? 1e30f : (float)(2.0 * sin(wh) * (1.0 + 1e-6));
+        } else {
+            below_thr = T_lo > 0.0 ? (float)(T_lo * T_lo * (1.0 - 1e-6)) : -1.0f;
+            above_thr = isinf(T_hi) ? 3e38f : (float)(T_hi * T_hi * (1.0 + 1e-6));
+        }
+        for (int b = t; b < SEL_BINS; b += SEL_THREADS) sh.hist[b] = 0;
+        if (t == 0) sh.ncand = 0;
+        __syncthreads();
+        unsigned below = 0;
+        // each lane classifies one tile; the warp then walks the straddling ones
+        for (int tbase = warp * 32; tbase < a.ntiles; tbase += SEL_WARPS * 32) {
+            const int mytile = tbase + lane;
+            int cls = 1;
+            if (mytile < a.ntiles) cls = classify_tile<GEO>(a.tb[mytile], c, below_thr, above_thr);
+            if (cls < 0) below += (unsigned)min(SEL_TILE, n - mytile * SEL_TILE);
+            unsigned straddle = __ballot_sync(0xffffffffu, cls == 0);
+            while (straddle) {
+                const int k = __ffs(straddle) - 1;
+                straddle &= straddle - 1;
+                const int tile = tbase + k;
+                const int j = tile * SEL_TILE + lane;
+                bool in = false;
+                uint64_t key = 0;
+                if (j < n) {
+                    float d32;
+                    bool sure = true;
+                    if (GEO) {
+                        d32 = geo_dist32(c.fa, c.fb, c.fc, a.pts[3 * (size_t)j], a.pts[3 * (size_t)j + 1],
+                                         a.pts[3 * (size_t)j + 2]);
+                        // far-apart pairs (half-angle near pi/2): the FP32 formula is not trusted
+                        sure = isfinite(d32) && d32 < 15000.0f;
+                    } else {
+                        d32 = sqrtf(planar_d2_32(c.fa, a.pts[j]));
+                    }
+                    double d = (double)d32;
+                    bool eval = true;
+                    if (EXACT) {
+                        const double dl = sure ? d * (1.0 - a.eps) - a.delta : -1.0;
+                        const double dh = sure ? d * (1.0 + a.eps) + a.delta : INF;
+                        eval = false;
+                        if (dh < T_lo) below++;
+                        else if (!(dl > T_hi)) eval = true;
+                        if (eval) d = pair_dist<GEO>(a.P, j, c.fu, c.fv, c.fuR, c.fvR);
+                    }
+                    if (eval) {
+                        if (d < T_lo) below++;
+                        else if (d <= T_hi) {
+                            in = true;
+                            key = dkey(d);
+                        }
+                    }
+                }
+                const unsigned act = __ballot_sync(0xffffffffu, in);
+                if (act) {
+                    if (in) {
+                        const unsigned bin = bucket_of(w, key);
+                        const unsigned peers = __match_any_sync(act, bin);
+                        if (lane == __ffs(peers) - 1) atomicAdd(&sh.hist[bin], (unsigned)__popc(peers));
+                    }
+                    const int leader = __ffs(act) - 1;
+                    unsigned base = 0;
+                    if (lane == leader) base = atomicAdd(&sh.ncand, (unsigned)__popc(act));
+                    base = __shfl_sync(0xffffffffu, base, leader);
+                    if (in) {
+                        const unsigned slot = base + __popc(act & ((1u << lane) - 1u));
+                        if (slot < SEL_CAP) sh.cand[slot] = key;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) below += __shfl_xor_sync(0xffffffffu, below, off);
+        if (lane == 0) sh.below_w[warp] = below;
+        __syncthreads();
+        if (pass == 0 && cache_row)
+            for (int b = t; b < SEL_BINS; b += SEL_THREADS) cache_row[b] = sh.hist[b];
+        unsigned below_all = 0;
+        for (int q = 0; q < SEL_WARPS; q++) below_all += sh.below_w[q];
+        const unsigned ncand = sh.ncand;
+        if (a.rank <= below_all || a.rank > below_all + ncand) {
+            __syncthreads();
+            return false;
+        }
+        const unsigned krem = a.rank - below_all;
+        if (ncand <= (unsigned)SEL_CAP) {
+            bitonic_sort(sh, ncand);
+            result = keyd(sh.cand[krem - 1]);
+            __syncthreads();
+            return true;
+        }
+        scan_pick(sh, krem);
+        uint64_t lo, hi;
+        bin_range(w, sh.chosen_bin, lo, hi);
+        __syncthreads();
+        if (lo == hi) {
+            result = keyd(lo);
+            return true;
+        }
+        T_lo = keyd(lo);
+        T_hi = keyd(hi);
+        w = linear_window(lo, hi);
+    }
+    return false;
+}
+
+template <bool GEO, bool EXACT>
+__global__ void __launch_bounds__(SEL_THREADS) k_select(SelectArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SelShared& sh = *reinterpret_cast<SelShared*>(smem_raw);
-    for (int row = blockIdx.x; row < P.n; row += gridDim.x) {
-        const double fu = P.u[row], fv = P.v[row];
-        const double fuR = GEO ? P.uR[row] : 0.0, fvR = GEO ? P.vR[row] : 0.0;
-        Window w{klo, shift0, 0ull, ~0ull};
-        unsigned krem = rank;
-        hist_pass<GEO>(sh, P, w, fu, fv, fuR, fvR);
-        scan_pick(sh, krem);
-        unsigned b = sh.chosen_bin, cnt = sh.count;
-        krem -= sh.below;
-        uint64_t lo, hi;
-        bin_range(w, b, lo, hi);
-        __syncthreads();
-        while (cnt > (unsigned)SEL_CAP && lo != hi) {
-            uint64_t span = hi - lo;
-            int bits = 64 - __clzll((long long)span);
-            int s = bits > SEL_LOG_BINS ? bits - SEL_LOG_BINS : 0;
-            w = Window{lo, s, lo, hi};
-            hist_pass<GEO>(sh, P, w, fu, fv, fuR, fvR);
-            scan_pick(sh, krem);
-            b = sh.chosen_bin;
-            cnt = sh.count;
-            krem -= sh.below;
-            bin_range(w, b, lo, hi);
-            __syncthreads();
-        }
-        double result;
-        if (cnt == 0) {
-            result = __longlong_as_double(0x7ff8000000000000ll);  // unreachable for 1 <= rank <= n
-        } else if (lo == hi) {
-            result = keyd(lo);
+    const int t = threadIdx.x;
+    const DevPoints P = a.P;
+    const int n = a.n;
+    const double INF = __longlong_as_double(0x7ff0000000000000ll);
+    // coarse logarithmic window of the first pass over a whole row
+    const uint64_t klo = (uint64_t)__double_as_longlong(a.dlo) | 0x8000000000000000ull;
+    const uint64_t khi = (uint64_t)__double_as_longlong(a.dhi) | 0x8000000000000000ull;
+    const uint64_t kspan = khi > klo ? khi - klo : 1;
+    const int kbits = 64 - __clzll((long long)kspan);
+    const Window wlog{klo, kbits > SEL_LOG_BINS ? kbits - SEL_LOG_BINS : 0, dkey(0.0), dkey(INF)};
+
+    for (int row = blockIdx.x; row < n; row += gridDim.x) {
+        RowCtx c;
+        c.fu = P.u[row];
+        c.fv = P.v[row];
+        c.fuR = GEO ? P.uR[row] : 0.0;
+        c.fvR = GEO ? P.vR[row] : 0.0;
+        if (GEO) {
+            c.fa = a.pts[3 * (size_t)row];
+            c.fb = a.pts[3 * (size_t)row + 1];
+            c.fc = a.pts[3 * (size_t)row + 2];
+            c.qx = c.fa.x + c.fb.x;
+            c.qy = c.fa.y + c.fb.y;
+            c.qz = c.fa.z + c.fb.z;
         } else {
-            gather_pass<GEO>(sh, P, lo, hi, fu, fv, fuR, fvR);
-            const unsigned nc = min(sh.ncand, (unsigned)SEL_CAP);
-            bitonic_sort(sh, nc);
-            result = (krem >= 1 && krem <= nc) ? keyd(sh.cand[krem - 1]) : __longlong_as_double(0x7ff8000000000000ll);
+            c.fa = a.pts[row];
+            c.fb = c.fc = c.fa;
+            c.qx = c.fa.x + c.fa.y;
+            c.qy = c.fa.z + c.fa.w;
+            c.qz = 0.0f;
         }
-        if (threadIdx.x == 0) out[row] = result;
+        unsigned* cache_row = a.hist_cache ? a.hist_cache + (size_t)row * SEL_BINS : nullptr;
+        // stage A: the rank's FP32 proxy value
+        double T_lo = 0.0, T_hi = INF;
+        Window w = wlog;
+        bool ok = true;
+        if (cache_row && a.cache_valid) {
+            for (int b = t; b < SEL_BINS; b += SEL_THREADS) sh.hist[b] = cache_row[b];
+            __syncthreads();
+            scan_pick(sh, a.rank);
+            uint64_t lo, hi;
+            bin_range(wlog, sh.chosen_bin, lo, hi);
+            ok = sh.count > 0;
+            __syncthreads();
+            T_lo = keyd(lo);
+            T_hi = keyd(hi);
+            w = linear_window(lo, hi);
+            cache_row = nullptr;
+        }
+        double q = __longlong_as_double(0x7ff8000000000000ll);
+        if (ok) ok = select_row<GEO, false>(sh, a, c, T_lo, T_hi, w, a.cache_valid ? nullptr : cache_row, q);
+        double result = q;
+        // stage B: the reference's FP64 value, inside the proxy band around q
+        if (EXACT && ok) {
+            const double lo = q * (1.0 - a.eps) - a.delta, hi = q * (1.0 + a.eps) + a.delta;
+            const double blo = lo > 0.0 ? lo : 0.0;
+            ok = select_row<GEO, true>(sh, a, c, blo, hi, linear_window(dkey(blo), dkey(hi)), nullptr, result);
+        }
+        if (t == 0) {
+            if (!ok) {
+                atomicMax(a.err, 2);
+                result = __longlong_as_double(0x7ff8000000000000ll);
+            }
+            a.out[row] = result;
+        }
         __syncthreads();
     }
 }
@@ -261,32 +404,25 @@ cudaError_t launch_to_float(int n, const double* in, float* out, cudaStream_t st
 
 size_t select_smem_bytes() { return sizeof(SelShared); }
 
-cudaError_t launch_select(const DevPoints& P, bool geographic, unsigned rank, double dlo, double dhi,
-                          double* out, int num_sms, cudaStream_t stream)
+cudaError_t launch_select(const SelectArgs& a, bool geographic, bool exact, int num_sms, cudaStream_t stream)
 {
-    if (rank < 1 || rank > (unsigned)P.n) return cudaErrorInvalidValue;
-    // coarse logarithmic window: keys of [dlo, dhi] spread over the 4096 bins
-    uint64_t klo, khi;
-    {
-        uint64_t blo, bhi;
-        memcpy(&blo, &dlo, 8);
-        memcpy(&bhi, &dhi, 8);
-        klo = blo | 0x8000000000000000ull;
-        khi = bhi | 0x8000000000000000ull;
-    }
-    uint64_t span = khi > klo ? khi - klo : 1;
-    int bits = 64 - __builtin_clzll(span);
-    int shift0 = bits > SEL_LOG_BINS ? bits - SEL_LOG_BINS : 0;
-    int grid = num_sms * 6;
-    if (grid > P.n) grid = P.n;
-    size_t smem = sizeof(SelShared);
+    if (a.rank < 1 || a.rank > (unsigned)a.n) return cudaErrorInvalidValue;
+    int grid = num_sms * 12;
+    if (grid > a.n) grid = a.n;
+    const size_t smem = sizeof(SelShared);
+#define GW_SEL(G, E)                                                                                  \
+    do {                                                                                              \
+        cudaFuncSetAttribute(k_select<G, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        k_select<G, E><<<grid, SEL_THREADS, smem, stream>>>(a);                                       \
+    } while (0)
     if (geographic) {
-        cudaFuncSetAttribute(k_select<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_select<true><<<grid, SEL_THREADS, smem, stream>>>(P, rank, klo, shift0, out);
+        if (exact) GW_SEL(true, true);
+        else GW_SEL(true, false);
     } else {
-        cudaFuncSetAttribute(k_select<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_select<false><<<grid, SEL_THREADS, smem, stream>>>(P, rank, klo, shift0, out);
+        if (exact) GW_SEL(false, true);
+        else GW_SEL(false, false);
     }
+#undef GW_SEL
     return cudaGetLastError();
 }
 

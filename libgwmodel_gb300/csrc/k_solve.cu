@@ -226,7 +226,7 @@ constexpr int HAT_TILE = kTile;
 
 template <bool GEO>
 __global__ void __launch_bounds__(HAT_THREADS)
-    k_hat(DevPoints P, const TileBox* __restrict__ tiles, const TileCap* __restrict__ caps,
+    k_hat(DevPoints P, const float4* __restrict__ tb16, const float* __restrict__ tile_thr,
           const double* __restrict__ X, int p,
           const double* __restrict__ v, const double* __restrict__ thr, double bw, int kernel, int skip,
           double* __restrict__ qdiag, double* __restrict__ S, int row_target, double* __restrict__ s_row)
@@ -235,42 +235,27 @@ __global__ void __launch_bounds__(HAT_THREADS)
     double* sX = hsm;                          // HAT_THREADS x p (x_j of this block)
     double* sV = sX + HAT_THREADS * p;         // HAT_TILE x p   (v_i of the staged rows)
     __shared__ double su[HAT_TILE], sv[HAT_TILE], suR[HAT_TILE], svR[HAT_TILE], sr[HAT_TILE];
-    __shared__ TileBox sblock;
-    __shared__ TileCap scap;
+    __shared__ float4 sbound;
     const int n = P.n, t = threadIdx.x;
     const int j0 = blockIdx.x * HAT_THREADS, j = j0 + t;
     for (int e = t; e < HAT_THREADS * p; e += HAT_THREADS) {
         int jj = j0 + e / p;
         sX[e] = jj < n ? X[(size_t)j0 * p + e] : 0.0;
     }
-    if (t == 0) {
-        TileBox b = tiles[j0 / HAT_TILE];
-        int last = min(j0 + HAT_THREADS, n) - 1;
-        for (int q = j0 / HAT_TILE + 1; q <= last / HAT_TILE; q++) {
-            TileBox c = tiles[q];
-            b.ulo = fmin(b.ulo, c.ulo); b.uhi = fmax(b.uhi, c.uhi);
-            b.vlo = fmin(b.vlo, c.vlo); b.vhi = fmax(b.vhi, c.vhi);
-        }
-        sblock = b;
-        if (GEO && caps) scap = cap_union(caps, j0 / HAT_TILE, last / HAT_TILE);
-    }
+    if (t == 0) sbound = tb_union<GEO>(tb16, j0 / HAT_TILE, (min(j0 + HAT_THREADS, n) - 1) / HAT_TILE);
     __syncthreads();
     double du = 0.0, dv = 0.0, duR = 0.0, dvR = 0.0;
     if (j < n) {
         du = P.u[j]; dv = P.v[j];
         if (GEO) { duR = P.uR[j]; dvR = P.vR[j]; }
     }
-    const bool can_skip = skip && (!GEO || caps) && kernel >= GW_KERNEL_BISQUARE;
+    const bool can_skip = skip && tile_thr && kernel >= GW_KERNEL_BISQUARE;
+    const float4 fbound = sbound;
     double acc = 0.0;
     const int ntiles = (n + HAT_TILE - 1) / HAT_TILE;
     for (int tile = 0; tile < ntiles; tile++) {
         const int i0 = tile * HAT_TILE;
-        if (can_skip) {
-            double rmax = -1.0;
-            for (int q = 0; q < HAT_TILE && i0 + q < n; q++) rmax = fmax(rmax, thr ? thr[i0 + q] : bw);
-            const double lb = GEO ? cap_lower_bound(scap, caps[tile]) * (1.0 - 1e-9) : box_lower_bound(sblock, tiles[tile]);
-            if (rmax > 0.0 && lb * (1.0 - 1e-14) >= rmax) continue;
-        }
+        if (can_skip && tb_far<GEO>(fbound, tb16[tile], tile_thr[tile])) continue;  // uniform over the CTA
         if (t < HAT_TILE) {
             int i = i0 + t;
             bool ok = i < n;
@@ -366,7 +351,29 @@ __global__ void k_gather_subset(int n, int p, ColumnSet cs, const double* __rest
     }
 }
 
+template <bool GEO>
+__global__ void k_tile_far_thr(int n, int tile, const double* __restrict__ thr, double bw, float* __restrict__ out)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ntiles = (n + tile - 1) / tile;
+    if (t >= ntiles) return;
+    double rmax = -1.0;
+    for (int q = t * tile; q < min(n, (t + 1) * tile); q++) rmax = fmax(rmax, thr ? thr[q] : bw);
+    out[t] = tb_far_threshold<GEO>(rmax);
+}
+
 }  // namespace
+
+cudaError_t launch_tile_far_thr(int n, int tile, bool geographic, const double* thr, double bw, float* tile_thr,
+                                cudaStream_t stream)
+{
+    const int ntiles = (n + tile - 1) / tile;
+    if (geographic)
+        k_tile_far_thr<true><<<(ntiles + 255) / 256, 256, 0, stream>>>(n, tile, thr, bw, tile_thr);
+    else
+        k_tile_far_thr<false><<<(ntiles + 255) / 256, 256, 0, stream>>>(n, tile, thr, bw, tile_thr);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_column_sums(int n, int m, const double* Z, double* part, int nb, double* out, cudaStream_t stream)
 {
@@ -424,7 +431,7 @@ cudaError_t launch_reduce_partials(const double* partials, int nblocks, double* 
     return cudaGetLastError();
 }
 
-cudaError_t launch_hat_pass(const DevPoints& P, bool geographic, const TileBox* tiles, const TileCap* caps,
+cudaError_t launch_hat_pass(const DevPoints& P, bool geographic, const float4* tb16, const float* tile_thr,
                             const double* X, int p,
                             const double* v, const double* thr, double bw, int kernel, bool skip_tiles,
                             double* qdiag, double* S, int row_target, double* s_row, cudaStream_t stream)
@@ -432,10 +439,10 @@ cudaError_t launch_hat_pass(const DevPoints& P, bool geographic, const TileBox* 
     int grid = (P.n + HAT_THREADS - 1) / HAT_THREADS;
     size_t smem = (size_t)(HAT_THREADS + HAT_TILE) * p * sizeof(double);
     if (geographic)
-        k_hat<true><<<grid, HAT_THREADS, smem, stream>>>(P, tiles, caps, X, p, v, thr, bw, kernel, skip_tiles ? 1 : 0,
+        k_hat<true><<<grid, HAT_THREADS, smem, stream>>>(P, tb16, tile_thr, X, p, v, thr, bw, kernel, skip_tiles ? 1 : 0,
                                                          qdiag, S, row_target, s_row);
     else
-        k_hat<false><<<grid, HAT_THREADS, smem, stream>>>(P, tiles, caps, X, p, v, thr, bw, kernel, skip_tiles ? 1 : 0,
+        k_hat<false><<<grid, HAT_THREADS, smem, stream>>>(P, tb16, tile_thr, X, p, v, thr, bw, kernel, skip_tiles ? 1 : 0,
                                                           qdiag, S, row_target, s_row);
     return cudaGetLastError();
 }

@@ -33,7 +33,7 @@ __device__ __forceinline__ float geo_dist32(const float4& fa, const float4& fb, 
     const float C = fmaxf(1.0f - S, 0.0f);
     const float sq = sqrtf(S), cq = sqrtf(C);
     const float w = atan2f(sq, cq);
-    const float R = sq * cq / w;
+    const float R = __fdividef(sq * cq, w);
     const float dlat = (pa.w - fa.w) + (pb.w - fb.w);            // degrees
     const float G = dlat * 8.7266462599716478846e-3f;            // (pi/180)/2
     const float sG = sin_poly(G);
@@ -41,8 +41,8 @@ __device__ __forceinline__ float geo_dist32(const float4& fa, const float4& fb, 
     const float sF = pc.x * fc.y + pc.y * fc.x;                  // sin((lat_a+lat_b)/2)
     const float cF = pc.y * fc.y - pc.x * fc.x;
     const float sF2 = sF * sF, cF2 = cF * cF;
-    const float H1 = (3.0f * R - 1.0f) / (2.0f * C);
-    const float H2 = (3.0f * R + 1.0f) / (2.0f * S);
+    const float H1 = __fdividef(3.0f * R - 1.0f, 2.0f * C);
+    const float H2 = __fdividef(3.0f * R + 1.0f, 2.0f * S);
     const float f = 1.0f / 298.257223563f;
     return 2.0f * 6378.137f * w * (1.0f + f * H1 * sF2 * cG2 - f * H2 * cF2 * sG2);
 }

@@ -394,6 +394,27 @@ class Engine:
         check(lib().gwgpu_engine_max_distance(self._h, ctypes.byref(v)))
         return v.value
 
+    def golden(self, adaptive, kernel, criterion, lower, upper, cap=512):
+        """Golden-section bandwidth search on the resident data: (bandwidth, [(bw, criterion), ...])."""
+        bw = ctypes.c_double()
+        cnt = ctypes.c_int()
+        lb, lv = np.zeros(cap), np.zeros(cap)
+        check(lib().gwgpu_engine_golden(self._h, int(bool(adaptive)), int(kernel), int(criterion), float(lower),
+                                        float(upper), ctypes.byref(bw), ctypes.byref(cnt), dptr(lb), dptr(lv), cap))
+        k = min(cnt.value, cap)
+        return bw.value, list(zip(lb[:k].tolist(), lv[:k].tolist()))
+
+    def clear_cache(self):
+        check(lib().gwgpu_engine_clear_cache(self._h))
+
+    def record_event(self, slot):
+        check(lib().gwgpu_engine_event_record(self._h, int(slot)))
+
+    def elapsed_ms(self, first, second):
+        ms = ctypes.c_float()
+        check(lib().gwgpu_engine_event_elapsed(self._h, int(first), int(second), ctypes.byref(ms)))
+        return ms.value
+
     def thresholds(self, bw, adaptive=True):
         out = np.zeros(self.n)
         check(lib().gwgpu_engine_thresholds(self._h, float(bw), int(bool(adaptive)), dptr(out)))

@@ -189,3 +189,25 @@ def test_not_spd_is_dbl_max():
     assert e.criterion(50, True, O.BISQUARE, O.AIC) == np.finfo(np.float64).max
     with pytest.raises(Exception):
         e.fit(50, True, O.BISQUARE, True)
+
+
+def test_thresholds_reuse_cached_histograms(planar, geo):
+    """Many bandwidths on one engine: later selects start from the cached
+    per-row histograms and must stay bit-exact."""
+    for pbm, geographic in ((planar, False), (geo, True)):
+        e = engine_for(pbm.x, pbm.y, pbm.coords, geographic)
+        pb = O.Problem(pbm.x, pbm.y, pbm.coords, geographic=geographic)
+        dists = [pb.distance_row(i) for i in range(pb.n)]
+        for bw in (pb.n // 2, 25, pb.n // 5, 120.5, pb.n - 1, 64, pb.n + 10):
+            got = e.thresholds(bw)
+            want = np.array([O.adaptive_threshold(d, bw) for d in dists])
+            assert np.array_equal(got, want), (geographic, bw, np.flatnonzero(got != want)[:5])
+
+
+def test_mixed_thresholds_close_to_exact(geo):
+    """The mixed path selects on FP32 proxy distances: within 1e-5 relative."""
+    e = engine_for(geo.x, geo.y, geo.coords, True)
+    exact = e.thresholds(150)
+    e.set_precision(1)
+    approx = e.thresholds(150)
+    assert np.max(np.abs(approx - exact) / exact) < 1e-5
