@@ -173,6 +173,30 @@ int gwgpu_engine_reset_stats(gwgpu_engine* e);
  * contraction (TF32 inputs, FP32 output; N a multiple of 16 up to 256). */
 int gwgpu_engine_tc_selftest(gwgpu_engine* e, int N, const float* A, const float* B, float* D);
 
+/* ------------------------------------------------ no-allocation entry point */
+
+/* Criterion of one bandwidth from normal equations the caller already holds
+ * on the device, without allocating any device memory.  No counterpart in
+ * libgwmodel.  For callers that cannot let a library call cudaMalloc: code
+ * that owns all device memory through its own pool, must not allocate after
+ * start-up, or is about to be recorded into a CUDA graph.
+ *
+ * Inputs (device pointers): G, n x (p(p+1)/2 + p) row-major -- per location
+ * the upper triangle of X^T W_i X packed by rows, then X^T W_i y (for CV with
+ * w_ii = 0); X, n x p row-major; y, n; thr, per-row bandwidth or NULL for the
+ * fixed `bandwidth` (it only gives w_ii through `kernel`).  Outputs (device):
+ * beta, n x p row-major; sums[5] = tr(S), RSS (or CV sum), 0, failed local
+ * solves, and the criterion (AICc or CV; DBL_MAX on failure).  Runs
+ * asynchronously on `stream` (a cudaStream_t, NULL for the default stream).
+ *
+ * Limits: n in [3, 65536], p in [1, 32].  Scratch is a fixed ~1.2 MB
+ * __device__ array shared by all calls on a device: calls that overlap on
+ * the GPU race, so serialise them.  The first call on a device resolves the
+ * array's address (cudaGetSymbolAddress); make it before any stream capture. */
+int gwgpu_criterion_noalloc(int n, int p, int criterion, int kernel, double bandwidth, const double* G,
+                            const double* X, const double* y, const double* thr, double* beta, double* sums,
+                            void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -98,6 +98,7 @@ SIGNATURES = [
     ("gwgpu_engine_enable_stats", _i, [_vp, _i]),
     ("gwgpu_engine_get_stats", _i, [_vp, ctypes.POINTER(Stats)]),
     ("gwgpu_engine_reset_stats", _i, [_vp]),
+    ("gwgpu_criterion_noalloc", _i, [_i, _i, _i, _i, _d, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     ("gwgpu_engine_tc_selftest", _i, [_vp, _i, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
                                       ctypes.POINTER(ctypes.c_float)]),
 ]

@@ -68,6 +68,12 @@ private:
 
 }  // namespace
 
+namespace gwgpu {
+// Sets the calling thread's gwgpu_last_error() message (used by entry points
+// defined in other translation units).
+void set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
+}  // namespace gwgpu
+
 struct gwgpu_gwr {
     gwm::GWRBasic alg;
     double bandwidth = 0.0;
