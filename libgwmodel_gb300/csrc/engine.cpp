@@ -267,7 +267,7 @@ void Engine::buildProxy()
         }
         uc /= n;
         vc /= n;
-        pts.resize(n);
+        pts.assign((size_t)ntiles32_ * 32, make_float4(0.f, 0.f, 0.f, 0.f));  // whole tiles for bulk copies
         for (int s = 0; s < n; s++) {
             float a, b, c, d;
             split(hu_[s] - uc, a, b);
@@ -275,7 +275,7 @@ void Engine::buildProxy()
             pts[s] = make_float4(a, b, c, d);
         }
     } else {
-        pts.resize((size_t)3 * n);
+        pts.assign((size_t)3 * ntiles32_ * 32, make_float4(0.f, 0.f, 0.f, 0.f));
         const double DE2RA = M_PI / 180;
         for (int s = 0; s < n; s++) {
             const double lat = hv_[s] * DE2RA, lon = hu_[s] * DE2RA;
@@ -759,12 +759,19 @@ void Engine::fit(double bw, bool adaptive, int kernel, bool storeS, FitOutput& o
     check(cudaMemsetAsync(S_.get(), 0, sizeof(double) * S_.size(), stream_), "memset S");
     check(launch_tile_far_thr(n, kTile, geographic_, thrPtr(adaptive), bw, tile_thr16_.get(), stream_), "tile thr");
     stats_.kernel_launches += 2;  // tile thresholds and the hat pass
-    check(launch_hat_pass(points(), geographic_, tb16_.get(), tile_thr16_.get(), mixed ? xs_.get() : x_.get(), p,
-                          vvec_.get(),
-                          thrPtr(adaptive), bw, kernel,
-                          true, qdiag_.get(), storeS ? S_.get() : nullptr, storeS ? -1 : last_sorted,
-                          storeS ? nullptr : S_.get(), stream_),
-          "hat pass");
+    if (mixed) {
+        if (adaptive) check(launch_to_float(n_, thr_.get(), thr32_.get(), stream_), "thr32");
+        check(launch_hat_mixed(n, geographic_, pts32_.get(), tb16_.get(), tile_thr16_.get(), xs_.get(), p,
+                               vvec_.get(), adaptive ? thr32_.get() : nullptr, (float)bw, kernel, qdiag_.get(),
+                               storeS ? S_.get() : nullptr, storeS ? -1 : last_sorted, storeS ? nullptr : S_.get(),
+                               stream_),
+              "hat pass");
+    } else {
+        check(launch_hat_pass(points(), geographic_, tb16_.get(), tile_thr16_.get(), x_.get(), p, vvec_.get(),
+                              thrPtr(adaptive), bw, kernel, true, qdiag_.get(), storeS ? S_.get() : nullptr,
+                              storeS ? -1 : last_sorted, storeS ? nullptr : S_.get(), stream_),
+              "hat pass");
+    }
     std::vector<double> hb((size_t)n * p), hse((size_t)n * p), hq(n), hsii(n), hres(n);
     check(cudaMemcpyAsync(hb.data(), beta_.get(), sizeof(double) * hb.size(), cudaMemcpyDeviceToHost, stream_), "D2H");
     check(cudaMemcpyAsync(hse.data(), bse_.get(), sizeof(double) * hse.size(), cudaMemcpyDeviceToHost, stream_), "D2H");

@@ -141,6 +141,11 @@ struct RefineArgs {
 };
 cudaError_t launch_refine_residual(const RefineArgs& a, bool geographic, cudaStream_t stream);
 
+// Mixed-precision hat pass: the FP32 weights of the tensor-core contraction.
+cudaError_t launch_hat_mixed(int n, bool geographic, const float4* pts, const float4* tb16, const float* tile_thr,
+                             const double* X, int p, const double* v, const float* thr32, float bw, int kernel,
+                             double* qdiag, double* S, int row_target, double* s_row, cudaStream_t stream);
+
 // tile_thr[t] = far-test threshold of the largest r_i (thr, or bw) over tile t of `tile` points.
 cudaError_t launch_tile_far_thr(int n, int tile, bool geographic, const double* thr, double bw, float* tile_thr,
                                 cudaStream_t stream);

@@ -36,6 +36,7 @@ constexpr uint32_t TC_WAIT = 1u << 22;
 struct Smem {
     uint64_t bar_b[2];
     uint64_t bar_mma[2];
+    uint64_t bar_p[2];
     uint32_t tmem_base;
     int abort;
 };
@@ -77,6 +78,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
         for (int s = 0; s < 2; s++) {
             mbar_init(&ctl.bar_b[s], 1);
             mbar_init(&ctl.bar_mma[s], 1);
+            mbar_init(&ctl.bar_p[s], 1);
         }
         ctl.abort = 0;
         fence_mbar_init();
@@ -85,6 +87,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
     __syncthreads();
     fence_after_sync();
     const uint32_t tmem = ctl.tmem_base;
+    constexpr int NF = GEO ? 3 : 1;                      // float4 per point
+    constexpr uint32_t P_BYTES = NF * 16u * TC_BK;       // point data of one tile
 
     // focus point
     float4 fa = make_float4(0.f, 0.f, 0.f, 0.f), fb = fa, fc = fa;
@@ -117,6 +121,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
     // tiles this CTA must visit, one bit per 32-point tile
     uint32_t* tmask = reinterpret_cast<uint32_t*>(stage0 + 2 * (size_t)stage_bytes);
     const int nwords = (a.ntiles + 31) / 32;
+    // point data of the current and the next tile (prefetched by TMA)
+    float4* ptsbuf = reinterpret_cast<float4*>(stage0 + 2 * (size_t)stage_bytes + (((size_t)nwords * 4 + 15) & ~(size_t)15));
     for (int wd = t; wd < nwords; wd += TC_THREADS) {
         uint32_t bits = 0;
         for (int b = 0; b < 32; b++) {
@@ -164,11 +170,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
 
     int word = 0;
     uint32_t bits = nwords > 0 ? tmask[0] : 0u;
-    while (!aborted) {
+    auto next_tile = [&]() -> int {
         while (bits == 0 && ++word < nwords) bits = tmask[word];
-        if (bits == 0) break;
-        const int tile = word * 32 + (__ffs(bits) - 1);
+        if (bits == 0) return -1;
+        const int tl = word * 32 + (__ffs(bits) - 1);
         bits &= bits - 1;
+        return tl;
+    };
+    // thread 0 records what it has in flight, for a clean exit after an abort
+    int last_b = -1;    // issue index of the last Z copy
+    int last_p = -1;    // issue index whose point data was last requested
+    int last_mma = -1;  // issue index of the last MMA commit
+    int tile = next_tile();
+    if (tile >= 0 && t == 0) {
+        mbar_arrive_expect_tx(&ctl.bar_p[0], P_BYTES);
+        bulk_g2s(ptsbuf, a.pts + (size_t)NF * TC_BK * tile, P_BYTES, &ctl.bar_p[0]);
+        last_p = 0;
+    }
+    while (tile >= 0 && !aborted) {
+        const int ntile = next_tile();
         const int s = issued & 1;
         unsigned char* st = stage0 + (size_t)s * stage_bytes;
         unsigned char* A_hi = st;
@@ -182,25 +202,43 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
         if (t == 0) {
             mbar_arrive_expect_tx(&ctl.bar_b[s], 2u * b_bytes);
             bulk_g2s(B_hi, a.zimg + (size_t)tile * 2u * b_bytes, 2u * b_bytes, &ctl.bar_b[s]);
+            last_b = issued;
+            if (ntile >= 0) {
+                // the other buffer was last read before the previous iteration's barrier
+                mbar_arrive_expect_tx(&ctl.bar_p[s ^ 1], P_BYTES);
+                bulk_g2s(ptsbuf + (size_t)(s ^ 1) * NF * TC_BK, a.pts + (size_t)NF * TC_BK * ntile, P_BYTES,
+                         &ctl.bar_p[s ^ 1]);
+                last_p = issued + 1;
+            }
         }
+        if (!mbar_wait(&ctl.bar_p[s], (uint32_t)((issued >> 1) & 1), TC_WAIT)) atomicExch(&ctl.abort, 1);
+        const float4* tp = ptsbuf + (size_t)s * NF * TC_BK;
         // weight tile: thread (r, quarter) fills points [8*quarter, 8*quarter + 8) of row r
-        const int jbase = tile * TC_BK + quarter * 8;
+        const int kbase = quarter * 8;
 #pragma unroll
         for (int q4 = 0; q4 < 2; q4++) {
             float hi[4], lo[4];
 #pragma unroll
             for (int e = 0; e < 4; e++) {
-                const int j = jbase + q4 * 4 + e;
+                const int k = kbase + q4 * 4 + e;
+                const int j = tile * TC_BK + k;
                 float w = 0.0f;
                 if (row_ok && j < a.n) {
-                    w = mixed_weight<GEO>(a.pts, j, fa, fb, fc, a.kernel, rr, inv_r2);
+                    float d2;
+                    if (GEO) {
+                        const float d = geo_dist32(fa, fb, fc, tp[3 * k], tp[3 * k + 1], tp[3 * k + 2]);
+                        d2 = d * d;
+                    } else {
+                        d2 = planar_d2_32(fa, tp[k]);
+                    }
+                    w = weight32(a.kernel, d2, rr, inv_r2);
                     if (a.exclude_self && i == j) w = 0.0f;
                     if (a.wpow == 2) w = w * w;
                 }
                 hi[e] = to_tf32(w);
                 lo[e] = to_tf32(w - hi[e]);
             }
-            const uint32_t off = sw128_offset((uint32_t)r, (uint32_t)(quarter * 8 + q4 * 4));
+            const uint32_t off = sw128_offset((uint32_t)r, (uint32_t)(kbase + q4 * 4));
             *reinterpret_cast<float4*>(A_hi + off) = make_float4(hi[0], hi[1], hi[2], hi[3]);
             *reinterpret_cast<float4*>(A_lo + off) = make_float4(lo[0], lo[1], lo[2], lo[3]);
         }
@@ -227,11 +265,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
                     mma_tf32(tmem, alo + dk, bhi + dk, idesc, 1u);
                 }
                 mma_commit(&ctl.bar_mma[s]);
+                last_mma = issued;
             }
         }
         issued++;
         in_chunk++;
         if (in_chunk >= a.flush_tiles) flush(issued - 1);
+        tile = ntile;
     }
     if (!aborted && in_chunk > 0) flush(issued - 1);
     __syncthreads();
@@ -251,11 +291,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
         }
     } else if (t == 0) {
         atomicExch(a.err, 1);
-        // leave no MMA in flight before TMEM is freed
-        if (issued > 0) {
-            const int ls = issued - 1;
-            mbar_wait(&ctl.bar_mma[ls & 1], (uint32_t)((ls >> 1) & 1), TC_WAIT);
-        }
+        // leave no MMA and no bulk copy in flight before TMEM and the CTA go away
+        if (last_mma >= 0) mbar_wait(&ctl.bar_mma[last_mma & 1], (uint32_t)((last_mma >> 1) & 1), TC_WAIT);
+        if (last_b >= 0) mbar_wait(&ctl.bar_b[last_b & 1], (uint32_t)((last_b >> 1) & 1), TC_WAIT);
+        if (last_p >= 0) mbar_wait(&ctl.bar_p[last_p & 1], (uint32_t)((last_p >> 1) & 1), TC_WAIT);
     }
     fence_before_sync();
     __syncthreads();
@@ -337,7 +376,8 @@ __global__ void k_build_zimg(int n, int mcols, int npad, const double* __restric
 
 size_t contract_tc_smem_bytes(int npad, int ntiles)
 {
-    return 1024 + 2 * (2 * (size_t)TC_A_BYTES + 2 * (size_t)npad * 128) + 4 * (size_t)((ntiles + 31) / 32);
+    const size_t mask = ((size_t)((ntiles + 31) / 32) * 4 + 15) & ~(size_t)15;
+    return 1024 + 2 * (2 * (size_t)TC_A_BYTES + 2 * (size_t)npad * 128) + mask + 2 * 3 * 16 * TC_BK;
 }
 
 cudaError_t launch_contract_tc(const TcArgs& a, bool geographic, cudaStream_t stream)

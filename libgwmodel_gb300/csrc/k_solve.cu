@@ -13,6 +13,7 @@
 //  * k_maxdist      CRSDistance::maxDistance (CRSDistance.cpp:133-143)
 #include "gw_common.cuh"
 #include "gw_kernels.h"
+#include "mixed_weight.cuh"
 
 namespace gwgpu {
 
@@ -293,6 +294,86 @@ __global__ void __launch_bounds__(HAT_THREADS)
     if (j < n) qdiag[j] = acc;
 }
 
+// Mixed-precision hat pass: the weights are the FP32 weights of the tensor-core
+// contraction (FP32 proxy distance, FP32 threshold); dot products and sums in FP64.
+template <bool GEO>
+__global__ void __launch_bounds__(HAT_THREADS)
+    k_hat_mixed(int n, const float4* __restrict__ pts, const float4* __restrict__ tb16,
+                const float* __restrict__ tile_thr, const double* __restrict__ X, int p,
+                const double* __restrict__ v, const float* __restrict__ thr32, float bw, int kernel,
+                double* __restrict__ qdiag, double* __restrict__ S, int row_target, double* __restrict__ s_row)
+{
+    extern __shared__ double hsm[];
+    double* sX = hsm;                       // HAT_THREADS x p
+    double* sV = sX + HAT_THREADS * p;      // HAT_TILE x p
+    constexpr int NF = GEO ? 3 : 1;
+    __shared__ float4 sf[HAT_TILE][NF];
+    __shared__ float sr[HAT_TILE], sinv[HAT_TILE];
+    __shared__ float4 sbound;
+    const int t = threadIdx.x;
+    const int j0 = blockIdx.x * HAT_THREADS, j = j0 + t;
+    for (int e = t; e < HAT_THREADS * p; e += HAT_THREADS) {
+        int jj = j0 + e / p;
+        sX[e] = jj < n ? X[(size_t)j0 * p + e] : 0.0;
+    }
+    if (t == 0) sbound = tb_union<GEO>(tb16, j0 / HAT_TILE, (min(j0 + HAT_THREADS, n) - 1) / HAT_TILE);
+    __syncthreads();
+    float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), pb = pa, pc = pa;
+    if (j < n) {
+        pa = pts[NF * (size_t)j];
+        if (GEO) {
+            pb = pts[3 * (size_t)j + 1];
+            pc = pts[3 * (size_t)j + 2];
+        }
+    }
+    const bool can_skip = tile_thr && kernel >= GW_KERNEL_BISQUARE;
+    const float4 fbound = sbound;
+    double acc = 0.0;
+    const int ntiles = (n + HAT_TILE - 1) / HAT_TILE;
+    for (int tile = 0; tile < ntiles; tile++) {
+        const int i0 = tile * HAT_TILE;
+        if (can_skip && tb_far<GEO>(fbound, tb16[tile], tile_thr[tile])) continue;  // uniform over the CTA
+        if (t < HAT_TILE) {
+            const int i = i0 + t;
+            const bool ok = i < n;
+            for (int q = 0; q < NF; q++) sf[t][q] = ok ? pts[NF * (size_t)i + q] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float r = ok ? (thr32 ? thr32[i] : bw) : 1.0f;
+            sr[t] = r;
+            sinv[t] = 1.0f / (r * r);
+        }
+        for (int e = t; e < HAT_TILE * p; e += HAT_THREADS) {
+            int i = i0 + e / p;
+            sV[e] = i < n ? v[(size_t)i0 * p + e] : 0.0;
+        }
+        __syncthreads();
+        if (j < n) {
+            const int iend = min(HAT_TILE, n - i0);
+            for (int q = 0; q < iend; q++) {
+                float d2;
+                if (GEO) {
+                    const float d = geo_dist32(sf[q][0], sf[q][1], sf[q][2], pa, pb, pc);
+                    d2 = d * d;
+                } else {
+                    d2 = planar_d2_32(sf[q][0], pa);
+                }
+                const double w = (double)weight32(kernel, d2, sr[q], sinv[q]);
+                double s = 0.0;
+                if (w != 0.0) {
+                    double dot = 0.0;
+                    for (int r = 0; r < p; r++) dot += sV[q * p + r] * sX[t * p + r];
+                    s = w * dot;
+                }
+                const double e = (i0 + q == j) ? 1.0 - s : -s;
+                acc += e * e;
+                if (S) S[(size_t)(i0 + q) * n + j] = s;
+                if (i0 + q == row_target) s_row[j] = s;
+            }
+        }
+        __syncthreads();
+    }
+    if (j < n) qdiag[j] = acc;
+}
+
 template <bool GEO>
 __global__ void k_maxdist(DevPoints P, unsigned long long* __restrict__ key)
 {
@@ -444,6 +525,21 @@ cudaError_t launch_hat_pass(const DevPoints& P, bool geographic, const float4* t
     else
         k_hat<false><<<grid, HAT_THREADS, smem, stream>>>(P, tb16, tile_thr, X, p, v, thr, bw, kernel, skip_tiles ? 1 : 0,
                                                           qdiag, S, row_target, s_row);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_hat_mixed(int n, bool geographic, const float4* pts, const float4* tb16, const float* tile_thr,
+                             const double* X, int p, const double* v, const float* thr32, float bw, int kernel,
+                             double* qdiag, double* S, int row_target, double* s_row, cudaStream_t stream)
+{
+    int grid = (n + HAT_THREADS - 1) / HAT_THREADS;
+    size_t smem = (size_t)(HAT_THREADS + HAT_TILE) * p * sizeof(double);
+    if (geographic)
+        k_hat_mixed<true><<<grid, HAT_THREADS, smem, stream>>>(n, pts, tb16, tile_thr, X, p, v, thr32, bw, kernel,
+                                                               qdiag, S, row_target, s_row);
+    else
+        k_hat_mixed<false><<<grid, HAT_THREADS, smem, stream>>>(n, pts, tb16, tile_thr, X, p, v, thr32, bw, kernel,
+                                                                qdiag, S, row_target, s_row);
     return cudaGetLastError();
 }
 
