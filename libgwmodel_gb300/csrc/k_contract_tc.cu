@@ -52,9 +52,11 @@ __device__ __forceinline__ float2 df_add(float2 a, float v)
     return make_float2(hi, lo - (hi - s));
 }
 
-template <bool GEO>
+// KERN: the weight kernel when fixed at compile time, -1 to read it from the arguments.
+template <bool GEO, int KERN>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
 {
+    const int kernel = KERN >= 0 ? KERN : a.kernel;
     extern __shared__ unsigned char smem_dyn[];
     __shared__ Smem ctl;
     // 1024-byte aligned stage buffers: [A_hi A_lo B_hi B_lo] x 2
@@ -103,6 +105,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
     }
     const float rr = row_ok ? (a.thr ? a.thr[i] : a.bw) : 1.0f;
     const float inv_r2 = 1.0f / (rr * rr);
+    // pairs with a haversine term in [s_cut, 0.86] have weight 0 under a compact kernel
+    const float s_cut = (GEO && kernel >= GW_KERNEL_BISQUARE) ? geo_s_cut(rr) : __int_as_float(0x7f800000);
 
     // block bound and largest threshold for tile skipping
     __shared__ float red[TC_THREADS / 32];
@@ -117,7 +121,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
     for (int q = 1; q < TC_THREADS / 32; q++) rmax = fmaxf(rmax, red[q]);
     const float4 fbound = fbound_s;
     const float far_thr =
-        (a.skip && a.kernel >= GW_KERNEL_BISQUARE) ? tb_far_threshold<GEO>((double)rmax) : -1.0f;
+        (a.skip && kernel >= GW_KERNEL_BISQUARE) ? tb_far_threshold<GEO>((double)rmax) : -1.0f;
     // tiles this CTA must visit, one bit per 32-point tile
     uint32_t* tmask = reinterpret_cast<uint32_t*>(stage0 + 2 * (size_t)stage_bytes);
     const int nwords = (a.ntiles + 31) / 32;
@@ -224,16 +228,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
                 const int j = tile * TC_BK + k;
                 float w = 0.0f;
                 if (row_ok && j < a.n) {
-                    float d2;
+                    float d2 = 0.0f;
+                    bool beyond = false;
                     if (GEO) {
-                        const float d = geo_dist32(fa, fb, fc, tp[3 * k], tp[3 * k + 1], tp[3 * k + 2]);
-                        d2 = d * d;
+                        const float S = geo_haversine32(fa, fb, tp[3 * k], tp[3 * k + 1]);
+                        beyond = S >= s_cut && S <= 0.86f;
+                        if (!beyond) {
+                            const float d = geo_dist32_from_S(S, fa, fb, fc, tp[3 * k], tp[3 * k + 1], tp[3 * k + 2]);
+                            d2 = d * d;
+                        }
                     } else {
                         d2 = planar_d2_32(fa, tp[k]);
                     }
-                    w = weight32(a.kernel, d2, rr, inv_r2);
-                    if (a.exclude_self && i == j) w = 0.0f;
-                    if (a.wpow == 2) w = w * w;
+                    if (!beyond) {
+                        w = weight32(kernel, d2, rr, inv_r2);
+                        if (a.exclude_self && i == j) w = 0.0f;
+                        if (a.wpow == 2) w = w * w;
+                    }
                 }
                 hi[e] = to_tf32(w);
                 lo[e] = to_tf32(w - hi[e]);
@@ -386,12 +397,18 @@ cudaError_t launch_contract_tc(const TcArgs& a, bool geographic, cudaStream_t st
     const size_t smem = contract_tc_smem_bytes(a.npad, a.ntiles);
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
     const int grid = (a.n + TC_M - 1) / TC_M;
+    auto go = [&](auto kfn) {
+        cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        kfn<<<grid, TC_THREADS, smem, stream>>>(a);
+    };
     if (geographic) {
-        cudaFuncSetAttribute(k_contract_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_contract_tc<true><<<grid, TC_THREADS, smem, stream>>>(a);
+        if (a.kernel == GW_KERNEL_BISQUARE) go(k_contract_tc<true, GW_KERNEL_BISQUARE>);
+        else if (a.kernel == GW_KERNEL_GAUSSIAN) go(k_contract_tc<true, GW_KERNEL_GAUSSIAN>);
+        else go(k_contract_tc<true, -1>);
     } else {
-        cudaFuncSetAttribute(k_contract_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_contract_tc<false><<<grid, TC_THREADS, smem, stream>>>(a);
+        if (a.kernel == GW_KERNEL_BISQUARE) go(k_contract_tc<false, GW_KERNEL_BISQUARE>);
+        else if (a.kernel == GW_KERNEL_GAUSSIAN) go(k_contract_tc<false, GW_KERNEL_GAUSSIAN>);
+        else go(k_contract_tc<false, -1>);
     }
     return cudaGetLastError();
 }

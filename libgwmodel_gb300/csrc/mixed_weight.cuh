@@ -20,20 +20,53 @@ __device__ __forceinline__ float sin_poly(float x)
     return x - x * z * p;
 }
 
-// FP32 great-circle distance (km) of the reference's Lambert formula with the
-// haversine term taken from the 3-D chord of hi/lo unit vectors.
-__device__ __forceinline__ float geo_dist32(const float4& fa, const float4& fb, const float4& fc, const float4& pa,
-                                            const float4& pb, const float4& pc)
+// asin(x) / x for S = x^2 <= 0.25, from the Maclaurin series
+// asin x = sum_k (2k)! / (4^k (k!)^2 (2k + 1)) x^(2k+1) truncated after k = 10
+// (the first omitted term is below 2e-9 relative at S = 0.25).
+__device__ __forceinline__ float asin_over_x(float S)
+{
+    float p = 8.3903358096168155e-03f;      // k = 10: 46189 / 5505024
+    p = fmaf(p, S, 9.7616095291940789e-03f);  // k = 9: 12155 / 1245184
+    p = fmaf(p, S, 1.1551800896139706e-02f);  // k = 8: 6435 / 557056
+    p = fmaf(p, S, 1.3964843750000000e-02f);  // k = 7: 143 / 10240
+    p = fmaf(p, S, 1.7352764423076924e-02f);  // k = 6: 231 / 13312
+    p = fmaf(p, S, 2.2372159090909092e-02f);  // k = 5: 63 / 2816
+    p = fmaf(p, S, 3.0381944444444444e-02f);  // k = 4: 35 / 1152
+    p = fmaf(p, S, 4.4642857142857144e-02f);  // k = 3: 5 / 112
+    p = fmaf(p, S, 7.5000000000000000e-02f);  // k = 2: 3 / 40
+    p = fmaf(p, S, 1.6666666666666666e-01f);  // k = 1: 1 / 6
+    return fmaf(p, S, 1.0f);
+}
+
+// Haversine term S = sin^2(theta / 2) of the pair: a quarter of the squared
+// chord between the hi/lo unit vectors.
+__device__ __forceinline__ float geo_haversine32(const float4& fa, const float4& fb, const float4& pa, const float4& pb)
 {
     const float dx = (pa.x - fa.x) + (pb.x - fb.x);
     const float dy = (pa.y - fa.y) + (pb.y - fb.y);
     const float dz = (pa.z - fa.z) + (pb.z - fb.z);
-    const float S = 0.25f * fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    return 0.25f * fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+}
+
+// FP32 great-circle distance (km) of the reference's Lambert formula, given
+// the haversine term S of the pair.  With S = sin^2 w (w = theta / 2) and
+// C = 1 - S: w = sqrt(S) asin_over_x(S) and R = sqrt(S C) / w =
+// sqrt(C) / asin_over_x(S) for S <= 0.25; atan2 beyond.
+__device__ __forceinline__ float geo_dist32_from_S(float S, const float4& fa, const float4& fb, const float4& fc,
+                                                   const float4& pa, const float4& pb, const float4& pc)
+{
     if (!(S > 0.0f)) return 0.0f;
     const float C = fmaxf(1.0f - S, 0.0f);
-    const float sq = sqrtf(S), cq = sqrtf(C);
-    const float w = atan2f(sq, cq);
-    const float R = __fdividef(sq * cq, w);
+    float w, R;
+    if (S <= 0.25f) {
+        const float P = asin_over_x(S);
+        w = S * rsqrtf(S) * P;
+        R = __fdividef(C * rsqrtf(C), P);
+    } else {
+        const float sq = sqrtf(S), cq = sqrtf(C);
+        w = atan2f(sq, cq);
+        R = __fdividef(sq * cq, w);
+    }
     const float dlat = (pa.w - fa.w) + (pb.w - fb.w);            // degrees
     const float G = dlat * 8.7266462599716478846e-3f;            // (pi/180)/2
     const float sG = sin_poly(G);
@@ -45,6 +78,27 @@ __device__ __forceinline__ float geo_dist32(const float4& fa, const float4& fb, 
     const float H2 = __fdividef(3.0f * R + 1.0f, 2.0f * S);
     const float f = 1.0f / 298.257223563f;
     return 2.0f * 6378.137f * w * (1.0f + f * H1 * sF2 * cG2 - f * H2 * cF2 * sG2);
+}
+
+// FP32 great-circle distance (km) of the reference's Lambert formula with the
+// haversine term taken from the 3-D chord of hi/lo unit vectors.
+__device__ __forceinline__ float geo_dist32(const float4& fa, const float4& fb, const float4& fc, const float4& pa,
+                                            const float4& pb, const float4& pc)
+{
+    return geo_dist32_from_S(geo_haversine32(fa, fb, pa, pb), fa, fb, fc, pa, pb, pc);
+}
+
+// Haversine cut-off of a focus row for a compactly supported kernel with
+// threshold r (km): a pair with S above it lies beyond r, so its weight is 0.
+// The Lambert distance satisfies D >= 2 a w (1 - 2.6 f) for w <= 1.2 rad and
+// w >= sin w = sqrt(S); the 1e-3 margin is far above the FP32 rounding of S
+// and D, so the cut never drops a pair whose computed weight is nonzero.
+// Returns +inf (no cut) where the bound does not apply.
+__device__ __forceinline__ float geo_s_cut(float r)
+{
+    const float x = r * (1.0f + 1e-3f) / (2.0f * 6378.137f * (1.0f - 2.6f / 298.257223563f));
+    const float s = x * x;
+    return (r > 0.0f && s < 0.86f) ? s : __int_as_float(0x7f800000);
 }
 
 __device__ __forceinline__ float weight32(int kernel, float d2, float r, float inv_r2)
