@@ -275,19 +275,17 @@ void Engine::buildProxy()
             pts[s] = make_float4(a, b, c, d);
         }
     } else {
-        pts.assign((size_t)3 * ntiles32_ * 32, make_float4(0.f, 0.f, 0.f, 0.f));
+        pts.assign((size_t)2 * ntiles32_ * 32, make_float4(0.f, 0.f, 0.f, 0.f));
         const double DE2RA = M_PI / 180;
         for (int s = 0; s < n; s++) {
             const double lat = hv_[s] * DE2RA, lon = hu_[s] * DE2RA;
             const double px = std::cos(lat) * std::cos(lon), py = std::cos(lat) * std::sin(lon), pz = std::sin(lat);
-            float xh, xl, yh, yl, zh, zl, lh, ll;
+            float xh, xl, yh, yl, zh, zl;
             split(px, xh, xl);
             split(py, yh, yl);
             split(pz, zh, zl);
-            split(hv_[s], lh, ll);
-            pts[3 * (size_t)s] = make_float4(xh, yh, zh, lh);
-            pts[3 * (size_t)s + 1] = make_float4(xl, yl, zl, ll);
-            pts[3 * (size_t)s + 2] = make_float4((float)std::sin(lat / 2), (float)std::cos(lat / 2), 0.f, 0.f);
+            pts[2 * (size_t)s] = make_float4(xh, yh, zh, 0.f);
+            pts[2 * (size_t)s + 1] = make_float4(xl, yl, zl, 0.f);
         }
     }
     if (geographic_) {

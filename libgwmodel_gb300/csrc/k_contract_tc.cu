@@ -89,16 +89,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
     __syncthreads();
     fence_after_sync();
     const uint32_t tmem = ctl.tmem_base;
-    constexpr int NF = GEO ? 3 : 1;                      // float4 per point
+    constexpr int NF = GEO ? 2 : 1;                      // float4 per point record
     constexpr uint32_t P_BYTES = NF * 16u * TC_BK;       // point data of one tile
 
     // focus point
-    float4 fa = make_float4(0.f, 0.f, 0.f, 0.f), fb = fa, fc = fa;
+    float4 fa = make_float4(0.f, 0.f, 0.f, 0.f), fb = fa;
     if (row_ok) {
         if (GEO) {
-            fa = a.pts[3 * (size_t)i];
-            fb = a.pts[3 * (size_t)i + 1];
-            fc = a.pts[3 * (size_t)i + 2];
+            fa = a.pts[2 * (size_t)i];
+            fb = a.pts[2 * (size_t)i + 1];
         } else {
             fa = a.pts[i];
         }
@@ -231,12 +230,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
                     float d2 = 0.0f;
                     bool beyond = false;
                     if (GEO) {
-                        const float S = geo_haversine32(fa, fb, tp[3 * k], tp[3 * k + 1]);
-                        beyond = S >= s_cut && S <= 0.86f;
-                        if (!beyond) {
-                            const float d = geo_dist32_from_S(S, fa, fb, fc, tp[3 * k], tp[3 * k + 1], tp[3 * k + 2]);
-                            d2 = d * d;
-                        }
+                        d2 = geo_d2_32(fa, fb, tp[2 * k], tp[2 * k + 1], s_cut, beyond);
                     } else {
                         d2 = planar_d2_32(fa, tp[k]);
                     }
@@ -388,7 +382,7 @@ __global__ void k_build_zimg(int n, int mcols, int npad, const double* __restric
 size_t contract_tc_smem_bytes(int npad, int ntiles)
 {
     const size_t mask = ((size_t)((ntiles + 31) / 32) * 4 + 15) & ~(size_t)15;
-    return 1024 + 2 * (2 * (size_t)TC_A_BYTES + 2 * (size_t)npad * 128) + mask + 2 * 3 * 16 * TC_BK;
+    return 1024 + 2 * (2 * (size_t)TC_A_BYTES + 2 * (size_t)npad * 128) + mask + 2 * 2 * 16 * TC_BK;
 }
 
 cudaError_t launch_contract_tc(const TcArgs& a, bool geographic, cudaStream_t stream)

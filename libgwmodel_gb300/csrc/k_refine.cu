@@ -33,12 +33,11 @@ __global__ void __launch_bounds__(RF_THREADS) k_refine(RefineArgs a)
     const int i = row0 + t;
     const bool ok = i < a.n;
 
-    float4 fa = make_float4(0.f, 0.f, 0.f, 0.f), fb = fa, fc = fa;
+    float4 fa = make_float4(0.f, 0.f, 0.f, 0.f), fb = fa;
     if (ok) {
         if (GEO) {
-            fa = a.pts[3 * (size_t)i];
-            fb = a.pts[3 * (size_t)i + 1];
-            fc = a.pts[3 * (size_t)i + 2];
+            fa = a.pts[2 * (size_t)i];
+            fb = a.pts[2 * (size_t)i + 1];
         } else {
             fa = a.pts[i];
         }
@@ -75,7 +74,7 @@ __global__ void __launch_bounds__(RF_THREADS) k_refine(RefineArgs a)
         if (ok) {
             const int qend = min(RF_TILE, a.n - j0);
             for (int q = 0; q < qend; q++) {
-                const float w = mixed_weight<GEO>(a.pts, j0 + q, fa, fb, fc, a.kernel, rr, inv_r2);
+                const float w = mixed_weight<GEO>(a.pts, j0 + q, fa, fb, a.kernel, rr, inv_r2);
                 if (w == 0.0f) continue;
                 const double* xj = rsm + q * pp;
                 double e = xj[p];

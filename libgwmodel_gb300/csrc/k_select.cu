@@ -142,7 +142,7 @@ __device__ void bitonic_sort(SelShared& sh, unsigned count)
 
 struct RowCtx {
     double fu, fv, fuR, fvR;  // FP64 focus coordinates (exact formula)
-    float4 fa, fb, fc;        // FP32 proxy data of the focus point
+    float4 fa, fb;            // FP32 proxy record of the focus point
     float qx, qy, qz;         // planar: relative coordinates; geographic: unit vector
 };
 
@@ -219,8 +219,7 @@ __device__ bool select_row(SelShared& sh, const SelectArgs& a, const RowCtx& c, 
                     float d32;
                     bool sure = true;
                     if (GEO) {
-                        d32 = geo_dist32(c.fa, c.fb, c.fc, a.pts[3 * (size_t)j], a.pts[3 * (size_t)j + 1],
-                                         a.pts[3 * (size_t)j + 2]);
+                        d32 = geo_dist32(c.fa, c.fb, a.pts[2 * (size_t)j], a.pts[2 * (size_t)j + 1]);
                         // far-apart pairs (half-angle near pi/2): the FP32 formula is not trusted
                         sure = isfinite(d32) && d32 < 15000.0f;
                     } else {
@@ -320,15 +319,14 @@ __global__ void __launch_bounds__(SEL_THREADS) k_select(SelectArgs a)
         c.fuR = GEO ? P.uR[row] : 0.0;
         c.fvR = GEO ? P.vR[row] : 0.0;
         if (GEO) {
-            c.fa = a.pts[3 * (size_t)row];
-            c.fb = a.pts[3 * (size_t)row + 1];
-            c.fc = a.pts[3 * (size_t)row + 2];
+            c.fa = a.pts[2 * (size_t)row];
+            c.fb = a.pts[2 * (size_t)row + 1];
             c.qx = c.fa.x + c.fb.x;
             c.qy = c.fa.y + c.fb.y;
             c.qz = c.fa.z + c.fb.z;
         } else {
             c.fa = a.pts[row];
-            c.fb = c.fc = c.fa;
+            c.fb = c.fa;
             c.qx = c.fa.x + c.fa.y;
             c.qy = c.fa.z + c.fa.w;
             c.qz = 0.0f;

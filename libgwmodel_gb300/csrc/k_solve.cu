@@ -306,7 +306,7 @@ __global__ void __launch_bounds__(HAT_THREADS)
     extern __shared__ double hsm[];
     double* sX = hsm;                       // HAT_THREADS x p
     double* sV = sX + HAT_THREADS * p;      // HAT_TILE x p
-    constexpr int NF = GEO ? 3 : 1;
+    constexpr int NF = GEO ? 2 : 1;
     __shared__ float4 sf[HAT_TILE][NF];
     __shared__ float sr[HAT_TILE], sinv[HAT_TILE];
     __shared__ float4 sbound;
@@ -318,13 +318,10 @@ __global__ void __launch_bounds__(HAT_THREADS)
     }
     if (t == 0) sbound = tb_union<GEO>(tb16, j0 / HAT_TILE, (min(j0 + HAT_THREADS, n) - 1) / HAT_TILE);
     __syncthreads();
-    float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), pb = pa, pc = pa;
+    float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), pb = pa;
     if (j < n) {
         pa = pts[NF * (size_t)j];
-        if (GEO) {
-            pb = pts[3 * (size_t)j + 1];
-            pc = pts[3 * (size_t)j + 2];
-        }
+        if (GEO) pb = pts[2 * (size_t)j + 1];
     }
     const bool can_skip = tile_thr && kernel >= GW_KERNEL_BISQUARE;
     const float4 fbound = sbound;
@@ -349,13 +346,7 @@ __global__ void __launch_bounds__(HAT_THREADS)
         if (j < n) {
             const int iend = min(HAT_TILE, n - i0);
             for (int q = 0; q < iend; q++) {
-                float d2;
-                if (GEO) {
-                    const float d = geo_dist32(sf[q][0], sf[q][1], sf[q][2], pa, pb, pc);
-                    d2 = d * d;
-                } else {
-                    d2 = planar_d2_32(sf[q][0], pa);
-                }
+                const float d2 = GEO ? geo_d2_32(sf[q][0], sf[q][1], pa, pb) : planar_d2_32(sf[q][0], pa);
                 const double w = (double)weight32(kernel, d2, sr[q], sinv[q]);
                 double s = 0.0;
                 if (w != 0.0) {

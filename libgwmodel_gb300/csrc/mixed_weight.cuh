@@ -7,85 +7,81 @@
 
 namespace gwgpu {
 
-__device__ __forceinline__ float sin_poly(float x)
-{
-    // Taylor series to x^13, |x| <= pi/2
-    float z = x * x;
-    float p = -1.6059043836821614e-10f;        // -1/13!
-    p = fmaf(p, z, 2.505210838544172e-08f);    //  1/11!
-    p = fmaf(p, z, -2.7557319223985893e-06f);  // -1/9!
-    p = fmaf(p, z, 1.984126984126984e-04f);    //  1/7!
-    p = fmaf(p, z, -8.333333333333333e-03f);   // -1/5!  (sign alternates: x - x^3/6 + ...)
-    p = fmaf(p, z, 1.6666666666666666e-01f);   //  1/3!
-    return x - x * z * p;
-}
+// Point records of the mixed path.  Geographic: the unit vector of the point
+// split into FP32 hi + lo, as two float4 (x_hi, y_hi, z_hi, 0), (x_lo, y_lo,
+// z_lo, 0), so z = sin(lat).  Planar: one float4 (u_hi, u_lo, v_hi, v_lo)
+// relative to the centroid.
 
-// asin(x) / x for S = x^2 <= 0.25, from the Maclaurin series
-// asin x = sum_k (2k)! / (4^k (k!)^2 (2k + 1)) x^(2k+1) truncated after k = 10
-// (the first omitted term is below 2e-9 relative at S = 0.25).
+// asin(x) / x as a polynomial in S = x^2 on [0, 0.25]: the degree-6 Chebyshev
+// interpolant at the Chebyshev nodes of that interval, converted to monomials
+// (largest relative deviation 3e-10, below FP32 rounding).
 __device__ __forceinline__ float asin_over_x(float S)
 {
-    float p = 8.3903358096168155e-03f;      // k = 10: 46189 / 5505024
-    p = fmaf(p, S, 9.7616095291940789e-03f);  // k = 9: 12155 / 1245184
-    p = fmaf(p, S, 1.1551800896139706e-02f);  // k = 8: 6435 / 557056
-    p = fmaf(p, S, 1.3964843750000000e-02f);  // k = 7: 143 / 10240
-    p = fmaf(p, S, 1.7352764423076924e-02f);  // k = 6: 231 / 13312
-    p = fmaf(p, S, 2.2372159090909092e-02f);  // k = 5: 63 / 2816
-    p = fmaf(p, S, 3.0381944444444444e-02f);  // k = 4: 35 / 1152
-    p = fmaf(p, S, 4.4642857142857144e-02f);  // k = 3: 5 / 112
-    p = fmaf(p, S, 7.5000000000000000e-02f);  // k = 2: 3 / 40
-    p = fmaf(p, S, 1.6666666666666666e-01f);  // k = 1: 1 / 6
-    return fmaf(p, S, 1.0f);
+    float p = 3.7677137224475400e-02f;
+    p = fmaf(p, S, 1.4295256834232772e-02f);
+    p = fmaf(p, S, 3.1857188680749646e-02f);
+    p = fmaf(p, S, 4.4508709525055284e-02f);
+    p = fmaf(p, S, 7.5005713808768180e-02f);
+    p = fmaf(p, S, 1.6666657639578963e-01f);
+    return fmaf(p, S, 1.0000000002307778f);
 }
 
-// Haversine term S = sin^2(theta / 2) of the pair: a quarter of the squared
-// chord between the hi/lo unit vectors.
-__device__ __forceinline__ float geo_haversine32(const float4& fa, const float4& fb, const float4& pa, const float4& pb)
+constexpr float kGeoA = 6378.137f;                  // WGS-84 semi-major axis (km)
+constexpr float kGeoF = 1.0f / 298.257223563f;      // WGS-84 flattening
+constexpr float kGeoK = 4.0f * kGeoA * kGeoA;       // (2a)^2
+
+// Squared great-circle distance (km^2) of the reference's Lambert formula
+// (CRSDistance.cpp:15-81) in FP32, from hi/lo unit vectors.  With latitudes
+// phi, the half angle w and S = sin^2 w = |chord|^2 / 4, C = 1 - S:
+//   sin^2F cos^2G = ((sin phi_a + sin phi_b) / 2)^2  and
+//   cos^2F sin^2G = ((sin phi_a - sin phi_b) / 2)^2,
+// so with A = w / sqrt(S) and R = sqrt(S C) / w = sqrt(C) / A the formula
+// D = 2 a w (1 + f (H1 sin^2F cos^2G - H2 cos^2F sin^2G)), H1 = (3R - 1)/(2C),
+// H2 = (3R + 1)/(2S), becomes D^2 = (2a)^2 S (A (1 + c))^2 with
+//   c = (f / 8) [(3 sqrt C - A) zs^2 S - (3 sqrt C + A) dz^2 C] / (A S C),
+// zs = sin phi_a + sin phi_b, dz = sin phi_a - sin phi_b.  A comes from
+// asin_over_x for S <= 0.25 and from atan2 beyond.  The value is symmetric in
+// the two points bit for bit.  When s_cut is given (a compact kernel's
+// haversine cut-off, see geo_s_cut) a pair with S in [s_cut, 0.86] sets
+// beyond and returns 0 without the rest of the formula.
+__device__ __forceinline__ float geo_d2_32(const float4& fa, const float4& fb, const float4& pa, const float4& pb,
+                                           float s_cut, bool& beyond)
 {
     const float dx = (pa.x - fa.x) + (pb.x - fb.x);
     const float dy = (pa.y - fa.y) + (pb.y - fb.y);
     const float dz = (pa.z - fa.z) + (pb.z - fb.z);
-    return 0.25f * fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-}
-
-// FP32 great-circle distance (km) of the reference's Lambert formula, given
-// the haversine term S of the pair.  With S = sin^2 w (w = theta / 2) and
-// C = 1 - S: w = sqrt(S) asin_over_x(S) and R = sqrt(S C) / w =
-// sqrt(C) / asin_over_x(S) for S <= 0.25; atan2 beyond.
-__device__ __forceinline__ float geo_dist32_from_S(float S, const float4& fa, const float4& fb, const float4& fc,
-                                                   const float4& pa, const float4& pb, const float4& pc)
-{
-    if (!(S > 0.0f)) return 0.0f;
+    const float S = 0.25f * fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    beyond = S >= s_cut && S <= 0.86f;
+    if (beyond) return 0.0f;
+    if (!(S > 1e-30f)) return kGeoK * fmaxf(S, 0.0f);
+    const float zs = (pa.z + fa.z) + (pb.z + fb.z);
     const float C = fmaxf(1.0f - S, 0.0f);
-    float w, R;
+    const float cq = C * rsqrtf(C);
+    float A;
     if (S <= 0.25f) {
-        const float P = asin_over_x(S);
-        w = S * rsqrtf(S) * P;
-        R = __fdividef(C * rsqrtf(C), P);
+        A = asin_over_x(S);
     } else {
-        const float sq = sqrtf(S), cq = sqrtf(C);
-        w = atan2f(sq, cq);
-        R = __fdividef(sq * cq, w);
+        const float sq = sqrtf(S);
+        A = __fdividef(atan2f(sq, cq), sq);
     }
-    const float dlat = (pa.w - fa.w) + (pb.w - fb.w);            // degrees
-    const float G = dlat * 8.7266462599716478846e-3f;            // (pi/180)/2
-    const float sG = sin_poly(G);
-    const float sG2 = sG * sG, cG2 = 1.0f - sG2;
-    const float sF = pc.x * fc.y + pc.y * fc.x;                  // sin((lat_a+lat_b)/2)
-    const float cF = pc.y * fc.y - pc.x * fc.x;
-    const float sF2 = sF * sF, cF2 = cF * cF;
-    const float H1 = __fdividef(3.0f * R - 1.0f, 2.0f * C);
-    const float H2 = __fdividef(3.0f * R + 1.0f, 2.0f * S);
-    const float f = 1.0f / 298.257223563f;
-    return 2.0f * 6378.137f * w * (1.0f + f * H1 * sF2 * cG2 - f * H2 * cF2 * sG2);
+    const float t1 = fmaf(3.0f, cq, -A), t2 = fmaf(3.0f, cq, A);
+    const float num = fmaf(t1 * (zs * zs), S, -(t2 * (dz * dz)) * C);
+    const float c = (0.125f * kGeoF) * __fdividef(num, A * S * C);
+    const float Q = fmaf(A, c, A);
+    return kGeoK * S * (Q * Q);
 }
 
-// FP32 great-circle distance (km) of the reference's Lambert formula with the
-// haversine term taken from the 3-D chord of hi/lo unit vectors.
-__device__ __forceinline__ float geo_dist32(const float4& fa, const float4& fb, const float4& fc, const float4& pa,
-                                            const float4& pb, const float4& pc)
+__device__ __forceinline__ float geo_d2_32(const float4& fa, const float4& fb, const float4& pa, const float4& pb)
 {
-    return geo_dist32_from_S(geo_haversine32(fa, fb, pa, pb), fa, fb, fc, pa, pb, pc);
+    bool beyond;
+    return geo_d2_32(fa, fb, pa, pb, __int_as_float(0x7f800000), beyond);
+}
+
+// FP32 great-circle distance (km), the square root of geo_d2_32.
+__device__ __forceinline__ float geo_dist32(const float4& fa, const float4& fb, const float4& pa, const float4& pb)
+{
+    const float d2 = geo_d2_32(fa, fb, pa, pb);
+    return d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
 }
 
 // Haversine cut-off of a focus row for a compactly supported kernel with
@@ -96,7 +92,7 @@ __device__ __forceinline__ float geo_dist32(const float4& fa, const float4& fb, 
 // Returns +inf (no cut) where the bound does not apply.
 __device__ __forceinline__ float geo_s_cut(float r)
 {
-    const float x = r * (1.0f + 1e-3f) / (2.0f * 6378.137f * (1.0f - 2.6f / 298.257223563f));
+    const float x = r * (1.0f + 1e-3f) / (2.0f * kGeoA * (1.0f - 2.6f * kGeoF));
     const float s = x * x;
     return (r > 0.0f && s < 0.86f) ? s : __int_as_float(0x7f800000);
 }
@@ -131,19 +127,13 @@ __device__ __forceinline__ float planar_d2_32(const float4& f, const float4& p)
     return fmaf(dx, dx, dy * dy);
 }
 
-// Weight of data point j (coordinates at pts) for a focus point with the
-// given FP32 data, threshold r and 1/r^2 -- exactly what the contraction uses.
+// Weight of data point j (record at pts) for a focus point with record (fa,
+// fb), threshold r and 1/r^2 -- exactly what the contraction uses.
 template <bool GEO>
 __device__ __forceinline__ float mixed_weight(const float4* __restrict__ pts, int j, const float4& fa,
-                                              const float4& fb, const float4& fc, int kernel, float r, float inv_r2)
+                                              const float4& fb, int kernel, float r, float inv_r2)
 {
-    float d2;
-    if (GEO) {
-        float d = geo_dist32(fa, fb, fc, pts[3 * (size_t)j], pts[3 * (size_t)j + 1], pts[3 * (size_t)j + 2]);
-        d2 = d * d;
-    } else {
-        d2 = planar_d2_32(fa, pts[j]);
-    }
+    const float d2 = GEO ? geo_d2_32(fa, fb, pts[2 * (size_t)j], pts[2 * (size_t)j + 1]) : planar_d2_32(fa, pts[j]);
     return weight32(kernel, d2, r, inv_r2);
 }
 
