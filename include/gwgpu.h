@@ -138,6 +138,13 @@ typedef struct gwgpu_stats {
     int select_launches;
     double select_ms;
     long long kernel_launches;  /* every kernel the engine launched */
+    long long contract_tiles;   /* 128 x 32 weight tiles the mixed contraction processed */
+    /* mixed contraction, clock64 cycles summed over CTAs: producer waits for a
+       weight stage, for point records, weight work, accumulator drains; control
+       waits for weights, for Z / accumulator, MMA issue; producer tile loop;
+       then the largest tile loop of one CTA, prologue, kernel start to end
+       (summed), and the largest tile count of one CTA */
+    double contract_phase_cycles[12];
 } gwgpu_stats;
 
 int gwgpu_engine_create(int device, gwgpu_engine** out);
@@ -145,6 +152,9 @@ void gwgpu_engine_destroy(gwgpu_engine* e);
 int gwgpu_engine_set_data(gwgpu_engine* e, int n, int p, const double* x, const double* y, const double* coords,
                           int geographic);
 int gwgpu_engine_set_precision(gwgpu_engine* e, int precision);
+/* Mixed path: 32-point data tiles summed in FP32 on the tensor core before
+   each double-float drain (default 64, at least 2). */
+int gwgpu_engine_set_flush_tiles(gwgpu_engine* e, int tiles);
 /* One bandwidth criterion (DBL_MAX when a local system is not SPD). */
 int gwgpu_engine_criterion(gwgpu_engine* e, double bandwidth, int adaptive, int kernel, int criterion,
                            double* value);

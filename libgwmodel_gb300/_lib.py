@@ -39,7 +39,8 @@ class Stats(ctypes.Structure):
     _fields_ = [("criterion_evals", ctypes.c_int), ("contract_launches", ctypes.c_int),
                 ("contract_ms", ctypes.c_double), ("contract_flops", ctypes.c_double),
                 ("contract_bytes", ctypes.c_double), ("select_launches", ctypes.c_int),
-                ("select_ms", ctypes.c_double), ("kernel_launches", ctypes.c_longlong)]
+                ("select_ms", ctypes.c_double), ("kernel_launches", ctypes.c_longlong),
+                ("contract_tiles", ctypes.c_longlong), ("contract_phase_cycles", ctypes.c_double * 12)]
 
 
 # (name, restype, argtypes) of every function declared in include/gwgpu.h
@@ -86,6 +87,7 @@ SIGNATURES = [
     ("gwgpu_engine_destroy", None, [_vp]),
     ("gwgpu_engine_set_data", _i, [_vp, _i, _i, _dp, _dp, _dp, _i]),
     ("gwgpu_engine_set_precision", _i, [_vp, _i]),
+    ("gwgpu_engine_set_flush_tiles", _i, [_vp, _i]),
     ("gwgpu_engine_criterion", _i, [_vp, _d, _i, _i, _i, _dp]),
     ("gwgpu_engine_global_criterion", _i, [_vp, _i, _ip, _dp]),
     ("gwgpu_engine_fit", _i, [_vp, _d, _i, _i, _i, _dp, _dp, _dp, _dp, _dp]),

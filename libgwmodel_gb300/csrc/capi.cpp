@@ -403,6 +403,14 @@ int gwgpu_engine_set_precision(gwgpu_engine* e, int precision)
     return GWGPU_OK;
 }
 
+int gwgpu_engine_set_flush_tiles(gwgpu_engine* e, int tiles)
+{
+    ENG_CHECK(e);
+    if (tiles < 2 || tiles > 1 << 20) return fail(GWGPU_ERR_INVALID, "flush tiles must be in [2, 2^20]");
+    e->eng.setFlushTiles(tiles);
+    return GWGPU_OK;
+}
+
 int gwgpu_engine_criterion(gwgpu_engine* e, double bandwidth, int adaptive, int kernel, int criterion, double* value)
 {
     ENG_CHECK(e);
@@ -515,6 +523,8 @@ int gwgpu_engine_get_stats(gwgpu_engine* e, gwgpu_stats* out)
     out->select_launches = s.select_launches;
     out->select_ms = s.select_ms;
     out->kernel_launches = s.kernel_launches;
+    out->contract_tiles = s.contract_tiles;
+    for (int q = 0; q < 12; q++) out->contract_phase_cycles[q] = s.contract_phase_cycles[q];
     return GWGPU_OK;
 }
 

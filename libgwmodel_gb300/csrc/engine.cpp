@@ -19,15 +19,30 @@ void check(cudaError_t e, const char* what)
 
 namespace {
 
-uint64_t spread_bits(uint32_t x)
+// Position of cell (x, y) along the Hilbert curve over a 2^31 x 2^31 grid
+// (Hilbert's space-filling curve, by the usual quadrant rotate-and-reflect
+// recursion from the top bit down).  Unlike the Z-order curve it never jumps:
+// consecutive cells are neighbours, so any run of consecutive points is
+// spatially compact.
+uint64_t hilbert_index(uint32_t x, uint32_t y)
 {
-    uint64_t v = x;
-    v = (v | (v << 16)) & 0x0000FFFF0000FFFFull;
-    v = (v | (v << 8)) & 0x00FF00FF00FF00FFull;
-    v = (v | (v << 4)) & 0x0F0F0F0F0F0F0F0Full;
-    v = (v | (v << 2)) & 0x3333333333333333ull;
-    v = (v | (v << 1)) & 0x5555555555555555ull;
-    return v;
+    const uint32_t n = 1u << 31;
+    uint64_t d = 0;
+    for (uint32_t s = n >> 1; s > 0; s >>= 1) {
+        const uint32_t rx = (x & s) ? 1u : 0u;
+        const uint32_t ry = (y & s) ? 1u : 0u;
+        d += (uint64_t)s * s * ((3u * rx) ^ ry);
+        if (ry == 0) {
+            if (rx == 1) {
+                x = n - 1 - x;
+                y = n - 1 - y;
+            }
+            const uint32_t tmp = x;
+            x = y;
+            y = tmp;
+        }
+    }
+    return d;
 }
 
 // Geographic bounds of consecutive tiles of `size` points (sorted order).
@@ -120,7 +135,7 @@ void Engine::setData(int n, int p, const double* x, const double* y, const doubl
     gall_valid_ = false;
     mixed_ready_ = false;
 
-    // Morton order of the coordinates
+    // Hilbert order of the coordinates
     double umin = coords[0], umax = coords[0], vmin = coords[n], vmax = coords[n];
     for (int i = 0; i < n; i++) {
         umin = std::min(umin, coords[i]);
@@ -135,7 +150,7 @@ void Engine::setData(int n, int p, const double* x, const double* y, const doubl
         double fu = (coords[i] - umin) * su, fv = (coords[n + i] - vmin) * sv;
         uint32_t qu = std::isfinite(fu) ? (uint32_t)std::min(std::max(fu, 0.0), 2147483647.0) : 0u;
         uint32_t qv = std::isfinite(fv) ? (uint32_t)std::min(std::max(fv, 0.0), 2147483647.0) : 0u;
-        keyed[i] = {spread_bits(qu) | (spread_bits(qv) << 1), i};
+        keyed[i] = {hilbert_index(qu, qv), i};
     }
     std::sort(keyed.begin(), keyed.end());
     perm_.resize(n);
@@ -467,12 +482,20 @@ void Engine::contractMixed(double* G, int ldg, int mcols, double bw, bool adapti
     a.kernel = kernel;
     a.exclude_self = exclude_self ? 1 : 0;
     a.skip = 1;
-    a.flush_tiles = 32;
+    a.flush_tiles = flush_tiles_;
     a.wpow = wpow;
     a.acc = acc_.get();
     a.G = G;
     a.ldg = ldg;
     a.err = err_.get();
+    if (stats_on_) {
+        if (!tile_count_.get()) tile_count_.alloc(1);
+        if (!tc_prof_.get()) tc_prof_.alloc(kTcProfSlots);
+        check(cudaMemsetAsync(tile_count_.get(), 0, sizeof(unsigned long long), stream_), "memset tiles");
+        check(cudaMemsetAsync(tc_prof_.get(), 0, sizeof(unsigned long long) * kTcProfSlots, stream_), "memset prof");
+        a.tiles = tile_count_.get();
+        a.prof = tc_prof_.get();
+    }
     check(launch_contract_tc(a, geographic_, stream_), "contract_tc");
     stats_.kernel_launches += 1;
     if (stats_on_) {
@@ -486,6 +509,17 @@ void Engine::contractMixed(double* G, int ldg, int mcols, double bw, bool adapti
         if (adaptive && kernel >= GW_KERNEL_BISQUARE) pairs = (double)n_ * std::max(0.0, std::min(bw, (double)n_) - 1);
         stats_.contract_flops += 2.0 * mcols * pairs;
         stats_.contract_bytes += 2.0 * npad_ * 128.0 * ntiles32_ * 2 + 8.0 * n_ * mcols + 16.0 * n_;
+        unsigned long long tiles = 0;
+        check(cudaMemcpy(&tiles, tile_count_.get(), sizeof(tiles), cudaMemcpyDeviceToHost), "D2H tiles");
+        stats_.contract_tiles += (long long)tiles;
+        unsigned long long pc[kTcProfSlots];
+        check(cudaMemcpy(pc, tc_prof_.get(), sizeof(pc), cudaMemcpyDeviceToHost), "D2H prof");
+        for (int q = 0; q < kTcProfSlots && q < 12; q++) {
+            if (q == kTcProfLoopMax || q == kTcProfTilesMax)
+                stats_.contract_phase_cycles[q] = std::max(stats_.contract_phase_cycles[q], (double)pc[q]);
+            else
+                stats_.contract_phase_cycles[q] += (double)pc[q];
+        }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
     }
@@ -547,6 +581,12 @@ const double* Engine::orderStatistic(unsigned rank)
     a.delta = sel_delta_;
     a.out = r->v.get();
     a.err = sel_err_.get();
+    if (hist_.get() && !hist_valid_) {
+        check(launch_select_hist(a, geographic_, num_sms_, stream_), "select histograms");
+        stats_.kernel_launches += 1;
+        hist_valid_ = true;
+        a.cache_valid = 1;
+    }
     check(launch_select(a, geographic_, exact, num_sms_, stream_), "select");
     stats_.kernel_launches += 1;
     if (hist_.get()) hist_valid_ = true;

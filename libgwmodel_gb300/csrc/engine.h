@@ -67,6 +67,8 @@ struct EngineStats {
     double contract_ms = 0.0;      // sum of event-timed contraction launches
     double contract_flops = 0.0;   // algorithmic 2 * m * P, P = nonzero weight pairs
     double contract_bytes = 0.0;   // algorithmic Z + G + coordinate bytes
+    long long contract_tiles = 0;  // 128 x 32 weight tiles the mixed contraction processed
+    double contract_phase_cycles[12] = {};  // mixed contraction: clock64 cycles per TcProf phase
     int select_launches = 0;
     double select_ms = 0.0;
     double solve_ms = 0.0;
@@ -92,9 +94,12 @@ public:
     Engine& operator=(const Engine&) = delete;
 
     // Copies X (n x p column-major), y and coords (n x 2 column-major) to the
-    // device in Morton order.
+    // device in Hilbert order.
     void setData(int n, int p, const double* x, const double* y, const double* coords, bool geographic);
     void setPrecision(int precision) { precision_ = precision; }
+    // Tiles per FP32 accumulation chunk of the tensor-core contraction (>= 2).
+    void setFlushTiles(int tiles) { flush_tiles_ = tiles; }
+    int flushTiles() const { return flush_tiles_; }
     // Refinement steps of the mixed final fit (and of each search criterion when refine_search).
     void setRefinement(int steps, bool refine_search)
     {
@@ -157,6 +162,7 @@ private:
     int n_ = 0, p_ = 0, m_ = 0, mm_ = 0;
     bool geographic_ = false;
     int precision_ = kFP64;
+    int flush_tiles_ = 64;
     double dlo_ = 0.0, dhi_ = 0.0;
     std::vector<int> perm_;  // sorted position -> original index
     std::vector<double> hx_, hy_, hu_, hv_;  // host copies in sorted order
@@ -201,6 +207,8 @@ private:
     DevBuf<float2> acc_;
     DevBuf<float> thr32_;
     DevBuf<int> err_;
+    DevBuf<unsigned long long> tile_count_;
+    DevBuf<unsigned long long> tc_prof_;  // phase cycles of the contraction (stats)  // processed-tile counter of the contraction (stats)
     DevBuf<double> tinv_, tvec_;   // transform of the fit's covariance diagonal
     DevBuf<unsigned long long> key_;
     double* host_sums_ = nullptr;  // pinned

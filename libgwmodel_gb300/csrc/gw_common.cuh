@@ -9,10 +9,10 @@
 namespace gwgpu {
 
 constexpr int kMaxP = 32;        // columns of X handled by the warp-per-location solve
-constexpr int kTile = 16;        // points per data tile (skip granularity, Morton order)
+constexpr int kTile = 16;        // points per data tile (skip granularity, Hilbert order)
 constexpr int kRowBlock = 64;    // focus rows per contraction CTA
 
-// Point coordinates in Morton order, structure of arrays.  Planar: u = x,
+// Point coordinates in Hilbert order, structure of arrays.  Planar: u = x,
 // v = y.  Geographic: u = longitude, v = latitude in degrees and uR/vR the
 // same in radians, rounded as the reference rounds lon * (M_PI / 180).
 struct DevPoints {
@@ -23,7 +23,7 @@ struct DevPoints {
     const double* vR;
 };
 
-// Axis-aligned bounds of one data tile of kTile consecutive (Morton) points.
+// Axis-aligned bounds of one data tile of kTile consecutive (Hilbert-ordered) points.
 struct TileBox {
     double ulo, uhi, vlo, vhi;
 };

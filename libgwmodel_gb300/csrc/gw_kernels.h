@@ -28,6 +28,9 @@ struct SelectArgs {
 // exact: FP64 order statistics (bit-exact); otherwise the FP32 proxy's.
 cudaError_t launch_select(const SelectArgs& a, bool geographic, bool exact, int num_sms, cudaStream_t stream);
 size_t select_smem_bytes();
+// Fills hist_cache with every row's whole-row proxy histogram (the cache a
+// first select pass would store); the selects after it run with cache_valid.
+cudaError_t launch_select_hist(const SelectArgs& a, bool geographic, int num_sms, cudaStream_t stream);
 
 // thr = fixbw of BandwidthWeight.cpp:40-53 from order statistics d0 (rank
 // floor(bw), or the row maximum when bw >= n) and d1 (rank floor(bw)+1, may
@@ -108,7 +111,7 @@ cudaError_t launch_gather_subset(int n, int p, const ColumnSet& cs, const double
 // Mixed-precision W.Z contraction on tcgen05 (k_contract_tc.cu).
 struct TcArgs {
     int n, mcols, npad, ntiles;   // ntiles: 32-point tiles
-    const float4* pts;            // planar: {u_hi, u_lo, v_hi, v_lo}; geographic: 3 float4 per point
+    const float4* pts;            // planar: {u_hi, u_lo, v_hi, v_lo}; geographic: 2 float4 (hi/lo unit vector)
     const float4* tb;             // FP32 bound of each 32-point tile (planar box or geographic cap)
     const unsigned char* zimg;    // per tile: [hi | lo] swizzled images, npad x 128 bytes each
     const float* thr;             // per-row threshold, or null for the fixed bandwidth bw
@@ -118,8 +121,27 @@ struct TcArgs {
     double* G;                    // n x ldg FP64 output (first mcols columns)
     int ldg;
     int* err;                     // set to 1 if a bounded wait timed out
+    unsigned long long* tiles;    // if not null: += 128 x 32 weight tiles processed
+    unsigned long long* prof;     // if not null: += clock64 cycles per phase (kTcProfSlots slots)
 };
-size_t contract_tc_smem_bytes(int npad, int ntiles);
+// Phase slots of TcArgs::prof, summed over CTAs (producer: warp 0 lane 0;
+// control: the issuing thread).
+enum TcProf {
+    kTcProfStageWait,   // producer: waiting for a free weight stage
+    kTcProfPointsWait,  // producer: waiting for the tile's point records
+    kTcProfWeights,     // producer: weights, split and shared-memory stores
+    kTcProfFlush,       // producer: draining accumulators
+    kTcProfAWait,       // control: waiting for the weight tile
+    kTcProfZWait,       // control: waiting for the Z tile and a free accumulator
+    kTcProfIssue,       // control: MMA issue and Z prefetch
+    kTcProfLoop,        // producer: whole tile loop
+    kTcProfLoopMax,     // producer: largest tile loop of one CTA (maximum, not a sum)
+    kTcProfPrologue,    // producer: kernel start to tile loop
+    kTcProfEpilogue,    // producer: tile loop end to kernel end
+    kTcProfTilesMax,    // largest number of tiles one CTA processed (maximum, not cycles)
+    kTcProfSlots
+};
+size_t contract_tc_smem_bytes(int npad, int ntiles, int nb);
 cudaError_t launch_contract_tc(const TcArgs& a, bool geographic, cudaStream_t stream);
 cudaError_t launch_build_zimg(int n, int mcols, int npad, const double* Z, int ldz, unsigned char* img,
                               cudaStream_t stream);

@@ -1,21 +1,27 @@
 // k_contract_tc.cu -- mixed-precision W.Z contraction on the tcgen05 tensor cores.
 //
-// G[i, :] = sum_j w_ij Z~[j, :] for a block of 128 focus rows per CTA:
-//  * producer: 256 threads compute the 128 x 32 weight tile of each stage in
-//    FP32 from the coordinates (planar or WGS-84 great-circle), split every
-//    weight into TF32 hi + lo and store both in the 128-byte-swizzled K-major
-//    layout the tensor core reads;
+// G[i, :] = sum_j w_ij Z~[j, :] for a block of 128 focus rows per CTA, as a
+// warp-specialised pipeline synchronised by mbarriers only:
+//  * 16 producer warps compute the 128 x 32 weight tile of each 32-point
+//    data tile in FP32 from the point records (planar or WGS-84 great-circle,
+//    prefetched into shared memory by a bulk copy two tiles ahead), split
+//    every weight into TF32 hi + lo and store both in the 128-byte-swizzled
+//    K-major layout the tensor core reads (two weight stages);
 //  * the matching Z~ tile (scaled/centred products, split hi + lo, stored in
-//    global memory already in the swizzled image) arrives by one 1-D TMA bulk
-//    copy on an mbarrier;
-//  * one thread issues 3 x 4 tcgen05.mma.kind::tf32 (hi.hi + hi.lo + lo.hi,
-//    K = 8 each) into a 128 x N FP32 accumulator in TMEM and commits to an
-//    mbarrier; two stages double-buffer producer and tensor core;
-//  * every flush_tiles stages the accumulator is read back with tcgen05.ld
-//    and added into double-float (hi, lo) accumulators in global memory, so
-//    FP32 rounding never sums more than a chunk of points.
+//    global memory already in the swizzled image) arrives by one 1-D bulk copy
+//    up to three tiles ahead;
+//  * one thread of the control warp issues 3 x 4 tcgen05.mma.kind::tf32
+//    (hi.hi + hi.lo + lo.hi, K = 8 each) into a 128 x N FP32 accumulator in
+//    TMEM and commits to an mbarrier;
+//  * chunks of flush_tiles tiles alternate between two TMEM accumulators; the
+//    producers read a finished chunk back with tcgen05.ld one tile later and
+//    add it into double-float (hi, lo) sums in global memory, so FP32 rounding
+//    never sums more than a chunk of points and the tensor core never waits
+//    for a drain.
 // Compactly supported kernels skip data tiles farther than the block's
-// largest threshold (planar boxes).  Waits are bounded and report through err.
+// largest threshold (FP32 tile bounds) and, for great-circle distances, pairs
+// beyond the row's haversine cut-off.  Every wait is bounded and reports
+// through err.
 #include "gw_common.cuh"
 #include "gw_kernels.h"
 #include "mixed_weight.cuh"
@@ -27,18 +33,49 @@ namespace {
 
 using namespace tc05;
 
-constexpr int TC_THREADS = 512;
+constexpr int TC_PROD_WARPS = 16;
+constexpr int TC_PROD = TC_PROD_WARPS * 32;   // producer threads
+constexpr int TC_THREADS = TC_PROD + 32;       // plus one control warp
 constexpr int TC_M = 128;
 constexpr int TC_BK = 32;  // points per stage (128 bytes of TF32 per row)
 constexpr uint32_t TC_A_BYTES = TC_M * 128;  // one split part of the weight tile
 constexpr uint32_t TC_WAIT = 1u << 22;
+constexpr uint32_t TC_ACC_COLS = 256;  // TMEM column of the second accumulator
+constexpr int TC_MAX_NB = 3;           // Z stages at most
+constexpr uint32_t TC_P_MAX = 2u * 16u * TC_BK;  // point records of one tile, geographic
 
 struct Smem {
-    uint64_t bar_b[2];
-    uint64_t bar_mma[2];
-    uint64_t bar_p[2];
+    uint64_t full_a[2];          // weight tile k written: one arrival per producer warp
+    uint64_t mma_done[2];        // tcgen05.commit of tile k (every earlier MMA is done too)
+    uint64_t full_b[TC_MAX_NB];  // Z tile landed (bulk copy)
+    uint64_t full_p[2];          // point records landed (bulk copy)
+    uint64_t tmem_free[2];       // accumulator drained: one arrival per producer warp
     uint32_t tmem_base;
     int abort;
+    float4 fbound;
+    float red[TC_PROD_WARPS];
+};
+
+// Walks the tile mask in issue order.
+struct TileWalker {
+    const uint32_t* mask;
+    int nwords, word;
+    uint32_t bits;
+    __device__ void init(const uint32_t* m, int nw)
+    {
+        mask = m;
+        nwords = nw;
+        word = 0;
+        bits = nw > 0 ? m[0] : 0u;
+    }
+    __device__ int next()
+    {
+        while (bits == 0 && ++word < nwords) bits = mask[word];
+        if (bits == 0) return -1;
+        const int tl = word * 32 + (__ffs(bits) - 1);
+        bits &= bits - 1;
+        return tl;
+    }
 };
 
 // Double-float accumulate: (hi, lo) += v.
@@ -52,55 +89,63 @@ __device__ __forceinline__ float2 df_add(float2 a, float v)
     return make_float2(hi, lo - (hi - s));
 }
 
+__device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity)
+{
+    return __all_sync(0xffffffffu, mbar_wait(bar, parity, TC_WAIT));
+}
+
+// Warp roles: warps 0-15 produce the weight tiles (thread (r, quarter) fills
+// points [8 quarter, 8 quarter + 8) of row r) and drain the accumulators;
+// lane 0 of warp 16 issues the bulk copies and the MMAs.  Tile k uses weight
+// stage k % 2, Z stage k % nb and point buffer k % 2; chunk c = k / F of F
+// tiles accumulates in TMEM accumulator c % 2, which the producers drain into
+// the double-float sums one tile after the chunk's last MMA was issued.
 // KERN: the weight kernel when fixed at compile time, -1 to read it from the arguments.
 template <bool GEO, int KERN>
-__global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
+__global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a, int nb)
 {
     const int kernel = KERN >= 0 ? KERN : a.kernel;
     extern __shared__ unsigned char smem_dyn[];
     __shared__ Smem ctl;
-    // 1024-byte aligned stage buffers: [A_hi A_lo B_hi B_lo] x 2
     const uint32_t base_u32 = smem_u32(smem_dyn);
     const uint32_t pad = (1024u - (base_u32 & 1023u)) & 1023u;
-    unsigned char* stage0 = smem_dyn + pad;
+    unsigned char* sA = smem_dyn + pad;  // 2 stages x [A_hi | A_lo]
     const uint32_t b_bytes = (uint32_t)a.npad * 128u;
-    const uint32_t stage_bytes = 2u * TC_A_BYTES + 2u * b_bytes;
+    unsigned char* sB = sA + 4 * (size_t)TC_A_BYTES;  // nb stages x [B_hi | B_lo]
+    constexpr int NF = GEO ? 2 : 1;                    // float4 per point record
+    constexpr uint32_t P_BYTES = NF * 16u * TC_BK;     // point records of one tile
+    float4* ptsbuf = reinterpret_cast<float4*>(sB + (size_t)nb * 2 * b_bytes);  // 2 x P_BYTES
+    uint32_t* tmask = reinterpret_cast<uint32_t*>(sB + (size_t)nb * 2 * b_bytes + 2 * TC_P_MAX);
+    const int nwords = (a.ntiles + 31) / 32;
 
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    const int r = t & (TC_M - 1), quarter = t >> 7;
+    const long long kstart = (a.prof && t == 0) ? clock64() : 0;
+    const bool producer = warp < TC_PROD_WARPS;
+    const int r = t & (TC_M - 1), quarter = (t >> 7) & 3;
     const int row0 = blockIdx.x * TC_M;
     const int i = row0 + r;
-    const bool row_ok = i < a.n;
+    const bool row_ok = producer && i < a.n;
 
-    if (warp == 0) {
-        tmem_alloc(&ctl.tmem_base, 256);
+    if (warp == TC_PROD_WARPS) {
+        tmem_alloc(&ctl.tmem_base, 512);
         tmem_relinquish();
     }
     if (t == 0) {
         for (int s = 0; s < 2; s++) {
-            mbar_init(&ctl.bar_b[s], 1);
-            mbar_init(&ctl.bar_mma[s], 1);
-            mbar_init(&ctl.bar_p[s], 1);
+            mbar_init(&ctl.full_a[s], TC_PROD_WARPS);
+            mbar_init(&ctl.mma_done[s], 1);
+            mbar_init(&ctl.full_p[s], 1);
+            mbar_init(&ctl.tmem_free[s], TC_PROD_WARPS);
         }
+        for (int s = 0; s < TC_MAX_NB; s++) mbar_init(&ctl.full_b[s], 1);
         ctl.abort = 0;
         fence_mbar_init();
     }
-    fence_before_sync();
-    __syncthreads();
-    fence_after_sync();
-    const uint32_t tmem = ctl.tmem_base;
-    constexpr int NF = GEO ? 2 : 1;                      // float4 per point record
-    constexpr uint32_t P_BYTES = NF * 16u * TC_BK;       // point data of one tile
-
-    // focus point
+    // focus record
     float4 fa = make_float4(0.f, 0.f, 0.f, 0.f), fb = fa;
     if (row_ok) {
-        if (GEO) {
-            fa = a.pts[2 * (size_t)i];
-            fb = a.pts[2 * (size_t)i + 1];
-        } else {
-            fa = a.pts[i];
-        }
+        fa = a.pts[NF * (size_t)i];
+        if (GEO) fb = a.pts[2 * (size_t)i + 1];
     }
     const float rr = row_ok ? (a.thr ? a.thr[i] : a.bw) : 1.0f;
     const float inv_r2 = 1.0f / (rr * rr);
@@ -108,24 +153,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
     const float s_cut = (GEO && kernel >= GW_KERNEL_BISQUARE) ? geo_s_cut(rr) : __int_as_float(0x7f800000);
 
     // block bound and largest threshold for tile skipping
-    __shared__ float red[TC_THREADS / 32];
-    __shared__ float4 fbound_s;
     float rmax = row_ok ? rr : 0.0f;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, off));
-    if (lane == 0) red[warp] = rmax;
-    if (t == 0) fbound_s = tb_union<GEO>(a.tb, row0 / TC_BK, (min(row0 + TC_M, a.n) - 1) / TC_BK);
+    if (producer && lane == 0) ctl.red[warp] = rmax;
+    if (t == 0) ctl.fbound = tb_union<GEO>(a.tb, row0 / TC_BK, (min(row0 + TC_M, a.n) - 1) / TC_BK);
+    fence_before_sync();
     __syncthreads();
-    rmax = red[0];
-    for (int q = 1; q < TC_THREADS / 32; q++) rmax = fmaxf(rmax, red[q]);
-    const float4 fbound = fbound_s;
+    fence_after_sync();
+    const uint32_t tmem = ctl.tmem_base;
+    rmax = ctl.red[0];
+    for (int q = 1; q < TC_PROD_WARPS; q++) rmax = fmaxf(rmax, ctl.red[q]);
+    const float4 fbound = ctl.fbound;
     const float far_thr =
         (a.skip && kernel >= GW_KERNEL_BISQUARE) ? tb_far_threshold<GEO>((double)rmax) : -1.0f;
     // tiles this CTA must visit, one bit per 32-point tile
-    uint32_t* tmask = reinterpret_cast<uint32_t*>(stage0 + 2 * (size_t)stage_bytes);
-    const int nwords = (a.ntiles + 31) / 32;
-    // point data of the current and the next tile (prefetched by TMA)
-    float4* ptsbuf = reinterpret_cast<float4*>(stage0 + 2 * (size_t)stage_bytes + (((size_t)nwords * 4 + 15) & ~(size_t)15));
     for (int wd = t; wd < nwords; wd += TC_THREADS) {
         uint32_t bits = 0;
         for (int b = 0; b < 32; b++) {
@@ -136,174 +178,280 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a)
     }
     __syncthreads();
 
-    const uint32_t idesc = idesc_tf32(TC_M, a.npad);
-    int issued = 0;        // stages issued so far (non-skipped tiles)
-    int in_chunk = 0;      // stages accumulated in TMEM since the last flush
-    bool first_flush = true;
-    bool aborted = false;
-
-    auto flush = [&](int last_stage) {
-        // wait for the last MMA group, read TMEM, accumulate in double-float
-        const int s = last_stage & 1;
-        const uint32_t par = (uint32_t)((last_stage >> 1) & 1);
-        if (!mbar_wait(&ctl.bar_mma[s], par, TC_WAIT)) atomicExch(&ctl.abort, 1);
-        fence_after_sync();
-        const int quad = warp & 3, part = warp >> 2;
-        const int lrow = quad * 32 + lane;
-        const int grow = row0 + lrow;
-        const int ncol_part = a.npad / 4;
-        for (int c0 = part * ncol_part; c0 < (part + 1) * ncol_part; c0 += 16) {
-            uint32_t v[16];
-            tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0, v);
-            tmem_wait_ld();
-            if (grow < a.n) {
-                float2* acc = a.acc + (size_t)grow * a.npad + c0;
+    const int F = a.flush_tiles;
+    int k = 0;  // tiles done by this thread's role
+    if (producer) {
+        bool first_flush = true;
+        // drain accumulator c % 2 (its last MMA is tile `last`) into the double-float sums
+        auto flush = [&](int c, int last) -> bool {
+            if (!warp_wait(&ctl.mma_done[last & 1], (uint32_t)((last >> 1) & 1))) {
+                if (lane == 0) atomicExch(&ctl.abort, 1);
+                return false;
+            }
+            fence_after_sync();
+            const int quad = warp & 3, part = warp >> 2;
+            const int grow = row0 + quad * 32 + lane;
+            const int ncol_part = a.npad / 4;
+            const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(c & 1) * TC_ACC_COLS;
+            for (int c0 = part * ncol_part; c0 < (part + 1) * ncol_part; c0 += 16) {
+                uint32_t v[16];
+                tmem_ld16(tbase + (uint32_t)c0, v);
+                tmem_wait_ld();
+                if (grow < a.n) {
+                    float4* acc = reinterpret_cast<float4*>(a.acc + (size_t)grow * a.npad + c0);
+                    float4 o[8];
 #pragma unroll
-                for (int q = 0; q < 16; q++) {
-                    float x = __uint_as_float(v[q]);
-                    acc[q] = first_flush ? make_float2(x, 0.0f) : df_add(acc[q], x);
+                    for (int q = 0; q < 8; q++) o[q] = first_flush ? make_float4(0.f, 0.f, 0.f, 0.f) : acc[q];
+#pragma unroll
+                    for (int q = 0; q < 8; q++) {
+                        const float2 h0 = df_add(make_float2(o[q].x, o[q].y), __uint_as_float(v[2 * q]));
+                        const float2 h1 = df_add(make_float2(o[q].z, o[q].w), __uint_as_float(v[2 * q + 1]));
+                        acc[q] = make_float4(h0.x, h0.y, h1.x, h1.y);
+                    }
                 }
             }
-        }
-        fence_before_sync();
-        __syncthreads();
-        first_flush = false;
-        in_chunk = 0;
-    };
-
-    int word = 0;
-    uint32_t bits = nwords > 0 ? tmask[0] : 0u;
-    auto next_tile = [&]() -> int {
-        while (bits == 0 && ++word < nwords) bits = tmask[word];
-        if (bits == 0) return -1;
-        const int tl = word * 32 + (__ffs(bits) - 1);
-        bits &= bits - 1;
-        return tl;
-    };
-    // thread 0 records what it has in flight, for a clean exit after an abort
-    int last_b = -1;    // issue index of the last Z copy
-    int last_p = -1;    // issue index whose point data was last requested
-    int last_mma = -1;  // issue index of the last MMA commit
-    int tile = next_tile();
-    if (tile >= 0 && t == 0) {
-        mbar_arrive_expect_tx(&ctl.bar_p[0], P_BYTES);
-        bulk_g2s(ptsbuf, a.pts + (size_t)NF * TC_BK * tile, P_BYTES, &ctl.bar_p[0]);
-        last_p = 0;
-    }
-    while (tile >= 0 && !aborted) {
-        const int ntile = next_tile();
-        const int s = issued & 1;
-        unsigned char* st = stage0 + (size_t)s * stage_bytes;
-        unsigned char* A_hi = st;
-        unsigned char* A_lo = st + TC_A_BYTES;
-        unsigned char* B_hi = st + 2 * TC_A_BYTES;
-        if (issued >= 2 && in_chunk >= 2) {
-            // the MMAs that read this stage two issues ago must be done
-            const uint32_t par = (uint32_t)(((issued >> 1) - 1) & 1);
-            if (!mbar_wait(&ctl.bar_mma[s], par, TC_WAIT)) atomicExch(&ctl.abort, 1);
-        }
-        if (t == 0) {
-            mbar_arrive_expect_tx(&ctl.bar_b[s], 2u * b_bytes);
-            bulk_g2s(B_hi, a.zimg + (size_t)tile * 2u * b_bytes, 2u * b_bytes, &ctl.bar_b[s]);
-            last_b = issued;
-            if (ntile >= 0) {
-                // the other buffer was last read before the previous iteration's barrier
-                mbar_arrive_expect_tx(&ctl.bar_p[s ^ 1], P_BYTES);
-                bulk_g2s(ptsbuf + (size_t)(s ^ 1) * NF * TC_BK, a.pts + (size_t)NF * TC_BK * ntile, P_BYTES,
-                         &ctl.bar_p[s ^ 1]);
-                last_p = issued + 1;
+            fence_before_sync();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&ctl.tmem_free[c & 1]);
+            first_flush = false;
+            return true;
+        };
+        TileWalker walk;
+        walk.init(tmask, nwords);
+        int pending = -1;  // complete chunk not drained yet
+        bool ok = true;
+        const bool prof = a.prof && t == 0;
+        unsigned long long pc[kTcProfSlots] = {};
+        long long c0 = prof ? clock64() : 0, c1 = 0;
+        const long long loop0 = c0;
+        if (prof) pc[kTcProfPrologue] = (unsigned long long)(c0 - kstart);
+        for (int tile = walk.next(); tile >= 0; tile = walk.next(), k++) {
+            if (__any_sync(0xffffffffu, *(volatile int*)&ctl.abort != 0)) {
+                ok = false;
+                break;
             }
-        }
-        if (!mbar_wait(&ctl.bar_p[s], (uint32_t)((issued >> 1) & 1), TC_WAIT)) atomicExch(&ctl.abort, 1);
-        const float4* tp = ptsbuf + (size_t)s * NF * TC_BK;
-        // weight tile: thread (r, quarter) fills points [8*quarter, 8*quarter + 8) of row r
-        const int kbase = quarter * 8;
+            const int s = k & 1;
+            if (pending >= 0 && k >= (pending + 1) * F + 1) {
+                if (prof) c0 = clock64();
+                if (!flush(pending, (pending + 1) * F - 1)) {
+                    ok = false;
+                    break;
+                }
+                pending = -1;
+                if (prof) pc[kTcProfFlush] += clock64() - c0;
+            }
+            if (prof) c0 = clock64();
+            // weight stage s is free once the MMAs of tile k - 2 are done
+            const bool stage_ok = k < 2 || warp_wait(&ctl.mma_done[s], (uint32_t)(((k >> 1) - 1) & 1));
+            if (prof) {
+                c1 = clock64();
+                pc[kTcProfStageWait] += c1 - c0;
+                c0 = c1;
+            }
+            if (!stage_ok || !warp_wait(&ctl.full_p[s], (uint32_t)((k >> 1) & 1))) {
+                if (lane == 0) atomicExch(&ctl.abort, 1);
+                ok = false;
+                break;
+            }
+            if (prof) {
+                c1 = clock64();
+                pc[kTcProfPointsWait] += c1 - c0;
+                c0 = c1;
+            }
+            const float4* tp = ptsbuf + (size_t)s * NF * TC_BK;
+            unsigned char* A_hi = sA + (size_t)s * 2 * TC_A_BYTES;
+            unsigned char* A_lo = A_hi + TC_A_BYTES;
+            const int kbase = quarter * 8;
 #pragma unroll
-        for (int q4 = 0; q4 < 2; q4++) {
-            float hi[4], lo[4];
+            for (int q4 = 0; q4 < 2; q4++) {
+                float w[4];
+                bool in[4];
+                GeoChord g[4];
 #pragma unroll
-            for (int e = 0; e < 4; e++) {
-                const int k = kbase + q4 * 4 + e;
-                const int j = tile * TC_BK + k;
-                float w = 0.0f;
-                if (row_ok && j < a.n) {
-                    float d2 = 0.0f;
-                    bool beyond = false;
+                for (int e = 0; e < 4; e++) {
+                    const int kk = kbase + q4 * 4 + e;
+                    in[e] = row_ok && tile * TC_BK + kk < a.n;
                     if (GEO) {
-                        d2 = geo_d2_32(fa, fb, tp[2 * k], tp[2 * k + 1], s_cut, beyond);
-                    } else {
-                        d2 = planar_d2_32(fa, tp[k]);
+                        g[e] = geo_chord32(fa, fb, tp[2 * kk], tp[2 * kk + 1]);
+                        in[e] = in[e] && !geo_beyond(g[e].S, s_cut);
                     }
-                    if (!beyond) {
-                        w = weight32(kernel, d2, rr, inv_r2);
-                        if (a.exclude_self && i == j) w = 0.0f;
-                        if (a.wpow == 2) w = w * w;
-                    }
+                    w[e] = 0.0f;
                 }
-                hi[e] = to_tf32(w);
-                lo[e] = to_tf32(w - hi[e]);
-            }
-            const uint32_t off = sw128_offset((uint32_t)r, (uint32_t)(kbase + q4 * 4));
-            *reinterpret_cast<float4*>(A_hi + off) = make_float4(hi[0], hi[1], hi[2], hi[3]);
-            *reinterpret_cast<float4*>(A_lo + off) = make_float4(lo[0], lo[1], lo[2], lo[3]);
-        }
-        fence_proxy_async_smem();
-        __syncthreads();
-        if (ctl.abort) {
-            aborted = true;
-            break;
-        }
-        if (t == 0) {
-            if (!mbar_wait(&ctl.bar_b[s], (uint32_t)((issued >> 1) & 1), TC_WAIT)) {
-                atomicExch(&ctl.abort, 1);
-            } else {
-                fence_after_sync();
-                const uint64_t ahi = sw128_kmajor_desc(smem_u32(A_hi));
-                const uint64_t alo = sw128_kmajor_desc(smem_u32(A_lo));
-                const uint64_t bhi = sw128_kmajor_desc(smem_u32(B_hi));
-                const uint64_t blo = sw128_kmajor_desc(smem_u32(B_hi + b_bytes));
+                // the group is skipped only when every lane's four pairs are out
+                if (__any_sync(0xffffffffu, in[0] || in[1] || in[2] || in[3])) {
 #pragma unroll
-                for (int kk = 0; kk < 4; kk++) {
-                    const uint64_t dk = (uint64_t)(kk * 2);  // 32 bytes = 8 TF32 along K
-                    mma_tf32(tmem, ahi + dk, bhi + dk, idesc, (in_chunk > 0 || kk > 0) ? 1u : 0u);
-                    mma_tf32(tmem, ahi + dk, blo + dk, idesc, 1u);
-                    mma_tf32(tmem, alo + dk, bhi + dk, idesc, 1u);
+                    for (int e = 0; e < 4; e++) {
+                        const int kk = kbase + q4 * 4 + e;
+                        const float d2 = GEO ? geo_d2_from_chord(g[e]) : planar_d2_32(fa, tp[kk]);
+                        float v = weight32(kernel, d2, rr, inv_r2);
+                        if (a.exclude_self && i == tile * TC_BK + kk) v = 0.0f;
+                        if (a.wpow == 2) v = v * v;
+                        w[e] = in[e] ? v : 0.0f;
+                    }
                 }
-                mma_commit(&ctl.bar_mma[s]);
-                last_mma = issued;
+                float hi[4], lo[4];
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    hi[e] = to_tf32(w[e]);
+                    lo[e] = to_tf32(w[e] - hi[e]);
+                }
+                const uint32_t off = sw128_offset((uint32_t)r, (uint32_t)(kbase + q4 * 4));
+                *reinterpret_cast<float4*>(A_hi + off) = make_float4(hi[0], hi[1], hi[2], hi[3]);
+                *reinterpret_cast<float4*>(A_lo + off) = make_float4(lo[0], lo[1], lo[2], lo[3]);
             }
+            fence_proxy_async_smem();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&ctl.full_a[s]);
+            if (k % F == F - 1) pending = k / F;
+            if (prof) pc[kTcProfWeights] += clock64() - c0;
         }
-        issued++;
-        in_chunk++;
-        if (in_chunk >= a.flush_tiles) flush(issued - 1);
-        tile = ntile;
+        if (prof) c0 = clock64();
+        if (ok && pending >= 0) ok = flush(pending, (pending + 1) * F - 1);
+        if (ok && k % F != 0) ok = flush(k / F, k - 1);
+        if (prof) {
+            c1 = clock64();
+            pc[kTcProfFlush] += c1 - c0;
+            pc[kTcProfLoop] += c1 - loop0;
+            for (int q = 0; q < kTcProfSlots; q++)
+                if (q < kTcProfAWait || q == kTcProfLoop || q == kTcProfPrologue) atomicAdd(a.prof + q, pc[q]);
+            atomicMax(a.prof + kTcProfLoopMax, (unsigned long long)(c1 - loop0));
+            atomicMax(a.prof + kTcProfTilesMax, (unsigned long long)k);
+        }
+    } else if (lane == 0) {
+        TileWalker wz, wp, wm;  // Z copies (nb ahead), point copies (2 ahead), MMAs
+        wz.init(tmask, nwords);
+        wp.init(tmask, nwords);
+        wm.init(tmask, nwords);
+        int kz = 0, kp = 0;  // copies issued
+        int last_mma = -1;
+        auto issue_z = [&](int tl) {
+            const int sb = kz % nb;
+            unsigned char* B = sB + (size_t)sb * 2 * b_bytes;
+            mbar_arrive_expect_tx(&ctl.full_b[sb], 2u * b_bytes);
+            bulk_g2s(B, a.zimg + (size_t)tl * 2u * b_bytes, 2u * b_bytes, &ctl.full_b[sb]);
+            kz++;
+        };
+        auto issue_p = [&](int tl) {
+            const int sp = kp & 1;
+            mbar_arrive_expect_tx(&ctl.full_p[sp], P_BYTES);
+            bulk_g2s(ptsbuf + (size_t)sp * NF * TC_BK, a.pts + (size_t)NF * TC_BK * tl, P_BYTES, &ctl.full_p[sp]);
+            kp++;
+        };
+        for (int q = 0; q < nb; q++) {
+            const int tl = wz.next();
+            if (tl < 0) break;
+            issue_z(tl);
+        }
+        for (int q = 0; q < 2; q++) {
+            const int tl = wp.next();
+            if (tl < 0) break;
+            issue_p(tl);
+        }
+        const uint32_t idesc = idesc_tf32(TC_M, a.npad);
+        const bool prof = a.prof != nullptr;
+        unsigned long long pc[3] = {0, 0, 0};
+        long long c0 = 0, c1 = 0;
+        for (int tile = wm.next(); tile >= 0; tile = wm.next(), k++) {
+            if (*(volatile int*)&ctl.abort) break;
+            const int s = k & 1, sb = k % nb, c = k / F;
+            if (prof) c0 = clock64();
+            if (!mbar_wait(&ctl.full_a[s], (uint32_t)((k >> 1) & 1), TC_WAIT)) {
+                atomicExch(&ctl.abort, 1);
+                break;
+            }
+            if (prof) {
+                c1 = clock64();
+                pc[0] += c1 - c0;
+                c0 = c1;
+            }
+            // the producers are done with point buffer s: fetch the records of tile k + 2
+            if (kp == k + 2) {
+                const int tl = wp.next();
+                if (tl >= 0) issue_p(tl);
+            }
+            bool ok = mbar_wait(&ctl.full_b[sb], (uint32_t)((k / nb) & 1), TC_WAIT);
+            if (ok && k % F == 0 && c >= 2)
+                ok = mbar_wait(&ctl.tmem_free[c & 1], (uint32_t)(((c >> 1) - 1) & 1), TC_WAIT);
+            if (!ok) {
+                atomicExch(&ctl.abort, 1);
+                break;
+            }
+            if (prof) {
+                c1 = clock64();
+                pc[1] += c1 - c0;
+                c0 = c1;
+            }
+            fence_after_sync();
+            unsigned char* A_hi = sA + (size_t)s * 2 * TC_A_BYTES;
+            unsigned char* B_hi = sB + (size_t)sb * 2 * b_bytes;
+            const uint64_t ahi = sw128_kmajor_desc(smem_u32(A_hi));
+            const uint64_t alo = sw128_kmajor_desc(smem_u32(A_hi + TC_A_BYTES));
+            const uint64_t bhi = sw128_kmajor_desc(smem_u32(B_hi));
+            const uint64_t blo = sw128_kmajor_desc(smem_u32(B_hi + b_bytes));
+            const uint32_t d = tmem + (uint32_t)(c & 1) * TC_ACC_COLS;
+#pragma unroll
+            for (int kk = 0; kk < 4; kk++) {
+                const uint64_t dk = (uint64_t)(kk * 2);  // 32 bytes = 8 TF32 along K
+                mma_tf32(d, ahi + dk, bhi + dk, idesc, (k % F != 0 || kk > 0) ? 1u : 0u);
+                mma_tf32(d, ahi + dk, blo + dk, idesc, 1u);
+                mma_tf32(d, alo + dk, bhi + dk, idesc, 1u);
+            }
+            mma_commit(&ctl.mma_done[s]);
+            last_mma = k;
+            // Z stage of tile k - 1 is free once its MMAs are done: fetch tile k - 1 + nb
+            if (k >= 1 && kz == k - 1 + nb) {
+                if (!mbar_wait(&ctl.mma_done[(k - 1) & 1], (uint32_t)(((k - 1) >> 1) & 1), TC_WAIT)) {
+                    atomicExch(&ctl.abort, 1);
+                    break;
+                }
+                const int tl = wz.next();
+                if (tl >= 0) issue_z(tl);
+            }
+            if (prof) pc[2] += clock64() - c0;
+        }
+        if (prof) {
+            atomicAdd(a.prof + kTcProfAWait, pc[0]);
+            atomicAdd(a.prof + kTcProfZWait, pc[1]);
+            atomicAdd(a.prof + kTcProfIssue, pc[2]);
+        }
+        if (*(volatile int*)&ctl.abort) {
+            // leave no MMA and no bulk copy in flight before TMEM and the CTA go away
+            if (last_mma >= 0) mbar_wait(&ctl.mma_done[last_mma & 1], (uint32_t)((last_mma >> 1) & 1), TC_WAIT);
+            for (int j = kz - nb > 0 ? kz - nb : 0; j < kz; j++)
+                mbar_wait(&ctl.full_b[j % nb], (uint32_t)((j / nb) & 1), TC_WAIT);
+            for (int j = kp - 2 > 0 ? kp - 2 : 0; j < kp; j++)
+                mbar_wait(&ctl.full_p[j & 1], (uint32_t)((j >> 1) & 1), TC_WAIT);
+        }
     }
-    if (!aborted && in_chunk > 0) flush(issued - 1);
+    __syncwarp();
+    fence_before_sync();
     __syncthreads();
-    aborted = aborted || ctl.abort;
+    fence_after_sync();
+    const bool aborted = ctl.abort != 0;
     // epilogue: double-float -> FP64 rows (only columns of Z)
-    if (!aborted) {
-        for (int e = t; e < TC_M * a.mcols; e += TC_THREADS) {
+    if (!aborted && producer) {
+        const float2* __restrict__ acc = a.acc;
+        double* __restrict__ G = a.G;
+#pragma unroll 4
+        for (int e = t; e < TC_M * a.mcols; e += TC_PROD) {
             const int lr = e / a.mcols, c = e - lr * a.mcols;
             const int grow = row0 + lr;
             if (grow >= a.n) continue;
             double v = 0.0;
-            if (!first_flush) {
-                const float2 x = a.acc[(size_t)grow * a.npad + c];
+            if (k > 0) {
+                const float2 x = acc[(size_t)grow * a.npad + c];
                 v = (double)x.x + (double)x.y;
             }
-            a.G[(size_t)grow * a.ldg + c] = v;
+            G[(size_t)grow * a.ldg + c] = v;
         }
-    } else if (t == 0) {
+    } else if (aborted && t == 0) {
         atomicExch(a.err, 1);
-        // leave no MMA and no bulk copy in flight before TMEM and the CTA go away
-        if (last_mma >= 0) mbar_wait(&ctl.bar_mma[last_mma & 1], (uint32_t)((last_mma >> 1) & 1), TC_WAIT);
-        if (last_b >= 0) mbar_wait(&ctl.bar_b[last_b & 1], (uint32_t)((last_b >> 1) & 1), TC_WAIT);
-        if (last_p >= 0) mbar_wait(&ctl.bar_p[last_p & 1], (uint32_t)((last_p >> 1) & 1), TC_WAIT);
     }
+    if (t == 0 && a.tiles && !aborted) atomicAdd(a.tiles, (unsigned long long)k);
+    if (t == 0 && a.prof) atomicAdd(a.prof + kTcProfEpilogue, (unsigned long long)(clock64() - kstart));
     fence_before_sync();
     __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, 256);
+    if (warp == TC_PROD_WARPS) tmem_dealloc(tmem, 512);
 }
 
 // D[128 x N] = A[128 x 32] * B[N x 32]^T through the same layouts (TF32 in, FP32 out).
@@ -379,21 +527,24 @@ __global__ void k_build_zimg(int n, int mcols, int npad, const double* __restric
 
 }  // namespace
 
-size_t contract_tc_smem_bytes(int npad, int ntiles)
+size_t contract_tc_smem_bytes(int npad, int ntiles, int nb)
 {
-    const size_t mask = ((size_t)((ntiles + 31) / 32) * 4 + 15) & ~(size_t)15;
-    return 1024 + 2 * (2 * (size_t)TC_A_BYTES + 2 * (size_t)npad * 128) + mask + 2 * 2 * 16 * TC_BK;
+    const size_t mask = (size_t)((ntiles + 31) / 32) * 4;
+    return 1024 + 4 * (size_t)TC_A_BYTES + (size_t)nb * 2 * npad * 128 + 2 * TC_P_MAX + mask;
 }
 
 cudaError_t launch_contract_tc(const TcArgs& a, bool geographic, cudaStream_t stream)
 {
     if (a.npad % 64 != 0 || a.npad < 64 || a.npad > 256 || a.mcols > a.npad) return cudaErrorInvalidValue;
-    const size_t smem = contract_tc_smem_bytes(a.npad, a.ntiles);
+    if (a.flush_tiles < 2) return cudaErrorInvalidValue;
+    int nb = TC_MAX_NB;
+    while (nb > 2 && contract_tc_smem_bytes(a.npad, a.ntiles, nb) > 227 * 1024) nb--;
+    const size_t smem = contract_tc_smem_bytes(a.npad, a.ntiles, nb);
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
     const int grid = (a.n + TC_M - 1) / TC_M;
     auto go = [&](auto kfn) {
         cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        kfn<<<grid, TC_THREADS, smem, stream>>>(a);
+        kfn<<<grid, TC_THREADS, smem, stream>>>(a, nb);
     };
     if (geographic) {
         if (a.kernel == GW_KERNEL_BISQUARE) go(k_contract_tc<true, GW_KERNEL_BISQUARE>);

@@ -8,7 +8,7 @@
 //  * window [T_lo, T_hi]: order statistics of neighbouring ranks computed by
 //    earlier golden-section evaluations bracket the answer (0 and +inf when
 //    none), so most of the row is classified without looking at points;
-//  * tiles of 32 Morton-ordered points carry an FP32 bound (planar box or 3-D
+//  * tiles of 32 Hilbert-ordered points carry an FP32 bound (planar box or 3-D
 //    cap): a tile entirely below T_lo only adds its count, a tile entirely
 //    above T_hi is skipped, only straddling tiles are looked at point by point
 //    (one point per lane);
@@ -74,6 +74,17 @@ __device__ __forceinline__ Window linear_window(uint64_t lo, uint64_t hi)
     uint64_t span = hi - lo;
     int bits = span ? 64 - __clzll((long long)span) : 0;
     return Window{lo, bits > SEL_LOG_BINS ? bits - SEL_LOG_BINS : 0, lo, hi};
+}
+
+// Coarse window over positive distances [dlo, dhi] for whole-row histograms.
+__device__ __forceinline__ Window coarse_window(const SelectArgs& a)
+{
+    const uint64_t klo = (uint64_t)__double_as_longlong(a.dlo) | 0x8000000000000000ull;
+    const uint64_t khi = (uint64_t)__double_as_longlong(a.dhi) | 0x8000000000000000ull;
+    const uint64_t kspan = khi > klo ? khi - klo : 1;
+    const int kbits = 64 - __clzll((long long)kspan);
+    return Window{klo, kbits > SEL_LOG_BINS ? kbits - SEL_LOG_BINS : 0, dkey(0.0),
+                  dkey(__longlong_as_double(0x7ff0000000000000ll))};
 }
 
 // Finds the bin where the cumulative count reaches krem (1-based).
@@ -306,11 +317,7 @@ __global__ void __launch_bounds__(SEL_THREADS) k_select(SelectArgs a)
     const int n = a.n;
     const double INF = __longlong_as_double(0x7ff0000000000000ll);
     // coarse logarithmic window of the first pass over a whole row
-    const uint64_t klo = (uint64_t)__double_as_longlong(a.dlo) | 0x8000000000000000ull;
-    const uint64_t khi = (uint64_t)__double_as_longlong(a.dhi) | 0x8000000000000000ull;
-    const uint64_t kspan = khi > klo ? khi - klo : 1;
-    const int kbits = 64 - __clzll((long long)kspan);
-    const Window wlog{klo, kbits > SEL_LOG_BINS ? kbits - SEL_LOG_BINS : 0, dkey(0.0), dkey(INF)};
+    const Window wlog = coarse_window(a);
 
     for (int row = blockIdx.x; row < n; row += gridDim.x) {
         RowCtx c;
@@ -369,6 +376,62 @@ __global__ void __launch_bounds__(SEL_THREADS) k_select(SelectArgs a)
     }
 }
 
+// Whole-row histograms for the cache: every row's SEL_BINS-bin histogram of
+// FP32 proxy distances over the coarse window [dlo, dhi] -- the same counts
+// a first select pass over a whole row produces, with the same proxy values.
+// HS_ROWS focus rows per CTA share every point record load.  Warp w walks
+// groups of 32 tiles; at step q lane l takes point q of tile l, so the 32
+// lanes land on points far apart along the curve and rarely hit the same bin.
+constexpr int HS_ROWS = 8;
+constexpr int HS_THREADS = 512;
+
+template <bool GEO>
+__global__ void __launch_bounds__(HS_THREADS, 1) k_select_hist(SelectArgs a)
+{
+    extern __shared__ __align__(16) unsigned hs[];  // HS_ROWS x SEL_BINS
+    __shared__ float4 rf[HS_ROWS][2];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int n = a.n;
+    const Window wlog = coarse_window(a);
+    constexpr int NF = GEO ? 2 : 1;
+    const int ngroups = (a.ntiles + 31) / 32;
+    for (int row0 = blockIdx.x * HS_ROWS; row0 < n; row0 += gridDim.x * HS_ROWS) {
+        const int nrows = min(HS_ROWS, n - row0);
+        for (int b = t; b < HS_ROWS * SEL_BINS; b += HS_THREADS) hs[b] = 0;
+        if (t < HS_ROWS * NF) {
+            const int r = t / NF, q = t % NF;
+            rf[r][q] = r < nrows ? a.pts[NF * (size_t)(row0 + r) + q] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        __syncthreads();
+        float4 ra[HS_ROWS], rb[HS_ROWS];
+#pragma unroll
+        for (int r = 0; r < HS_ROWS; r++) {
+            ra[r] = rf[r][0];
+            rb[r] = GEO ? rf[r][1] : ra[r];
+        }
+        for (int g = warp; g < ngroups; g += HS_THREADS / 32) {
+            const int tile = g * 32 + lane;
+            for (int q = 0; q < SEL_TILE; q++) {
+                const int j = tile * SEL_TILE + q;
+                if (tile >= a.ntiles || j >= n) continue;
+                const float4 pa = a.pts[NF * (size_t)j];
+                const float4 pb = GEO ? a.pts[2 * (size_t)j + 1] : pa;
+#pragma unroll
+                for (int r = 0; r < HS_ROWS; r++) {
+                    if (r >= nrows) break;
+                    const float d32 = GEO ? geo_dist32(ra[r], rb[r], pa, pb) : sqrtf(planar_d2_32(ra[r], pa));
+                    const double d = (double)d32;
+                    if (d <= __longlong_as_double(0x7ff0000000000000ll))
+                        atomicAdd(&hs[r * SEL_BINS + bucket_of(wlog, dkey(d))], 1u);
+                }
+            }
+        }
+        __syncthreads();
+        for (int e = t; e < nrows * SEL_BINS; e += HS_THREADS) a.hist_cache[(size_t)row0 * SEL_BINS + e] = hs[e];
+        __syncthreads();
+    }
+}
+
 // fixbw of BandwidthWeight.cpp:40-53 from the selected order statistics:
 // dn < 1: d0 + (d1 - d0) * bx;  dn >= 1: dn * max(dist).
 __global__ void k_threshold_combine(int n, double bw, const double* __restrict__ d0,
@@ -421,6 +484,22 @@ cudaError_t launch_select(const SelectArgs& a, bool geographic, bool exact, int 
         else GW_SEL(false, false);
     }
 #undef GW_SEL
+    return cudaGetLastError();
+}
+
+cudaError_t launch_select_hist(const SelectArgs& a, bool geographic, int num_sms, cudaStream_t stream)
+{
+    if (!a.hist_cache || a.n < 1) return cudaErrorInvalidValue;
+    const size_t smem = (size_t)HS_ROWS * SEL_BINS * sizeof(unsigned);
+    int grid = (a.n + HS_ROWS - 1) / HS_ROWS;
+    if (grid > num_sms) grid = num_sms;
+    if (geographic) {
+        cudaFuncSetAttribute(k_select_hist<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_select_hist<true><<<grid, HS_THREADS, smem, stream>>>(a);
+    } else {
+        cudaFuncSetAttribute(k_select_hist<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_select_hist<false><<<grid, HS_THREADS, smem, stream>>>(a);
+    }
     return cudaGetLastError();
 }
 

@@ -30,52 +30,65 @@ constexpr float kGeoA = 6378.137f;                  // WGS-84 semi-major axis (k
 constexpr float kGeoF = 1.0f / 298.257223563f;      // WGS-84 flattening
 constexpr float kGeoK = 4.0f * kGeoA * kGeoA;       // (2a)^2
 
-// Squared great-circle distance (km^2) of the reference's Lambert formula
-// (CRSDistance.cpp:15-81) in FP32, from hi/lo unit vectors.  With latitudes
-// phi, the half angle w and S = sin^2 w = |chord|^2 / 4, C = 1 - S:
-//   sin^2F cos^2G = ((sin phi_a + sin phi_b) / 2)^2  and
-//   cos^2F sin^2G = ((sin phi_a - sin phi_b) / 2)^2,
-// so with A = w / sqrt(S) and R = sqrt(S C) / w = sqrt(C) / A the formula
-// D = 2 a w (1 + f (H1 sin^2F cos^2G - H2 cos^2F sin^2G)), H1 = (3R - 1)/(2C),
-// H2 = (3R + 1)/(2S), becomes D^2 = (2a)^2 S (A (1 + c))^2 with
-//   c = (f / 8) [(3 sqrt C - A) zs^2 S - (3 sqrt C + A) dz^2 C] / (A S C),
-// zs = sin phi_a + sin phi_b, dz = sin phi_a - sin phi_b.  A comes from
-// asin_over_x for S <= 0.25 and from atan2 beyond.  The value is symmetric in
-// the two points bit for bit.  When s_cut is given (a compact kernel's
-// haversine cut-off, see geo_s_cut) a pair with S in [s_cut, 0.86] sets
-// beyond and returns 0 without the rest of the formula.
-__device__ __forceinline__ float geo_d2_32(const float4& fa, const float4& fb, const float4& pa, const float4& pb,
-                                           float s_cut, bool& beyond)
+// Chord terms of a pair of geographic records: S = sin^2 w = |chord|^2 / 4
+// (w = half the central angle), dz = sin phi_p - sin phi_f and
+// zs = sin phi_p + sin phi_f.
+struct GeoChord {
+    float S, dz, zs;
+};
+
+__device__ __forceinline__ GeoChord geo_chord32(const float4& fa, const float4& fb, const float4& pa, const float4& pb)
 {
     const float dx = (pa.x - fa.x) + (pb.x - fb.x);
     const float dy = (pa.y - fa.y) + (pb.y - fb.y);
     const float dz = (pa.z - fa.z) + (pb.z - fb.z);
-    const float S = 0.25f * fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    beyond = S >= s_cut && S <= 0.86f;
-    if (beyond) return 0.0f;
-    if (!(S > 1e-30f)) return kGeoK * fmaxf(S, 0.0f);
-    const float zs = (pa.z + fa.z) + (pb.z + fb.z);
+    GeoChord g;
+    g.S = 0.25f * fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    g.dz = dz;
+    g.zs = (pa.z + fa.z) + (pb.z + fb.z);
+    return g;
+}
+
+// Squared great-circle distance (km^2) of the reference's Lambert formula
+// (CRSDistance.cpp:15-81) in FP32, from the chord terms.  With latitudes phi:
+//   sin^2F cos^2G = ((sin phi_a + sin phi_b) / 2)^2  and
+//   cos^2F sin^2G = ((sin phi_a - sin phi_b) / 2)^2,
+// so with A = w / sqrt(S) and R = sqrt(S C) / w = sqrt(C) / A (C = 1 - S)
+// the formula D = 2 a w (1 + f (H1 sin^2F cos^2G - H2 cos^2F sin^2G)),
+// H1 = (3R - 1)/(2C), H2 = (3R + 1)/(2S), becomes D^2 = (2a)^2 S (A (1 + c))^2,
+//   c = (f / 8) [(3 sqrt C - A) zs^2 S - (3 sqrt C + A) dz^2 C] / (A S C).
+// A = asin_over_x(S) for S <= 0.25; beyond, asin x = pi/2 - 2 asin(sqrt y)
+// with y = (1 - x) / 2 <= 0.25 reuses the same polynomial.  Branch-free (the
+// cases are selects), so independent pairs interleave; symmetric in the two
+// points bit for bit.
+__device__ __forceinline__ float geo_d2_from_chord(const GeoChord& g)
+{
+    const float S = g.S;
     const float C = fmaxf(1.0f - S, 0.0f);
     const float cq = C * rsqrtf(C);
-    float A;
-    if (S <= 0.25f) {
-        A = asin_over_x(S);
-    } else {
-        const float sq = sqrtf(S);
-        A = __fdividef(atan2f(sq, cq), sq);
-    }
+    const bool near = S <= 0.25f;
+    const float rs = rsqrtf(S);
+    const float y = 0.5f - 0.5f * (S * rs);  // (1 - sqrt S) / 2
+    const float z = near ? S : y;
+    const float Pz = asin_over_x(z);
+    const float far_w = fmaf(-2.0f * (z * rsqrtf(z)), Pz, 1.5707963267948966f);  // asin(sqrt S)
+    const float A = near ? Pz : far_w * rs;
     const float t1 = fmaf(3.0f, cq, -A), t2 = fmaf(3.0f, cq, A);
-    const float num = fmaf(t1 * (zs * zs), S, -(t2 * (dz * dz)) * C);
+    const float num = fmaf(t1 * (g.zs * g.zs), S, -(t2 * (g.dz * g.dz)) * C);
     const float c = (0.125f * kGeoF) * __fdividef(num, A * S * C);
     const float Q = fmaf(A, c, A);
-    return kGeoK * S * (Q * Q);
+    const float d2 = kGeoK * S * (Q * Q);
+    return S > 1e-30f ? d2 : kGeoK * fmaxf(S, 0.0f);
 }
 
 __device__ __forceinline__ float geo_d2_32(const float4& fa, const float4& fb, const float4& pa, const float4& pb)
 {
-    bool beyond;
-    return geo_d2_32(fa, fb, pa, pb, __int_as_float(0x7f800000), beyond);
+    return geo_d2_from_chord(geo_chord32(fa, fb, pa, pb));
 }
+
+// True when a pair with haversine term S lies beyond a compact kernel's
+// threshold whose cut-off (geo_s_cut) is s_cut.
+__device__ __forceinline__ bool geo_beyond(float S, float s_cut) { return S >= s_cut && S <= 0.86f; }
 
 // FP32 great-circle distance (km), the square root of geo_d2_32.
 __device__ __forceinline__ float geo_dist32(const float4& fa, const float4& fb, const float4& pa, const float4& pb)

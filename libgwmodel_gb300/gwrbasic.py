@@ -366,6 +366,9 @@ class Engine:
     def set_precision(self, p):
         check(lib().gwgpu_engine_set_precision(self._h, int(p)))
 
+    def set_flush_tiles(self, tiles):
+        check(lib().gwgpu_engine_set_flush_tiles(self._h, int(tiles)))
+
     def criterion(self, bw, adaptive, kernel, criterion):
         v = ctypes.c_double()
         check(lib().gwgpu_engine_criterion(self._h, float(bw), int(bool(adaptive)), int(kernel), int(criterion),
@@ -426,7 +429,9 @@ class Engine:
     def stats(self):
         s = Stats()
         check(lib().gwgpu_engine_get_stats(self._h, ctypes.byref(s)))
-        return {k: getattr(s, k) for k, _ in Stats._fields_}
+        out = {k: getattr(s, k) for k, _ in Stats._fields_}
+        out["contract_phase_cycles"] = list(out["contract_phase_cycles"])
+        return out
 
     def reset_stats(self):
         check(lib().gwgpu_engine_reset_stats(self._h))
