@@ -56,6 +56,22 @@ __device__ __forceinline__ uint64_t dkey(double d)
     return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }
 
+// dkey((double)f) for f >= +0 (or +inf) from the bits of the float, in
+// integer arithmetic only: a normal float's double pattern is
+// (bits(f) + (896 << 23)) << 29 (exponent rebias 1023 - 127 = 896); a
+// subnormal m 2^-149 with top bit s becomes exponent s + 874 and mantissa
+// m << (52 - s).  Every case is a select, so no FP64 instruction is issued.
+__device__ __forceinline__ uint64_t dkey_f(float f)
+{
+    const uint32_t b = __float_as_uint(f);
+    const uint64_t normal = ((uint64_t)b + (896ull << 23)) << 29;
+    const int s = 31 - __clz(b | 1u);
+    const uint64_t sub = ((uint64_t)(s + 874) << 52) | (((uint64_t)b << (52 - s)) & 0x000fffffffffffffull);
+    uint64_t bits = b >= 0x00800000u ? normal : (b == 0u ? 0ull : sub);
+    bits = b >= 0x7f800000u ? (0x7ff0000000000000ull | ((uint64_t)(b & 0x7fffffu) << 29)) : bits;
+    return bits | 0x8000000000000000ull;
+}
+
 __device__ __forceinline__ double keyd(uint64_t k)
 {
     uint64_t b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;

@@ -208,6 +208,7 @@ __device__ bool select_row(SelShared& sh, const SelectArgs& a, const RowCtx& c, 
             below_thr = T_lo > 0.0 ? (float)(T_lo * T_lo * (1.0 - 1e-6)) : -1.0f;
             above_thr = isinf(T_hi) ? 3e38f : (float)(T_hi * T_hi * (1.0 + 1e-6));
         }
+        const uint64_t klo = dkey(T_lo), khi = dkey(T_hi);
         for (int b = t; b < SEL_BINS; b += SEL_THREADS) sh.hist[b] = 0;
         if (t == 0) sh.ncand = 0;
         __syncthreads();
@@ -236,21 +237,28 @@ __device__ bool select_row(SelShared& sh, const SelectArgs& a, const RowCtx& c, 
                     } else {
                         d32 = sqrtf(planar_d2_32(c.fa, a.pts[j]));
                     }
-                    double d = (double)d32;
-                    bool eval = true;
                     if (EXACT) {
+                        double d = (double)d32;
                         const double dl = sure ? d * (1.0 - a.eps) - a.delta : -1.0;
                         const double dh = sure ? d * (1.0 + a.eps) + a.delta : INF;
-                        eval = false;
+                        bool eval = false;
                         if (dh < T_lo) below++;
                         else if (!(dl > T_hi)) eval = true;
-                        if (eval) d = pair_dist<GEO>(a.P, j, c.fu, c.fv, c.fuR, c.fvR);
-                    }
-                    if (eval) {
-                        if (d < T_lo) below++;
-                        else if (d <= T_hi) {
+                        if (eval) {
+                            d = pair_dist<GEO>(a.P, j, c.fu, c.fv, c.fuR, c.fvR);
+                            if (d < T_lo) below++;
+                            else if (d <= T_hi) {
+                                in = true;
+                                key = dkey(d);
+                            }
+                        }
+                    } else if (d32 == d32) {
+                        // proxy values compared in key space (dkey is monotone)
+                        const uint64_t k32 = dkey_f(d32);
+                        if (k32 < klo) below++;
+                        else if (k32 <= khi) {
                             in = true;
-                            key = dkey(d);
+                            key = k32;
                         }
                     }
                 }
@@ -420,9 +428,7 @@ __global__ void __launch_bounds__(HS_THREADS, 1) k_select_hist(SelectArgs a)
                 for (int r = 0; r < HS_ROWS; r++) {
                     if (r >= nrows) break;
                     const float d32 = GEO ? geo_dist32(ra[r], rb[r], pa, pb) : sqrtf(planar_d2_32(ra[r], pa));
-                    const double d = (double)d32;
-                    if (d <= __longlong_as_double(0x7ff0000000000000ll))
-                        atomicAdd(&hs[r * SEL_BINS + bucket_of(wlog, dkey(d))], 1u);
+                    if (d32 == d32) atomicAdd(&hs[r * SEL_BINS + bucket_of(wlog, dkey_f(d32))], 1u);
                 }
             }
         }

@@ -49,12 +49,13 @@ __global__ void k_build_z(int n, int p, const double* __restrict__ X, const doub
     for (int a = 0; a < p; a++) z[mm + a] = x[a] * y[j];
 }
 
+// The factor keeps 1 / L_jj on its diagonal, so the substitutions multiply.
 // Forward substitution L z = rhs (lane r holds rhs_r; returns z_r).
 __device__ __forceinline__ double fwd_solve(const double* L, int ld, int p, int lane, double rhs)
 {
     double v = rhs;
     for (int j = 0; j < p; j++) {
-        double zj = __shfl_sync(FULL, v, j) / L[j * ld + j];
+        double zj = __shfl_sync(FULL, v, j) * L[j * ld + j];
         if (lane == j) v = zj;
         else if (lane > j && lane < p) v -= L[lane * ld + j] * zj;
     }
@@ -66,7 +67,7 @@ __device__ __forceinline__ double bwd_solve(const double* L, int ld, int p, int 
 {
     double v = rhs;
     for (int j = p - 1; j >= 0; j--) {
-        double xj = __shfl_sync(FULL, v, j) / L[j * ld + j];
+        double xj = __shfl_sync(FULL, v, j) * L[j * ld + j];
         if (lane == j) v = xj;
         else if (lane < j) v -= L[j * ld + lane] * xj;
     }
@@ -106,10 +107,10 @@ __global__ void __launch_bounds__(SV_WARPS * 32) k_solve(SolveArgs a)
             }
             double tjj = __shfl_sync(FULL, t, j);
             if (!(tjj > 0.0)) { fail = true; break; }
-            double ljj = sqrt(tjj);
+            const double rinv = rsqrt(tjj);  // 1 / L_jj
             __syncwarp();
-            if (lane == j) L[j * ld + j] = ljj;
-            else if (lane > j && lane < p) L[lane * ld + j] = t / ljj;
+            if (lane == j) L[j * ld + j] = rinv;
+            else if (lane > j && lane < p) L[lane * ld + j] = t * rinv;
             __syncwarp();
         }
         if (fail) {
