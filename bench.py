@@ -44,6 +44,7 @@ def parse():
     ap.add_argument("--n", type=int, default=200000, help="points (smaller values for profiling only)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     return ap.parse_args()
 
@@ -119,6 +120,43 @@ def ncu_traffic(name):
     with open(path) as f:
         m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", f.read())
     return float(m.group(1)) if m else None
+
+
+def fp64_search_ms():
+    """FP64 drop-in time per step of this workload from the committed measurement
+    (profiles/fp64_config2.md); the FP64 search takes minutes, so it is not rerun."""
+    path = os.path.join(ROOT, "profiles", "fp64_config2.md")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        m = re.search(r"fp64_ms_per_step:\s*([0-9.eE+]+)", f.read())
+    return float(m.group(1)) if m else None
+
+
+def rel_err(a, b):
+    """Largest absolute difference over the largest magnitude, per column."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    if a.ndim == 1:
+        return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+    return max(float(np.abs(a[:, k] - b[:, k]).max() / max(np.abs(b[:, k]).max(), 1e-300)) for k in range(a.shape[1]))
+
+
+def accuracy_vs_fp64(engine, pb, bw, local):
+    """Errors of the mixed path against the FP64 path at the selected bandwidth:
+    beta, betasSE, tr(S), tr(S^T S), qDiag and the AICc value."""
+    from libgwmodel_gb300 import Engine, Precision
+    e64 = Engine(local)
+    e64.set_data(pb.x, pb.y, pb.coords, pb.geographic)
+    e64.set_precision(Precision.FP64)
+    b64, se64, sh64, q64, _ = e64.fit(bw, True, pb.kernel, store_s=False)
+    c64 = e64.criterion(bw, True, pb.kernel, 0)
+    bmx, semx, shmx, qmx, _ = engine.fit(bw, True, pb.kernel, store_s=False)
+    cmx = engine.criterion(bw, True, pb.kernel, 0)
+    return {"bandwidth": bw, "beta_rel": rel_err(bmx, b64), "betasSE_rel": rel_err(semx, se64),
+            "trS_rel": abs(shmx[0] - sh64[0]) / abs(sh64[0]), "trStS_rel": abs(shmx[1] - sh64[1]) / abs(sh64[1]),
+            "qdiag_rel": rel_err(qmx, q64), "aicc_rel": abs(cmx - c64) / abs(c64), "beta_tolerance": 1e-6,
+            "note": "max |mixed - fp64| / max |fp64| per column; same bandwidth, FP64 drop-in as the reference"}
 
 
 def one_fit(engine, pb):
@@ -278,6 +316,12 @@ def run_ours(args):
         line["e2e"] = e2e
     if clk:
         line["clocks"] = clk
+    if prec == Precision.Mixed and rank == 0 and not args.no_accuracy:
+        line["accuracy_vs_fp64"] = accuracy_vs_fp64(engine, pb, bw, local)
+        f64 = fp64_search_ms() if args.n == 200000 else None
+        if f64:
+            line["fp64_ms_per_step"] = f64
+            line["speedup_vs_fp64"] = f64 / (ms / args.steps)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(pb, args.cpu_seconds)
     if rank == 0:

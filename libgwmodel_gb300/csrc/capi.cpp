@@ -531,7 +531,7 @@ int gwgpu_engine_get_stats(gwgpu_engine* e, gwgpu_stats* out)
 int gwgpu_engine_reset_stats(gwgpu_engine* e)
 {
     ENG_CHECK(e);
-    e->eng.stats() = gwgpu::EngineStats{};
+    e->eng.resetStats();
     return GWGPU_OK;
 }
 

@@ -104,6 +104,10 @@ Engine::~Engine()
     if (stream_) cudaStreamSynchronize(stream_);
     for (auto& e : events_)
         if (e) cudaEventDestroy(e);
+    for (auto& pt : pending_) {
+        cudaEventDestroy(pt.e0);
+        cudaEventDestroy(pt.e1);
+    }
     if (host_sums_) cudaFreeHost(host_sums_);
     if (stream_) cudaStreamDestroy(stream_);
 }
@@ -456,19 +460,65 @@ void Engine::ensureMixed()
     mixed_ready_ = true;
 }
 
+cudaEvent_t Engine::timerBegin()
+{
+    cudaEvent_t e0 = nullptr;
+    check(cudaEventCreate(&e0), "event");
+    check(cudaEventRecord(e0, stream_), "event record");
+    return e0;
+}
+
+void Engine::timerEnd(cudaEvent_t e0, int kind)
+{
+    cudaEvent_t e1 = nullptr;
+    check(cudaEventCreate(&e1), "event");
+    check(cudaEventRecord(e1, stream_), "event record");
+    pending_.push_back(PendingTiming{e0, e1, kind});
+}
+
+EngineStats& Engine::stats()
+{
+    for (auto& pt : pending_) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(pt.e1) == cudaSuccess && cudaEventElapsedTime(&ms, pt.e0, pt.e1) == cudaSuccess)
+            (pt.kind == 0 ? stats_.contract_ms : stats_.select_ms) += ms;
+        cudaEventDestroy(pt.e0);
+        cudaEventDestroy(pt.e1);
+    }
+    pending_.clear();
+    if (counters_dirty_ && tile_count_.get()) {
+        unsigned long long tiles = 0, pc[kTcProfSlots];
+        check(cudaMemcpyAsync(&tiles, tile_count_.get(), sizeof(tiles), cudaMemcpyDeviceToHost, stream_), "D2H");
+        check(cudaMemcpyAsync(pc, tc_prof_.get(), sizeof(pc), cudaMemcpyDeviceToHost, stream_), "D2H");
+        check(cudaMemsetAsync(tile_count_.get(), 0, sizeof(unsigned long long), stream_), "memset tiles");
+        check(cudaMemsetAsync(tc_prof_.get(), 0, sizeof(pc), stream_), "memset prof");
+        synchronize();
+        stats_.contract_tiles += (long long)tiles;
+        for (int q = 0; q < kTcProfSlots && q < 12; q++) {
+            if (q == kTcProfLoopMax || q == kTcProfTilesMax)
+                stats_.contract_phase_cycles[q] = std::max(stats_.contract_phase_cycles[q], (double)pc[q]);
+            else
+                stats_.contract_phase_cycles[q] += (double)pc[q];
+        }
+        counters_dirty_ = false;
+    }
+    return stats_;
+}
+
+void Engine::resetStats()
+{
+    stats();
+    stats_ = EngineStats{};
+}
+
 void Engine::contractMixed(double* G, int ldg, int mcols, double bw, bool adaptive, int kernel, bool exclude_self,
                            int wpow)
 {
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (adaptive) {
         check(launch_to_float(n_, thr_.get(), thr32_.get(), stream_), "thr32");
         stats_.kernel_launches += 1;
     }
-    if (stats_on_) {
-        cudaEventCreate(&e0);
-        cudaEventCreate(&e1);
-        cudaEventRecord(e0, stream_);
-    }
+    cudaEvent_t e0 = stats_on_ ? timerBegin() : nullptr;
     TcArgs a{};
     a.n = n_;
     a.mcols = mcols;
@@ -489,39 +539,26 @@ void Engine::contractMixed(double* G, int ldg, int mcols, double bw, bool adapti
     a.ldg = ldg;
     a.err = err_.get();
     if (stats_on_) {
-        if (!tile_count_.get()) tile_count_.alloc(1);
-        if (!tc_prof_.get()) tc_prof_.alloc(kTcProfSlots);
-        check(cudaMemsetAsync(tile_count_.get(), 0, sizeof(unsigned long long), stream_), "memset tiles");
-        check(cudaMemsetAsync(tc_prof_.get(), 0, sizeof(unsigned long long) * kTcProfSlots, stream_), "memset prof");
+        if (!tile_count_.get()) {
+            tile_count_.alloc(1);
+            tc_prof_.alloc(kTcProfSlots);
+            check(cudaMemsetAsync(tile_count_.get(), 0, sizeof(unsigned long long), stream_), "memset tiles");
+            check(cudaMemsetAsync(tc_prof_.get(), 0, sizeof(unsigned long long) * kTcProfSlots, stream_),
+                  "memset prof");
+        }
         a.tiles = tile_count_.get();
         a.prof = tc_prof_.get();
+        counters_dirty_ = true;
     }
     check(launch_contract_tc(a, geographic_, stream_), "contract_tc");
     stats_.kernel_launches += 1;
     if (stats_on_) {
-        cudaEventRecord(e1, stream_);
-        cudaEventSynchronize(e1);
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        stats_.contract_ms += ms;
+        timerEnd(e0, 0);
         stats_.contract_launches += 1;
         double pairs = (double)n_ * n_;
         if (adaptive && kernel >= GW_KERNEL_BISQUARE) pairs = (double)n_ * std::max(0.0, std::min(bw, (double)n_) - 1);
         stats_.contract_flops += 2.0 * mcols * pairs;
         stats_.contract_bytes += 2.0 * npad_ * 128.0 * ntiles32_ * 2 + 8.0 * n_ * mcols + 16.0 * n_;
-        unsigned long long tiles = 0;
-        check(cudaMemcpy(&tiles, tile_count_.get(), sizeof(tiles), cudaMemcpyDeviceToHost), "D2H tiles");
-        stats_.contract_tiles += (long long)tiles;
-        unsigned long long pc[kTcProfSlots];
-        check(cudaMemcpy(pc, tc_prof_.get(), sizeof(pc), cudaMemcpyDeviceToHost), "D2H prof");
-        for (int q = 0; q < kTcProfSlots && q < 12; q++) {
-            if (q == kTcProfLoopMax || q == kTcProfTilesMax)
-                stats_.contract_phase_cycles[q] = std::max(stats_.contract_phase_cycles[q], (double)pc[q]);
-            else
-                stats_.contract_phase_cycles[q] += (double)pc[q];
-        }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
     }
 }
 
@@ -599,12 +636,7 @@ void Engine::computeThresholds(double bw, bool adaptive)
     if (!adaptive) return;
     if (thr_valid_ && thr_bw_ == bw && thr_prec_ == precision_) return;
     const double dn = bw / n_;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    if (stats_on_) {
-        cudaEventCreate(&e0);
-        cudaEventCreate(&e1);
-        cudaEventRecord(e0, stream_);
-    }
+    cudaEvent_t e0 = stats_on_ ? timerBegin() : nullptr;
     if (dn < 1) {
         // d0 = vdist(int(b0) - 1), d1 = vdist(int(b0)) (BandwidthWeight.cpp:46-48)
         const double b0 = std::floor(bw), bx = bw - b0;
@@ -621,14 +653,8 @@ void Engine::computeThresholds(double bw, bool adaptive)
     stats_.kernel_launches += 1;
     }
     if (stats_on_) {
-        cudaEventRecord(e1, stream_);
-        cudaEventSynchronize(e1);
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        stats_.select_ms += ms;
+        timerEnd(e0, 1);
         stats_.select_launches += 1;
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
     }
     thr_valid_ = true;
     thr_bw_ = bw;
@@ -638,22 +664,13 @@ void Engine::computeThresholds(double bw, bool adaptive)
 void Engine::contract(const double* Z, int mcols, double* G, int ldg, double bw, bool adaptive, int kernel,
                       bool exclude_self, int wpow)
 {
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    if (stats_on_) {
-        cudaEventCreate(&e0);
-        cudaEventCreate(&e1);
-        cudaEventRecord(e0, stream_);
-    }
+    cudaEvent_t e0 = stats_on_ ? timerBegin() : nullptr;
     check(launch_contract64(points(), geographic_, tb16_.get(), Z, m_, mcols, G, ldg, thrPtr(adaptive), bw, kernel,
                             exclude_self, wpow, true, stream_),
           "contract64");
     stats_.kernel_launches += 1;
     if (stats_on_) {
-        cudaEventRecord(e1, stream_);
-        cudaEventSynchronize(e1);
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        stats_.contract_ms += ms;
+        timerEnd(e0, 0);
         stats_.contract_launches += 1;
         // useful pairs: dense kernels touch every pair; adaptive compact kernels
         // have b-1 neighbours with d < r_i per row (ties aside)
@@ -661,8 +678,6 @@ void Engine::contract(const double* Z, int mcols, double* G, int ldg, double bw,
         if (adaptive && kernel >= GW_KERNEL_BISQUARE) pairs = (double)n_ * std::max(0.0, std::min(bw, (double)n_) - 1);
         stats_.contract_flops += 2.0 * mcols * pairs;
         stats_.contract_bytes += 8.0 * ((double)n_ * m_ + (double)n_ * mcols) + 16.0 * n_;
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
     }
 }
 
@@ -754,7 +769,7 @@ double Engine::criterion(double bw, bool adaptive, int kernel, int crit)
         for (int it = 0; it < refine_steps_; it++) refine(bw, adaptive, kernel, r);
         if (refine_steps_ > 0) s[1] = r[1];
     }
-    if (stats_on_) stats_.criterion_evals++;
+    stats_.criterion_evals++;
     if (s[3] > 0.0) return DBL_MAX;
     if (crit == kCV) return std::isfinite(s[1]) ? s[1] : DBL_MAX;
     double v = aicc((double)n_, s[1], s[0]);

@@ -136,7 +136,10 @@ public:
     void thresholds(double bw, bool adaptive, std::vector<double>& out);
 
     void enableStats(bool on) { stats_on_ = on; }
-    EngineStats& stats() { return stats_; }
+    // Counters and event timings; resolving them waits for the recorded
+    // events, never for anything during a fit.
+    EngineStats& stats();
+    void resetStats();
     cudaStream_t stream() const { return stream_; }
     void synchronize();
 
@@ -208,7 +211,16 @@ private:
     DevBuf<float> thr32_;
     DevBuf<int> err_;
     DevBuf<unsigned long long> tile_count_;
-    DevBuf<unsigned long long> tc_prof_;  // phase cycles of the contraction (stats)  // processed-tile counter of the contraction (stats)
+    DevBuf<unsigned long long> tc_prof_;  // phase cycles of the contraction (stats)
+    // event pairs recorded around timed launches, resolved by stats()
+    struct PendingTiming {
+        cudaEvent_t e0, e1;
+        int kind;  // 0: contraction, 1: select
+    };
+    std::vector<PendingTiming> pending_;
+    bool counters_dirty_ = false;
+    cudaEvent_t timerBegin();
+    void timerEnd(cudaEvent_t e0, int kind);  // processed-tile counter of the contraction (stats)
     DevBuf<double> tinv_, tvec_;   // transform of the fit's covariance diagonal
     DevBuf<unsigned long long> key_;
     double* host_sums_ = nullptr;  // pinned
