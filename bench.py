@@ -45,6 +45,12 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--no-serve", action="store_true", help="skip the short serving run of the main line")
+    ap.add_argument("--serve", action="store_true", help="config-4 serving sweep instead of the config-2 line")
+    ap.add_argument("--rates", default="5,20,50,200")
+    ap.add_argument("--requests", type=int, default=60)
+    ap.add_argument("--slots", type=int, default=8)
+    ap.add_argument("--precision-serve", choices=["mixed", "fp64", "both"], default="mixed")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     return ap.parse_args()
 
@@ -157,6 +163,55 @@ def accuracy_vs_fp64(engine, pb, bw, local):
             "trS_rel": abs(shmx[0] - sh64[0]) / abs(sh64[0]), "trStS_rel": abs(shmx[1] - sh64[1]) / abs(sh64[1]),
             "qdiag_rel": rel_err(qmx, q64), "aicc_rel": abs(cmx - c64) / abs(c64), "beta_tolerance": 1e-6,
             "note": "max |mixed - fp64| / max |fp64| per column; same bandwidth, FP64 drop-in as the reference"}
+
+
+def serve_stream(rate, count, precision, slots=8, budget_gb=150.0, seed=4):
+    """Config 4: replay a Poisson request stream through the serving loop and
+    report latency percentiles (submit to result) and throughput."""
+    from libgwmodel_gb300 import datasets
+    from libgwmodel_gb300.serve import Server, percentile, run_stream
+    reqs = datasets.config4(rate, count, seed=seed)
+    srv = Server(0, hbm_budget_gb=budget_gb, slots=slots)
+    # warm-up: every slot grows its buffers to the largest dataset of the pool once
+    big = max((r.problem for r in reqs), key=lambda pb: pb.n * pb.p)
+    ids = [srv.submit(big, kind=0, bandwidth=50.0, precision=precision) for _ in range(slots)]
+    for i in ids:
+        srv.wait(i)
+    warm = srv.stats()
+    out, wall = run_stream(srv, reqs, precision=precision)
+    st = srv.stats()
+    srv.close()
+    ok = [r for r, _ in out if r["status"] == 0]
+    lat = [r["end_ms"] - r["submit_ms"] for r in ok]
+    fits = sum(rq.problem.n * (r["evaluations"] + 1) for rq, (r, _) in zip(reqs, out) if r["status"] == 0)
+    searches = [r["end_ms"] - r["submit_ms"] for rq, (r, _) in zip(reqs, out) if r["status"] == 0 and rq.kind == 1]
+    return {"rate_req_s": rate, "requests": count, "completed": len(ok), "failed": count - len(ok),
+            "p50_ms": percentile(lat, 50), "p99_ms": percentile(lat, 99), "mean_ms": float(np.mean(lat)) if lat else 0,
+            "search_p50_ms": percentile(searches, 50), "search_p99_ms": percentile(searches, 99),
+            "wall_s": wall, "requests_per_s": len(ok) / wall, "local_fits_per_s": fits / wall,
+            "max_concurrent": st["max_concurrent"], "peak_reserved_gb": st["peak_reserved_bytes"] / 1e9,
+            "warmup_requests": int(warm["completed"])}
+
+
+def run_serve(args):
+    rank, _, _ = dist_env()
+    if rank != 0:
+        return 0
+    from libgwmodel_gb300 import Precision
+    precs = ["mixed", "fp64"] if args.precision_serve == "both" else [args.precision_serve]
+    rates = [float(r) for r in args.rates.split(",")]
+    for pr in precs:
+        prec = Precision.Mixed if pr == "mixed" else Precision.FP64
+        rows = [serve_stream(r, args.requests, prec, slots=args.slots) for r in rates]
+        line = {"metric": "GWR serving latency, config-4 request stream (70% fits, 30% AICc searches)",
+                "value": rows[0]["p99_ms"], "unit": "ms (p99, first rate)", "higher_is_better": False,
+                "n_gpus": 1, "precision": pr, "slots": args.slots, "hbm_budget_gb": 150.0,
+                "data": "synthetic (seeded config-4 generator, numpy PCG64 seed 4)",
+                "config": {"workload": "config4: Poisson arrivals; n log-uniform [1e3, 1e5], p in 3..20, "
+                                       "planar/geographic 50/50, adaptive bisquare"},
+                "rates": rows}
+        print(json.dumps(line), flush=True)
+    return 0
 
 
 def one_fit(engine, pb):
@@ -322,6 +377,9 @@ def run_ours(args):
         if f64:
             line["fp64_ms_per_step"] = f64
             line["speedup_vs_fp64"] = f64 / (ms / args.steps)
+    if rank == 0 and not args.no_serve and args.n == 200000:
+        from libgwmodel_gb300 import Precision as _P
+        line["serve"] = serve_stream(20.0, 48, _P.Mixed)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(pb, args.cpu_seconds)
     if rank == 0:
@@ -335,6 +393,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.serve:
+        return run_serve(args)
     return run_ours(args)
 
 

@@ -207,6 +207,81 @@ int gwgpu_criterion_noalloc(int n, int p, int criterion, int kernel, double band
                             const double* X, const double* y, const double* thr, double* beta, double* sums,
                             void* stream);
 
+/* ------------------------------------------------------- serving loop
+ *
+ * A request loop on one GPU: fits with a given bandwidth and golden-section
+ * bandwidth searches (then the fit) of independent datasets, submitted from
+ * any thread as they arrive.  Each of `slots` worker slots keeps one engine
+ * (its device buffers grow and are reused, so steady-state serving calls
+ * neither cudaMalloc nor cudaFree) and its own stream; requests run as soon
+ * as a slot is free and the HBM budget admits them, so their kernels overlap
+ * on the device.  Admission is first come, first served: the oldest waiting
+ * request is admitted when the memory held by every slot, with the chosen
+ * slot grown to the request's estimate, stays within the budget; idle slots
+ * give their memory back when that is what blocks it.  A request whose
+ * estimate alone exceeds the budget is rejected at submit.
+ */
+typedef struct gwgpu_server gwgpu_server;
+
+#define GWGPU_REQ_FIT 0    /* fit at the given bandwidth */
+#define GWGPU_REQ_SEARCH 1 /* golden-section bandwidth search, then the fit */
+#define GWGPU_ERR_TIMEOUT 6 /* gwgpu_server_wait: not finished within the timeout */
+#define GWGPU_ERR_REJECTED 7 /* the request does not fit the HBM budget */
+
+typedef struct gwgpu_request {
+    int n, p;              /* data points; columns of X (intercept supplied by the caller) */
+    const double* coords;  /* n x 2 column-major (u, v) or (lon, lat); copied at submit */
+    const double* x;       /* n x p column-major; copied at submit */
+    const double* y;       /* n; copied at submit */
+    int geographic;        /* 1: great-circle distances */
+    int kind;              /* GWGPU_REQ_FIT or GWGPU_REQ_SEARCH */
+    int adaptive;          /* bandwidth in neighbours (1) or distance (0) */
+    int kernel;            /* GWGPU_GAUSSIAN ... GWGPU_BOXCAR */
+    int criterion;         /* search criterion: GWGPU_AIC or GWGPU_CV */
+    double bandwidth;      /* GWGPU_REQ_FIT only */
+    int precision;         /* GWGPU_FP64 or GWGPU_MIXED */
+} gwgpu_request;
+
+typedef struct gwgpu_result {
+    int status;            /* GWGPU_OK or the request's error code */
+    int slot;              /* worker slot that ran it */
+    int evaluations;       /* criterion evaluations of the search (0 for a fit) */
+    double bandwidth;      /* given or selected */
+    double aicc;           /* GWRBase::AICc of the final fit (GWRBase.h:90-94) */
+    double rss;            /* residual sum of squares of the final fit */
+    double shat[2];        /* tr(S), tr(S^T S) */
+    double submit_ms, start_ms, end_ms;  /* server clock, from its creation */
+    char error[160];       /* message when status != GWGPU_OK */
+} gwgpu_result;
+
+typedef struct gwgpu_server_stats {
+    long long submitted, completed, failed, rejected, running, queued;
+    double p50_ms, p99_ms, mean_ms;  /* latency (end - submit) of completed requests */
+    double first_start_ms, last_end_ms;
+    double local_fits;               /* sum over completed requests of n x (evaluations + 1) */
+    double reserved_bytes;           /* memory held by the slots now */
+    double peak_reserved_bytes;
+    int max_concurrent;              /* most requests running at once */
+} gwgpu_server_stats;
+
+int gwgpu_server_create(int device, double hbm_budget_bytes, int slots, gwgpu_server** out);
+/* Waits for every admitted request, then stops the workers. */
+int gwgpu_server_destroy(gwgpu_server* s);
+/* betas_out: n x p column-major output filled when the request finishes (may be null). */
+int gwgpu_server_submit(gwgpu_server* s, const gwgpu_request* r, double* betas_out, long long* id);
+/* Blocks until the request finished (timeout_ms < 0: no limit); the record is then forgotten. */
+int gwgpu_server_wait(gwgpu_server* s, long long id, double timeout_ms, gwgpu_result* out);
+int gwgpu_server_poll(gwgpu_server* s, long long id, int* done);
+int gwgpu_server_get_stats(gwgpu_server* s, gwgpu_server_stats* out);
+/* The estimate this server admits the request with (bytes; host only). */
+double gwgpu_server_estimate(gwgpu_server* s, const gwgpu_request* r);
+/* Upper bound of one slot's device memory for a request of this shape, with
+   the histogram cache counted (host only). */
+double gwgpu_estimate_bytes(int n, int p, int geographic, int precision, int adaptive);
+/* The admission rule (host only): the slot an idle worker set would give the
+   request, or -1 to wait.  reserved: bytes each slot holds; busy: 1 when running. */
+int gwgpu_admit_slot(double budget, int slots, const double* reserved, const int* busy, double estimate);
+
 #ifdef __cplusplus
 }
 #endif

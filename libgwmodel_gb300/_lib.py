@@ -13,7 +13,7 @@ import threading
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libgwgpu.so")
 
-OK, ERR_INVALID, ERR_CUDA, ERR_NOT_SPD, ERR_RUNTIME, ERR_RANGE = range(6)
+OK, ERR_INVALID, ERR_CUDA, ERR_NOT_SPD, ERR_RUNTIME, ERR_RANGE, ERR_TIMEOUT, ERR_REJECTED = range(8)
 
 _lock = threading.Lock()
 _lib = None
@@ -41,6 +41,30 @@ class Stats(ctypes.Structure):
                 ("contract_bytes", ctypes.c_double), ("select_launches", ctypes.c_int),
                 ("select_ms", ctypes.c_double), ("kernel_launches", ctypes.c_longlong),
                 ("contract_tiles", ctypes.c_longlong), ("contract_phase_cycles", ctypes.c_double * 12)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int), ("p", ctypes.c_int), ("coords", ctypes.POINTER(ctypes.c_double)),
+                ("x", ctypes.POINTER(ctypes.c_double)), ("y", ctypes.POINTER(ctypes.c_double)),
+                ("geographic", ctypes.c_int), ("kind", ctypes.c_int), ("adaptive", ctypes.c_int),
+                ("kernel", ctypes.c_int), ("criterion", ctypes.c_int), ("bandwidth", ctypes.c_double),
+                ("precision", ctypes.c_int)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("slot", ctypes.c_int), ("evaluations", ctypes.c_int),
+                ("bandwidth", ctypes.c_double), ("aicc", ctypes.c_double), ("rss", ctypes.c_double),
+                ("shat", ctypes.c_double * 2), ("submit_ms", ctypes.c_double), ("start_ms", ctypes.c_double),
+                ("end_ms", ctypes.c_double), ("error", ctypes.c_char * 160)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_longlong), ("completed", ctypes.c_longlong), ("failed", ctypes.c_longlong),
+                ("rejected", ctypes.c_longlong), ("running", ctypes.c_longlong), ("queued", ctypes.c_longlong),
+                ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double),
+                ("first_start_ms", ctypes.c_double), ("last_end_ms", ctypes.c_double),
+                ("local_fits", ctypes.c_double), ("reserved_bytes", ctypes.c_double),
+                ("peak_reserved_bytes", ctypes.c_double), ("max_concurrent", ctypes.c_int)]
 
 
 # (name, restype, argtypes) of every function declared in include/gwgpu.h
@@ -101,6 +125,15 @@ SIGNATURES = [
     ("gwgpu_engine_get_stats", _i, [_vp, ctypes.POINTER(Stats)]),
     ("gwgpu_engine_reset_stats", _i, [_vp]),
     ("gwgpu_criterion_noalloc", _i, [_i, _i, _i, _i, _d, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    ("gwgpu_server_create", _i, [_i, _d, _i, ctypes.POINTER(_vp)]),
+    ("gwgpu_server_destroy", _i, [_vp]),
+    ("gwgpu_server_submit", _i, [_vp, ctypes.POINTER(Request), _dp, ctypes.POINTER(ctypes.c_longlong)]),
+    ("gwgpu_server_wait", _i, [_vp, ctypes.c_longlong, _d, ctypes.POINTER(Result)]),
+    ("gwgpu_server_poll", _i, [_vp, ctypes.c_longlong, _ip]),
+    ("gwgpu_server_get_stats", _i, [_vp, ctypes.POINTER(ServerStats)]),
+    ("gwgpu_server_estimate", _d, [_vp, ctypes.POINTER(Request)]),
+    ("gwgpu_estimate_bytes", _d, [_i, _i, _i, _i, _i]),
+    ("gwgpu_admit_slot", _i, [_d, _i, _dp, _ip, _d]),
     ("gwgpu_engine_tc_selftest", _i, [_vp, _i, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
                                       ctypes.POINTER(ctypes.c_float)]),
 ]

@@ -204,8 +204,8 @@ void Engine::setData(int n, int p, const double* x, const double* y, const doubl
         uR_.alloc(n);
         vR_.alloc(n);
     } else {
-        uR_.release();
-        vR_.release();
+        uR_.clear();
+        vR_.clear();
     }
     x_.alloc((size_t)n * p);
     y_.alloc(n);
@@ -239,7 +239,7 @@ void Engine::setData(int n, int p, const double* x, const double* y, const doubl
               "H2D caps");
         synchronize();
     } else {
-        caps_.release();
+        caps_.clear();
     }
     check(launch_build_z(n, p, x_.get(), y_.get(), z_.get(), stream_), "build_z");
     synchronize();
@@ -247,8 +247,8 @@ void Engine::setData(int n, int p, const double* x, const double* y, const doubl
     hy_ = std::move(hy);
     hu_ = std::move(hu);
     hv_ = std::move(hv);
-    ranks_.clear();
-    hist_.release();
+    recycleRanks();
+    hist_.clear();
     hist_tried_ = false;
     hist_valid_ = false;
     buildProxy();
@@ -315,7 +315,7 @@ void Engine::buildProxy()
               "H2D caps32");
         synchronize();
     } else {
-        caps32_.release();
+        caps32_.clear();
     }
     rvec_.alloc((size_t)n * p);
     pts32_.alloc(pts.size());
@@ -590,16 +590,28 @@ const double* Engine::orderStatistic(unsigned rank)
     const bool exact = precision_ == kFP64;
     for (auto& e : ranks_)
         if (e->exact == exact && e->rank == rank) return e->v.get();
-    if (ranks_.size() >= 64) ranks_.clear();
+    if (ranks_.size() >= 64) recycleRanks();
     if (!hist_tried_) {
         hist_tried_ = true;
         const size_t bytes = (size_t)n_ * 4096 * sizeof(unsigned);
-        size_t free_b = 0, total_b = 0;
-        cudaMemGetInfo(&free_b, &total_b);
-        if (bytes < free_b / 4) hist_.alloc((size_t)n_ * 4096);
+        bool fits;
+        if (hist_limit_bytes_ >= 0) {
+            fits = bytes <= (size_t)hist_limit_bytes_;
+        } else {
+            size_t free_b = 0, total_b = 0;
+            cudaMemGetInfo(&free_b, &total_b);
+            fits = bytes < free_b / 4 || bytes <= hist_.capacityBytes();
+        }
+        if (fits) hist_.alloc((size_t)n_ * 4096);
         hist_valid_ = false;
     }
-    std::unique_ptr<RankStat> r(new RankStat);
+    std::unique_ptr<RankStat> r;
+    if (!rank_pool_.empty()) {
+        r = std::move(rank_pool_.back());
+        rank_pool_.pop_back();
+    } else {
+        r.reset(new RankStat);
+    }
     r->rank = rank;
     r->exact = exact;
     r->v.alloc(n_);
@@ -884,9 +896,49 @@ double Engine::golden(bool adaptive, int kernel, int crit, double lower, double 
     return xopt;
 }
 
+size_t Engine::estimateBytes(int n, int p, bool geographic, bool mixed, bool adaptive, long long hist_limit)
+{
+    const double N = n, P = p;
+    const double m = P * (P + 1) / 2 + P, mm = P * (P + 1) / 2;
+    const double npad = std::ceil(m / 64) * 64;
+    const double t16 = std::ceil(N / 16), t32 = std::ceil(N / 32);
+    const double g = geographic ? 1.0 : 0.0;
+    double b = 8 * N * (2 + 2 * g);                                  // u, v, uR, vR
+    b += 8 * N * (P + 1 + 2 * m + 3 + P + 2 + P);                    // x, y, z, g, thr, sel0/1, beta, sii, resid, rvec
+    b += 8 * 16384 + 64;                                              // partials, sums
+    b += 32 * t16 * (1 + g) + 32 * t32 * (1 + g);                     // tile boxes and caps (16 and 32 points)
+    b += 16 * t32 * 32 * (1 + g) + 16 * t32 + 20 * t16;               // point records, tile bounds, tile thresholds
+    b += 8 * N * kMaxP + 8 * (kMaxP * (kMaxP + 3) / 2 + kMaxP);       // variable-selection scratch
+    if (mixed) b += 8 * N * (P + 1 + m) + t32 * 2 * npad * 128 + 8 * N * npad + 4 * N;
+    b += 8 * N * (mm + 2 * P + 2);                                    // fit: G2, v, betasSE, qDiag, S row
+    if (adaptive) {
+        const double h = 4.0 * 4096 * N;
+        if (hist_limit < 0 || h <= (double)hist_limit) b += h;
+        b += 64 * 8 * N;                                              // cached order statistics
+    }
+    return (size_t)(b * 1.05) + (16u << 20);
+}
+
+size_t Engine::bytesHeld() const
+{
+    size_t b = u_.capacityBytes() + v_.capacityBytes() + uR_.capacityBytes() + vR_.capacityBytes() +
+               x_.capacityBytes() + y_.capacityBytes() + z_.capacityBytes() + g_.capacityBytes() +
+               thr_.capacityBytes() + sel0_.capacityBytes() + sel1_.capacityBytes() + beta_.capacityBytes() +
+               sii_.capacityBytes() + resid_.capacityBytes() + partials_.capacityBytes() + sums_.capacityBytes() +
+               tiles_.capacityBytes() + caps_.capacityBytes() + boxes32_.capacityBytes() + caps32_.capacityBytes() +
+               rvec_.capacityBytes() + pts32_.capacityBytes() + tbsel_.capacityBytes() + tb16_.capacityBytes() +
+               tile_thr16_.capacityBytes() + xs_.capacityBytes() + ys_.capacityBytes() + zs_.capacityBytes() +
+               zimg_.capacityBytes() + acc_.capacityBytes() + thr32_.capacityBytes() + g2_.capacityBytes() +
+               vvec_.capacityBytes() + bse_.capacityBytes() + qdiag_.capacityBytes() + S_.capacityBytes() +
+               hist_.capacityBytes() + xsub_.capacityBytes() + gsub_.capacityBytes();
+    for (auto& r : ranks_) b += r->v.capacityBytes();
+    for (auto& r : rank_pool_) b += r->v.capacityBytes();
+    return b;
+}
+
 void Engine::clearCaches()
 {
-    ranks_.clear();
+    recycleRanks();
     hist_valid_ = false;
     thr_valid_ = false;
     gall_valid_ = false;

@@ -40,25 +40,34 @@ public:
     ~DevBuf() { release(); }
     DevBuf(const DevBuf&) = delete;
     DevBuf& operator=(const DevBuf&) = delete;
+    // Grow-only: a smaller request keeps the allocation, so an engine that is
+    // reused for datasets of different sizes stops calling cudaMalloc and
+    // cudaFree (both synchronise the device) once it has seen the largest.
     void alloc(size_t count)
     {
-        if (count == count_ && ptr_) return;
+        if (count <= cap_ && ptr_) {
+            count_ = count;
+            return;
+        }
         release();
         if (count) check(cudaMalloc(&ptr_, count * sizeof(T)), "cudaMalloc");
-        count_ = count;
+        count_ = cap_ = count;
     }
+    // Empty (get() returns null) without freeing the allocation.
+    void clear() { count_ = 0; }
     void release()
     {
         if (ptr_) cudaFree(ptr_);
         ptr_ = nullptr;
-        count_ = 0;
+        count_ = cap_ = 0;
     }
-    T* get() const { return ptr_; }
+    T* get() const { return count_ ? ptr_ : nullptr; }
     size_t size() const { return count_; }
+    size_t capacityBytes() const { return cap_ * sizeof(T); }
 
 private:
     T* ptr_ = nullptr;
-    size_t count_ = 0;
+    size_t count_ = 0, cap_ = 0;
 };
 
 // Timing of the contraction launches, filled when stats are enabled.
@@ -107,6 +116,14 @@ public:
         refine_search_ = refine_search;
     }
     int precision() const { return precision_; }
+    // Largest histogram cache (bytes) the adaptive select may allocate; -1
+    // lets it take up to a quarter of the free device memory.
+    void setHistLimit(long long bytes) { hist_limit_bytes_ = bytes; }
+    // Upper bound of the device memory an engine holds after setData plus a
+    // search and a fit of a dataset of this shape (the allocations below).
+    static size_t estimateBytes(int n, int p, bool geographic, bool mixed, bool adaptive, long long hist_limit);
+    // Device memory currently held (capacity of every buffer).
+    size_t bytesHeld() const;
 
     int n() const { return n_; }
     int p() const { return p_; }
@@ -179,6 +196,13 @@ private:
         DevBuf<double> v;
     };
     std::vector<std::unique_ptr<RankStat>> ranks_;
+    std::vector<std::unique_ptr<RankStat>> rank_pool_;  // recycled order-statistic buffers
+    void recycleRanks()
+    {
+        for (auto& r : ranks_) rank_pool_.push_back(std::move(r));
+        ranks_.clear();
+    }
+    long long hist_limit_bytes_ = -1;  // histogram cache limit; -1: a quarter of the free memory
     DevBuf<unsigned> hist_;    // per-row histograms of proxy distances (n x 4096)
     bool hist_tried_ = false, hist_valid_ = false;
     const double* orderStatistic(unsigned rank);

@@ -9,6 +9,12 @@ seed, so every run and every machine sees the same inputs.
                sigma=1, fixed gaussian, CV search
 * ``config2``  n=200,000 geographic lon U(-10,30), lat U(35,60), p=17 with
                column scales log-uniform over [1e-2, 1e3], adaptive bisquare, AICc
+* ``config3``  64 independent problems, n log-uniform [500, 20,000], p uniform
+               {3..12}, planar coordinates from a mixture of 5 Gaussian clusters,
+               32 adaptive bisquare bandwidth candidates each
+* ``config4``  a Poisson request stream: 70% fits at a given adaptive bandwidth,
+               30% AICc bandwidth searches; n log-uniform [1,000, 100,000], p
+               uniform {3..20}, planar or geographic 50/50, data as config 0
 """
 from __future__ import annotations
 
@@ -84,3 +90,68 @@ def config2(n=200000, seed=2, k=16):
 
 
 CONFIGS = {"config0": config0, "config1": config1, "config2": config2}
+
+
+def _plain_problem(rng, n, p, geographic, name):
+    """Intercept + (p - 1) N(0,1) covariates, smooth local coefficients, noise 0.5."""
+    if geographic:
+        coords = np.column_stack([rng.uniform(-10, 30, n), rng.uniform(35, 60, n)])
+        u, v, length = coords[:, 0] * 5.0, coords[:, 1] * 5.0, 20.0
+    else:
+        coords = rng.uniform(0, 100, (n, 2))
+        u, v, length = coords[:, 0], coords[:, 1], 20.0
+    x = np.column_stack([np.ones(n), rng.standard_normal((n, p - 1))])
+    beta = _smooth_betas(rng, u, v, p, length)
+    y = (x * beta).sum(1) + rng.normal(0, 0.5, n)
+    return Problem(name, np.asfortranarray(x), y, np.asfortranarray(coords), geographic, True,
+                   KERNELS["bisquare"], 0, beta)
+
+
+def config3(seed=3, problems=64, candidates=32):
+    """The batched workload: (problems, candidate bandwidths per problem)."""
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(0, 1000, (5, 2))
+    spread = rng.uniform(20, 120, 5)
+    out, cands = [], []
+    for q in range(problems):
+        n = int(round(np.exp(rng.uniform(np.log(500), np.log(20000)))))
+        p = int(rng.integers(3, 13))
+        k = rng.integers(0, 5, n)
+        coords = centres[k] + rng.standard_normal((n, 2)) * spread[k, None]
+        x = np.column_stack([np.ones(n), rng.standard_normal((n, p - 1))])
+        beta = _smooth_betas(rng, coords[:, 0], coords[:, 1], p, 150.0)
+        y = (x * beta).sum(1) + rng.normal(0, 0.5, n)
+        out.append(Problem(f"config3/{q}", np.asfortranarray(x), y, np.asfortranarray(coords), False, True,
+                           KERNELS["bisquare"], 0, beta))
+        lo, hi = max(p + 2, 20), n
+        cands.append(np.unique(np.round(np.exp(np.linspace(np.log(lo), np.log(hi), candidates)))).astype(float))
+    return out, cands
+
+
+@dataclass
+class StreamRequest:
+    arrival_s: float       # seconds after the stream starts
+    problem: Problem
+    kind: int              # 0 fit at `bandwidth`, 1 AICc search then fit
+    bandwidth: float
+
+
+def config4(rate, count, seed=4, pool=48, n_min=1000, n_max=100000):
+    """`count` requests arriving as a Poisson process of `rate` per second.
+    Datasets come from a pool of `pool` seeded problems (a request copies its
+    data at submit, so sharing a dataset between requests changes nothing)."""
+    rng = np.random.default_rng(seed)
+    problems = []
+    for q in range(pool):
+        n = int(round(np.exp(rng.uniform(np.log(n_min), np.log(n_max)))))
+        p = int(rng.integers(3, 21))
+        problems.append(_plain_problem(rng, n, p, bool(rng.integers(0, 2)), f"config4/{q}"))
+    t = 0.0
+    reqs = []
+    for _ in range(count):
+        t += rng.exponential(1.0 / rate)
+        pb = problems[int(rng.integers(0, pool))]
+        kind = 1 if rng.uniform() < 0.3 else 0
+        bw = float(rng.integers(max(pb.p + 10, 30), min(300, pb.n - 1) + 1))
+        reqs.append(StreamRequest(t, pb, kind, bw))
+    return reqs
