@@ -282,6 +282,44 @@ double gwgpu_estimate_bytes(int n, int p, int geographic, int precision, int ada
    request, or -1 to wait.  reserved: bytes each slot holds; busy: 1 when running. */
 int gwgpu_admit_slot(double budget, int slots, const double* reserved, const int* busy, double estimate);
 
+/* ------------------------------------------------------- batched problems
+ *
+ * Many independent GWR problems (uneven n and p) and many bandwidth
+ * candidates per problem, evaluated together: every phase (threshold
+ * selects, tensor-core or FP64 contraction, per-location solves, per-pair
+ * reductions) is one launch over all (problem, candidate) pairs, and the
+ * sequence is captured once into a CUDA graph and replayed.  The schedule
+ * (FP32 chunk of the contraction, order of its work table, rows per solve
+ * block, select width) is picked by gwgpu_batch_autotune on the batch itself.
+ */
+typedef struct gwgpu_batch gwgpu_batch;
+
+typedef struct gwgpu_batch_info {
+    int problems, segments;     /* segments = (problem, candidate) pairs */
+    int flush_tiles, order, solve_rows, select_ctas;  /* schedule in use */
+    int tuned;                  /* 1 after gwgpu_batch_autotune */
+    double tuned_ms, last_ms;   /* best tuning time; wall time of the last evaluation */
+    int graph;                  /* 1 when the evaluation is a captured graph */
+    int launches_per_evaluate;  /* kernel launches in one evaluation */
+    int contract_ctas;          /* CTAs of the batched contraction */
+    double rows_total;          /* sum over segments of n */
+} gwgpu_batch_info;
+
+int gwgpu_batch_create(int device, gwgpu_batch** out);
+int gwgpu_batch_destroy(gwgpu_batch* b);
+/* Copies every problem: x[q] n[q] x p[q] column-major, y[q], coords[q] n[q] x 2 column-major. */
+int gwgpu_batch_set_problems(gwgpu_batch* b, int count, const int* n, const int* p, const double* const* x,
+                             const double* const* y, const double* const* coords, const int* geographic,
+                             int precision);
+/* counts[q] candidates bandwidths[q][0..counts[q]) for problem q (adaptive: whole neighbour counts <= n). */
+int gwgpu_batch_set_candidates(gwgpu_batch* b, const int* counts, const double* const* bandwidths, int adaptive,
+                               int kernel, int criterion);
+/* values: the AICc (or CV) of every pair, problem-major (DBL_MAX where a local system is not SPD). */
+int gwgpu_batch_evaluate(gwgpu_batch* b, int use_graph, double* values);
+int gwgpu_batch_autotune(gwgpu_batch* b, int repeats);
+int gwgpu_batch_set_tuning(gwgpu_batch* b, int flush_tiles, int order, int solve_rows, int select_ctas);
+int gwgpu_batch_get_info(gwgpu_batch* b, gwgpu_batch_info* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -67,6 +67,14 @@ class ServerStats(ctypes.Structure):
                 ("peak_reserved_bytes", ctypes.c_double), ("max_concurrent", ctypes.c_int)]
 
 
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("problems", ctypes.c_int), ("segments", ctypes.c_int), ("flush_tiles", ctypes.c_int),
+                ("order", ctypes.c_int), ("solve_rows", ctypes.c_int), ("select_ctas", ctypes.c_int),
+                ("tuned", ctypes.c_int), ("tuned_ms", ctypes.c_double), ("last_ms", ctypes.c_double),
+                ("graph", ctypes.c_int), ("launches_per_evaluate", ctypes.c_int), ("contract_ctas", ctypes.c_int),
+                ("rows_total", ctypes.c_double)]
+
+
 # (name, restype, argtypes) of every function declared in include/gwgpu.h
 _vp, _ip, _dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)
 _i, _d, _sz = ctypes.c_int, ctypes.c_double, ctypes.c_size_t
@@ -134,6 +142,14 @@ SIGNATURES = [
     ("gwgpu_server_estimate", _d, [_vp, ctypes.POINTER(Request)]),
     ("gwgpu_estimate_bytes", _d, [_i, _i, _i, _i, _i]),
     ("gwgpu_admit_slot", _i, [_d, _i, _dp, _ip, _d]),
+    ("gwgpu_batch_create", _i, [_i, ctypes.POINTER(_vp)]),
+    ("gwgpu_batch_destroy", _i, [_vp]),
+    ("gwgpu_batch_set_problems", _i, [_vp, _i, _ip, _ip, ctypes.POINTER(ctypes.POINTER(ctypes.c_double)), ctypes.POINTER(ctypes.POINTER(ctypes.c_double)), ctypes.POINTER(ctypes.POINTER(ctypes.c_double)), _ip, _i]),
+    ("gwgpu_batch_set_candidates", _i, [_vp, _ip, ctypes.POINTER(ctypes.POINTER(ctypes.c_double)), _i, _i, _i]),
+    ("gwgpu_batch_evaluate", _i, [_vp, _i, _dp]),
+    ("gwgpu_batch_autotune", _i, [_vp, _i]),
+    ("gwgpu_batch_set_tuning", _i, [_vp, _i, _i, _i, _i]),
+    ("gwgpu_batch_get_info", _i, [_vp, ctypes.POINTER(BatchInfo)]),
     ("gwgpu_engine_tc_selftest", _i, [_vp, _i, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
                                       ctypes.POINTER(ctypes.c_float)]),
 ]

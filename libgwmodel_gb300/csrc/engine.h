@@ -164,6 +164,7 @@ public:
     void tcSelftest(int N, const float* A, const float* B, float* D);
 
 private:
+    friend class BatchEngine;  // builds per-segment kernel arguments over the engine's device data
     void ensureMixed();
     void buildProxy();
     void contractMixed(double* G, int ldg, int mcols, double bw, bool adaptive, int kernel, bool exclude_self,

@@ -8,6 +8,10 @@
 
 namespace gwgpu {
 
+// Raises (never lowers) the dynamic shared memory limit of kernel fn on the
+// current device to `bytes`; safe to call from concurrent host threads.
+cudaError_t raise_smem_limit(const void* fn, size_t bytes);
+
 // Solve modes of launch_solve.
 enum SolveMode { kSolveAIC = 0, kSolveCV = 1, kSolveFit = 2, kSolveRefine = 3 };
 
@@ -31,6 +35,17 @@ size_t select_smem_bytes();
 // Fills hist_cache with every row's whole-row proxy histogram (the cache a
 // first select pass would store); the selects after it run with cache_valid.
 cudaError_t launch_select_hist(const SelectArgs& a, bool geographic, int num_sms, cudaStream_t stream);
+// Batched forms over many datasets and ranks in one launch each (device
+// arrays of per-segment arguments; segment s owns the flattened items
+// [start[s], start[s + 1])): whole-row histograms (items are groups of 8
+// rows), selects (items are rows) and the FP32 copy of the thresholds.
+cudaError_t launch_select_hist_batch(const SelectArgs* segs, const long long* start, int nseg, bool geographic,
+                                     int num_sms, cudaStream_t stream);
+cudaError_t launch_select_batch(const SelectArgs* segs, const long long* start, int nseg, bool geographic, bool exact,
+                                int num_sms, cudaStream_t stream);
+cudaError_t launch_to_float_batch(const double* const* in, float* const* out, const long long* start, int nseg,
+                                  int num_sms, cudaStream_t stream);
+constexpr int kSelHistRows = 8;  // rows per histogram item
 
 // thr = fixbw of BandwidthWeight.cpp:40-53 from order statistics d0 (rank
 // floor(bw), or the row maximum when bw >= n) and d1 (rank floor(bw)+1, may
@@ -81,6 +96,13 @@ struct SolveArgs {
     const double* rvec;
 };
 cudaError_t launch_solve(const SolveArgs& a, int* nblocks, cudaStream_t stream);
+// Criterion solves (kSolveAIC / kSolveCV) of many segments in one launch:
+// block b solves rows [work[b].y, work[b].z) of segment work[b].x and writes
+// partial slot work[b].w of that segment (device arrays; p <= max_p).
+cudaError_t launch_solve_batch(const SolveArgs* segs, const int4* work, int nwork, int mode, int max_p,
+                               cudaStream_t stream);
+// out[4 s .. 4 s + 3] = fixed-order sums of partial blocks [first[s], first[s + 1]).
+cudaError_t launch_reduce_batch(const double* partials, const int* first, int nseg, double* out, cudaStream_t stream);
 
 // Sums nblocks x 4 partials into out[4] in a fixed order.
 cudaError_t launch_reduce_partials(const double* partials, int nblocks, double* out, cudaStream_t stream);
@@ -143,6 +165,11 @@ enum TcProf {
 };
 size_t contract_tc_smem_bytes(int npad, int ntiles, int nb);
 cudaError_t launch_contract_tc(const TcArgs& a, bool geographic, cudaStream_t stream);
+// Many contractions in one launch: CTA b computes row block work[b].y of
+// segment work[b].x (device arrays; every segment's npad <= max_npad and
+// ntiles <= max_ntiles; flush_tiles and the weight kernel are shared).
+cudaError_t launch_contract_tc_batch(const TcArgs* segs, const int2* work, int nwork, int max_npad, int max_ntiles,
+                                     int flush_tiles, bool geographic, int kernel, cudaStream_t stream);
 cudaError_t launch_build_zimg(int n, int mcols, int npad, const double* Z, int ldz, unsigned char* img,
                               cudaStream_t stream);
 // D[128 x N] = A[128 x 32] B[N x 32]^T through tcgen05 (device pointers).

@@ -101,9 +101,13 @@ __device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity)
 // tiles accumulates in TMEM accumulator c % 2, which the producers drain into
 // the double-float sums one tile after the chunk's last MMA was issued.
 // KERN: the weight kernel when fixed at compile time, -1 to read it from the arguments.
-template <bool GEO, int KERN>
-__global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a, int nb)
+// BATCH: CTA b works on segment work[b].x (arguments segs[work[b].x]) at row
+// block work[b].y, so one launch covers many datasets and bandwidths.
+template <bool GEO, int KERN, bool BATCH>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_contract_tc(TcArgs a0, int nb, const TcArgs* __restrict__ segs, const int2* __restrict__ work)
 {
+    const TcArgs a = BATCH ? segs[work[blockIdx.x].x] : a0;
     const int kernel = KERN >= 0 ? KERN : a.kernel;
     extern __shared__ unsigned char smem_dyn[];
     __shared__ Smem ctl;
@@ -122,7 +126,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_contract_tc(TcArgs a, int nb)
     const long long kstart = (a.prof && t == 0) ? clock64() : 0;
     const bool producer = warp < TC_PROD_WARPS;
     const int r = t & (TC_M - 1), quarter = (t >> 7) & 3;
-    const int row0 = blockIdx.x * TC_M;
+    const int row0 = BATCH ? work[blockIdx.x].y : blockIdx.x * TC_M;
     const int i = row0 + r;
     const bool row_ok = producer && i < a.n;
 
@@ -543,17 +547,41 @@ cudaError_t launch_contract_tc(const TcArgs& a, bool geographic, cudaStream_t st
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
     const int grid = (a.n + TC_M - 1) / TC_M;
     auto go = [&](auto kfn) {
-        cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        kfn<<<grid, TC_THREADS, smem, stream>>>(a, nb);
+        raise_smem_limit((const void*)kfn, smem);
+        kfn<<<grid, TC_THREADS, smem, stream>>>(a, nb, nullptr, nullptr);
     };
     if (geographic) {
-        if (a.kernel == GW_KERNEL_BISQUARE) go(k_contract_tc<true, GW_KERNEL_BISQUARE>);
-        else if (a.kernel == GW_KERNEL_GAUSSIAN) go(k_contract_tc<true, GW_KERNEL_GAUSSIAN>);
-        else go(k_contract_tc<true, -1>);
+        if (a.kernel == GW_KERNEL_BISQUARE) go(k_contract_tc<true, GW_KERNEL_BISQUARE, false>);
+        else if (a.kernel == GW_KERNEL_GAUSSIAN) go(k_contract_tc<true, GW_KERNEL_GAUSSIAN, false>);
+        else go(k_contract_tc<true, -1, false>);
     } else {
-        if (a.kernel == GW_KERNEL_BISQUARE) go(k_contract_tc<false, GW_KERNEL_BISQUARE>);
-        else if (a.kernel == GW_KERNEL_GAUSSIAN) go(k_contract_tc<false, GW_KERNEL_GAUSSIAN>);
-        else go(k_contract_tc<false, -1>);
+        if (a.kernel == GW_KERNEL_BISQUARE) go(k_contract_tc<false, GW_KERNEL_BISQUARE, false>);
+        else if (a.kernel == GW_KERNEL_GAUSSIAN) go(k_contract_tc<false, GW_KERNEL_GAUSSIAN, false>);
+        else go(k_contract_tc<false, -1, false>);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_contract_tc_batch(const TcArgs* segs, const int2* work, int nwork, int max_npad, int max_ntiles,
+                                     int flush_tiles, bool geographic, int kernel, cudaStream_t stream)
+{
+    if (max_npad % 64 != 0 || max_npad < 64 || max_npad > 256 || flush_tiles < 2 || nwork < 1)
+        return cudaErrorInvalidValue;
+    int nb = TC_MAX_NB;
+    while (nb > 2 && contract_tc_smem_bytes(max_npad, max_ntiles, nb) > 227 * 1024) nb--;
+    const size_t smem = contract_tc_smem_bytes(max_npad, max_ntiles, nb);
+    if (smem > 227 * 1024) return cudaErrorInvalidValue;
+    TcArgs none{};
+    auto go = [&](auto kfn) {
+        raise_smem_limit((const void*)kfn, smem);
+        kfn<<<nwork, TC_THREADS, smem, stream>>>(none, nb, segs, work);
+    };
+    if (geographic) {
+        if (kernel == GW_KERNEL_BISQUARE) go(k_contract_tc<true, GW_KERNEL_BISQUARE, true>);
+        else go(k_contract_tc<true, -1, true>);
+    } else {
+        if (kernel == GW_KERNEL_BISQUARE) go(k_contract_tc<false, GW_KERNEL_BISQUARE, true>);
+        else go(k_contract_tc<false, -1, true>);
     }
     return cudaGetLastError();
 }
@@ -570,7 +598,7 @@ cudaError_t launch_tc_selftest(const float* A, const float* B, float* D, int N, 
 {
     if (N % 16 != 0 || N < 16 || N > 256) return cudaErrorInvalidValue;
     const size_t smem = 1024 + TC_A_BYTES + (size_t)N * 128;
-    cudaFuncSetAttribute(k_tc_selftest, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    raise_smem_limit((const void*)k_tc_selftest, smem);
     k_tc_selftest<<<1, 128, smem, stream>>>(A, B, D, N, err);
     return cudaGetLastError();
 }

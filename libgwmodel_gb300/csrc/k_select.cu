@@ -315,72 +315,116 @@ __device__ bool select_row(SelShared& sh, const SelectArgs& a, const RowCtx& c, 
     return false;
 }
 
+// The adaptive threshold of one row (stage A on the proxies from the cached
+// histogram when there is one, stage B on the reference's FP64 values).
+template <bool GEO, bool EXACT>
+__device__ void select_one(SelShared& sh, const SelectArgs& a, int row, const Window& wlog)
+{
+    const int t = threadIdx.x;
+    const DevPoints P = a.P;
+    const double INF = __longlong_as_double(0x7ff0000000000000ll);
+    RowCtx c;
+    c.fu = P.u[row];
+    c.fv = P.v[row];
+    c.fuR = GEO ? P.uR[row] : 0.0;
+    c.fvR = GEO ? P.vR[row] : 0.0;
+    if (GEO) {
+        c.fa = a.pts[2 * (size_t)row];
+        c.fb = a.pts[2 * (size_t)row + 1];
+        c.qx = c.fa.x + c.fb.x;
+        c.qy = c.fa.y + c.fb.y;
+        c.qz = c.fa.z + c.fb.z;
+    } else {
+        c.fa = a.pts[row];
+        c.fb = c.fa;
+        c.qx = c.fa.x + c.fa.y;
+        c.qy = c.fa.z + c.fa.w;
+        c.qz = 0.0f;
+    }
+    unsigned* cache_row = a.hist_cache ? a.hist_cache + (size_t)row * SEL_BINS : nullptr;
+    // stage A: the rank's FP32 proxy value
+    double T_lo = 0.0, T_hi = INF;
+    Window w = wlog;
+    bool ok = true;
+    if (cache_row && a.cache_valid) {
+        for (int b = t; b < SEL_BINS; b += SEL_THREADS) sh.hist[b] = cache_row[b];
+        __syncthreads();
+        scan_pick(sh, a.rank);
+        uint64_t lo, hi;
+        bin_range(wlog, sh.chosen_bin, lo, hi);
+        ok = sh.count > 0;
+        __syncthreads();
+        T_lo = keyd(lo);
+        T_hi = keyd(hi);
+        w = linear_window(lo, hi);
+        cache_row = nullptr;
+    }
+    double q = __longlong_as_double(0x7ff8000000000000ll);
+    if (ok) ok = select_row<GEO, false>(sh, a, c, T_lo, T_hi, w, a.cache_valid ? nullptr : cache_row, q);
+    double result = q;
+    // stage B: the reference's FP64 value, inside the proxy band around q
+    if (EXACT && ok) {
+        const double lo = q * (1.0 - a.eps) - a.delta, hi = q * (1.0 + a.eps) + a.delta;
+        const double blo = lo > 0.0 ? lo : 0.0;
+        ok = select_row<GEO, true>(sh, a, c, blo, hi, linear_window(dkey(blo), dkey(hi)), nullptr, result);
+    }
+    if (t == 0) {
+        if (!ok) {
+            atomicMax(a.err, 2);
+            result = __longlong_as_double(0x7ff8000000000000ll);
+        }
+        a.out[row] = result;
+    }
+    __syncthreads();
+}
+
 template <bool GEO, bool EXACT>
 __global__ void __launch_bounds__(SEL_THREADS) k_select(SelectArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SelShared& sh = *reinterpret_cast<SelShared*>(smem_raw);
-    const int t = threadIdx.x;
-    const DevPoints P = a.P;
-    const int n = a.n;
-    const double INF = __longlong_as_double(0x7ff0000000000000ll);
     // coarse logarithmic window of the first pass over a whole row
     const Window wlog = coarse_window(a);
+    for (int row = blockIdx.x; row < a.n; row += gridDim.x) select_one<GEO, EXACT>(sh, a, row, wlog);
+}
 
-    for (int row = blockIdx.x; row < n; row += gridDim.x) {
-        RowCtx c;
-        c.fu = P.u[row];
-        c.fv = P.v[row];
-        c.fuR = GEO ? P.uR[row] : 0.0;
-        c.fvR = GEO ? P.vR[row] : 0.0;
-        if (GEO) {
-            c.fa = a.pts[2 * (size_t)row];
-            c.fb = a.pts[2 * (size_t)row + 1];
-            c.qx = c.fa.x + c.fb.x;
-            c.qy = c.fa.y + c.fb.y;
-            c.qz = c.fa.z + c.fb.z;
-        } else {
-            c.fa = a.pts[row];
-            c.fb = c.fa;
-            c.qx = c.fa.x + c.fa.y;
-            c.qy = c.fa.z + c.fa.w;
-            c.qz = 0.0f;
-        }
-        unsigned* cache_row = a.hist_cache ? a.hist_cache + (size_t)row * SEL_BINS : nullptr;
-        // stage A: the rank's FP32 proxy value
-        double T_lo = 0.0, T_hi = INF;
-        Window w = wlog;
-        bool ok = true;
-        if (cache_row && a.cache_valid) {
-            for (int b = t; b < SEL_BINS; b += SEL_THREADS) sh.hist[b] = cache_row[b];
-            __syncthreads();
-            scan_pick(sh, a.rank);
-            uint64_t lo, hi;
-            bin_range(wlog, sh.chosen_bin, lo, hi);
-            ok = sh.count > 0;
-            __syncthreads();
-            T_lo = keyd(lo);
-            T_hi = keyd(hi);
-            w = linear_window(lo, hi);
-            cache_row = nullptr;
-        }
-        double q = __longlong_as_double(0x7ff8000000000000ll);
-        if (ok) ok = select_row<GEO, false>(sh, a, c, T_lo, T_hi, w, a.cache_valid ? nullptr : cache_row, q);
-        double result = q;
-        // stage B: the reference's FP64 value, inside the proxy band around q
-        if (EXACT && ok) {
-            const double lo = q * (1.0 - a.eps) - a.delta, hi = q * (1.0 + a.eps) + a.delta;
-            const double blo = lo > 0.0 ? lo : 0.0;
-            ok = select_row<GEO, true>(sh, a, c, blo, hi, linear_window(dkey(blo), dkey(hi)), nullptr, result);
-        }
-        if (t == 0) {
-            if (!ok) {
-                atomicMax(a.err, 2);
-                result = __longlong_as_double(0x7ff8000000000000ll);
-            }
-            a.out[row] = result;
-        }
+// Index of the segment holding flattened item `item`: the last seg with start[seg] <= item.
+__device__ __forceinline__ int find_segment(const long long* __restrict__ start, int nseg, long long item)
+{
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= item) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Many selects in one launch: segment s (its own dataset and rank) owns the
+// flattened rows [start[s], start[s + 1]).
+template <bool GEO, bool EXACT>
+__global__ void __launch_bounds__(SEL_THREADS)
+    k_select_batch(const SelectArgs* __restrict__ segs, const long long* __restrict__ start, int nseg)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SelShared& sh = *reinterpret_cast<SelShared*>(smem_raw);
+    __shared__ SelectArgs sa;
+    __shared__ int cur;
+    if (threadIdx.x == 0) cur = -1;
+    const long long total = start[nseg];
+    __syncthreads();
+    for (long long item = blockIdx.x; item < total; item += gridDim.x) {
+        const int seg = find_segment(start, nseg, item);
+        const bool change = seg != cur;  // uniform: cur is stable since the last barrier
         __syncthreads();
+        if (change) {
+            if (threadIdx.x == 0) {
+                sa = segs[seg];
+                cur = seg;
+            }
+            __syncthreads();
+        }
+        select_one<GEO, EXACT>(sh, sa, (int)(item - start[seg]), coarse_window(sa));
     }
 }
 
@@ -393,48 +437,94 @@ __global__ void __launch_bounds__(SEL_THREADS) k_select(SelectArgs a)
 constexpr int HS_ROWS = 8;
 constexpr int HS_THREADS = 512;
 
+// Histograms of rows [row0, row0 + HS_ROWS) of one dataset into its cache.
 template <bool GEO>
-__global__ void __launch_bounds__(HS_THREADS, 1) k_select_hist(SelectArgs a)
+__device__ void hist_rows(unsigned* hs, float4 (*rf)[2], const SelectArgs& a, int row0)
 {
-    extern __shared__ __align__(16) unsigned hs[];  // HS_ROWS x SEL_BINS
-    __shared__ float4 rf[HS_ROWS][2];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const int n = a.n;
     const Window wlog = coarse_window(a);
     constexpr int NF = GEO ? 2 : 1;
     const int ngroups = (a.ntiles + 31) / 32;
-    for (int row0 = blockIdx.x * HS_ROWS; row0 < n; row0 += gridDim.x * HS_ROWS) {
-        const int nrows = min(HS_ROWS, n - row0);
-        for (int b = t; b < HS_ROWS * SEL_BINS; b += HS_THREADS) hs[b] = 0;
-        if (t < HS_ROWS * NF) {
-            const int r = t / NF, q = t % NF;
-            rf[r][q] = r < nrows ? a.pts[NF * (size_t)(row0 + r) + q] : make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-        __syncthreads();
-        float4 ra[HS_ROWS], rb[HS_ROWS];
+    const int nrows = min(HS_ROWS, n - row0);
+    for (int b = t; b < HS_ROWS * SEL_BINS; b += HS_THREADS) hs[b] = 0;
+    if (t < HS_ROWS * NF) {
+        const int r = t / NF, q = t % NF;
+        rf[r][q] = r < nrows ? a.pts[NF * (size_t)(row0 + r) + q] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    float4 ra[HS_ROWS], rb[HS_ROWS];
 #pragma unroll
-        for (int r = 0; r < HS_ROWS; r++) {
-            ra[r] = rf[r][0];
-            rb[r] = GEO ? rf[r][1] : ra[r];
-        }
-        for (int g = warp; g < ngroups; g += HS_THREADS / 32) {
-            const int tile = g * 32 + lane;
-            for (int q = 0; q < SEL_TILE; q++) {
-                const int j = tile * SEL_TILE + q;
-                if (tile >= a.ntiles || j >= n) continue;
-                const float4 pa = a.pts[NF * (size_t)j];
-                const float4 pb = GEO ? a.pts[2 * (size_t)j + 1] : pa;
+    for (int r = 0; r < HS_ROWS; r++) {
+        ra[r] = rf[r][0];
+        rb[r] = GEO ? rf[r][1] : ra[r];
+    }
+    for (int g = warp; g < ngroups; g += HS_THREADS / 32) {
+        const int tile = g * 32 + lane;
+        for (int q = 0; q < SEL_TILE; q++) {
+            const int j = tile * SEL_TILE + q;
+            if (tile >= a.ntiles || j >= n) continue;
+            const float4 pa = a.pts[NF * (size_t)j];
+            const float4 pb = GEO ? a.pts[2 * (size_t)j + 1] : pa;
 #pragma unroll
-                for (int r = 0; r < HS_ROWS; r++) {
-                    if (r >= nrows) break;
-                    const float d32 = GEO ? geo_dist32(ra[r], rb[r], pa, pb) : sqrtf(planar_d2_32(ra[r], pa));
-                    if (d32 == d32) atomicAdd(&hs[r * SEL_BINS + bucket_of(wlog, dkey_f(d32))], 1u);
-                }
+            for (int r = 0; r < HS_ROWS; r++) {
+                if (r >= nrows) break;
+                const float d32 = GEO ? geo_dist32(ra[r], rb[r], pa, pb) : sqrtf(planar_d2_32(ra[r], pa));
+                if (d32 == d32) atomicAdd(&hs[r * SEL_BINS + bucket_of(wlog, dkey_f(d32))], 1u);
             }
         }
+    }
+    __syncthreads();
+    for (int e = t; e < nrows * SEL_BINS; e += HS_THREADS) a.hist_cache[(size_t)row0 * SEL_BINS + e] = hs[e];
+    __syncthreads();
+}
+
+template <bool GEO>
+__global__ void __launch_bounds__(HS_THREADS, 1) k_select_hist(SelectArgs a)
+{
+    extern __shared__ __align__(16) unsigned hs[];  // HS_ROWS x SEL_BINS
+    __shared__ float4 rf[HS_ROWS][2];
+    for (int row0 = blockIdx.x * HS_ROWS; row0 < a.n; row0 += gridDim.x * HS_ROWS) hist_rows<GEO>(hs, rf, a, row0);
+}
+
+// Histogram caches of many datasets in one launch: segment s owns the row
+// groups [start[s], start[s + 1]) of HS_ROWS rows each.
+template <bool GEO>
+__global__ void __launch_bounds__(HS_THREADS, 1)
+    k_select_hist_batch(const SelectArgs* __restrict__ segs, const long long* __restrict__ start, int nseg)
+{
+    extern __shared__ __align__(16) unsigned hs[];
+    __shared__ float4 rf[HS_ROWS][2];
+    __shared__ SelectArgs sa;
+    __shared__ int cur;
+    if (threadIdx.x == 0) cur = -1;
+    __syncthreads();
+    const long long total = start[nseg];
+    for (long long item = blockIdx.x; item < total; item += gridDim.x) {
+        const int seg = find_segment(start, nseg, item);
+        const bool change = seg != cur;
         __syncthreads();
-        for (int e = t; e < nrows * SEL_BINS; e += HS_THREADS) a.hist_cache[(size_t)row0 * SEL_BINS + e] = hs[e];
-        __syncthreads();
+        if (change) {
+            if (threadIdx.x == 0) {
+                sa = segs[seg];
+                cur = seg;
+            }
+            __syncthreads();
+        }
+        hist_rows<GEO>(hs, rf, sa, (int)(item - start[seg]) * HS_ROWS);
+    }
+}
+
+// thr[i] = (float)v[i] over the flattened rows of many segments.
+__global__ void k_to_float_batch(const double* const* __restrict__ in, float* const* __restrict__ out,
+                                 const long long* __restrict__ start, int nseg)
+{
+    const long long total = start[nseg];
+    for (long long item = blockIdx.x * (long long)blockDim.x + threadIdx.x; item < total;
+         item += (long long)gridDim.x * blockDim.x) {
+        const int seg = find_segment(start, nseg, item);
+        const long long i = item - start[seg];
+        out[seg][i] = (float)in[seg][i];
     }
 }
 
@@ -479,7 +569,7 @@ cudaError_t launch_select(const SelectArgs& a, bool geographic, bool exact, int 
     const size_t smem = sizeof(SelShared);
 #define GW_SEL(G, E)                                                                                  \
     do {                                                                                              \
-        cudaFuncSetAttribute(k_select<G, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        raise_smem_limit((const void*)k_select<G, E>, smem); \
         k_select<G, E><<<grid, SEL_THREADS, smem, stream>>>(a);                                       \
     } while (0)
     if (geographic) {
@@ -500,12 +590,54 @@ cudaError_t launch_select_hist(const SelectArgs& a, bool geographic, int num_sms
     int grid = (a.n + HS_ROWS - 1) / HS_ROWS;
     if (grid > num_sms) grid = num_sms;
     if (geographic) {
-        cudaFuncSetAttribute(k_select_hist<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        raise_smem_limit((const void*)k_select_hist<true>, smem);
         k_select_hist<true><<<grid, HS_THREADS, smem, stream>>>(a);
     } else {
-        cudaFuncSetAttribute(k_select_hist<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        raise_smem_limit((const void*)k_select_hist<false>, smem);
         k_select_hist<false><<<grid, HS_THREADS, smem, stream>>>(a);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_select_hist_batch(const SelectArgs* segs, const long long* start, int nseg, bool geographic,
+                                     int num_sms, cudaStream_t stream)
+{
+    const size_t smem = (size_t)HS_ROWS * SEL_BINS * sizeof(unsigned);
+    if (geographic) {
+        raise_smem_limit((const void*)k_select_hist_batch<true>, smem);
+        k_select_hist_batch<true><<<num_sms, HS_THREADS, smem, stream>>>(segs, start, nseg);
+    } else {
+        raise_smem_limit((const void*)k_select_hist_batch<false>, smem);
+        k_select_hist_batch<false><<<num_sms, HS_THREADS, smem, stream>>>(segs, start, nseg);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_select_batch(const SelectArgs* segs, const long long* start, int nseg, bool geographic, bool exact,
+                                int num_sms, cudaStream_t stream)
+{
+    const int grid = num_sms * 12;
+    const size_t smem = sizeof(SelShared);
+#define GW_SELB(G, E)                                                                                       \
+    do {                                                                                                    \
+        raise_smem_limit((const void*)k_select_batch<G, E>, smem); \
+        k_select_batch<G, E><<<grid, SEL_THREADS, smem, stream>>>(segs, start, nseg);                       \
+    } while (0)
+    if (geographic) {
+        if (exact) GW_SELB(true, true);
+        else GW_SELB(true, false);
+    } else {
+        if (exact) GW_SELB(false, true);
+        else GW_SELB(false, false);
+    }
+#undef GW_SELB
+    return cudaGetLastError();
+}
+
+cudaError_t launch_to_float_batch(const double* const* in, float* const* out, const long long* start, int nseg,
+                                  int num_sms, cudaStream_t stream)
+{
+    k_to_float_batch<<<num_sms * 4, 256, 0, stream>>>(in, out, start, nseg);
     return cudaGetLastError();
 }
 

@@ -74,9 +74,15 @@ __device__ __forceinline__ double bwd_solve(const double* L, int ld, int p, int 
     return v;
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(SV_WARPS * 32) k_solve(SolveArgs a)
+// BATCH: block b solves rows [work[b].y, work[b].z) of segment work[b].x
+// (arguments segs[work[b].x]) and writes its partial sums to slot work[b].w
+// of that segment's partials; otherwise the blocks stride over all rows.
+template <int MODE, bool BATCH>
+__global__ void __launch_bounds__(SV_WARPS * 32)
+    k_solve(SolveArgs a0, const SolveArgs* __restrict__ segs, const int4* __restrict__ work)
 {
+    const int4 wk = BATCH ? work[blockIdx.x] : make_int4(0, 0, 0, 0);
+    const SolveArgs a = BATCH ? segs[wk.x] : a0;
     extern __shared__ double smem[];
     const int p = a.p, ld = p + 1, mm = p * (p + 1) / 2;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -90,7 +96,10 @@ __global__ void __launch_bounds__(SV_WARPS * 32) k_solve(SolveArgs a)
     __shared__ double part[SV_WARPS][4];
 
     double acc_s = 0.0, acc_r = 0.0, acc_t = 0.0, acc_f = 0.0;
-    for (int row = blockIdx.x * SV_WARPS + warp; row < a.n; row += gridDim.x * SV_WARPS) {
+    const int row_first = BATCH ? wk.y + warp : blockIdx.x * SV_WARPS + warp;
+    const int row_end = BATCH ? wk.z : a.n;
+    const int row_step = BATCH ? SV_WARPS : gridDim.x * SV_WARPS;
+    for (int row = row_first; row < row_end; row += row_step) {
         const double* g = a.G + (size_t)row * a.ldg;
         if (lane < p)
             for (int c = 0; c <= lane; c++) L[lane * ld + c] = g[packed_index(c, lane, p)];
@@ -203,7 +212,7 @@ __global__ void __launch_bounds__(SV_WARPS * 32) k_solve(SolveArgs a)
     if (threadIdx.x < 4) {
         double s = 0.0;
         for (int w = 0; w < SV_WARPS; w++) s += part[w][threadIdx.x];
-        a.partials[blockIdx.x * 4 + threadIdx.x] = s;
+        a.partials[(BATCH ? wk.w : blockIdx.x) * 4 + threadIdx.x] = s;
     }
 }
 
@@ -479,22 +488,62 @@ cudaError_t launch_solve(const SolveArgs& a, int* nblocks, cudaStream_t stream)
     *nblocks = grid;
     switch (a.mode) {
     case kSolveAIC:
-        cudaFuncSetAttribute(k_solve<kSolveAIC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_solve<kSolveAIC><<<grid, SV_WARPS * 32, smem, stream>>>(a);
+        raise_smem_limit((const void*)k_solve<kSolveAIC, false>, smem);
+        k_solve<kSolveAIC, false><<<grid, SV_WARPS * 32, smem, stream>>>(a, nullptr, nullptr);
         break;
     case kSolveCV:
-        cudaFuncSetAttribute(k_solve<kSolveCV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_solve<kSolveCV><<<grid, SV_WARPS * 32, smem, stream>>>(a);
+        raise_smem_limit((const void*)k_solve<kSolveCV, false>, smem);
+        k_solve<kSolveCV, false><<<grid, SV_WARPS * 32, smem, stream>>>(a, nullptr, nullptr);
         break;
     case kSolveRefine:
-        cudaFuncSetAttribute(k_solve<kSolveRefine>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_solve<kSolveRefine><<<grid, SV_WARPS * 32, smem, stream>>>(a);
+        raise_smem_limit((const void*)k_solve<kSolveRefine, false>, smem);
+        k_solve<kSolveRefine, false><<<grid, SV_WARPS * 32, smem, stream>>>(a, nullptr, nullptr);
         break;
     default:
-        cudaFuncSetAttribute(k_solve<kSolveFit>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_solve<kSolveFit><<<grid, SV_WARPS * 32, smem, stream>>>(a);
+        raise_smem_limit((const void*)k_solve<kSolveFit, false>, smem);
+        k_solve<kSolveFit, false><<<grid, SV_WARPS * 32, smem, stream>>>(a, nullptr, nullptr);
         break;
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_solve_batch(const SolveArgs* segs, const int4* work, int nwork, int mode, int max_p,
+                               cudaStream_t stream)
+{
+    if (max_p < 1 || max_p > kMaxP || nwork < 1 || (mode != kSolveAIC && mode != kSolveCV)) return cudaErrorInvalidValue;
+    const size_t smem = (size_t)(max_p * (max_p + 1) + max_p) * SV_WARPS * sizeof(double);
+    if (mode == kSolveAIC) {
+        raise_smem_limit((const void*)k_solve<kSolveAIC, true>, smem);
+        k_solve<kSolveAIC, true><<<nwork, SV_WARPS * 32, smem, stream>>>(SolveArgs{}, segs, work);
+    } else {
+        raise_smem_limit((const void*)k_solve<kSolveCV, true>, smem);
+        k_solve<kSolveCV, true><<<nwork, SV_WARPS * 32, smem, stream>>>(SolveArgs{}, segs, work);
+    }
+    return cudaGetLastError();
+}
+
+// out[4 s + q] = sum of partials[4 b + q] over blocks b in [first[s], first[s + 1]), in order.
+__global__ void k_reduce_batch(const double* __restrict__ partials, const int* __restrict__ first,
+                               double* __restrict__ out)
+{
+    const int s = blockIdx.x;
+    __shared__ double sh[256][4];
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int b = first[s] + (int)threadIdx.x; b < first[s + 1]; b += 256)
+        for (int q = 0; q < 4; q++) acc[q] += partials[b * 4 + q];
+    for (int q = 0; q < 4; q++) sh[threadIdx.x][q] = acc[q];
+    __syncthreads();
+    for (int stride = 128; stride > 0; stride >>= 1) {
+        if (threadIdx.x < stride)
+            for (int q = 0; q < 4; q++) sh[threadIdx.x][q] += sh[threadIdx.x + stride][q];
+        __syncthreads();
+    }
+    if (threadIdx.x < 4) out[4 * s + threadIdx.x] = sh[0][threadIdx.x];
+}
+
+cudaError_t launch_reduce_batch(const double* partials, const int* first, int nseg, double* out, cudaStream_t stream)
+{
+    k_reduce_batch<<<nseg, 256, 0, stream>>>(partials, first, out);
     return cudaGetLastError();
 }
 
