@@ -83,8 +83,10 @@ __device__ __forceinline__ Window coarse_window(const SelectArgs& a)
     const uint64_t khi = (uint64_t)__double_as_longlong(a.dhi) | 0x8000000000000000ull;
     const uint64_t kspan = khi > klo ? khi - klo : 1;
     const int kbits = 64 - __clzll((long long)kspan);
-    return Window{klo, kbits > SEL_LOG_BINS ? kbits - SEL_LOG_BINS : 0, dkey(0.0),
-                  dkey(__longlong_as_double(0x7ff0000000000000ll))};
+    const int shift = kbits > SEL_LOG_BINS ? kbits - SEL_LOG_BINS : 0;
+    // base aligned to a bin boundary, so a bin is a plain shift of the key
+    const uint64_t base = klo & ~((1ull << shift) - 1ull);
+    return Window{base, shift, dkey(0.0), dkey(__longlong_as_double(0x7ff0000000000000ll))};
 }
 
 // Finds the bin where the cumulative count reaches krem (1-based).
@@ -196,17 +198,20 @@ __device__ bool select_row(SelShared& sh, const SelectArgs& a, const RowCtx& c, 
     const int n = a.n;
     const double INF = __longlong_as_double(0x7ff0000000000000ll);
     for (int pass = 0; pass < SEL_MAX_PASSES; pass++) {
+        // chord (geographic) or squared-distance (planar) bounds of the window
+        // in FP32 with a 1e-5 margin (no FP64 in the per-row work)
         float below_thr, above_thr;
+        const float tlo = (float)T_lo, thi = (float)T_hi;
         if (GEO) {
-            const double a2 = 2.0 * 6378.137;
-            const double f = 1.0 / 298.257223563;
-            const double wl = T_lo / (a2 * (1.0 + f));
-            below_thr = wl <= 0.0 ? -1.0f : (wl >= 1.5 ? 1e30f : (float)(2.0 * sin(wl) * (1.0 - 1e-6)));
-            const double wh = T_hi / (a2 * (1.0 - 2.6 * f));
-            above_thr = (wh >= 1.2) ? 1e30f : (float)(2.0 * sin(wh) * (1.0 + 1e-6));
+            const float a2 = 2.0f * 6378.137f;
+            const float f = 1.0f / 298.257223563f;
+            const float wl = tlo / (a2 * (1.0f + f));
+            below_thr = !(wl > 0.0f) ? -1.0f : (wl >= 1.5f ? 1e30f : 2.0f * sinf(wl) * (1.0f - 1e-5f));
+            const float wh = thi / (a2 * (1.0f - 2.6f * f));
+            above_thr = !(wh < 1.2f) ? 1e30f : 2.0f * sinf(wh) * (1.0f + 1e-5f);
         } else {
-            below_thr = T_lo > 0.0 ? (float)(T_lo * T_lo * (1.0 - 1e-6)) : -1.0f;
-            above_thr = isinf(T_hi) ? 3e38f : (float)(T_hi * T_hi * (1.0 + 1e-6));
+            below_thr = tlo > 0.0f ? tlo * tlo * (1.0f - 1e-5f) : -1.0f;
+            above_thr = !(thi < 1.8e19f) ? 3e38f : thi * thi * (1.0f + 1e-5f);
         }
         const uint64_t klo = dkey(T_lo), khi = dkey(T_hi);
         for (int b = t; b < SEL_BINS; b += SEL_THREADS) sh.hist[b] = 0;
@@ -447,6 +452,14 @@ __device__ void hist_rows(unsigned* hs, float4 (*rf)[2], const SelectArgs& a, in
     constexpr int NF = GEO ? 2 : 1;
     const int ngroups = (a.ntiles + 31) / 32;
     const int nrows = min(HS_ROWS, n - row0);
+    // bucket_of(wlog, dkey_f(d)) for a normal float d in 32/64-bit integer steps:
+    // with the aligned base and 29 <= shift <= 52 it is
+    // (bits(d) >> (shift - 29)) + (896 << 23 >> (shift - 29)) + (2^63 >> shift) - (base >> shift)
+    const bool fastbin = wlog.shift >= 29 && wlog.shift <= 52;
+    const int s2 = fastbin ? wlog.shift - 29 : 0;
+    const long long kbin = fastbin ? (long long)((896ull << 23) >> s2) + (long long)((1ull << 63) >> wlog.shift) -
+                                         (long long)(wlog.base >> wlog.shift)
+                                   : 0;
     for (int b = t; b < HS_ROWS * SEL_BINS; b += HS_THREADS) hs[b] = 0;
     if (t < HS_ROWS * NF) {
         const int r = t / NF, q = t % NF;
@@ -470,7 +483,17 @@ __device__ void hist_rows(unsigned* hs, float4 (*rf)[2], const SelectArgs& a, in
             for (int r = 0; r < HS_ROWS; r++) {
                 if (r >= nrows) break;
                 const float d32 = GEO ? geo_dist32(ra[r], rb[r], pa, pb) : sqrtf(planar_d2_32(ra[r], pa));
-                if (d32 == d32) atomicAdd(&hs[r * SEL_BINS + bucket_of(wlog, dkey_f(d32))], 1u);
+                if (d32 == d32) {
+                    const uint32_t fb = __float_as_uint(d32);
+                    unsigned bin;
+                    if (fastbin) {
+                        const long long q = (long long)(fb >> s2) + kbin;
+                        bin = fb < 0x00800000u ? 0u : (unsigned)min(max(q, 0ll), (long long)(SEL_BINS - 1));
+                    } else {
+                        bin = bucket_of(wlog, dkey_f(d32));
+                    }
+                    atomicAdd(&hs[r * SEL_BINS + bin], 1u);
+                }
             }
         }
     }
