@@ -155,6 +155,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const float inv_r2 = 1.0f / (rr * rr);
     // pairs with a haversine term in [s_cut, 0.86] have weight 0 under a compact kernel
     const float s_cut = (GEO && kernel >= GW_KERNEL_BISQUARE) ? geo_s_cut(rr) : __int_as_float(0x7f800000);
+    const float fz = fa.z + fb.z;  // sin(lat) of the focus
+    const int self_j = a.exclude_self ? i : -1;
+    const bool square = a.wpow == 2;
 
     // block bound and largest threshold for tile skipping
     float rmax = row_ok ? rr : 0.0f;
@@ -276,20 +279,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     const int kk = kbase + q4 * 4 + e;
                     in[e] = row_ok && tile * TC_BK + kk < a.n;
                     if (GEO) {
-                        g[e] = geo_chord32(fa, fb, tp[2 * kk], tp[2 * kk + 1]);
+                        g[e] = geo_chord32(fa, fb, fz, tp[2 * kk], tp[2 * kk + 1]);
                         in[e] = in[e] && !geo_beyond(g[e].S, s_cut);
                     }
                     w[e] = 0.0f;
                 }
                 // the group is skipped only when every lane's four pairs are out
                 if (__any_sync(0xffffffffu, in[0] || in[1] || in[2] || in[3])) {
+                    // every pair of the warp within 60 degrees: no far-angle branch
+                    const bool near = !GEO || __all_sync(0xffffffffu, fmaxf(fmaxf(g[0].S, g[1].S),
+                                                                          fmaxf(g[2].S, g[3].S)) <= 0.25f);
 #pragma unroll
                     for (int e = 0; e < 4; e++) {
                         const int kk = kbase + q4 * 4 + e;
-                        const float d2 = GEO ? geo_d2_from_chord(g[e]) : planar_d2_32(fa, tp[kk]);
+                        float d2;
+                        if (GEO) d2 = near ? geo_d2_near(g[e]) : geo_d2_from_chord(g[e]);
+                        else d2 = planar_d2_32(fa, tp[kk]);
                         float v = weight32(kernel, d2, rr, inv_r2);
-                        if (a.exclude_self && i == tile * TC_BK + kk) v = 0.0f;
-                        if (a.wpow == 2) v = v * v;
+                        v = (tile * TC_BK + kk == self_j) ? 0.0f : v;
+                        v = square ? v * v : v;
                         w[e] = in[e] ? v : 0.0f;
                     }
                 }

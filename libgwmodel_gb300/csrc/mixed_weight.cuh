@@ -12,18 +12,17 @@ namespace gwgpu {
 // z_lo, 0), so z = sin(lat).  Planar: one float4 (u_hi, u_lo, v_hi, v_lo)
 // relative to the centroid.
 
-// asin(x) / x as a polynomial in S = x^2 on [0, 0.25]: the degree-6 Chebyshev
+// asin(x) / x as a polynomial in S = x^2 on [0, 0.25]: the degree-5 Chebyshev
 // interpolant at the Chebyshev nodes of that interval, converted to monomials
-// (largest relative deviation 3e-10, below FP32 rounding).
+// (largest relative deviation 4.8e-9, below FP32 rounding).
 __device__ __forceinline__ float asin_over_x(float S)
 {
-    float p = 3.7677137224475400e-02f;
-    p = fmaf(p, S, 1.4295256834232772e-02f);
-    p = fmaf(p, S, 3.1857188680749646e-02f);
-    p = fmaf(p, S, 4.4508709525055284e-02f);
-    p = fmaf(p, S, 7.5005713808768180e-02f);
-    p = fmaf(p, S, 1.6666657639578963e-01f);
-    return fmaf(p, S, 1.0000000002307778f);
+    float p = 4.2417373813264260e-02f;
+    p = fmaf(p, S, 2.3993999622970812e-02f);
+    p = fmaf(p, S, 4.5520635638035500e-02f);
+    p = fmaf(p, S, 7.4946966873681580e-02f);
+    p = fmaf(p, S, 1.6666782005777223e-01f);
+    return fmaf(p, S, 9.9999999598373800e-01f);
 }
 
 constexpr float kGeoA = 6378.137f;                  // WGS-84 semi-major axis (km)
@@ -32,12 +31,13 @@ constexpr float kGeoK = 4.0f * kGeoA * kGeoA;       // (2a)^2
 
 // Chord terms of a pair of geographic records: S = sin^2 w = |chord|^2 / 4
 // (w = half the central angle), dz = sin phi_p - sin phi_f and
-// zs = sin phi_p + sin phi_f.
+// zs = sin phi_p + sin phi_f, from the focus's fz = sin phi_f (hi + lo).
 struct GeoChord {
     float S, dz, zs;
 };
 
-__device__ __forceinline__ GeoChord geo_chord32(const float4& fa, const float4& fb, const float4& pa, const float4& pb)
+__device__ __forceinline__ GeoChord geo_chord32(const float4& fa, const float4& fb, float fz, const float4& pa,
+                                                const float4& pb)
 {
     const float dx = (pa.x - fa.x) + (pb.x - fb.x);
     const float dy = (pa.y - fa.y) + (pb.y - fb.y);
@@ -45,34 +45,23 @@ __device__ __forceinline__ GeoChord geo_chord32(const float4& fa, const float4& 
     GeoChord g;
     g.S = 0.25f * fmaf(dx, dx, fmaf(dy, dy, dz * dz));
     g.dz = dz;
-    g.zs = (pa.z + fa.z) + (pb.z + fb.z);
+    g.zs = fmaf(2.0f, fz, dz);
     return g;
 }
 
 // Squared great-circle distance (km^2) of the reference's Lambert formula
-// (CRSDistance.cpp:15-81) in FP32, from the chord terms.  With latitudes phi:
+// (CRSDistance.cpp:15-81) in FP32, given A = w / sqrt(S).  With latitudes phi:
 //   sin^2F cos^2G = ((sin phi_a + sin phi_b) / 2)^2  and
 //   cos^2F sin^2G = ((sin phi_a - sin phi_b) / 2)^2,
-// so with A = w / sqrt(S) and R = sqrt(S C) / w = sqrt(C) / A (C = 1 - S)
-// the formula D = 2 a w (1 + f (H1 sin^2F cos^2G - H2 cos^2F sin^2G)),
-// H1 = (3R - 1)/(2C), H2 = (3R + 1)/(2S), becomes D^2 = (2a)^2 S (A (1 + c))^2,
+// so with R = sqrt(S C) / w = sqrt(C) / A (C = 1 - S) the formula
+// D = 2 a w (1 + f (H1 sin^2F cos^2G - H2 cos^2F sin^2G)), H1 = (3R - 1)/(2C),
+// H2 = (3R + 1)/(2S), becomes D^2 = (2a)^2 S (A (1 + c))^2 with
 //   c = (f / 8) [(3 sqrt C - A) zs^2 S - (3 sqrt C + A) dz^2 C] / (A S C).
-// A = asin_over_x(S) for S <= 0.25; beyond, asin x = pi/2 - 2 asin(sqrt y)
-// with y = (1 - x) / 2 <= 0.25 reuses the same polynomial.  Branch-free (the
-// cases are selects), so independent pairs interleave; symmetric in the two
-// points bit for bit.
-__device__ __forceinline__ float geo_d2_from_chord(const GeoChord& g)
+__device__ __forceinline__ float geo_lambert_d2(const GeoChord& g, float A)
 {
     const float S = g.S;
     const float C = fmaxf(1.0f - S, 0.0f);
     const float cq = C * rsqrtf(C);
-    const bool near = S <= 0.25f;
-    const float rs = rsqrtf(S);
-    const float y = 0.5f - 0.5f * (S * rs);  // (1 - sqrt S) / 2
-    const float z = near ? S : y;
-    const float Pz = asin_over_x(z);
-    const float far_w = fmaf(-2.0f * (z * rsqrtf(z)), Pz, 1.5707963267948966f);  // asin(sqrt S)
-    const float A = near ? Pz : far_w * rs;
     const float t1 = fmaf(3.0f, cq, -A), t2 = fmaf(3.0f, cq, A);
     const float num = fmaf(t1 * (g.zs * g.zs), S, -(t2 * (g.dz * g.dz)) * C);
     const float c = (0.125f * kGeoF) * __fdividef(num, A * S * C);
@@ -81,9 +70,28 @@ __device__ __forceinline__ float geo_d2_from_chord(const GeoChord& g)
     return S > 1e-30f ? d2 : kGeoK * fmaxf(S, 0.0f);
 }
 
+// Half angles up to 60 degrees (S <= 0.25): A from the polynomial directly.
+// The caller makes sure S <= 0.25.
+__device__ __forceinline__ float geo_d2_near(const GeoChord& g) { return geo_lambert_d2(g, asin_over_x(g.S)); }
+
+// Any S: beyond 0.25, asin x = pi/2 - 2 asin(sqrt y) with y = (1 - x) / 2
+// <= 0.25 reuses the polynomial.  Branch-free (the cases are selects), and
+// equal to geo_d2_near wherever S <= 0.25.
+__device__ __forceinline__ float geo_d2_from_chord(const GeoChord& g)
+{
+    const float S = g.S;
+    const bool near = S <= 0.25f;
+    const float rs = rsqrtf(S);
+    const float y = 0.5f - 0.5f * (S * rs);  // (1 - sqrt S) / 2
+    const float z = near ? S : y;
+    const float Pz = asin_over_x(z);
+    const float far_w = fmaf(-2.0f * (z * rsqrtf(z)), Pz, 1.5707963267948966f);  // asin(sqrt S)
+    return geo_lambert_d2(g, near ? Pz : far_w * rs);
+}
+
 __device__ __forceinline__ float geo_d2_32(const float4& fa, const float4& fb, const float4& pa, const float4& pb)
 {
-    return geo_d2_from_chord(geo_chord32(fa, fb, pa, pb));
+    return geo_d2_from_chord(geo_chord32(fa, fb, fa.z + fb.z, pa, pb));
 }
 
 // True when a pair with haversine term S lies beyond a compact kernel's
