@@ -106,6 +106,10 @@ int gwgpu_gwr_set_telegram(gwgpu_gwr* g, const gwgpu_telegram* t);
 
 /* GWRBasic::fit().  GWGPU_OK also when cancelled: check gwgpu_gwr_status. */
 int gwgpu_gwr_fit(gwgpu_gwr* g);
+/* GWRBasic::predict: coefficients at nr locations (nr x 2 column-major) at the
+   spatial weight's bandwidth; betas: nr x p column-major (may be null; the
+   getters then return the nr x p matrix). */
+int gwgpu_gwr_predict(gwgpu_gwr* g, int nr, const double* locations, double* betas);
 int gwgpu_gwr_status(gwgpu_gwr* g);
 
 /* Shapes after fit (p shrinks when variables were selected). */
@@ -171,6 +175,10 @@ int gwgpu_engine_golden(gwgpu_engine* e, int adaptive, int kernel, int criterion
                         double* bandwidth, int* count, double* list_bw, double* list_value, int cap);
 /* Drop the dataset's cached order statistics and distance histograms. */
 int gwgpu_engine_clear_cache(gwgpu_engine* e);
+/* Coefficients at nr prediction locations (nr x 2 column-major) from the
+   resident data at the given bandwidth (FP64, exact thresholds); betas nr x p. */
+int gwgpu_engine_predict(gwgpu_engine* e, int nr, const double* locations, double bandwidth, int adaptive,
+                         int kernel, double* betas);
 /* CUDA events on the engine's stream, slots 0..7: device-side timing. */
 int gwgpu_engine_event_record(gwgpu_engine* e, int slot);
 int gwgpu_engine_event_elapsed(gwgpu_engine* e, int first, int second, float* ms);

@@ -173,6 +173,9 @@ public:
     bool isValid();
 
     mat fit();
+    // GWRBasic::predict (GWRBasic.cpp:130-155): coefficients at the given
+    // locations (rows of a nRp x 2 matrix) at the spatial weight's bandwidth.
+    mat predict(const mat& locations);
 
     // results
     const mat& betas() const { return mBetas; }

@@ -103,6 +103,7 @@ SIGNATURES = [
     ("gwgpu_gwr_set_precision", _i, [_vp, _i]),
     ("gwgpu_gwr_set_telegram", _i, [_vp, ctypes.POINTER(Telegram)]),
     ("gwgpu_gwr_fit", _i, [_vp]),
+    ("gwgpu_gwr_predict", _i, [_vp, _i, _dp, _dp]),
     ("gwgpu_gwr_status", _i, [_vp]),
     ("gwgpu_gwr_shape", _i, [_vp, _ip, _ip, _ip]),
     ("gwgpu_gwr_betas", _i, [_vp, _dp]),
@@ -126,6 +127,7 @@ SIGNATURES = [
     ("gwgpu_engine_max_distance", _i, [_vp, _dp]),
     ("gwgpu_engine_golden", _i, [_vp, _i, _i, _i, _d, _d, _dp, _ip, _dp, _dp, _i]),
     ("gwgpu_engine_clear_cache", _i, [_vp]),
+    ("gwgpu_engine_predict", _i, [_vp, _i, _dp, _d, _i, _i, _dp]),
     ("gwgpu_engine_event_record", _i, [_vp, _i]),
     ("gwgpu_engine_event_elapsed", _i, [_vp, _i, _i, ctypes.POINTER(ctypes.c_float)]),
     ("gwgpu_engine_thresholds", _i, [_vp, _d, _i, _dp]),

@@ -258,6 +258,17 @@ int gwgpu_gwr_fit(gwgpu_gwr* g)
     return guarded([&] { g->alg.fit(); });
 }
 
+int gwgpu_gwr_predict(gwgpu_gwr* g, int nr, const double* locations, double* betas)
+{
+    GWR_CHECK(g);
+    if (nr < 1 || !locations) return fail(GWGPU_ERR_INVALID, "need at least one prediction location");
+    return guarded([&] {
+        gwm::mat loc((std::size_t)nr, 2, locations);
+        gwm::mat b = g->alg.predict(loc);
+        if (betas) std::memcpy(betas, b.memptr(), sizeof(double) * b.n_elem());
+    });
+}
+
 int gwgpu_gwr_status(gwgpu_gwr* g)
 {
     if (!g) return -1;
@@ -470,6 +481,19 @@ int gwgpu_engine_golden(gwgpu_engine* e, int adaptive, int kernel, int criterion
             k++;
         }
         if (count) *count = k;
+    });
+}
+
+int gwgpu_engine_predict(gwgpu_engine* e, int nr, const double* locations, double bandwidth, int adaptive,
+                         int kernel, double* betas)
+{
+    ENG_CHECK(e);
+    if (nr < 1 || !locations || !betas) return fail(GWGPU_ERR_INVALID, "null argument");
+    if (kernel < 0 || kernel > 4) return fail(GWGPU_ERR_INVALID, "unknown kernel");
+    return guarded([&] {
+        std::vector<double> b;
+        e->eng.predict(nr, locations, bandwidth, adaptive != 0, kernel, b);
+        std::memcpy(betas, b.data(), sizeof(double) * b.size());
     });
 }
 

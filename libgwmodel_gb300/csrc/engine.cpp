@@ -81,6 +81,78 @@ std::vector<TileCap> make_caps(const std::vector<double>& lon, const std::vector
     return caps;
 }
 
+void split_fp32(double v, float& hi, float& lo)
+{
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
+
+// FP32 records of the points (hu, hv), padded to whole 32-point tiles: planar
+// (u - uc, v - vc) split hi/lo in one float4; geographic the unit vector split
+// hi/lo in two float4 (its z is sin(lat)).
+std::vector<float4> point_records(const std::vector<double>& hu, const std::vector<double>& hv, bool geographic,
+                                  double uc, double vc)
+{
+    const int n = (int)hu.size();
+    const size_t nt32 = (size_t)(n + 31) / 32;
+    std::vector<float4> pts;
+    if (!geographic) {
+        pts.assign(nt32 * 32, make_float4(0.f, 0.f, 0.f, 0.f));
+        for (int s = 0; s < n; s++) {
+            float a, b, c, d;
+            split_fp32(hu[s] - uc, a, b);
+            split_fp32(hv[s] - vc, c, d);
+            pts[s] = make_float4(a, b, c, d);
+        }
+    } else {
+        pts.assign(2 * nt32 * 32, make_float4(0.f, 0.f, 0.f, 0.f));
+        const double DE2RA = M_PI / 180;
+        for (int s = 0; s < n; s++) {
+            const double lat = hv[s] * DE2RA, lon = hu[s] * DE2RA;
+            const double px = std::cos(lat) * std::cos(lon), py = std::cos(lat) * std::sin(lon), pz = std::sin(lat);
+            float xh, xl, yh, yl, zh, zl;
+            split_fp32(px, xh, xl);
+            split_fp32(py, yh, yl);
+            split_fp32(pz, zh, zl);
+            pts[2 * (size_t)s] = make_float4(xh, yh, zh, 0.f);
+            pts[2 * (size_t)s + 1] = make_float4(xl, yl, zl, 0.f);
+        }
+    }
+    return pts;
+}
+
+// FP32 bounds of consecutive tiles of `size` points, rounded outward: planar
+// boxes relative to (uc, vc) widened by `slack`, geographic 3-D caps.
+
+std::vector<float4> tile_bounds(const std::vector<double>& hu, const std::vector<double>& hv, bool geographic,
+                                int size, double uc, double vc, double slack)
+{
+    const int n = (int)hu.size();
+    const int nt = (n + size - 1) / size;
+    std::vector<float4> tb(nt);
+    if (!geographic) {
+        for (int t = 0; t < nt; t++) {
+            double ulo = hu[t * size], uhi = ulo, vlo = hv[t * size], vhi = vlo;
+            for (int s = t * size; s < std::min(n, (t + 1) * size); s++) {
+                ulo = std::min(ulo, hu[s]);
+                uhi = std::max(uhi, hu[s]);
+                vlo = std::min(vlo, hv[s]);
+                vhi = std::max(vhi, hv[s]);
+            }
+            tb[t] = make_float4(nextafterf((float)(ulo - uc - slack), -INFINITY),
+                                nextafterf((float)(uhi - uc + slack), INFINITY),
+                                nextafterf((float)(vlo - vc - slack), -INFINITY),
+                                nextafterf((float)(vhi - vc + slack), INFINITY));
+        }
+    } else {
+        std::vector<TileCap> cp = make_caps(hu, hv, size);
+        for (int t = 0; t < nt; t++)
+            tb[t] = make_float4((float)cp[t].cx, (float)cp[t].cy, (float)cp[t].cz,
+                                nextafterf((float)cp[t].rho, INFINITY) * (1.0f + 1e-6f) + 1e-7f);
+    }
+    return tb;
+}
+
 // GWRBase::AICc (GWRBase.h:90-94) from RSS and tr(S).
 double aicc(double n, double rss, double trS)
 {
@@ -273,40 +345,21 @@ void Engine::buildProxy()
         }
         bx[t] = b;
     }
-    std::vector<float4> pts;
-    auto split = [](double v, float& hi, float& lo) {
-        hi = (float)v;
-        lo = (float)(v - (double)hi);
-    };
+    // planar frame of the FP32 records and bounds: the centroid, and a slack of
+    // a few ulp of the largest relative coordinate
+    uc_ = vc_ = 0.0;
+    double maxabs = 0.0;
     if (!geographic_) {
-        double uc = 0.0, vc = 0.0;
         for (int s = 0; s < n; s++) {
-            uc += hu_[s];
-            vc += hv_[s];
+            uc_ += hu_[s];
+            vc_ += hv_[s];
         }
-        uc /= n;
-        vc /= n;
-        pts.assign((size_t)ntiles32_ * 32, make_float4(0.f, 0.f, 0.f, 0.f));  // whole tiles for bulk copies
-        for (int s = 0; s < n; s++) {
-            float a, b, c, d;
-            split(hu_[s] - uc, a, b);
-            split(hv_[s] - vc, c, d);
-            pts[s] = make_float4(a, b, c, d);
-        }
-    } else {
-        pts.assign((size_t)2 * ntiles32_ * 32, make_float4(0.f, 0.f, 0.f, 0.f));
-        const double DE2RA = M_PI / 180;
-        for (int s = 0; s < n; s++) {
-            const double lat = hv_[s] * DE2RA, lon = hu_[s] * DE2RA;
-            const double px = std::cos(lat) * std::cos(lon), py = std::cos(lat) * std::sin(lon), pz = std::sin(lat);
-            float xh, xl, yh, yl, zh, zl;
-            split(px, xh, xl);
-            split(py, yh, yl);
-            split(pz, zh, zl);
-            pts[2 * (size_t)s] = make_float4(xh, yh, zh, 0.f);
-            pts[2 * (size_t)s + 1] = make_float4(xl, yl, zl, 0.f);
-        }
+        uc_ /= n;
+        vc_ /= n;
+        for (int s = 0; s < n; s++) maxabs = std::max(maxabs, std::max(std::fabs(hu_[s] - uc_), std::fabs(hv_[s] - vc_)));
     }
+    slack_ = std::ldexp(maxabs, -20);
+    std::vector<float4> pts = point_records(hu_, hv_, geographic_, uc_, vc_);
     if (geographic_) {
         std::vector<TileCap> c32 = make_caps(hu_, hv_, 32);
         caps32_.alloc(c32.size());
@@ -323,43 +376,8 @@ void Engine::buildProxy()
           "H2D pts32");
     check(cudaMemcpyAsync(boxes32_.get(), bx.data(), sizeof(TileBox) * bx.size(), cudaMemcpyHostToDevice, stream_),
           "H2D boxes");
-    // FP32 tile bounds of 32- and 16-point tiles (rounded outward, with an
-    // absolute slack of a few ulp of the largest relative coordinate)
-    auto make_tb = [&](int size) {
-        const int nt = (n + size - 1) / size;
-        std::vector<float4> tb(nt);
-        if (!geographic_) {
-            double uc = 0.0, vc = 0.0, maxabs = 0.0;
-            for (int s = 0; s < n; s++) {
-                uc += hu_[s];
-                vc += hv_[s];
-            }
-            uc /= n;
-            vc /= n;
-            for (int s = 0; s < n; s++) maxabs = std::max(maxabs, std::max(std::fabs(hu_[s] - uc), std::fabs(hv_[s] - vc)));
-            const double slack = std::ldexp(maxabs, -20);
-            for (int t = 0; t < nt; t++) {
-                double ulo = hu_[t * size], uhi = ulo, vlo = hv_[t * size], vhi = vlo;
-                for (int s = t * size; s < std::min(n, (t + 1) * size); s++) {
-                    ulo = std::min(ulo, hu_[s]);
-                    uhi = std::max(uhi, hu_[s]);
-                    vlo = std::min(vlo, hv_[s]);
-                    vhi = std::max(vhi, hv_[s]);
-                }
-                tb[t] = make_float4(nextafterf((float)(ulo - uc - slack), -INFINITY),
-                                    nextafterf((float)(uhi - uc + slack), INFINITY),
-                                    nextafterf((float)(vlo - vc - slack), -INFINITY),
-                                    nextafterf((float)(vhi - vc + slack), INFINITY));
-            }
-        } else {
-            std::vector<TileCap> cp = make_caps(hu_, hv_, size);
-            for (int t = 0; t < nt; t++)
-                tb[t] = make_float4((float)cp[t].cx, (float)cp[t].cy, (float)cp[t].cz,
-                                    nextafterf((float)cp[t].rho, INFINITY) * (1.0f + 1e-6f) + 1e-7f);
-        }
-        return tb;
-    };
-    std::vector<float4> tb = make_tb(32), t16 = make_tb(16);
+    std::vector<float4> tb = tile_bounds(hu_, hv_, geographic_, 32, uc_, vc_, slack_);
+    std::vector<float4> t16 = tile_bounds(hu_, hv_, geographic_, 16, uc_, vc_, slack_);
     if (!geographic_) {
         sel_eps_ = std::ldexp(1.0, -18);
         sel_delta_ = std::ldexp(dhi_, -36);
@@ -934,6 +952,163 @@ size_t Engine::bytesHeld() const
     for (auto& r : ranks_) b += r->v.capacityBytes();
     for (auto& r : rank_pool_) b += r->v.capacityBytes();
     return b;
+}
+
+void Engine::predict(int nr, const double* locations, double bw, bool adaptive, int kernel,
+                     std::vector<double>& betas)
+{
+    if (n_ == 0) throw std::logic_error("no data");
+    if (nr < 1) throw std::invalid_argument("no prediction locations");
+    check(cudaSetDevice(device_), "cudaSetDevice");
+    const int p = p_;
+    // prediction points in Hilbert order (for compact focus blocks)
+    double umin = locations[0], umax = umin, vmin = locations[nr], vmax = vmin;
+    for (int i = 0; i < nr; i++) {
+        umin = std::min(umin, locations[i]);
+        umax = std::max(umax, locations[i]);
+        vmin = std::min(vmin, locations[nr + i]);
+        vmax = std::max(vmax, locations[nr + i]);
+    }
+    const double su = umax > umin ? 2147483647.0 / (umax - umin) : 0.0;
+    const double sv = vmax > vmin ? 2147483647.0 / (vmax - vmin) : 0.0;
+    std::vector<std::pair<uint64_t, int>> keyed(nr);
+    for (int i = 0; i < nr; i++) {
+        const double fu = (locations[i] - umin) * su, fv = (locations[nr + i] - vmin) * sv;
+        const uint32_t qu = std::isfinite(fu) ? (uint32_t)std::min(std::max(fu, 0.0), 2147483647.0) : 0u;
+        const uint32_t qv = std::isfinite(fv) ? (uint32_t)std::min(std::max(fv, 0.0), 2147483647.0) : 0u;
+        keyed[i] = {hilbert_index(qu, qv), i};
+    }
+    std::sort(keyed.begin(), keyed.end());
+    std::vector<double> fu(nr), fv(nr), fuR, fvR;
+    const double DE2RA = M_PI / 180;
+    for (int s = 0; s < nr; s++) {
+        fu[s] = locations[keyed[s].second];
+        fv[s] = locations[nr + keyed[s].second];
+    }
+    if (geographic_) {
+        fuR.resize(nr);
+        fvR.resize(nr);
+        for (int s = 0; s < nr; s++) {
+            fuR[s] = fu[s] * DE2RA;
+            fvR[s] = fv[s] * DE2RA;
+        }
+    }
+    // the focus bounds share the data's planar frame; widen the slack to cover both
+    double slack = slack_;
+    if (!geographic_) {
+        double maxabs = 0.0;
+        for (int s = 0; s < nr; s++) maxabs = std::max(maxabs, std::max(std::fabs(fu[s] - uc_), std::fabs(fv[s] - vc_)));
+        slack = std::max(slack, std::ldexp(maxabs, -20));
+    }
+    std::vector<float4> fpts = point_records(fu, fv, geographic_, uc_, vc_);
+    std::vector<float4> ftb = tile_bounds(fu, fv, geographic_, kTile, uc_, vc_, slack);
+    pf_u_.alloc(nr);
+    pf_v_.alloc(nr);
+    check(cudaMemcpyAsync(pf_u_.get(), fu.data(), sizeof(double) * nr, cudaMemcpyHostToDevice, stream_), "H2D");
+    check(cudaMemcpyAsync(pf_v_.get(), fv.data(), sizeof(double) * nr, cudaMemcpyHostToDevice, stream_), "H2D");
+    if (geographic_) {
+        pf_uR_.alloc(nr);
+        pf_vR_.alloc(nr);
+        check(cudaMemcpyAsync(pf_uR_.get(), fuR.data(), sizeof(double) * nr, cudaMemcpyHostToDevice, stream_), "H2D");
+        check(cudaMemcpyAsync(pf_vR_.get(), fvR.data(), sizeof(double) * nr, cudaMemcpyHostToDevice, stream_), "H2D");
+    }
+    pf_pts_.alloc(fpts.size());
+    check(cudaMemcpyAsync(pf_pts_.get(), fpts.data(), sizeof(float4) * fpts.size(), cudaMemcpyHostToDevice, stream_),
+          "H2D");
+    pf_tb16_.alloc(ftb.size());
+    check(cudaMemcpyAsync(pf_tb16_.get(), ftb.data(), sizeof(float4) * ftb.size(), cudaMemcpyHostToDevice, stream_),
+          "H2D");
+    DevPoints F;
+    F.n = nr;
+    F.u = pf_u_.get();
+    F.v = pf_v_.get();
+    F.uR = geographic_ ? pf_uR_.get() : nullptr;
+    F.vR = geographic_ ? pf_vR_.get() : nullptr;
+
+    // thresholds: fixbw of BandwidthWeight.cpp:40-53 over each location's distances to the data
+    const double* thr = nullptr;
+    if (adaptive) {
+        pf_thr_.alloc(nr);
+        pf_d0_.alloc(nr);
+        auto select = [&](unsigned rank, double* out) {
+            SelectArgs a{};
+            a.n = n_;
+            a.ntiles = ntiles32_;
+            a.P = points();
+            a.pts = pts32_.get();
+            a.tb = tbsel_.get();
+            a.hist_cache = nullptr;
+            a.cache_valid = 0;
+            a.rank = rank;
+            a.dlo = dlo_;
+            a.dhi = dhi_;
+            a.eps = sel_eps_;
+            a.delta = sel_delta_;
+            a.out = out;
+            a.err = sel_err_.get();
+            a.F = F;
+            a.fpts = pf_pts_.get();
+            check(launch_select(a, geographic_, true, num_sms_, stream_), "predict select");
+            stats_.kernel_launches += 1;
+        };
+        const double dn = bw / n_;
+        if (dn < 1) {
+            const double b0 = std::floor(bw), bx = bw - b0;
+            const long long r0 = (long long)(int)b0;
+            if (r0 < 1 || r0 >= n_) throw std::out_of_range("Mat::operator(): index out of bounds");
+            select((unsigned)r0, pf_d0_.get());
+            const double* d1 = nullptr;
+            if (bx != 0.0) {
+                pf_d1_.alloc(nr);
+                select((unsigned)(r0 + 1), pf_d1_.get());
+                d1 = pf_d1_.get();
+            }
+            check(launch_threshold_combine_rows(nr, n_, bw, pf_d0_.get(), d1, pf_thr_.get(), stream_), "threshold");
+        } else {
+            select((unsigned)n_, pf_d0_.get());
+            check(launch_threshold_combine_rows(nr, n_, bw, pf_d0_.get(), nullptr, pf_thr_.get(), stream_),
+                  "threshold");
+        }
+        stats_.kernel_launches += 1;
+        thr = pf_thr_.get();
+    }
+    // X^T W_i X, X^T W_i y at every location, then beta_i = (X^T W_i X)^-1 X^T W_i y
+    pf_g_.alloc((size_t)nr * m_);
+    check(launch_contract64_focus(points(), tb16_.get(), F, pf_tb16_.get(), geographic_, z_.get(), m_, m_, pf_g_.get(),
+                                  m_, thr, bw, kernel, false, 1, true, stream_),
+          "predict contraction");
+    pf_beta_.alloc((size_t)nr * p);
+    SolveArgs a{};
+    a.n = nr;
+    a.p = p;
+    a.mode = kSolvePredict;
+    a.kernel = kernel;
+    a.G = pf_g_.get();
+    a.ldg = m_;
+    a.thr = thr;
+    a.bw = bw;
+    a.beta = pf_beta_.get();
+    a.partials = partials_.get();
+    a.tcol = -1;
+    int nb = 0;
+    check(launch_solve(a, &nb, stream_), "predict solve");
+    check(launch_reduce_partials(partials_.get(), nb, sums_.get(), stream_), "reduce");
+    stats_.kernel_launches += 4;
+    std::vector<double> hb((size_t)nr * p);
+    check(cudaMemcpyAsync(hb.data(), pf_beta_.get(), sizeof(double) * hb.size(), cudaMemcpyDeviceToHost, stream_),
+          "D2H");
+    check(cudaMemcpyAsync(host_sums_, sums_.get(), 4 * sizeof(double), cudaMemcpyDeviceToHost, stream_), "D2H");
+    check(cudaMemcpyAsync(host_sums_ + 5, sel_err_.get(), sizeof(int), cudaMemcpyDeviceToHost, stream_), "D2H");
+    synchronize();
+    int serr = 0;
+    std::memcpy(&serr, host_sums_ + 5, sizeof(int));
+    if (serr) throw CudaError("adaptive threshold select failed (code " + std::to_string(serr) + ")");
+    if (host_sums_[3] > 0.0) throw NotSPDError("inv_sympd(): matrix is singular or not positive definite");
+    betas.assign((size_t)nr * p, 0.0);
+    for (int s = 0; s < nr; s++) {
+        const int i = keyed[s].second;
+        for (int k = 0; k < p; k++) betas[(size_t)i + (size_t)k * nr] = hb[(size_t)s * p + k];
+    }
 }
 
 void Engine::clearCaches()

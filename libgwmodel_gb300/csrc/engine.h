@@ -136,6 +136,11 @@ public:
     void fit(double bw, bool adaptive, int kernel, bool storeS, FitOutput& out);
     // CRSDistance::maxDistance.
     double maxDistance();
+    // GWRBasic::predict (GWRBasic.cpp:130-191, predictSerial/Omp/Cuda): beta at
+    // nr prediction locations (nr x 2 column-major) from the data's weights at
+    // bandwidth bw, in FP64 with the exact thresholds (both numeric forms);
+    // betas: nr x p column-major.  Throws NotSPDError like the reference.
+    void predict(int nr, const double* locations, double bw, bool adaptive, int kernel, std::vector<double>& betas);
     // Golden-section bandwidth search on the device-resident data
     // (BandwidthSelector::optimize); returns the chosen bandwidth and fills
     // record with (bandwidth, criterion).
@@ -224,6 +229,7 @@ private:
     // mixed-precision state (built on first use): X~ = (X - mu) / s, y~ likewise
     bool mixed_ready_ = false;
     int npad_ = 0, ntiles32_ = 0, intercept_col_ = -1;
+    double uc_ = 0.0, vc_ = 0.0, slack_ = 0.0;  // planar frame of the FP32 records and tile bounds
     std::vector<double> mu_, sc_;  // per column mean (0 if not centred) and scale
     double mu_y_ = 0.0, s_y_ = 1.0;
     DevBuf<double> xs_, ys_, zs_;
@@ -237,6 +243,10 @@ private:
     DevBuf<int> err_;
     DevBuf<unsigned long long> tile_count_;
     DevBuf<unsigned long long> tc_prof_;  // phase cycles of the contraction (stats)
+    // prediction points (Hilbert order): FP64 coordinates, FP32 records, 16-point
+    // tile bounds, thresholds, normal equations and coefficients
+    DevBuf<double> pf_u_, pf_v_, pf_uR_, pf_vR_, pf_thr_, pf_d0_, pf_d1_, pf_g_, pf_beta_;
+    DevBuf<float4> pf_pts_, pf_tb16_;
     // event pairs recorded around timed launches, resolved by stats()
     struct PendingTiming {
         cudaEvent_t e0, e1;

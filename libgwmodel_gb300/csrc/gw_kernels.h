@@ -13,7 +13,7 @@ namespace gwgpu {
 cudaError_t raise_smem_limit(const void* fn, size_t bytes);
 
 // Solve modes of launch_solve.
-enum SolveMode { kSolveAIC = 0, kSolveCV = 1, kSolveFit = 2, kSolveRefine = 3 };
+enum SolveMode { kSolveAIC = 0, kSolveCV = 1, kSolveFit = 2, kSolveRefine = 3, kSolvePredict = 4 };
 
 // Per-row k-th smallest distance (1-based rank), k_select.cu.
 struct SelectArgs {
@@ -28,6 +28,10 @@ struct SelectArgs {
     double eps, delta;             // proxy band: d in [p (1 - eps) - delta, p (1 + eps) + delta]
     double* out;
     int* err;                      // 2: a row's select failed (value left NaN)
+    // Focus rows when they are not the data points (prediction): FP64
+    // coordinates and FP32 records of F.n focus points.  Null F.u: the data.
+    DevPoints F;
+    const float4* fpts;
 };
 // exact: FP64 order statistics (bit-exact); otherwise the FP32 proxy's.
 cudaError_t launch_select(const SelectArgs& a, bool geographic, bool exact, int num_sms, cudaStream_t stream);
@@ -52,6 +56,9 @@ constexpr int kSelHistRows = 8;  // rows per histogram item
 // be null when bw is integral).
 cudaError_t launch_threshold_combine(int n, double bw, const double* d0, const double* d1, double* thr,
                                      cudaStream_t stream);
+// The same for `rows` focus rows over n data points (dn = bw / n).
+cudaError_t launch_threshold_combine_rows(int rows, int n, double bw, const double* d0, const double* d1, double* thr,
+                                          cudaStream_t stream);
 
 // out[i] = (float)in[i].
 cudaError_t launch_to_float(int n, const double* in, float* out, cudaStream_t stream);
@@ -66,6 +73,12 @@ cudaError_t launch_build_z(int n, int p, const double* X, const double* y, doubl
 cudaError_t launch_contract64(const DevPoints& P, bool geographic, const float4* tb16, const double* Z, int ldz,
                               int mcols, double* G, int ldg, const double* thr, double bw, int kernel,
                               bool exclude_self, int wpow, bool skip_tiles, cudaStream_t stream);
+// The same with focus rows F (their 16-point tile bounds ftb16) that are not
+// the data points: G[i, :] for every focus row i over the data P (predict).
+cudaError_t launch_contract64_focus(const DevPoints& P, const float4* tb16, const DevPoints& F, const float4* ftb16,
+                                    bool geographic, const double* Z, int ldz, int mcols, double* G, int ldg,
+                                    const double* thr, double bw, int kernel, bool exclude_self, int wpow,
+                                    bool skip_tiles, cudaStream_t stream);
 
 // Warp-per-location Cholesky solve of A_i beta_i = b_i and the per-location
 // criterion terms; partial sums per block in partials[block*4 + {0..3}] =

@@ -287,4 +287,39 @@ mat GWRBasic::fit()
     return mBetas;
 }
 
+// GWRBasic::predict (GWRBasic.cpp:130-155) with predictSerial/Omp/Cuda
+// (GWRBasic.cpp:165-191, 665-707): the stages, stop checks and the zero
+// matrix of the reference's stop path (nDp x nVars) are kept.
+mat GWRBasic::predict(const mat& locations)
+{
+    GW_STAGE("Initialization");
+    const std::size_t nDp = mCoords.n_rows, nVars = mX.n_cols, nRp = locations.n_rows;
+    if (mCoords.n_cols != 2 || locations.n_cols != 2)
+        throw std::runtime_error("The dimension of data points or focus points is not 2.");
+    if (mX.n_rows != nDp || mY.n_rows != nDp) throw std::runtime_error("X, y and coords differ in rows");
+    const bool geographic = mSpatialWeight.distance()->geographic();
+    if (!mImpl->engine || mImpl->device != mGpuId) {
+        mImpl->engine.reset(new gwgpu::Engine(mGpuId));
+        mImpl->device = mGpuId;
+    }
+    gwgpu::Engine& eng = *mImpl->engine;
+    eng.setPrecision((int)mPrecision);
+    eng.setData((int)nDp, (int)nVars, mX.memptr(), mY.memptr(), mCoords.memptr(), geographic);
+    GW_STOP_RETURN(mat(nDp, nVars));
+
+    GW_STAGE("Prediction");
+    const BandwidthWeight& bw = *mSpatialWeight.weight();
+    std::vector<double> b;
+    try {
+        eng.predict((int)nRp, locations.memptr(), bw.bandwidth(), bw.adaptive(), (int)bw.kernel(), b);
+    } catch (const gwgpu::NotSPDError& e) {
+        GW_LOG(LOG_ERR, e.what());
+        throw std::runtime_error(e.what());
+    }
+    mTelegram->progress(nRp, nRp, __func__, kFile);
+    mBetas = mat(nRp, nVars, b.data());
+    GW_STOP_RETURN(mat(nDp, nVars));
+    return mBetas;
+}
+
 }  // namespace gwm

@@ -25,9 +25,9 @@ constexpr int CT_ROWS_PER_THREAD = CT_BM / 16;
 
 template <bool GEO, int NC>
 __global__ void __launch_bounds__(CT_THREADS)
-    k_contract64(DevPoints P, const float4* __restrict__ tb16, const double* __restrict__ Z, int ldz, int mcols,
-                 double* __restrict__ G, int ldg, const double* __restrict__ thr, double bw, int kernel,
-                 int exclude_self, int wpow, int skip_tiles)
+    k_contract64(DevPoints P, const float4* __restrict__ tb16, DevPoints F, const float4* __restrict__ ftb16,
+                 const double* __restrict__ Z, int ldz, int mcols, double* __restrict__ G, int ldg,
+                 const double* __restrict__ thr, double bw, int kernel, int exclude_self, int wpow, int skip_tiles)
 {
     constexpr int NCOL = NC * 16;
     __shared__ double sW[CT_BM][CT_BK + 1];
@@ -36,27 +36,27 @@ __global__ void __launch_bounds__(CT_THREADS)
     __shared__ double sred[CT_THREADS / 32];
     __shared__ float4 sbound;
 
-    const int n = P.n;
+    const int n = P.n, nf = F.n;  // data points, focus rows (the data themselves, or prediction points)
     const int t = threadIdx.x, tx = t & 15, ty = t >> 4;
     const int row0 = blockIdx.x * CT_BM;
 
     double rmax = bw;
     if (t < CT_BM) {
         int i = row0 + t;
-        bool ok = i < n;
-        sfu[t] = ok ? P.u[i] : 0.0;
-        sfv[t] = ok ? P.v[i] : 0.0;
-        sfuR[t] = (GEO && ok) ? P.uR[i] : 0.0;
-        sfvR[t] = (GEO && ok) ? P.vR[i] : 0.0;
+        bool ok = i < nf;
+        sfu[t] = ok ? F.u[i] : 0.0;
+        sfv[t] = ok ? F.v[i] : 0.0;
+        sfuR[t] = (GEO && ok) ? F.uR[i] : 0.0;
+        sfvR[t] = (GEO && ok) ? F.vR[i] : 0.0;
         sthr[t] = ok ? (thr ? thr[i] : bw) : 0.0;
     }
     if (thr) {
-        double r = (t < CT_BM && row0 + t < n) ? thr[row0 + t] : -1.0;
+        double r = (t < CT_BM && row0 + t < nf) ? thr[row0 + t] : -1.0;
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) r = fmax(r, __shfl_xor_sync(0xffffffffu, r, off));
         if ((t & 31) == 0) sred[t >> 5] = r;
     }
-    if (t == 0) sbound = tb_union<GEO>(tb16, row0 / CT_BK, (min(row0 + CT_BM, n) - 1) / CT_BK);
+    if (t == 0) sbound = tb_union<GEO>(ftb16, row0 / CT_BK, (min(row0 + CT_BM, nf) - 1) / CT_BK);
     __syncthreads();
     if (thr) {
         rmax = sred[0];
@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(CT_THREADS)
                 const int r = ty + 16 * q;
                 const int i = row0 + r;
                 double w = 0.0;
-                if (j < n && i < n) {
+                if (j < n && i < nf) {
                     double d;
                     if constexpr (GEO)
                         d = gw_gc_dist(du, sfu[r], dv, sfv[r], duR, sfuR[r], dvR, sfvR[r]);
@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(CT_THREADS)
 #pragma unroll
     for (int q = 0; q < CT_ROWS_PER_THREAD; q++) {
         const int i = row0 + ty + 16 * q;
-        if (i >= n) continue;
+        if (i >= nf) continue;
 #pragma unroll
         for (int c = 0; c < NC; c++) {
             const int col = tx + 16 * c;
@@ -137,25 +137,26 @@ __global__ void __launch_bounds__(CT_THREADS)
 }
 
 template <bool GEO, int NC>
-cudaError_t launch_nc(const DevPoints& P, const float4* tiles, const double* Z, int ldz,
-                      int mcols, double* G, int ldg, const double* thr, double bw, int kernel, bool exclude_self,
-                      int wpow, bool skip, cudaStream_t s)
+cudaError_t launch_nc(const DevPoints& P, const float4* tiles, const DevPoints& F, const float4* ftiles,
+                      const double* Z, int ldz, int mcols, double* G, int ldg, const double* thr, double bw,
+                      int kernel, bool exclude_self, int wpow, bool skip, cudaStream_t s)
 {
-    int grid = (P.n + CT_BM - 1) / CT_BM;
-    k_contract64<GEO, NC><<<grid, CT_THREADS, 0, s>>>(P, tiles, Z, ldz, mcols, G, ldg, thr, bw, kernel,
+    int grid = (F.n + CT_BM - 1) / CT_BM;
+    k_contract64<GEO, NC><<<grid, CT_THREADS, 0, s>>>(P, tiles, F, ftiles, Z, ldz, mcols, G, ldg, thr, bw, kernel,
                                                      exclude_self ? 1 : 0, wpow, skip ? 1 : 0);
     return cudaGetLastError();
 }
 
 template <bool GEO>
-cudaError_t launch_geo(const DevPoints& P, const float4* tiles, const double* Z, int ldz,
-                       int mcols, double* G, int ldg, const double* thr, double bw, int kernel, bool exclude_self,
-                       int wpow, bool skip, cudaStream_t s)
+cudaError_t launch_geo(const DevPoints& P, const float4* tiles, const DevPoints& F, const float4* ftiles,
+                       const double* Z, int ldz, int mcols, double* G, int ldg, const double* thr, double bw,
+                       int kernel, bool exclude_self, int wpow, bool skip, cudaStream_t s)
 {
     int nc = (mcols + 15) / 16;
 #define GW_NC_CASE(K) \
     case K:           \
-        return launch_nc<GEO, K>(P, tiles, Z, ldz, mcols, G, ldg, thr, bw, kernel, exclude_self, wpow, skip, s);
+        return launch_nc<GEO, K>(P, tiles, F, ftiles, Z, ldz, mcols, G, ldg, thr, bw, kernel, exclude_self, wpow, \
+                                 skip, s);
     switch (nc) {
         GW_NC_CASE(1) GW_NC_CASE(2) GW_NC_CASE(3) GW_NC_CASE(4) GW_NC_CASE(5) GW_NC_CASE(6) GW_NC_CASE(7)
         GW_NC_CASE(8) GW_NC_CASE(9) GW_NC_CASE(10) GW_NC_CASE(11) GW_NC_CASE(12) GW_NC_CASE(13)
@@ -171,12 +172,21 @@ cudaError_t launch_contract64(const DevPoints& P, bool geographic, const float4*
                               int mcols, double* G, int ldg, const double* thr, double bw, int kernel,
                               bool exclude_self, int wpow, bool skip_tiles, cudaStream_t stream)
 {
-    if (mcols < 1 || mcols > 256) return cudaErrorInvalidValue;
+    return launch_contract64_focus(P, tb16, P, tb16, geographic, Z, ldz, mcols, G, ldg, thr, bw, kernel, exclude_self,
+                                   wpow, skip_tiles, stream);
+}
+
+cudaError_t launch_contract64_focus(const DevPoints& P, const float4* tb16, const DevPoints& F, const float4* ftb16,
+                                    bool geographic, const double* Z, int ldz, int mcols, double* G, int ldg,
+                                    const double* thr, double bw, int kernel, bool exclude_self, int wpow,
+                                    bool skip_tiles, cudaStream_t stream)
+{
+    if (mcols < 1 || mcols > 256 || F.n < 1) return cudaErrorInvalidValue;
     if (geographic)
-        return launch_geo<true>(P, tb16, Z, ldz, mcols, G, ldg, thr, bw, kernel, exclude_self, wpow, skip_tiles,
-                                stream);
-    return launch_geo<false>(P, tb16, Z, ldz, mcols, G, ldg, thr, bw, kernel, exclude_self, wpow, skip_tiles,
-                             stream);
+        return launch_geo<true>(P, tb16, F, ftb16, Z, ldz, mcols, G, ldg, thr, bw, kernel, exclude_self, wpow,
+                                skip_tiles, stream);
+    return launch_geo<false>(P, tb16, F, ftb16, Z, ldz, mcols, G, ldg, thr, bw, kernel, exclude_self, wpow,
+                             skip_tiles, stream);
 }
 
 }  // namespace gwgpu

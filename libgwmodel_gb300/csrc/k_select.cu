@@ -326,7 +326,8 @@ template <bool GEO, bool EXACT>
 __device__ void select_one(SelShared& sh, const SelectArgs& a, int row, const Window& wlog)
 {
     const int t = threadIdx.x;
-    const DevPoints P = a.P;
+    const DevPoints P = a.F.u ? a.F : a.P;  // focus coordinates
+    const float4* fpts = a.F.u ? a.fpts : a.pts;
     const double INF = __longlong_as_double(0x7ff0000000000000ll);
     RowCtx c;
     c.fu = P.u[row];
@@ -334,13 +335,13 @@ __device__ void select_one(SelShared& sh, const SelectArgs& a, int row, const Wi
     c.fuR = GEO ? P.uR[row] : 0.0;
     c.fvR = GEO ? P.vR[row] : 0.0;
     if (GEO) {
-        c.fa = a.pts[2 * (size_t)row];
-        c.fb = a.pts[2 * (size_t)row + 1];
+        c.fa = fpts[2 * (size_t)row];
+        c.fb = fpts[2 * (size_t)row + 1];
         c.qx = c.fa.x + c.fb.x;
         c.qy = c.fa.y + c.fb.y;
         c.qz = c.fa.z + c.fb.z;
     } else {
-        c.fa = a.pts[row];
+        c.fa = fpts[row];
         c.fb = c.fa;
         c.qx = c.fa.x + c.fa.y;
         c.qy = c.fa.z + c.fa.w;
@@ -390,7 +391,8 @@ __global__ void __launch_bounds__(SEL_THREADS) k_select(SelectArgs a)
     SelShared& sh = *reinterpret_cast<SelShared*>(smem_raw);
     // coarse logarithmic window of the first pass over a whole row
     const Window wlog = coarse_window(a);
-    for (int row = blockIdx.x; row < a.n; row += gridDim.x) select_one<GEO, EXACT>(sh, a, row, wlog);
+    const int nrows = a.F.u ? a.F.n : a.n;
+    for (int row = blockIdx.x; row < nrows; row += gridDim.x) select_one<GEO, EXACT>(sh, a, row, wlog);
 }
 
 // Index of the segment holding flattened item `item`: the last seg with start[seg] <= item.
@@ -451,7 +453,9 @@ __device__ void hist_rows(unsigned* hs, float4 (*rf)[2], const SelectArgs& a, in
     const Window wlog = coarse_window(a);
     constexpr int NF = GEO ? 2 : 1;
     const int ngroups = (a.ntiles + 31) / 32;
-    const int nrows = min(HS_ROWS, n - row0);
+    const int nfocus = a.F.u ? a.F.n : n;
+    const float4* fpts = a.F.u ? a.fpts : a.pts;
+    const int nrows = min(HS_ROWS, nfocus - row0);
     // bucket_of(wlog, dkey_f(d)) for a normal float d in 32/64-bit integer steps:
     // with the aligned base and 29 <= shift <= 52 it is
     // (bits(d) >> (shift - 29)) + (896 << 23 >> (shift - 29)) + (2^63 >> shift) - (base >> shift)
@@ -463,7 +467,7 @@ __device__ void hist_rows(unsigned* hs, float4 (*rf)[2], const SelectArgs& a, in
     for (int b = t; b < HS_ROWS * SEL_BINS; b += HS_THREADS) hs[b] = 0;
     if (t < HS_ROWS * NF) {
         const int r = t / NF, q = t % NF;
-        rf[r][q] = r < nrows ? a.pts[NF * (size_t)(row0 + r) + q] : make_float4(0.f, 0.f, 0.f, 0.f);
+        rf[r][q] = r < nrows ? fpts[NF * (size_t)(row0 + r) + q] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     __syncthreads();
     float4 ra[HS_ROWS], rb[HS_ROWS];
@@ -507,7 +511,8 @@ __global__ void __launch_bounds__(HS_THREADS, 1) k_select_hist(SelectArgs a)
 {
     extern __shared__ __align__(16) unsigned hs[];  // HS_ROWS x SEL_BINS
     __shared__ float4 rf[HS_ROWS][2];
-    for (int row0 = blockIdx.x * HS_ROWS; row0 < a.n; row0 += gridDim.x * HS_ROWS) hist_rows<GEO>(hs, rf, a, row0);
+    const int nfocus = a.F.u ? a.F.n : a.n;
+    for (int row0 = blockIdx.x * HS_ROWS; row0 < nfocus; row0 += gridDim.x * HS_ROWS) hist_rows<GEO>(hs, rf, a, row0);
 }
 
 // Histogram caches of many datasets in one launch: segment s owns the row
@@ -553,11 +558,11 @@ __global__ void k_to_float_batch(const double* const* __restrict__ in, float* co
 
 // fixbw of BandwidthWeight.cpp:40-53 from the selected order statistics:
 // dn < 1: d0 + (d1 - d0) * bx;  dn >= 1: dn * max(dist).
-__global__ void k_threshold_combine(int n, double bw, const double* __restrict__ d0,
+__global__ void k_threshold_combine(int rows, int n, double bw, const double* __restrict__ d0,
                                     const double* __restrict__ d1, double* __restrict__ thr)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= rows) return;
     double dn = bw / n;
     if (dn < 1) {
         double b0 = floor(bw), bx = bw - b0;
@@ -587,8 +592,9 @@ size_t select_smem_bytes() { return sizeof(SelShared); }
 cudaError_t launch_select(const SelectArgs& a, bool geographic, bool exact, int num_sms, cudaStream_t stream)
 {
     if (a.rank < 1 || a.rank > (unsigned)a.n) return cudaErrorInvalidValue;
+    const int nrows = a.F.u ? a.F.n : a.n;
     int grid = num_sms * 12;
-    if (grid > a.n) grid = a.n;
+    if (grid > nrows) grid = nrows;
     const size_t smem = sizeof(SelShared);
 #define GW_SEL(G, E)                                                                                  \
     do {                                                                                              \
@@ -667,7 +673,13 @@ cudaError_t launch_to_float_batch(const double* const* in, float* const* out, co
 cudaError_t launch_threshold_combine(int n, double bw, const double* d0, const double* d1, double* thr,
                                      cudaStream_t stream)
 {
-    k_threshold_combine<<<(n + 255) / 256, 256, 0, stream>>>(n, bw, d0, d1, thr);
+    return launch_threshold_combine_rows(n, n, bw, d0, d1, thr, stream);
+}
+
+cudaError_t launch_threshold_combine_rows(int rows, int n, double bw, const double* d0, const double* d1, double* thr,
+                                          cudaStream_t stream)
+{
+    k_threshold_combine<<<(rows + 255) / 256, 256, 0, stream>>>(rows, n, bw, d0, d1, thr);
     return cudaGetLastError();
 }
 

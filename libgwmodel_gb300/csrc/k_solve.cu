@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(SV_WARPS * 32)
         if (lane < p)
             for (int c = 0; c <= lane; c++) L[lane * ld + c] = g[packed_index(c, lane, p)];
         const double bvec = lane < p ? g[mm + lane] : 0.0;
-        const double xr = lane < p ? a.X[(size_t)row * p + lane] : 0.0;
+        const double xr = (MODE != kSolvePredict && lane < p) ? a.X[(size_t)row * p + lane] : 0.0;
         __syncwarp();
         // Cholesky-Crout, lane r owns row r
         bool fail = false;
@@ -126,8 +126,10 @@ __global__ void __launch_bounds__(SV_WARPS * 32)
             if (lane < p) a.beta[(size_t)row * p + lane] = __longlong_as_double(0x7ff8000000000000ll);
             if (lane == 0) {
                 acc_f += 1.0;
-                a.resid[row] = __longlong_as_double(0x7ff8000000000000ll);
-                a.sii[row] = 0.0;
+                if (MODE != kSolvePredict) {
+                    a.resid[row] = __longlong_as_double(0x7ff8000000000000ll);
+                    a.sii[row] = 0.0;
+                }
             }
             __syncwarp();
             continue;
@@ -141,6 +143,11 @@ __global__ void __launch_bounds__(SV_WARPS * 32)
             beta = bwd_solve(L, ld, p, lane, fwd_solve(L, ld, p, lane, bvec));
         }
         if (lane < p) a.beta[(size_t)row * p + lane] = beta;
+        if (MODE == kSolvePredict) {
+            // a prediction point has no x_i or y_i: beta is the whole output (GWRBasic.cpp:166-190)
+            __syncwarp();
+            continue;
+        }
         const double yhat = warp_sum(lane < p ? xr * beta : 0.0);
         const double res = a.y[row] - yhat;
         double sii = 0.0;
@@ -494,6 +501,10 @@ cudaError_t launch_solve(const SolveArgs& a, int* nblocks, cudaStream_t stream)
     case kSolveCV:
         raise_smem_limit((const void*)k_solve<kSolveCV, false>, smem);
         k_solve<kSolveCV, false><<<grid, SV_WARPS * 32, smem, stream>>>(a, nullptr, nullptr);
+        break;
+    case kSolvePredict:
+        raise_smem_limit((const void*)k_solve<kSolvePredict, false>, smem);
+        k_solve<kSolvePredict, false><<<grid, SV_WARPS * 32, smem, stream>>>(a, nullptr, nullptr);
         break;
     case kSolveRefine:
         raise_smem_limit((const void*)k_solve<kSolveRefine, false>, smem);

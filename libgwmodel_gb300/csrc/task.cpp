@@ -117,8 +117,23 @@ public:
         return true;
     }
 
-    // GWRBasic::predict (GWRBasic.cpp:130-191) is not provided by this engine.
-    bool predict(bool) override { return false; }
+    // GWRBasicGpuTask::predict (GWRBasicGpuTask.cpp:49-66): any exception -> false.
+    bool predict(bool hasIntercept) override
+    {
+        if (mDistanceType != kCRSDistance) return false;
+        try {
+            gwm::CRSDistance d(mGeographic);
+            gwm::SpatialWeight sw(&mWeight, &d);
+            gwm::GWRBasic algorithm(mX, mY, mCoords, sw, true, hasIntercept);
+            algorithm.setParallelType(gwm::ParallelType::CUDA);
+            algorithm.setTelegram(std::unique_ptr<gwm::ITelegram>(new StdTelegram()));
+            algorithm.predict(mPredictLocations);
+            mBetas = algorithm.betas();
+        } catch (const std::exception&) {
+            return false;
+        }
+        return true;
+    }
 
 private:
     gwm::mat mX, mY, mCoords, mPredictLocations;

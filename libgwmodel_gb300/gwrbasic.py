@@ -259,6 +259,13 @@ class GWRBasic:
         check(lib().gwgpu_gwr_fit(self._h))
         return self.betas()
 
+    def predict(self, locations):
+        """GWRBasic::predict: coefficients (nRp x p) at the given locations."""
+        loc = np.asfortranarray(locations, dtype=np.float64)
+        nr = loc.shape[0]
+        check(lib().gwgpu_gwr_predict(self._h, nr, dptr(loc), None))
+        return self.betas()
+
     def status(self):
         return lib().gwgpu_gwr_status(self._h)
 
@@ -391,6 +398,14 @@ class Engine:
         check(lib().gwgpu_engine_fit(self._h, float(bw), int(bool(adaptive)), int(kernel), int(bool(store_s)),
                                      dptr(betas), dptr(se), dptr(shat), dptr(qdiag), dptr(S)))
         return betas, se, shat, qdiag, S
+
+    def predict(self, locations, bw, adaptive, kernel):
+        loc = np.asfortranarray(locations, dtype=np.float64)
+        nr = loc.shape[0]
+        out = np.zeros((nr, self.p), order="F")
+        check(lib().gwgpu_engine_predict(self._h, nr, dptr(loc), float(bw), int(bool(adaptive)), int(kernel),
+                                         dptr(out)))
+        return out
 
     def max_distance(self):
         v = ctypes.c_double()

@@ -488,6 +488,40 @@ int orc_fit_core(const orc_problem* pb, double bw, int adaptive, int kernel, int
     return ok ? 0 : -1;
 }
 
+/* GWRBasic::predictSerial (GWRBasic.cpp:165-191): beta at nr locations
+   (nr x 2 column-major) from the weights of each location's distances to the
+   data (CRSDistance with the prediction parameter {locations, coords},
+   GWRBasic.cpp:157-163: data point first, location second, as in a fit). */
+int orc_predict(const orc_problem* pb, int nr, const double* loc, double bw, int adaptive, int kernel,
+                double* betas)
+{
+    const int n = pb->n, p = pb->p, T = orc_threads(pb);
+    orc_ws* ws = (orc_ws*)malloc(sizeof(orc_ws) * (size_t)T);
+    for (int t = 0; t < T; t++) ws_alloc(&ws[t], n, p, 0);
+    int ok = 1;
+#pragma omp parallel for num_threads(T) schedule(dynamic, 1) reduction(&& : ok)
+    for (int r = 0; r < nr; r++)
+    {
+        orc_ws* w = &ws[orc_thread_id()];
+        const double uf = loc[r], vf = loc[(size_t)nr + r];
+        for (int j = 0; j < n; j++)
+        {
+            if (!pb->geographic)
+                w->d[j] = gw_planar_dist(U_(pb, j), V_(pb, j), uf, vf);
+            else if (pb->gc_mode == ORC_GC_PORTABLE)
+                w->d[j] = orc_gcdist_portable(U_(pb, j), uf, V_(pb, j), vf);
+            else
+                w->d[j] = orc_gcdist_libm(U_(pb, j), uf, V_(pb, j), vf);
+        }
+        if (orc_weight(w->d, n, bw, adaptive, kernel, w->w) != 0) { ok = 0; continue; }
+        if (local_solve(pb, pb->x, p, w) != 0) { ok = 0; continue; }
+        for (int k = 0; k < p; k++) betas[(size_t)r + (size_t)k * nr] = w->beta[k];
+    }
+    for (int t = 0; t < T; t++) ws_free(&ws[t]);
+    free(ws);
+    return ok ? 0 : -1;
+}
+
 /* ------------------------------------------------------------ golden search */
 
 typedef struct

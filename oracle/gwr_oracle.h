@@ -79,6 +79,10 @@ int orc_fit_core(const orc_problem* pb, double bw, int adaptive, int kernel, int
  * Writes the chosen bandwidth; list_bw/list_f (capacity cap) receive the
  * (bandwidth, criterion) pairs sorted by bandwidth (:83-95).  Returns the
  * number of pairs, or -1 for "Invalid initial values." */
+/* GWRBasic::predictSerial: betas (nr x p column-major) at nr locations (nr x 2 column-major). */
+int orc_predict(const orc_problem* pb, int nr, const double* loc, double bw, int adaptive, int kernel,
+                double* betas);
+
 int orc_golden(const orc_problem* pb, double bw0, int adaptive, int kernel, int criterion,
                double lower, double upper, double* bw_out, double* list_bw, double* list_f, int cap);
 

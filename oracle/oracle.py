@@ -83,6 +83,8 @@ def lib():
             L.orc_indep_vars_criterion.argtypes = [P, ip, i]
             L.orc_fit_core.restype = i
             L.orc_fit_core.argtypes = [P, d, i, i, i, dp, dp, dp, dp, dp]
+            L.orc_predict.restype = i
+            L.orc_predict.argtypes = [P, i, dp, d, i, i, dp]
             L.orc_golden.restype = i
             L.orc_golden.argtypes = [P, d, i, i, i, d, d, dp, dp, dp, i]
             L.orc_diagnostic.argtypes = [P, dp, dp, dp]
@@ -153,6 +155,16 @@ class Problem:
         if rc != 0:
             raise RuntimeError("inv_sympd(): matrix is singular or not positive definite")
         return betas, se, shat, qdiag, S
+
+    def predict(self, locations, bw, adaptive, kernel):
+        """GWRBasic::predictSerial: betas (nr x p) at the given locations."""
+        loc = np.asfortranarray(locations, dtype=np.float64)
+        nr = loc.shape[0]
+        betas = np.zeros((nr, self.p), order="F")
+        rc = lib().orc_predict(self.ref, nr, _dp(loc), float(bw), int(adaptive), int(kernel), _dp(betas))
+        if rc != 0:
+            raise RuntimeError("inv_sympd(): matrix is singular or not positive definite")
+        return betas
 
     def golden(self, bw0, adaptive, kernel, criterion, lower, upper, cap=512):
         bw = np.zeros(1)
