@@ -273,6 +273,16 @@ def run_serve(args):
     return 0
 
 
+def max_over_ranks(value, dist):
+    """The largest value over all ranks (the slowest replica sets the time)."""
+    if not dist:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def one_fit(engine, pb):
     """GWRBasic::fit body on resident data: golden search, then the final fit.
     Every step starts from empty caches: nothing computed by an earlier step
@@ -375,11 +385,7 @@ def run_ours(args):
     ms = engine.elapsed_ms(0, 1)
     clk = clocks.stop()
     stats = engine.stats()
-    if dist:
-        import torch
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dist)
     evals = stats["criterion_evals"] / args.steps
     fits_per_step = pb.n * (evals + 1)
     value = world * fits_per_step * args.steps / (ms / 1e3)
