@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--serve", action="store_true", help="config-4 serving sweep instead of the config-2 line")
     ap.add_argument("--batch", action="store_true", help="config-3 batched evaluation instead of the config-2 line")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--config1", action="store_true", help="config-1 FP64 drop-in line instead of the config-2 line")
     ap.add_argument("--rates", default="5,20,50,200")
     ap.add_argument("--requests", type=int, default=60)
     ap.add_argument("--slots", type=int, default=8)
@@ -248,6 +249,62 @@ def run_batch(args):
             "contract_ctas": info["contract_ctas"],
             "sequential_ms": seq_s * 1e3, "speedup_vs_sequential": seq_s / dt,
             "max_rel_diff_vs_sequential": err, "best_bandwidth_first5": best[:5]}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_config1(args):
+    """Config 1: the FP64 drop-in on n = 50,000 planar points, fixed gaussian
+    kernel, CV golden-section search over [0, maxDistance] then the fit, beside
+    the CPU restatement of the reference on a bounded sample of rows."""
+    rank, _, local = dist_env()
+    if rank != 0:
+        return 0
+    from libgwmodel_gb300 import Engine, Precision, datasets
+    pb = datasets.config1()
+    e = Engine(local)
+    e.set_data(pb.x, pb.y, pb.coords, False)
+    e.set_precision(Precision.FP64)
+    e.enable_stats(True)
+    upper = e.max_distance()
+    for _ in range(args.warmup):
+        e.clear_cache()
+        e.golden(False, 0, 1, 0.0, upper)
+    e.reset_stats()
+    e.record_event(0)
+    for _ in range(args.steps):
+        e.clear_cache()
+        bw, _ = e.golden(False, 0, 1, 0.0, upper)
+        e.fit(bw, False, 0, store_s=False)
+    e.record_event(1)
+    ms = e.elapsed_ms(0, 1) / args.steps
+    st = e.stats()
+    evals = st["criterion_evals"] / args.steps
+    value = pb.n * (evals + 1) / (ms / 1e3)
+    line = {"metric": "GWR local fits/s, config 1 FP64 drop-in (n=50k planar, fixed gaussian, CV search)",
+            "value": value, "unit": UNIT, "higher_is_better": True, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "dtype": "f64",
+            "data": "synthetic (seeded config-1 generator, numpy PCG64 seed 1)",
+            "config": {"workload": "config1: n=50000 planar U[0,1000]^2, p=9 (x1,x2 rho=0.7), fixed gaussian, "
+                                   "CV golden search over [0, maxDistance] + fit", "criterion_evals_per_step": evals,
+                       "selected_bandwidth": bw},
+            "gpu_launches": int(st["kernel_launches"]),
+            "contract_tflops": st["contract_flops"] / (st["contract_ms"] / 1e3) / 1e12 if st["contract_ms"] else 0}
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        threads = os.cpu_count() or 1
+        prob = O.Problem(pb.x, pb.y, pb.coords, geographic=False, threads=threads)
+        rows = threads * 4
+        t0 = time.perf_counter()
+        prob.criterion_rows(bw, False, 0, 1, 0, rows)
+        dt = time.perf_counter() - t0
+        rows = min(pb.n, max(rows, int(rows * min(args.cpu_seconds, 20.0) / max(dt, 1e-6))))
+        t0 = time.perf_counter()
+        prob.criterion_rows(bw, False, 0, 1, 0, rows)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": rows / dt, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"{rows} local fits of the CV criterion at bandwidth {bw:.4g} in {dt:.1f}s"}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -462,6 +519,8 @@ def main():
         return run_serve(args)
     if args.batch:
         return run_batch(args)
+    if args.config1:
+        return run_config1(args)
     return run_ours(args)
 
 

@@ -73,4 +73,18 @@ extern "C" GWMODELCUDA_API IGWRBasicGpuTask* GWRBasicGpuTaskPredict_Create(int n
                                                                            int nPredictPoints);
 extern "C" GWMODELCUDA_API void GWRBasicGpuTask_Del(IGWRBasicGpuTask* pInstance);
 
+/* Bulk I/O beside the per-element vtable calls (setX/setY/setCoords and the
+ * betas(i, k) getters cost one virtual call per element,
+ * GWRBasicGpuTask.h:128-146 of the reference).  They are plain functions, so
+ * the interface's vtable is unchanged; each returns 0, or -1 when the task is
+ * not one of this library's or a pointer is null.  Matrices are column-major:
+ * x nDp x nVar, coords nDp x 2, locations nPredictPoints x 2; the getters
+ * write rows x nVar where rows is nDp after fit() and nPredictPoints after
+ * predict(). */
+extern "C" GWMODELCUDA_API int GWRBasicGpuTask_SetData(IGWRBasicGpuTask* task, const double* x, const double* y,
+                                                       const double* coords);
+extern "C" GWMODELCUDA_API int GWRBasicGpuTask_SetPredictLocations(IGWRBasicGpuTask* task, const double* locations);
+extern "C" GWMODELCUDA_API int GWRBasicGpuTask_GetBetas(IGWRBasicGpuTask* task, double* out);
+extern "C" GWMODELCUDA_API int GWRBasicGpuTask_GetBetasSE(IGWRBasicGpuTask* task, double* out);
+
 #endif /* GWGPU_IGWRBASICGPUTASK_H */

@@ -161,6 +161,10 @@ TASK_SIGNATURES = [
     ("GWRBasicGpuTaskFit_Create", _vp, [_i, _i, _i]),
     ("GWRBasicGpuTaskPredict_Create", _vp, [_i, _i, _i, _i]),
     ("GWRBasicGpuTask_Del", None, [_vp]),
+    ("GWRBasicGpuTask_SetData", _i, [_vp, _dp, _dp, _dp]),
+    ("GWRBasicGpuTask_SetPredictLocations", _i, [_vp, _dp]),
+    ("GWRBasicGpuTask_GetBetas", _i, [_vp, _dp]),
+    ("GWRBasicGpuTask_GetBetasSE", _i, [_vp, _dp]),
 ]
 
 

@@ -1,6 +1,7 @@
 // task.cpp -- IGWRBasicGpuTask implementation over gwm::GWRBasic
 // (libgwmodel src/gwmodelcuda/GWRBasicGpuTask.cpp:10-66 and
 // include/gwmodelcuda/GWRBasicGpuTask.h:11-251 describe the behaviour).
+#include <cstring>
 #include "../../include/IGWRBasicGpuTask.h"
 
 #include <exception>
@@ -135,6 +136,20 @@ public:
         return true;
     }
 
+    // bulk I/O (the extern "C" GWRBasicGpuTask_* helpers)
+    void setData(const double* x, const double* y, const double* coords)
+    {
+        std::memcpy(mX.memptr(), x, sizeof(double) * mX.n_elem());
+        std::memcpy(mY.memptr(), y, sizeof(double) * mY.n_elem());
+        std::memcpy(mCoords.memptr(), coords, sizeof(double) * mCoords.n_elem());
+    }
+    void setPredictLocations(const double* locations)
+    {
+        std::memcpy(mPredictLocations.memptr(), locations, sizeof(double) * mPredictLocations.n_elem());
+    }
+    const gwm::mat& betasMatrix() const { return mBetas; }
+    const gwm::mat& betasSEMatrix() const { return mBetasSE; }
+
 private:
     gwm::mat mX, mY, mCoords, mPredictLocations;
     gwm::mat mBetas, mBetasSE, mSHat, mQDiag, mS;
@@ -154,6 +169,40 @@ private:
 };
 
 }  // namespace
+
+extern "C" int GWRBasicGpuTask_SetData(IGWRBasicGpuTask* task, const double* x, const double* y, const double* coords)
+{
+    auto* t = dynamic_cast<GWRBasicGpuTask*>(task);
+    if (!t || !x || !y || !coords) return -1;
+    t->setData(x, y, coords);
+    return 0;
+}
+
+extern "C" int GWRBasicGpuTask_SetPredictLocations(IGWRBasicGpuTask* task, const double* locations)
+{
+    auto* t = dynamic_cast<GWRBasicGpuTask*>(task);
+    if (!t || !locations) return -1;
+    t->setPredictLocations(locations);
+    return 0;
+}
+
+extern "C" int GWRBasicGpuTask_GetBetas(IGWRBasicGpuTask* task, double* out)
+{
+    auto* t = dynamic_cast<GWRBasicGpuTask*>(task);
+    if (!t || !out) return -1;
+    const gwm::mat& m = t->betasMatrix();
+    if (m.n_elem()) std::memcpy(out, m.memptr(), sizeof(double) * m.n_elem());
+    return 0;
+}
+
+extern "C" int GWRBasicGpuTask_GetBetasSE(IGWRBasicGpuTask* task, double* out)
+{
+    auto* t = dynamic_cast<GWRBasicGpuTask*>(task);
+    if (!t || !out) return -1;
+    const gwm::mat& m = t->betasSEMatrix();
+    if (m.n_elem()) std::memcpy(out, m.memptr(), sizeof(double) * m.n_elem());
+    return 0;
+}
 
 extern "C" IGWRBasicGpuTask* GWRBasicGpuTaskFit_Create(int nDp, int nVar, int distanceType)
 {

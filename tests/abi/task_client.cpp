@@ -2,7 +2,11 @@
 // desktop client binds libgwmodelcuda: dlopen() the library, look up the
 // extern "C" factories, and call the task through its vtable only.
 //
-//   task_client <libgwgpu.so> <input.bin> <mode: fit|predict>
+//   task_client <libgwgpu.so> <input.bin> <mode: fit|predict|bulkfit|bulkpredict>
+//
+// The bulk modes move the data and the coefficients with the extern "C"
+// GWRBasicGpuTask_SetData / _SetPredictLocations / _GetBetas helpers instead
+// of the per-element virtual calls.
 //
 // input.bin: int32 n, p, geographic, adaptive, kernel, criterion(-1: no
 // optimisation), n_pred; double bandwidth; then coords (n x 2 column-major),
@@ -20,6 +24,9 @@
 typedef IGWRBasicGpuTask* (*FitCreate)(int, int, int);
 typedef IGWRBasicGpuTask* (*PredictCreate)(int, int, int, int);
 typedef void (*Del)(IGWRBasicGpuTask*);
+typedef int (*SetData)(IGWRBasicGpuTask*, const double*, const double*, const double*);
+typedef int (*SetLoc)(IGWRBasicGpuTask*, const double*);
+typedef int (*GetMat)(IGWRBasicGpuTask*, double*);
 
 int main(int argc, char** argv)
 {
@@ -35,7 +42,10 @@ int main(int argc, char** argv)
     auto fitCreate = (FitCreate)dlsym(h, "GWRBasicGpuTaskFit_Create");
     auto predCreate = (PredictCreate)dlsym(h, "GWRBasicGpuTaskPredict_Create");
     auto del = (Del)dlsym(h, "GWRBasicGpuTask_Del");
-    if (!fitCreate || !predCreate || !del) {
+    auto setData = (SetData)dlsym(h, "GWRBasicGpuTask_SetData");
+    auto setLoc = (SetLoc)dlsym(h, "GWRBasicGpuTask_SetPredictLocations");
+    auto getBetas = (GetMat)dlsym(h, "GWRBasicGpuTask_GetBetas");
+    if (!fitCreate || !predCreate || !del || !setData || !setLoc || !getBetas) {
         std::fprintf(stderr, "missing factory\n");
         return 2;
     }
@@ -52,17 +62,23 @@ int main(int argc, char** argv)
         std::fread(loc.data(), sizeof(double), loc.size(), f) != loc.size())
         return 2;
     std::fclose(f);
-    const bool predict = argv[3][0] == 'p';
+    const bool bulk = argv[3][0] == 'b';
+    const bool predict = argv[3][bulk ? 4 : 0] == 'p';
     IGWRBasicGpuTask* t = predict ? predCreate(n, p, 0, nr) : fitCreate(n, p, 0);
-    for (int i = 0; i < n; i++) {
-        t->setY(i, y[i]);
-        for (int k = 0; k < p; k++) t->setX(i, k, x[(size_t)i + (size_t)k * n]);
-        t->setCoords(i, 0, coords[i]);  // (row, column, value), as the reference's quirk wants
-        t->setCoords(i, 1, coords[(size_t)n + i]);
-    }
-    for (int i = 0; predict && i < nr; i++) {  // a fit task holds no prediction locations
-        t->setPredictLocations(i, 0, loc[i]);
-        t->setPredictLocations(i, 1, loc[(size_t)nr + i]);
+    if (bulk) {
+        if (setData(t, x.data(), y.data(), coords.data()) != 0) return 3;
+        if (predict && setLoc(t, loc.data()) != 0) return 3;
+    } else {
+        for (int i = 0; i < n; i++) {
+            t->setY(i, y[i]);
+            for (int k = 0; k < p; k++) t->setX(i, k, x[(size_t)i + (size_t)k * n]);
+            t->setCoords(i, 0, coords[i]);  // (row, column, value), as the reference's quirk wants
+            t->setCoords(i, 1, coords[(size_t)n + i]);
+        }
+        for (int i = 0; predict && i < nr; i++) {  // a fit task holds no prediction locations
+            t->setPredictLocations(i, 0, loc[i]);
+            t->setPredictLocations(i, 1, loc[(size_t)nr + i]);
+        }
     }
     t->setCRSDistanceGergraphic(geo != 0);
     t->setBandwidthSize(bw);
@@ -79,9 +95,11 @@ int main(int argc, char** argv)
             std::printf("R aicc %.17g\nR rss %.17g\nR shat %.17g %.17g\n", t->diagnosticAICc(), t->diagnosticRSS(),
                         t->shat1(), t->shat2());
         }
+        std::vector<double> b((size_t)rows * p);
+        if (bulk && getBetas(t, b.data()) != 0) return 3;
         for (int i = 0; i < rows; i++) {
             std::printf("R");
-            for (int k = 0; k < p; k++) std::printf(" %.17g", t->betas(i, k));
+            for (int k = 0; k < p; k++) std::printf(" %.17g", bulk ? b[(size_t)i + (size_t)k * rows] : t->betas(i, k));
             std::printf("\n");
         }
     }

@@ -82,3 +82,21 @@ def test_task_fit_and_predict_match_engine(tmp_path):
     pred = np.array([[float(v) for v in l.split()] for l in lines[1:1 + loc.shape[0]]])
     want = e.predict(loc, bw, True, 2)
     assert np.abs(pred - want).max() <= 1e-12 * np.abs(want).max()
+    # the bulk helpers give exactly the per-element results
+    assert run(exe, inp, "bulkpredict") == lines
+    write_input(inp, pb, 100.0, 0, loc)
+    assert run(exe, inp, "bulkfit") == run(exe, inp, "fit")
+
+
+def test_bulk_helpers_reject_foreign_and_null_pointers():
+    import ctypes
+    L = _lib.lib()
+    t = L.GWRBasicGpuTaskFit_Create(10, 2, 0)
+    assert t
+    buf = np.zeros(40)
+    ptr = buf.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    assert L.GWRBasicGpuTask_SetData(t, ptr, ptr, ptr) == 0
+    assert L.GWRBasicGpuTask_SetData(t, None, ptr, ptr) == -1
+    assert L.GWRBasicGpuTask_GetBetas(None, ptr) == -1
+    assert L.GWRBasicGpuTask_GetBetas(t, ptr) == 0  # nothing fitted yet: an empty matrix
+    L.GWRBasicGpuTask_Del(t)
