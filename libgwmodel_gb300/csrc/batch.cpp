@@ -266,6 +266,7 @@ private:
         a.P = e.points();
         a.pts = e.pts32_.get();
         a.tb = e.tbsel_.get();
+        a.stb = e.stb_.get();
         a.hist_cache = e.hist_.get();
         a.cache_valid = 1;
         a.rank = rank;

@@ -378,6 +378,10 @@ void Engine::buildProxy()
           "H2D boxes");
     std::vector<float4> tb = tile_bounds(hu_, hv_, geographic_, 32, uc_, vc_, slack_);
     std::vector<float4> t16 = tile_bounds(hu_, hv_, geographic_, 16, uc_, vc_, slack_);
+    std::vector<float4> t1024 = tile_bounds(hu_, hv_, geographic_, 1024, uc_, vc_, slack_);
+    stb_.alloc(t1024.size());
+    check(cudaMemcpyAsync(stb_.get(), t1024.data(), sizeof(float4) * t1024.size(), cudaMemcpyHostToDevice, stream_),
+          "H2D super-tile bounds");
     if (!geographic_) {
         sel_eps_ = std::ldexp(1.0, -18);
         sel_delta_ = std::ldexp(dhi_, -36);
@@ -639,6 +643,7 @@ const double* Engine::orderStatistic(unsigned rank)
     a.P = points();
     a.pts = pts32_.get();
     a.tb = tbsel_.get();
+    a.stb = stb_.get();
     a.hist_cache = hist_.get();
     a.cache_valid = hist_valid_ ? 1 : 0;
     a.rank = rank;
@@ -948,7 +953,7 @@ size_t Engine::bytesHeld() const
                tile_thr16_.capacityBytes() + xs_.capacityBytes() + ys_.capacityBytes() + zs_.capacityBytes() +
                zimg_.capacityBytes() + acc_.capacityBytes() + thr32_.capacityBytes() + g2_.capacityBytes() +
                vvec_.capacityBytes() + bse_.capacityBytes() + qdiag_.capacityBytes() + S_.capacityBytes() +
-               hist_.capacityBytes() + xsub_.capacityBytes() + gsub_.capacityBytes();
+               hist_.capacityBytes() + xsub_.capacityBytes() + gsub_.capacityBytes() + stb_.capacityBytes();
     for (auto& r : ranks_) b += r->v.capacityBytes();
     for (auto& r : rank_pool_) b += r->v.capacityBytes();
     return b;
@@ -1037,6 +1042,7 @@ void Engine::predict(int nr, const double* locations, double bw, bool adaptive, 
             a.P = points();
             a.pts = pts32_.get();
             a.tb = tbsel_.get();
+            a.stb = stb_.get();
             a.hist_cache = nullptr;
             a.cache_valid = 0;
             a.rank = rank;

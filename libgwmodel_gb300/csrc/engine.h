@@ -247,6 +247,7 @@ private:
     // tile bounds, thresholds, normal equations and coefficients
     DevBuf<double> pf_u_, pf_v_, pf_uR_, pf_vR_, pf_thr_, pf_d0_, pf_d1_, pf_g_, pf_beta_;
     DevBuf<float4> pf_pts_, pf_tb16_;
+    DevBuf<float4> stb_;  // bounds of the 1024-point super-tiles (select)
     // event pairs recorded around timed launches, resolved by stats()
     struct PendingTiming {
         cudaEvent_t e0, e1;

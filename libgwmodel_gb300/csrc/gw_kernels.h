@@ -21,6 +21,7 @@ struct SelectArgs {
     DevPoints P;                   // FP64 coordinates (exact formula)
     const float4* pts;             // FP32 hi/lo proxy data (as the mixed path)
     const float4* tb;              // per tile: planar box (ulo, uhi, vlo, vhi) or cap (cx, cy, cz, rho)
+    const float4* stb;             // per super-tile of 32 tiles (1024 points): the same bound, or null
     unsigned* hist_cache;          // n x 4096 proxy histograms of whole rows, or null
     int cache_valid;               // 1: hist_cache holds every row's histogram
     unsigned rank;

@@ -218,69 +218,83 @@ __device__ bool select_row(SelShared& sh, const SelectArgs& a, const RowCtx& c, 
         if (t == 0) sh.ncand = 0;
         __syncthreads();
         unsigned below = 0;
-        // each lane classifies one tile; the warp then walks the straddling ones
-        for (int tbase = warp * 32; tbase < a.ntiles; tbase += SEL_WARPS * 32) {
-            const int mytile = tbase + lane;
-            int cls = 1;
-            if (mytile < a.ntiles) cls = classify_tile<GEO>(a.tb[mytile], c, below_thr, above_thr);
-            if (cls < 0) below += (unsigned)min(SEL_TILE, n - mytile * SEL_TILE);
-            unsigned straddle = __ballot_sync(0xffffffffu, cls == 0);
-            while (straddle) {
-                const int k = __ffs(straddle) - 1;
-                straddle &= straddle - 1;
-                const int tile = tbase + k;
-                const int j = tile * SEL_TILE + lane;
-                bool in = false;
-                uint64_t key = 0;
-                if (j < n) {
-                    float d32;
-                    bool sure = true;
-                    if (GEO) {
-                        d32 = geo_dist32(c.fa, c.fb, a.pts[2 * (size_t)j], a.pts[2 * (size_t)j + 1]);
-                        // far-apart pairs (half-angle near pi/2): the FP32 formula is not trusted
-                        sure = isfinite(d32) && d32 < 15000.0f;
-                    } else {
-                        d32 = sqrtf(planar_d2_32(c.fa, a.pts[j]));
-                    }
-                    if (EXACT) {
-                        double d = (double)d32;
-                        const double dl = sure ? d * (1.0 - a.eps) - a.delta : -1.0;
-                        const double dh = sure ? d * (1.0 + a.eps) + a.delta : INF;
-                        bool eval = false;
-                        if (dh < T_lo) below++;
-                        else if (!(dl > T_hi)) eval = true;
-                        if (eval) {
-                            d = pair_dist<GEO>(a.P, j, c.fu, c.fv, c.fuR, c.fvR);
-                            if (d < T_lo) below++;
-                            else if (d <= T_hi) {
+        // each lane classifies one super-tile of 32 tiles (interleaved over the
+        // warps, so a row's ring of straddling super-tiles spreads across them);
+        // a straddling super-tile is walked tile by tile, a straddling tile
+        // point by point
+        const int nst = (a.ntiles + 31) / 32;
+        for (int sgrp = 0; sgrp * SEL_WARPS * 32 < nst; sgrp++) {
+            const int mys = warp + SEL_WARPS * (lane + 32 * sgrp);
+            int scls = 1;
+            if (mys < nst) scls = a.stb ? classify_tile<GEO>(a.stb[mys], c, below_thr, above_thr) : 0;
+            if (scls < 0) below += (unsigned)min(32 * SEL_TILE, n - mys * 32 * SEL_TILE);
+            unsigned sstr = __ballot_sync(0xffffffffu, scls == 0);
+            while (sstr) {
+                const int ks = __ffs(sstr) - 1;
+                sstr &= sstr - 1;
+                const int tbase = (warp + SEL_WARPS * (ks + 32 * sgrp)) * 32;
+                const int mytile = tbase + lane;
+                int cls = 1;
+                if (mytile < a.ntiles) cls = classify_tile<GEO>(a.tb[mytile], c, below_thr, above_thr);
+                if (cls < 0) below += (unsigned)min(SEL_TILE, n - mytile * SEL_TILE);
+                unsigned straddle = __ballot_sync(0xffffffffu, cls == 0);
+                while (straddle) {
+                    const int k = __ffs(straddle) - 1;
+                    straddle &= straddle - 1;
+                    const int tile = tbase + k;
+                    const int j = tile * SEL_TILE + lane;
+                    bool in = false;
+                    uint64_t key = 0;
+                    if (j < n) {
+                        float d32;
+                        bool sure = true;
+                        if (GEO) {
+                            d32 = geo_dist32(c.fa, c.fb, a.pts[2 * (size_t)j], a.pts[2 * (size_t)j + 1]);
+                            // far-apart pairs (half-angle near pi/2): the FP32 formula is not trusted
+                            sure = isfinite(d32) && d32 < 15000.0f;
+                        } else {
+                            d32 = sqrtf(planar_d2_32(c.fa, a.pts[j]));
+                        }
+                        if (EXACT) {
+                            double d = (double)d32;
+                            const double dl = sure ? d * (1.0 - a.eps) - a.delta : -1.0;
+                            const double dh = sure ? d * (1.0 + a.eps) + a.delta : INF;
+                            bool eval = false;
+                            if (dh < T_lo) below++;
+                            else if (!(dl > T_hi)) eval = true;
+                            if (eval) {
+                                d = pair_dist<GEO>(a.P, j, c.fu, c.fv, c.fuR, c.fvR);
+                                if (d < T_lo) below++;
+                                else if (d <= T_hi) {
+                                    in = true;
+                                    key = dkey(d);
+                                }
+                            }
+                        } else if (d32 == d32) {
+                            // proxy values compared in key space (dkey is monotone)
+                            const uint64_t k32 = dkey_f(d32);
+                            if (k32 < klo) below++;
+                            else if (k32 <= khi) {
                                 in = true;
-                                key = dkey(d);
+                                key = k32;
                             }
                         }
-                    } else if (d32 == d32) {
-                        // proxy values compared in key space (dkey is monotone)
-                        const uint64_t k32 = dkey_f(d32);
-                        if (k32 < klo) below++;
-                        else if (k32 <= khi) {
-                            in = true;
-                            key = k32;
+                    }
+                    const unsigned act = __ballot_sync(0xffffffffu, in);
+                    if (act) {
+                        if (in) {
+                            const unsigned bin = bucket_of(w, key);
+                            const unsigned peers = __match_any_sync(act, bin);
+                            if (lane == __ffs(peers) - 1) atomicAdd(&sh.hist[bin], (unsigned)__popc(peers));
                         }
-                    }
-                }
-                const unsigned act = __ballot_sync(0xffffffffu, in);
-                if (act) {
-                    if (in) {
-                        const unsigned bin = bucket_of(w, key);
-                        const unsigned peers = __match_any_sync(act, bin);
-                        if (lane == __ffs(peers) - 1) atomicAdd(&sh.hist[bin], (unsigned)__popc(peers));
-                    }
-                    const int leader = __ffs(act) - 1;
-                    unsigned base = 0;
-                    if (lane == leader) base = atomicAdd(&sh.ncand, (unsigned)__popc(act));
-                    base = __shfl_sync(0xffffffffu, base, leader);
-                    if (in) {
-                        const unsigned slot = base + __popc(act & ((1u << lane) - 1u));
-                        if (slot < SEL_CAP) sh.cand[slot] = key;
+                        const int leader = __ffs(act) - 1;
+                        unsigned base = 0;
+                        if (lane == leader) base = atomicAdd(&sh.ncand, (unsigned)__popc(act));
+                        base = __shfl_sync(0xffffffffu, base, leader);
+                        if (in) {
+                            const unsigned slot = base + __popc(act & ((1u << lane) - 1u));
+                            if (slot < SEL_CAP) sh.cand[slot] = key;
+                        }
                     }
                 }
             }
