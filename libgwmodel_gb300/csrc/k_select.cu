@@ -245,16 +245,20 @@ __device__ bool select_row(SelShared& sh, const SelectArgs& a, const RowCtx& c, 
                     const int j = tile * SEL_TILE + lane;
                     bool in = false;
                     uint64_t key = 0;
+                    // the proxy distance of every lane (records are padded to whole tiles),
+                    // with the near-angle form when the whole warp is within 60 degrees
+                    float d32;
+                    if (GEO) {
+                        const GeoChord g = geo_chord32(c.fa, c.fb, c.fa.z + c.fb.z, a.pts[2 * (size_t)j],
+                                                       a.pts[2 * (size_t)j + 1]);
+                        const float d2 = __all_sync(0xffffffffu, g.S <= 0.25f) ? geo_d2_near(g) : geo_d2_from_chord(g);
+                        d32 = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
+                    } else {
+                        d32 = sqrtf(planar_d2_32(c.fa, a.pts[j]));
+                    }
                     if (j < n) {
-                        float d32;
-                        bool sure = true;
-                        if (GEO) {
-                            d32 = geo_dist32(c.fa, c.fb, a.pts[2 * (size_t)j], a.pts[2 * (size_t)j + 1]);
-                            // far-apart pairs (half-angle near pi/2): the FP32 formula is not trusted
-                            sure = isfinite(d32) && d32 < 15000.0f;
-                        } else {
-                            d32 = sqrtf(planar_d2_32(c.fa, a.pts[j]));
-                        }
+                        // far-apart pairs (half-angle near pi/2): the FP32 formula is not trusted
+                        const bool sure = !GEO || (isfinite(d32) && d32 < 15000.0f);
                         if (EXACT) {
                             double d = (double)d32;
                             const double dl = sure ? d * (1.0 - a.eps) - a.delta : -1.0;
@@ -493,14 +497,34 @@ __device__ void hist_rows(unsigned* hs, float4 (*rf)[2], const SelectArgs& a, in
     for (int g = warp; g < ngroups; g += HS_THREADS / 32) {
         const int tile = g * 32 + lane;
         for (int q = 0; q < SEL_TILE; q++) {
-            const int j = tile * SEL_TILE + q;
-            if (tile >= a.ntiles || j >= n) continue;
+            const bool valid = tile < a.ntiles && tile * SEL_TILE + q < n;
+            const int j = tile < a.ntiles ? tile * SEL_TILE + q : 0;  // records are padded to whole tiles
             const float4 pa = a.pts[NF * (size_t)j];
             const float4 pb = GEO ? a.pts[2 * (size_t)j + 1] : pa;
+            float d32r[HS_ROWS];
+            if (GEO) {
+                GeoChord g[HS_ROWS];
+                float smax = 0.0f;
+#pragma unroll
+                for (int r = 0; r < HS_ROWS; r++) {
+                    g[r] = geo_chord32(ra[r], rb[r], ra[r].z + rb[r].z, pa, pb);
+                    smax = fmaxf(smax, g[r].S);
+                }
+                const bool near = __all_sync(0xffffffffu, smax <= 0.25f);
+#pragma unroll
+                for (int r = 0; r < HS_ROWS; r++) {
+                    const float d2 = near ? geo_d2_near(g[r]) : geo_d2_from_chord(g[r]);
+                    d32r[r] = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < HS_ROWS; r++) d32r[r] = sqrtf(planar_d2_32(ra[r], pa));
+            }
+            if (!valid) continue;
 #pragma unroll
             for (int r = 0; r < HS_ROWS; r++) {
                 if (r >= nrows) break;
-                const float d32 = GEO ? geo_dist32(ra[r], rb[r], pa, pb) : sqrtf(planar_d2_32(ra[r], pa));
+                const float d32 = d32r[r];
                 if (d32 == d32) {
                     const uint32_t fb = __float_as_uint(d32);
                     unsigned bin;
