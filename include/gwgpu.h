@@ -159,6 +159,9 @@ int gwgpu_engine_set_precision(gwgpu_engine* e, int precision);
 /* Mixed path: 32-point data tiles summed in FP32 on the tensor core before
    each double-float drain (default 64, at least 2). */
 int gwgpu_engine_set_flush_tiles(gwgpu_engine* e, int tiles);
+/* Mixed path: FP64 refinement steps of the final fit (default 1), and
+   whether each AICc criterion of the search is refined too (default 0). */
+int gwgpu_engine_set_refinement(gwgpu_engine* e, int steps, int refine_search);
 /* One bandwidth criterion (DBL_MAX when a local system is not SPD). */
 int gwgpu_engine_criterion(gwgpu_engine* e, double bandwidth, int adaptive, int kernel, int criterion,
                            double* value);

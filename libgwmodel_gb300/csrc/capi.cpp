@@ -414,6 +414,14 @@ int gwgpu_engine_set_precision(gwgpu_engine* e, int precision)
     return GWGPU_OK;
 }
 
+int gwgpu_engine_set_refinement(gwgpu_engine* e, int steps, int refine_search)
+{
+    ENG_CHECK(e);
+    if (steps < 0 || steps > 8) return fail(GWGPU_ERR_INVALID, "refinement steps must be in [0, 8]");
+    e->eng.setRefinement(steps, refine_search != 0);
+    return GWGPU_OK;
+}
+
 int gwgpu_engine_set_flush_tiles(gwgpu_engine* e, int tiles)
 {
     ENG_CHECK(e);

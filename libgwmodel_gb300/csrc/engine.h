@@ -223,7 +223,7 @@ private:
     bool gall_valid_ = false;
     DevBuf<TileBox> tiles_;
     DevBuf<TileCap> caps_;      // geographic bounds of the 16-point tiles
-    int refine_steps_ = 2;
+    int refine_steps_ = 1;
     bool refine_search_ = false;
 
     // mixed-precision state (built on first use): X~ = (X - mu) / s, y~ likewise

@@ -373,6 +373,9 @@ class Engine:
     def set_precision(self, p):
         check(lib().gwgpu_engine_set_precision(self._h, int(p)))
 
+    def set_refinement(self, steps, refine_search=False):
+        check(lib().gwgpu_engine_set_refinement(self._h, int(steps), int(bool(refine_search))))
+
     def set_flush_tiles(self, tiles):
         check(lib().gwgpu_engine_set_flush_tiles(self._h, int(tiles)))
 
