@@ -618,3 +618,267 @@ void orc_diagnostic(const orc_problem* pb, const double* betas, const double* sh
     double r2_adj = 1 - (1 - r2) * (n - 1) / (edf - 1);
     out[0] = rss; out[1] = AIC; out[2] = AICc; out[3] = enp; out[4] = edf; out[5] = r2; out[6] = r2_adj;
 }
+
+/* ------------------------------------------------------------------ MGWR */
+
+/* GWRMultiscale (GWRMultiscale.cpp:68-317, serial forms :362-639): per-variable
+   bandwidths by backfitting.  The per-variable criteria are GWRBasic's
+   criteria of the one-column problem (x_i, y_i) (:560-638), the initial
+   all-variable criterion is GWRBasic's on the centred X (:484-558), and the
+   bandwidth searches are BandwidthSelector::optimize with MGWR's bounds. */
+
+/* fitAllSerial with the hat matrix (:362-394): betas, betasSE = rowsum(ci^2),
+   S0 rows si = x_i ci and SArray_k(i, :) = x(i, k) ci(k, :) (:216-224). */
+static int mgwr_fit_all(const orc_problem* pb, double bw, int adaptive, int kernel, int hat, double* betas,
+                        double* betas_se, double* S0, double* SA)
+{
+    const int n = pb->n, p = pb->p, T = orc_threads(pb);
+    orc_ws* ws = (orc_ws*)malloc(sizeof(orc_ws) * (size_t)T);
+    for (int t = 0; t < T; t++) ws_alloc(&ws[t], n, p, 1);
+    int ok = 1;
+#pragma omp parallel for num_threads(T) schedule(dynamic, 1) reduction(&& : ok)
+    for (int i = 0; i < n; i++)
+    {
+        orc_ws* w = &ws[orc_thread_id()];
+        orc_distance_row(pb, i, w->d);
+        if (orc_weight(w->d, n, bw, adaptive, kernel, w->w) != 0 || local_solve(pb, pb->x, p, w) != 0)
+        {
+            ok = 0;
+            continue;
+        }
+        for (int k = 0; k < p; k++) betas[(size_t)i + (size_t)k * n] = w->beta[k];
+        if (!hat) continue;
+        hat_row(pb, pb->x, p, i, w);
+        for (int k = 0; k < p; k++)
+        {
+            double s = 0.0;
+            for (int j = 0; j < n; j++) s += w->ci[k + (size_t)j * p] * w->ci[k + (size_t)j * p];
+            betas_se[(size_t)i + (size_t)k * n] = s;
+        }
+        for (int j = 0; j < n; j++)
+        {
+            S0[(size_t)i + (size_t)j * n] = w->si[j];
+            for (int k = 0; k < p; k++)
+                SA[(size_t)k * n * n + (size_t)i + (size_t)j * n] =
+                    pb->x[(size_t)i + (size_t)k * n] * w->ci[k + (size_t)j * p];
+        }
+    }
+    for (int t = 0; t < T; t++) ws_free(&ws[t]);
+    free(ws);
+    return ok ? 0 : -1;
+}
+
+/* fitVarSerial (:420-482) on the one-column problem: betas and S rows si. */
+static int mgwr_fit_var(const orc_problem* pb1, double bw, int adaptive, int kernel, int hat, double* beta,
+                        double* S)
+{
+    const int n = pb1->n, T = orc_threads(pb1);
+    orc_ws* ws = (orc_ws*)malloc(sizeof(orc_ws) * (size_t)T);
+    for (int t = 0; t < T; t++) ws_alloc(&ws[t], n, 1, 1);
+    int ok = 1;
+#pragma omp parallel for num_threads(T) schedule(dynamic, 1) reduction(&& : ok)
+    for (int i = 0; i < n; i++)
+    {
+        orc_ws* w = &ws[orc_thread_id()];
+        orc_distance_row(pb1, i, w->d);
+        if (orc_weight(w->d, n, bw, adaptive, kernel, w->w) != 0 || local_solve(pb1, pb1->x, 1, w) != 0)
+        {
+            ok = 0;
+            continue;
+        }
+        beta[i] = w->beta[0];
+        if (!hat) continue;
+        hat_row(pb1, pb1->x, 1, i, w);
+        for (int j = 0; j < n; j++) S[(size_t)i + (size_t)j * n] = w->si[j];
+    }
+    for (int t = 0; t < T; t++) ws_free(&ws[t]);
+    free(ws);
+    return ok ? 0 : -1;
+}
+
+/* C = A * B + A, all n x n column-major (the S * SArrayi + S update, :298-300). */
+static void mat_mul_add(int n, const double* A, const double* B, double* C)
+{
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < n; i++)
+        {
+            double s = 0.0;
+            for (int k = 0; k < n; k++) s += A[(size_t)i + (size_t)k * n] * B[(size_t)k + (size_t)j * n];
+            C[(size_t)i + (size_t)j * n] = s + A[(size_t)i + (size_t)j * n];
+        }
+}
+
+static double mgwr_rss(int n, int p, const double* x, const double* y, const double* betas)
+{
+    double s = 0.0;
+    for (int i = 0; i < n; i++)
+    {
+        double f = 0.0;
+        for (int k = 0; k < p; k++) f += betas[(size_t)i + (size_t)k * n] * x[(size_t)i + (size_t)k * n];
+        const double r = y[i] - f;
+        s += r * r;
+    }
+    return s;
+}
+
+int orc_mgwr_fit(const orc_problem* pb0, const orc_mgwr_opts* o, orc_mgwr_out* out)
+{
+    const int n = pb0->n, p = pb0->p;
+    const double maxd = orc_max_distance(pb0);
+    /* centring of the predictors (:90-99) */
+    double* xc = (double*)malloc(sizeof(double) * (size_t)n * (size_t)p);
+    memcpy(xc, pb0->x, sizeof(double) * (size_t)n * (size_t)p);
+    for (int k = o->has_intercept ? 1 : 0; k < p; k++)
+        if (o->centered[k])
+        {
+            double m = 0.0;
+            for (int i = 0; i < n; i++) m += xc[(size_t)i + (size_t)k * n];
+            m /= n;
+            for (int i = 0; i < n; i++) xc[(size_t)i + (size_t)k * n] -= m;
+        }
+    orc_problem pb = *pb0;
+    pb.x = xc;
+    double* bws = out->bws;
+    int* init = (int*)malloc(sizeof(int) * (size_t)p);
+    for (int k = 0; k < p; k++)
+    {
+        bws[k] = o->bw0[k];
+        init[k] = o->init_type[k];
+    }
+    double* yi = (double*)malloc(sizeof(double) * (size_t)n);
+    orc_problem pb1 = pb;
+    pb1.p = 1;
+    pb1.y = yi;
+    int rc = 0;
+    /* initial per-variable bandwidths (:104-133), against y itself */
+    memcpy(yi, pb0->y, sizeof(double) * (size_t)n);
+    for (int k = 0; k < p; k++)
+    {
+        if (init[k] != ORC_MGWR_INIT_NULL) continue;
+        pb1.x = xc + (size_t)k * n;
+        const int ad = o->adaptive[k];
+        const double lo = o->has_lower ? o->lower : (ad ? o->adaptive_lower : maxd / 5000.0);
+        const double hi = o->has_upper ? o->upper : (ad ? n : maxd);
+        double b;
+        if (orc_golden(&pb1, bws[k], ad, o->kernel[k], o->approach[k] == ORC_MGWR_CV ? ORC_CV : ORC_AIC, lo, hi, &b,
+                       NULL, NULL, 0) == 0)
+            bws[k] = b;
+    }
+    /* initial all-variable bandwidth (:135-155) with the first variable's weight */
+    {
+        const int ad = o->adaptive[0];
+        const double lo = o->has_lower ? o->lower : (ad ? o->adaptive_lower : maxd / 5000.0);
+        const double hi = o->has_upper ? o->upper : (ad ? n : maxd);
+        if (orc_golden(&pb, bws[0], ad, o->kernel[0], o->approach[0] == ORC_MGWR_CV ? ORC_CV : ORC_AIC, lo, hi,
+                       &out->init_bw, NULL, NULL, 0) != 0)
+        {
+            rc = -2; /* "Cannot select initial bandwidth." */
+            goto done;
+        }
+    }
+    {
+        const int hat = o->has_hat_matrix;
+        double* S0 = hat ? (double*)calloc((size_t)n * n, sizeof(double)) : NULL;
+        double* SA = hat ? (double*)calloc((size_t)p * n * n, sizeof(double)) : NULL;
+        double* S = hat ? (double*)calloc((size_t)n * n, sizeof(double)) : NULL;
+        double* SAi = hat ? (double*)malloc(sizeof(double) * (size_t)n * n) : NULL;
+        double* betas = out->betas;
+        double* resid = (double*)malloc(sizeof(double) * (size_t)n);
+        int* same = (int*)calloc((size_t)p, sizeof(int));
+        /* backfitting (:208-317) */
+        if (mgwr_fit_all(&pb, out->init_bw, o->adaptive[0], o->kernel[0], hat, betas, out->betas_se, S0, SA) != 0)
+        {
+            rc = -3;
+            goto done2;
+        }
+        for (int i = 0; i < n; i++)
+        {
+            double f = 0.0;
+            for (int k = 0; k < p; k++) f += betas[(size_t)i + (size_t)k * n] * xc[(size_t)i + (size_t)k * n];
+            resid[i] = pb0->y[i] - f;
+        }
+        double RSS0 = 0.0, RSS1 = DBL_MAX, crit = DBL_MAX;
+        for (int i = 0; i < n; i++) RSS0 += resid[i] * resid[i];
+        int iter;
+        for (iter = 1; iter <= o->max_iteration && crit > o->criterion_threshold; iter++)
+        {
+            for (int k = 0; k < p; k++)
+            {
+                const double* xk = xc + (size_t)k * n;
+                for (int i = 0; i < n; i++) yi[i] = resid[i] + betas[(size_t)i + (size_t)k * n] * xk[i];
+                pb1.x = xk;
+                if (init[k] != ORC_MGWR_INIT_SPECIFIED)
+                {
+                    const int ad = o->adaptive[k];
+                    const double lo = o->has_lower ? o->lower : (ad ? o->adaptive_lower : maxd / 5000.0);
+                    const double hi = o->has_upper ? o->upper : (ad ? n : maxd);
+                    double b = bws[k];
+                    orc_golden(&pb1, bws[k], ad, o->kernel[k], o->approach[k] == ORC_MGWR_CV ? ORC_CV : ORC_AIC, lo,
+                               hi, &b, NULL, NULL, 0);
+                    if (fabs(b - bws[k]) > o->select_threshold[k])
+                        same[k] = 0;
+                    else if (++same[k] >= o->retry_times)
+                        init[k] = ORC_MGWR_INIT_SPECIFIED;
+                    bws[k] = b;
+                }
+                double* bk = betas + (size_t)k * n;
+                if (mgwr_fit_var(&pb1, bws[k], o->adaptive[k], o->kernel[k], hat, bk, S) != 0)
+                {
+                    rc = -3;
+                    goto done2;
+                }
+                if (hat)
+                {
+                    double* SAk = SA + (size_t)k * n * n;
+                    for (size_t e = 0; e < (size_t)n * n; e++) SAi[e] = SAk[e] - S0[e];
+                    mat_mul_add(n, S, SAi, SAk);
+                    for (size_t e = 0; e < (size_t)n * n; e++) S0[e] = SAk[e] - SAi[e];
+                }
+                for (int i = 0; i < n; i++)
+                {
+                    double f = 0.0;
+                    for (int q = 0; q < p; q++) f += betas[(size_t)i + (size_t)q * n] * xc[(size_t)i + (size_t)q * n];
+                    resid[i] = pb0->y[i] - f;
+                }
+            }
+            RSS1 = mgwr_rss(n, p, xc, pb0->y, betas);
+            crit = o->criterion_type == ORC_MGWR_CVR ? fabs(RSS1 - RSS0) : sqrt(fabs(RSS1 - RSS0) / RSS1);
+            RSS0 = RSS1;
+        }
+        out->iterations = iter - 1;
+        out->rss = RSS0;
+        /* diagnostics (:174-180, CalcDiagnostic :41-66) */
+        double trS = 0.0, trStS = 0.0;
+        if (hat)
+        {
+            for (int i = 0; i < n; i++) trS += S0[(size_t)i + (size_t)i * n];
+            for (size_t e = 0; e < (size_t)n * n; e++) trStS += S0[e] * S0[e];
+        }
+        out->shat[0] = trS;
+        out->shat[1] = trStS;
+        double ym = 0.0, tss = 0.0;
+        for (int i = 0; i < n; i++) ym += pb0->y[i];
+        ym /= n;
+        for (int i = 0; i < n; i++) tss += (pb0->y[i] - ym) * (pb0->y[i] - ym);
+        const double nn = (double)n;
+        const double edf = nn - 2 * trS + trStS;
+        out->diag[0] = RSS0;
+        out->diag[1] = nn * log(RSS0 / nn) + nn * log(2 * M_PI) + nn * ((nn + trS) / (nn - 2 - trS));
+        out->diag[2] = 2 * trS - trStS;
+        out->diag[3] = edf;
+        out->diag[4] = 1 - RSS0 / tss;
+        out->diag[5] = 1 - (1 - out->diag[4]) * (nn - 1) / (edf - 1);
+    done2:
+        free(S0);
+        free(SA);
+        free(S);
+        free(SAi);
+        free(resid);
+        free(same);
+    }
+done:
+    free(xc);
+    free(init);
+    free(yi);
+    return rc;
+}

@@ -93,6 +93,43 @@ void orc_diagnostic(const orc_problem* pb, const double* betas, const double* sh
 /* Local Cholesky inverse of an SPD p x p matrix in place (inv_sympd); 0 or -1. */
 int orc_inv_sympd(double* a, int p);
 
+/* GWRMultiscale::fit (serial forms). */
+#define ORC_MGWR_INIT_NULL 0
+#define ORC_MGWR_INIT_INITIAL 1
+#define ORC_MGWR_INIT_SPECIFIED 2
+#define ORC_MGWR_CV 0
+#define ORC_MGWR_AIC 1
+#define ORC_MGWR_CVR 0
+#define ORC_MGWR_DCVR 1
+typedef struct orc_mgwr_opts
+{
+    const int* adaptive;           /* per variable */
+    const int* kernel;
+    const double* bw0;             /* initial bandwidths */
+    const int* init_type;          /* ORC_MGWR_INIT_* */
+    const int* approach;           /* ORC_MGWR_CV / ORC_MGWR_AIC */
+    const int* centered;
+    const double* select_threshold;
+    int retry_times, max_iteration, criterion_type;
+    double criterion_threshold;
+    int adaptive_lower;
+    int has_lower, has_upper;
+    double lower, upper;
+    int has_hat_matrix, has_intercept;
+} orc_mgwr_opts;
+typedef struct orc_mgwr_out
+{
+    double* betas;     /* n x p */
+    double* betas_se;  /* n x p (hat matrix only) */
+    double* bws;       /* p */
+    double init_bw;
+    double shat[2];
+    double rss;
+    double diag[6];    /* RSS, AICc, ENP, EDF, R2, adjusted R2 */
+    int iterations;
+} orc_mgwr_out;
+int orc_mgwr_fit(const orc_problem* pb, const orc_mgwr_opts* o, orc_mgwr_out* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -55,6 +55,23 @@ class _Problem(ctypes.Structure):
                 ("geographic", ctypes.c_int), ("gc_mode", ctypes.c_int), ("threads", ctypes.c_int)]
 
 
+class _MgwrOpts(ctypes.Structure):
+    _IP, _DP = ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)
+    _fields_ = [("adaptive", _IP), ("kernel", _IP), ("bw0", _DP), ("init_type", _IP), ("approach", _IP),
+                ("centered", _IP), ("select_threshold", _DP), ("retry_times", ctypes.c_int),
+                ("max_iteration", ctypes.c_int), ("criterion_type", ctypes.c_int),
+                ("criterion_threshold", ctypes.c_double), ("adaptive_lower", ctypes.c_int),
+                ("has_lower", ctypes.c_int), ("has_upper", ctypes.c_int), ("lower", ctypes.c_double),
+                ("upper", ctypes.c_double), ("has_hat_matrix", ctypes.c_int), ("has_intercept", ctypes.c_int)]
+
+
+class _MgwrOut(ctypes.Structure):
+    _DP = ctypes.POINTER(ctypes.c_double)
+    _fields_ = [("betas", _DP), ("betas_se", _DP), ("bws", _DP), ("init_bw", ctypes.c_double),
+                ("shat", ctypes.c_double * 2), ("rss", ctypes.c_double), ("diag", ctypes.c_double * 6),
+                ("iterations", ctypes.c_int)]
+
+
 def lib():
     global _lib
     with _lock:
@@ -85,6 +102,8 @@ def lib():
             L.orc_fit_core.argtypes = [P, d, i, i, i, dp, dp, dp, dp, dp]
             L.orc_predict.restype = i
             L.orc_predict.argtypes = [P, i, dp, d, i, i, dp]
+            L.orc_mgwr_fit.restype = i
+            L.orc_mgwr_fit.argtypes = [P, ctypes.POINTER(_MgwrOpts), ctypes.POINTER(_MgwrOut)]
             L.orc_golden.restype = i
             L.orc_golden.argtypes = [P, d, i, i, i, d, d, dp, dp, dp, i]
             L.orc_diagnostic.argtypes = [P, dp, dp, dp]
@@ -165,6 +184,32 @@ class Problem:
         if rc != 0:
             raise RuntimeError("inv_sympd(): matrix is singular or not positive definite")
         return betas
+
+    def mgwr(self, bw0, adaptive, kernel, init_type, approach, centered, select_threshold, retry_times=5,
+             max_iteration=500, criterion_type=1, criterion_threshold=1e-6, adaptive_lower=10, lower=None,
+             upper=None, hat_matrix=True, intercept=True):
+        """GWRMultiscale::fit: per-variable lists (one entry per column of X).
+        init_type 0 Null / 1 Initial / 2 Specified; approach 0 CV / 1 AIC;
+        criterion_type 0 CVR / 1 dCVR.  Returns a dict of the outputs."""
+        n, p = self.n, self.p
+        ia = lambda v: (ctypes.c_int * p)(*[int(t) for t in v])
+        da = lambda v: (ctypes.c_double * p)(*[float(t) for t in v])
+        o = _MgwrOpts(ia(adaptive), ia(kernel), da(bw0), ia(init_type), ia(approach), ia(centered),
+                      da(select_threshold), int(retry_times), int(max_iteration), int(criterion_type),
+                      float(criterion_threshold), int(adaptive_lower), int(lower is not None),
+                      int(upper is not None), float(lower or 0.0), float(upper or 0.0), int(hat_matrix),
+                      int(intercept))
+        betas = np.zeros((n, p), order="F")
+        se = np.zeros((n, p), order="F")
+        bws = np.zeros(p)
+        out = _MgwrOut(_dp(betas), _dp(se), _dp(bws), 0.0, (ctypes.c_double * 2)(), 0.0, (ctypes.c_double * 6)(), 0)
+        rc = lib().orc_mgwr_fit(self.ref, ctypes.byref(o), ctypes.byref(out))
+        if rc != 0:
+            raise RuntimeError(f"orc_mgwr_fit failed ({rc})")
+        d = list(out.diag)
+        return {"betas": betas, "betas_se": se, "bandwidths": bws, "init_bw": out.init_bw, "shat": list(out.shat),
+                "rss": out.rss, "iterations": out.iterations,
+                "diagnostic": dict(zip(["RSS", "AICc", "ENP", "EDF", "RSquare", "RSquareAdjust"], d))}
 
     def golden(self, bw0, adaptive, kernel, criterion, lower, upper, cap=512):
         bw = np.zeros(1)

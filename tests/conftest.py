@@ -29,3 +29,29 @@ def londonhp():
     y = data[:, 0].copy()
     x = np.column_stack([np.ones(len(y)), data[:, 1:4]])
     return {"coords": coords, "x": x, "y": y, "expected": g["expected"], "tol": g["tolerance_abs"]}
+
+
+def mgwr_kwargs(case, p):
+    """Oracle / engine keyword arguments of one MGWR known-answer case of the golden
+    fixture (per-variable lists of length p)."""
+    init = {"Null": 0, "Initial": 1, "Specified": 2}[case["init"]]
+    approach = {"CV": 0, "AIC": 1}[case["approach"]]
+    return dict(bw0=[case["bw0"]] * p, adaptive=[int(case["adaptive"])] * p, kernel=[2] * p,
+                init_type=[init] * p, approach=[approach] * p,
+                centered=[int(c) for c in case["centered"]],
+                select_threshold=[case["select_threshold"]] * p, retry_times=case["retry_times"],
+                criterion_type={"CVR": 0, "dCVR": 1}[case["criterion"]],
+                lower=case.get("lower"), upper=case.get("upper"), hat_matrix=case["hat_matrix"])
+
+
+@pytest.fixture(scope="session")
+def londonhp_mgwr():
+    """The londonhp100 fixture as test/testGWRMultiscale.cpp:31-32 uses it:
+    y = PURCHASE, X = [1, FLOORSZ, PROF], with that file's known answers."""
+    with open(os.path.join(ROOT, "tests", "golden", "londonhp100.json")) as f:
+        g = json.load(f)
+    coords = np.array(g["coords"], dtype=np.float64)
+    data = np.array(g["data"], dtype=np.float64)
+    y = data[:, 0].copy()
+    x = np.column_stack([np.ones(len(y)), data[:, 1], data[:, 3]])
+    return {"coords": coords, "x": x, "y": y, "cases": g["mgwr"], "tol": g["mgwr_tolerance_abs"]}

@@ -62,14 +62,66 @@ def main(ref="/root/reference"):
             "RSquare": 0.706143867720706, "RSquareAdjust": 0.678982114793865,
         },
     }
+    # test/testGWRMultiscale.cpp:31-32: y = PURCHASE, x = [1, FLOORSZ, PROF]; every section
+    # uses a bisquare kernel, centres the two non-intercept columns and a select threshold of
+    # 1e-5 per variable.  Bandwidths are asserted to 0.1 (fixed) or exactly (adaptive), the
+    # diagnostics to 1e-6.  "criterion" is the back-fitting convergence measure; sections that
+    # do not set it use the default, dCVR.
+    mgwr_common = {"x_columns": [1, 3], "y_column": 0, "kernel": "bisquare",
+                   "centered": [False, True, True], "select_threshold": 1e-5}
+    mgwr = {
+        "fixed_null_cv_hat": {
+            "source": "test/testGWRMultiscale.cpp:45-88",
+            "adaptive": False, "bw0": 0, "init": "Null", "approach": "CV",
+            "hat_matrix": True, "criterion": "dCVR", "retry_times": 0,
+            "bandwidths": [4623.78, 12665.70, 12665.70], "bandwidth_tol": 0.1,
+            "AICc": 2437.09277417389, "RSquare": 0.744649364494,
+            "RSquareAdjust": 0.712344894394,
+        },
+        "adaptive_initial_aic_hat_dcvr": {
+            "source": "test/testGWRMultiscale.cpp:90-133",
+            "adaptive": True, "bw0": 36, "init": "Initial", "approach": "AIC",
+            "hat_matrix": True, "criterion": "dCVR", "retry_times": 5,
+            "bandwidths": [45, 98, 98], "bandwidth_tol": 0.1,
+            "AICc": 2437.935218705351, "RSquare": 0.7486787930045755,
+            "RSquareAdjust": 0.7118919517893492,
+        },
+        "adaptive_null_cv_nohat": {
+            "source": "test/testGWRMultiscale.cpp:135-173",
+            "adaptive": True, "bw0": 0, "init": "Null", "approach": "CV",
+            "hat_matrix": False, "criterion": "dCVR", "retry_times": 0,
+            "bandwidths": [35, 98, 98], "bandwidth_tol": 0.0,
+            "RSquare": 0.757377391669,
+        },
+        "adaptive_initial_cv_hat_cvr": {
+            "source": "test/testGWRMultiscale.cpp:175-218",
+            "adaptive": True, "bw0": 36, "init": "Initial", "approach": "CV",
+            "hat_matrix": True, "criterion": "CVR", "retry_times": 5,
+            "bandwidths": [35, 98, 98], "bandwidth_tol": 0.0,
+            "AICc": 2438.256543496552, "RSquare": 0.757377391669,
+            "RSquareAdjust": 0.715598248225,
+        },
+        "adaptive_null_cv_hat_cvr_bounds": {
+            "source": "test/testGWRMultiscale.cpp:220-258",
+            "adaptive": True, "bw0": 36, "init": "Null", "approach": "CV",
+            "hat_matrix": True, "criterion": "CVR", "retry_times": 5,
+            "lower": 50, "upper": 100,
+            "bandwidths": [52, 99, 99], "bandwidth_tol": 0.0,
+        },
+    }
+    for case in mgwr.values():
+        for k, v in mgwr_common.items():
+            case.setdefault(k, v)
     out = {
         "about": "londonhp100 fixture of libgwmodel test/data (x, y; PURCHASE, FLOORSZ, "
-                 "UNEMPLOY, PROF) and the known answers of test/testGWRBasic.cpp; "
-                 "generated by tests/golden/make_golden.py",
+                 "UNEMPLOY, PROF) and the known answers of test/testGWRBasic.cpp and "
+                 "test/testGWRMultiscale.cpp; generated by tests/golden/make_golden.py",
         "tolerance_abs": 1e-8,
         "coords": coords,
         "data": data,
         "expected": expected,
+        "mgwr_tolerance_abs": 1e-6,
+        "mgwr": mgwr,
     }
     with open(os.path.join(HERE, "londonhp100.json"), "w") as f:
         json.dump(out, f, indent=1)
