@@ -129,6 +129,63 @@ int gwgpu_gwr_selected_vars(gwgpu_gwr* g, int* count, int* vars);
 /* indepVarsSelectionCriterionList(): entry i has lens[i] variables starting at vars[offset]. */
 int gwgpu_gwr_var_criterion_list(gwgpu_gwr* g, int* count, int* total_vars, int* lens, int* vars, double* value);
 
+/* -------------------------------------------------- GWRMultiscale surface */
+
+/* gwm::GWRMultiscale (include/gwmodelpp/GWRMultiscale.h:35-1040): multiscale
+   GWR by back-fitting.  Per-variable arrays have p entries, p = the columns of
+   X given to gwgpu_mgwr_set_independent_variables (set X first). */
+typedef struct gwgpu_mgwr gwgpu_mgwr;
+
+/* BandwidthInitilizeType, BandwidthSelectionCriterionType, BackFittingCriterionType */
+#define GWGPU_MGWR_INIT_NULL 0
+#define GWGPU_MGWR_INIT_INITIAL 1
+#define GWGPU_MGWR_INIT_SPECIFIED 2
+#define GWGPU_MGWR_CV 0
+#define GWGPU_MGWR_AIC 1
+#define GWGPU_MGWR_CVR 0
+#define GWGPU_MGWR_DCVR 1
+
+int gwgpu_mgwr_create(gwgpu_mgwr** out);
+void gwgpu_mgwr_destroy(gwgpu_mgwr* g);
+int gwgpu_mgwr_set_coords(gwgpu_mgwr* g, int n, const double* coords /* n x 2 */);
+int gwgpu_mgwr_set_dependent_variable(gwgpu_mgwr* g, int n, const double* y);
+int gwgpu_mgwr_set_independent_variables(gwgpu_mgwr* g, int n, int p, const double* x /* n x p */);
+/* setSpatialWeights: variable k gets BandwidthWeight(bandwidths[k], adaptive[k],
+   kernels[k]); every variable shares CRSDistance(geographic). */
+int gwgpu_mgwr_set_spatial_weights(gwgpu_mgwr* g, int p, const double* bandwidths, const int* adaptive,
+                                   const int* kernels, int geographic);
+int gwgpu_mgwr_set_bandwidth_initilize(gwgpu_mgwr* g, int p, const int* types);
+int gwgpu_mgwr_set_bandwidth_selection_approach(gwgpu_mgwr* g, int p, const int* approaches);
+int gwgpu_mgwr_set_preditor_centered(gwgpu_mgwr* g, int p, const int* centered);
+int gwgpu_mgwr_set_bandwidth_select_threshold(gwgpu_mgwr* g, int p, const double* thresholds);
+int gwgpu_mgwr_set_bandwidth_select_retry_times(gwgpu_mgwr* g, int times);
+int gwgpu_mgwr_set_max_iteration(gwgpu_mgwr* g, int iterations);
+int gwgpu_mgwr_set_criterion_type(gwgpu_mgwr* g, int type);
+int gwgpu_mgwr_set_criterion_threshold(gwgpu_mgwr* g, double threshold);
+int gwgpu_mgwr_set_adaptive_lower(gwgpu_mgwr* g, int lower);
+int gwgpu_mgwr_set_golden_upper_bounds(gwgpu_mgwr* g, double value);
+int gwgpu_mgwr_set_golden_lower_bounds(gwgpu_mgwr* g, double value);
+int gwgpu_mgwr_set_has_hat_matrix(gwgpu_mgwr* g, int on);
+int gwgpu_mgwr_set_has_intercept(gwgpu_mgwr* g, int on);
+int gwgpu_mgwr_set_parallel_type(gwgpu_mgwr* g, int type);
+int gwgpu_mgwr_set_gpu_id(gwgpu_mgwr* g, int gpu);
+/* GWGPU_FP64 (default) or GWGPU_MIXED for the bandwidth searches; fits and the hat matrix stay FP64. */
+int gwgpu_mgwr_set_precision(gwgpu_mgwr* g, int precision);
+int gwgpu_mgwr_set_telegram(gwgpu_mgwr* g, const gwgpu_telegram* t);
+/* GWRMultiscale::fit().  GWGPU_OK also when cancelled: check gwgpu_mgwr_status. */
+int gwgpu_mgwr_fit(gwgpu_mgwr* g);
+int gwgpu_mgwr_status(gwgpu_mgwr* g);
+int gwgpu_mgwr_betas(gwgpu_mgwr* g, double* out /* n x p */);
+/* diag(C C^T) of the initial fit and betas / betasSE (hat matrix only; zeros otherwise) */
+int gwgpu_mgwr_betas_se(gwgpu_mgwr* g, double* out /* n x p */);
+int gwgpu_mgwr_betas_tv(gwgpu_mgwr* g, double* out /* n x p */);
+/* bandwidths of spatialWeights() after fit */
+int gwgpu_mgwr_bandwidths(gwgpu_mgwr* g, double* out /* p */);
+/* RSS, AIC (0: the reference leaves it unset), AICc, ENP, EDF, RSquare, RSquareAdjust */
+int gwgpu_mgwr_diagnostic(gwgpu_mgwr* g, double* out /* 7 */);
+/* the initial all-variable bandwidth and the back-fitting iterations run */
+int gwgpu_mgwr_info(gwgpu_mgwr* g, double* initial_bandwidth, int* iterations);
+
 /* --------------------------------------------------------- engine layer */
 
 typedef struct gwgpu_engine gwgpu_engine;

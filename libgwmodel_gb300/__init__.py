@@ -5,6 +5,7 @@ C ABI (include/gwgpu.h).  This package is its Python face.
 """
 from .gwrbasic import (BandwidthWeight, CRSDistance, Engine, GwgpuError, GWRBasic, LogLevel, Logger,
                        ParallelType, Precision, RegressionDiagnostic, SpatialWeight, Status)
+from .mgwr import GWRMultiscale
 
-__all__ = ["GWRBasic", "CRSDistance", "BandwidthWeight", "SpatialWeight", "RegressionDiagnostic", "Logger",
+__all__ = ["GWRBasic", "GWRMultiscale", "CRSDistance", "BandwidthWeight", "SpatialWeight", "RegressionDiagnostic", "Logger",
            "ParallelType", "Status", "Precision", "LogLevel", "Engine", "GwgpuError"]

@@ -116,6 +116,37 @@ SIGNATURES = [
     ("gwgpu_gwr_bandwidth_criterion_list", _i, [_vp, _ip, _dp, _dp]),
     ("gwgpu_gwr_selected_vars", _i, [_vp, _ip, _ip]),
     ("gwgpu_gwr_var_criterion_list", _i, [_vp, _ip, _ip, _ip, _ip, _dp]),
+    ("gwgpu_mgwr_create", _i, [ctypes.POINTER(_vp)]),
+    ("gwgpu_mgwr_destroy", None, [_vp]),
+    ("gwgpu_mgwr_set_coords", _i, [_vp, _i, _dp]),
+    ("gwgpu_mgwr_set_dependent_variable", _i, [_vp, _i, _dp]),
+    ("gwgpu_mgwr_set_independent_variables", _i, [_vp, _i, _i, _dp]),
+    ("gwgpu_mgwr_set_spatial_weights", _i, [_vp, _i, _dp, _ip, _ip, _i]),
+    ("gwgpu_mgwr_set_bandwidth_initilize", _i, [_vp, _i, _ip]),
+    ("gwgpu_mgwr_set_bandwidth_selection_approach", _i, [_vp, _i, _ip]),
+    ("gwgpu_mgwr_set_preditor_centered", _i, [_vp, _i, _ip]),
+    ("gwgpu_mgwr_set_bandwidth_select_threshold", _i, [_vp, _i, _dp]),
+    ("gwgpu_mgwr_set_bandwidth_select_retry_times", _i, [_vp, _i]),
+    ("gwgpu_mgwr_set_max_iteration", _i, [_vp, _i]),
+    ("gwgpu_mgwr_set_criterion_type", _i, [_vp, _i]),
+    ("gwgpu_mgwr_set_criterion_threshold", _i, [_vp, _d]),
+    ("gwgpu_mgwr_set_adaptive_lower", _i, [_vp, _i]),
+    ("gwgpu_mgwr_set_golden_upper_bounds", _i, [_vp, _d]),
+    ("gwgpu_mgwr_set_golden_lower_bounds", _i, [_vp, _d]),
+    ("gwgpu_mgwr_set_has_hat_matrix", _i, [_vp, _i]),
+    ("gwgpu_mgwr_set_has_intercept", _i, [_vp, _i]),
+    ("gwgpu_mgwr_set_parallel_type", _i, [_vp, _i]),
+    ("gwgpu_mgwr_set_gpu_id", _i, [_vp, _i]),
+    ("gwgpu_mgwr_set_precision", _i, [_vp, _i]),
+    ("gwgpu_mgwr_set_telegram", _i, [_vp, ctypes.POINTER(Telegram)]),
+    ("gwgpu_mgwr_fit", _i, [_vp]),
+    ("gwgpu_mgwr_status", _i, [_vp]),
+    ("gwgpu_mgwr_betas", _i, [_vp, _dp]),
+    ("gwgpu_mgwr_betas_se", _i, [_vp, _dp]),
+    ("gwgpu_mgwr_betas_tv", _i, [_vp, _dp]),
+    ("gwgpu_mgwr_bandwidths", _i, [_vp, _dp]),
+    ("gwgpu_mgwr_diagnostic", _i, [_vp, _dp]),
+    ("gwgpu_mgwr_info", _i, [_vp, _dp, _ip]),
     ("gwgpu_engine_create", _i, [_i, ctypes.POINTER(_vp)]),
     ("gwgpu_engine_destroy", None, [_vp]),
     ("gwgpu_engine_set_data", _i, [_vp, _i, _i, _dp, _dp, _dp, _i]),

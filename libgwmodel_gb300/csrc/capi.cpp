@@ -1,14 +1,17 @@
 // capi.cpp -- extern "C" layer of include/gwgpu.h over gwm::GWRBasic and the engine.
 #include "../../include/gwgpu.h"
 
+#include <algorithm>
 #include <cfloat>
 #include <cstring>
 #include <map>
 #include <memory>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "../../include/gwmodel_gb300/GWRBasic.h"
+#include "../../include/gwmodel_gb300/GWRMultiscale.h"
 #include "engine.h"
 
 namespace {
@@ -80,6 +83,10 @@ struct gwgpu_gwr {
     bool adaptive = true;
     int kernel = GWGPU_GAUSSIAN;
     bool geographic = false;
+};
+
+struct gwgpu_mgwr {
+    gwm::GWRMultiscale alg;
 };
 
 struct gwgpu_engine {
@@ -573,6 +580,277 @@ int gwgpu_engine_tc_selftest(gwgpu_engine* e, int N, const float* A, const float
     if (!A || !B || !D) return fail(GWGPU_ERR_INVALID, "null pointer");
     if (N < 16 || N > 256 || N % 16) return fail(GWGPU_ERR_INVALID, "N must be a multiple of 16 in [16, 256]");
     return guarded([&] { e->eng.tcSelftest(N, A, B, D); });
+}
+
+// ------------------------------------------------------------------ mgwr
+
+#define MGWR_CHECK(g) \
+    if (!(g)) return fail(GWGPU_ERR_INVALID, "null handle")
+
+int gwgpu_mgwr_create(gwgpu_mgwr** out)
+{
+    if (!out) return fail(GWGPU_ERR_INVALID, "null pointer");
+    return guarded([&] { *out = new gwgpu_mgwr(); });
+}
+
+void gwgpu_mgwr_destroy(gwgpu_mgwr* g) { delete g; }
+
+int gwgpu_mgwr_set_coords(gwgpu_mgwr* g, int n, const double* coords)
+{
+    MGWR_CHECK(g);
+    if (n < 0 || (!coords && n)) return fail(GWGPU_ERR_INVALID, "bad coords");
+    return guarded([&] { g->alg.setCoords(gwm::mat(n, 2, coords)); });
+}
+
+int gwgpu_mgwr_set_dependent_variable(gwgpu_mgwr* g, int n, const double* y)
+{
+    MGWR_CHECK(g);
+    if (n < 0 || (!y && n)) return fail(GWGPU_ERR_INVALID, "bad y");
+    return guarded([&] { g->alg.setDependentVariable(gwm::vec(n, 1, y)); });
+}
+
+int gwgpu_mgwr_set_independent_variables(gwgpu_mgwr* g, int n, int p, const double* x)
+{
+    MGWR_CHECK(g);
+    if (n < 0 || p < 0 || (!x && n && p)) return fail(GWGPU_ERR_INVALID, "bad x");
+    return guarded([&] { g->alg.setIndependentVariables(gwm::mat(n, p, x)); });
+}
+
+int gwgpu_mgwr_set_spatial_weights(gwgpu_mgwr* g, int p, const double* bandwidths, const int* adaptive,
+                                   const int* kernels, int geographic)
+{
+    MGWR_CHECK(g);
+    if (p < 0 || (p && (!bandwidths || !adaptive || !kernels))) return fail(GWGPU_ERR_INVALID, "bad arrays");
+    for (int k = 0; k < p; k++)
+        if (kernels[k] < 0 || kernels[k] > 4) return fail(GWGPU_ERR_INVALID, "unknown kernel");
+    return guarded([&] {
+        std::vector<gwm::SpatialWeight> sw;
+        gwm::CRSDistance d(geographic != 0);
+        for (int k = 0; k < p; k++) {
+            gwm::BandwidthWeight w(bandwidths[k], adaptive[k] != 0, (gwm::BandwidthWeight::KernelFunctionType)kernels[k]);
+            sw.emplace_back(&w, &d);
+        }
+        g->alg.setSpatialWeights(sw);
+    });
+}
+
+int gwgpu_mgwr_set_bandwidth_initilize(gwgpu_mgwr* g, int p, const int* types)
+{
+    MGWR_CHECK(g);
+    if (p < 0 || (p && !types)) return fail(GWGPU_ERR_INVALID, "bad array");
+    for (int k = 0; k < p; k++)
+        if (types[k] < 0 || types[k] > 2) return fail(GWGPU_ERR_INVALID, "unknown initialisation type");
+    return guarded([&] {
+        std::vector<gwm::GWRMultiscale::BandwidthInitilizeType> v;
+        for (int k = 0; k < p; k++) v.push_back((gwm::GWRMultiscale::BandwidthInitilizeType)types[k]);
+        g->alg.setBandwidthInitilize(v);
+    });
+}
+
+int gwgpu_mgwr_set_bandwidth_selection_approach(gwgpu_mgwr* g, int p, const int* approaches)
+{
+    MGWR_CHECK(g);
+    if (p < 0 || (p && !approaches)) return fail(GWGPU_ERR_INVALID, "bad array");
+    for (int k = 0; k < p; k++)
+        if (approaches[k] != GWGPU_MGWR_CV && approaches[k] != GWGPU_MGWR_AIC)
+            return fail(GWGPU_ERR_INVALID, "unknown selection approach");
+    return guarded([&] {
+        std::vector<gwm::GWRMultiscale::BandwidthSelectionCriterionType> v;
+        for (int k = 0; k < p; k++) v.push_back((gwm::GWRMultiscale::BandwidthSelectionCriterionType)approaches[k]);
+        g->alg.setBandwidthSelectionApproach(v);
+    });
+}
+
+int gwgpu_mgwr_set_preditor_centered(gwgpu_mgwr* g, int p, const int* centered)
+{
+    MGWR_CHECK(g);
+    if (p < 0 || (p && !centered)) return fail(GWGPU_ERR_INVALID, "bad array");
+    std::vector<bool> v;
+    for (int k = 0; k < p; k++) v.push_back(centered[k] != 0);
+    g->alg.setPreditorCentered(v);
+    return GWGPU_OK;
+}
+
+int gwgpu_mgwr_set_bandwidth_select_threshold(gwgpu_mgwr* g, int p, const double* thresholds)
+{
+    MGWR_CHECK(g);
+    if (p < 0 || (p && !thresholds)) return fail(GWGPU_ERR_INVALID, "bad array");
+    g->alg.setBandwidthSelectThreshold(std::vector<double>(thresholds, thresholds + p));
+    return GWGPU_OK;
+}
+
+int gwgpu_mgwr_set_bandwidth_select_retry_times(gwgpu_mgwr* g, int times)
+{
+    MGWR_CHECK(g);
+    if (times < 0) return fail(GWGPU_ERR_INVALID, "negative retry times");
+    g->alg.setBandwidthSelectRetryTimes((std::size_t)times);
+    return GWGPU_OK;
+}
+
+int gwgpu_mgwr_set_max_iteration(gwgpu_mgwr* g, int iterations)
+{
+    MGWR_CHECK(g);
+    if (iterations < 0) return fail(GWGPU_ERR_INVALID, "negative iteration count");
+    g->alg.setMaxIteration((std::size_t)iterations);
+    return GWGPU_OK;
+}
+
+int gwgpu_mgwr_set_criterion_type(gwgpu_mgwr* g, int type)
+{
+    MGWR_CHECK(g);
+    if (type != GWGPU_MGWR_CVR && type != GWGPU_MGWR_DCVR) return fail(GWGPU_ERR_INVALID, "unknown criterion type");
+    g->alg.setCriterionType((gwm::GWRMultiscale::BackFittingCriterionType)type);
+    return GWGPU_OK;
+}
+
+int gwgpu_mgwr_set_criterion_threshold(gwgpu_mgwr* g, double threshold)
+{
+    MGWR_CHECK(g);
+    g->alg.setCriterionThreshold(threshold);
+    return GWGPU_OK;
+}
+
+int gwgpu_mgwr_set_adaptive_lower(gwgpu_mgwr* g, int lower)
+{
+    MGWR_CHECK(g);
+    g->alg.setAdaptiveLower(lower);
+    return GWGPU_OK;
+}
+
+int gwgpu_mgwr_set_golden_upper_bounds(gwgpu_mgwr* g, double value)
+{
+    MGWR_CHECK(g);
+    g->alg.setGoldenUpperBounds(value);
+    return GWGPU_OK;
+}
+
+int gwgpu_mgwr_set_golden_lower_bounds(gwgpu_mgwr* g, double value)
+{
+    MGWR_CHECK(g);
+    g->alg.setGoldenLowerBounds(value);
+    return GWGPU_OK;
+}
+
+int gwgpu_mgwr_set_has_hat_matrix(gwgpu_mgwr* g, int on)
+{
+    MGWR_CHECK(g);
+    g->alg.setHasHatMatrix(on != 0);
+    return GWGPU_OK;
+}
+
+int gwgpu_mgwr_set_has_intercept(gwgpu_mgwr* g, int on)
+{
+    MGWR_CHECK(g);
+    g->alg.setHasIntercept(on != 0);
+    return GWGPU_OK;
+}
+
+int gwgpu_mgwr_set_parallel_type(gwgpu_mgwr* g, int type)
+{
+    MGWR_CHECK(g);
+    g->alg.setParallelType((gwm::ParallelType)type);
+    return GWGPU_OK;
+}
+
+int gwgpu_mgwr_set_gpu_id(gwgpu_mgwr* g, int gpu)
+{
+    MGWR_CHECK(g);
+    g->alg.setGPUId(gpu);
+    return GWGPU_OK;
+}
+
+int gwgpu_mgwr_set_precision(gwgpu_mgwr* g, int precision)
+{
+    MGWR_CHECK(g);
+    if (precision != GWGPU_FP64 && precision != GWGPU_MIXED) return fail(GWGPU_ERR_INVALID, "unknown precision");
+    g->alg.setPrecision(precision == GWGPU_MIXED ? gwm::Precision::Mixed : gwm::Precision::FP64);
+    return GWGPU_OK;
+}
+
+int gwgpu_mgwr_set_telegram(gwgpu_mgwr* g, const gwgpu_telegram* t)
+{
+    MGWR_CHECK(g);
+    return guarded([&] {
+        if (t)
+            g->alg.setTelegram(std::unique_ptr<gwm::ITelegram>(new CTelegram(*t)));
+        else
+            g->alg.setTelegram(std::unique_ptr<gwm::ITelegram>(new gwm::Logger()));
+    });
+}
+
+int gwgpu_mgwr_fit(gwgpu_mgwr* g)
+{
+    MGWR_CHECK(g);
+    return guarded([&] { g->alg.fit(); });
+}
+
+int gwgpu_mgwr_status(gwgpu_mgwr* g)
+{
+    if (!g) return -1;
+    return g->alg.status() == gwm::Status::Success ? GWGPU_STATUS_SUCCESS : GWGPU_STATUS_TERMINATED;
+}
+
+static int mgwr_copy(const gwm::mat& m, std::size_t n, std::size_t p, double* out)
+{
+    if (!out) return fail(GWGPU_ERR_INVALID, "null output");
+    if (m.n_elem() == 0) {
+        std::fill(out, out + n * p, 0.0);
+        return GWGPU_OK;
+    }
+    std::copy(m.memptr(), m.memptr() + m.n_elem(), out);
+    return GWGPU_OK;
+}
+
+int gwgpu_mgwr_betas(gwgpu_mgwr* g, double* out)
+{
+    MGWR_CHECK(g);
+    return mgwr_copy(g->alg.betas(), g->alg.independentVariables().n_rows, g->alg.independentVariables().n_cols, out);
+}
+
+int gwgpu_mgwr_betas_se(gwgpu_mgwr* g, double* out)
+{
+    MGWR_CHECK(g);
+    return mgwr_copy(g->alg.betasSE(), g->alg.independentVariables().n_rows, g->alg.independentVariables().n_cols,
+                     out);
+}
+
+int gwgpu_mgwr_betas_tv(gwgpu_mgwr* g, double* out)
+{
+    MGWR_CHECK(g);
+    return mgwr_copy(g->alg.betasTV(), g->alg.independentVariables().n_rows, g->alg.independentVariables().n_cols,
+                     out);
+}
+
+int gwgpu_mgwr_bandwidths(gwgpu_mgwr* g, double* out)
+{
+    MGWR_CHECK(g);
+    if (!out) return fail(GWGPU_ERR_INVALID, "null output");
+    const auto& sw = g->alg.spatialWeights();
+    for (std::size_t k = 0; k < sw.size(); k++) out[k] = sw[k].weight()->bandwidth();
+    return GWGPU_OK;
+}
+
+int gwgpu_mgwr_diagnostic(gwgpu_mgwr* g, double* out)
+{
+    MGWR_CHECK(g);
+    if (!out) return fail(GWGPU_ERR_INVALID, "null output");
+    gwm::RegressionDiagnostic d = g->alg.diagnostic();
+    out[0] = d.RSS;
+    out[1] = d.AIC;
+    out[2] = d.AICc;
+    out[3] = d.ENP;
+    out[4] = d.EDF;
+    out[5] = d.RSquare;
+    out[6] = d.RSquareAdjust;
+    return GWGPU_OK;
+}
+
+int gwgpu_mgwr_info(gwgpu_mgwr* g, double* initial_bandwidth, int* iterations)
+{
+    MGWR_CHECK(g);
+    if (initial_bandwidth) *initial_bandwidth = g->alg.initialBandwidth();
+    if (iterations) *iterations = (int)g->alg.iterations();
+    return GWGPU_OK;
 }
 
 }  // extern "C"

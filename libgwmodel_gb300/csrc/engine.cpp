@@ -327,6 +327,103 @@ void Engine::setData(int n, int p, const double* x, const double* y, const doubl
 }
 
 
+void Engine::setVariables(int p, const double* x, const double* y)
+{
+    if (n_ == 0) throw std::logic_error("no data");
+    if (p < 1 || p > kMaxP) throw std::invalid_argument("number of independent variables must be in [1, 32]");
+    check(cudaSetDevice(device_), "cudaSetDevice");
+    const int n = n_;
+    p_ = p;
+    mm_ = p * (p + 1) / 2;
+    m_ = mm_ + p;
+    gall_valid_ = false;
+    mixed_ready_ = false;
+    hx_.resize((size_t)n * p);
+    hy_.resize(n);
+    for (int s = 0; s < n; s++) {
+        const int i = perm_[s];
+        for (int k = 0; k < p; k++) hx_[(size_t)s * p + k] = x[(size_t)i + (size_t)k * n];
+        hy_[s] = y[i];
+    }
+    x_.alloc((size_t)n * p);
+    z_.alloc((size_t)n * m_);
+    g_.alloc((size_t)n * m_);
+    beta_.alloc((size_t)n * p);
+    rvec_.alloc((size_t)n * p);
+    check(cudaMemcpyAsync(x_.get(), hx_.data(), sizeof(double) * hx_.size(), cudaMemcpyHostToDevice, stream_),
+          "H2D x");
+    check(cudaMemcpyAsync(y_.get(), hy_.data(), sizeof(double) * n, cudaMemcpyHostToDevice, stream_), "H2D y");
+    check(launch_build_z(n, p, x_.get(), y_.get(), z_.get(), stream_), "build_z");
+    stats_.kernel_launches += 1;
+    synchronize();
+}
+
+void Engine::fitDevice(double bw, bool adaptive, int kernel, bool se, double* S, double* ainv)
+{
+    if (n_ == 0) throw std::logic_error("no data");
+    check(cudaSetDevice(device_), "cudaSetDevice");
+    const int n = n_, p = p_;
+    const int saved = precision_;
+    precision_ = kFP64;
+    struct Restore {
+        int& slot;
+        int value;
+        double*& out;
+        ~Restore()
+        {
+            slot = value;
+            out = nullptr;
+        }
+    } restore{precision_, saved, ainv_out_};
+    g2_.alloc((size_t)n * mm_);
+    vvec_.alloc((size_t)n * p);
+    bse_.alloc((size_t)n * p);
+    qdiag_.alloc(n);
+    computeThresholds(bw, adaptive);
+    contract(z_.get(), m_, g_.get(), m_, bw, adaptive, kernel, false, 1);
+    if (se)
+        contract(z_.get(), mm_, g2_.get(), mm_, bw, adaptive, kernel, false, 2);
+    else  // the solve still forms the (unused) SE terms from G2
+        check(cudaMemsetAsync(g2_.get(), 0, sizeof(double) * g2_.size(), stream_), "memset G2");
+    ainv_out_ = ainv;
+    double s[4];
+    solve(kSolveFit, bw, adaptive, kernel, s);
+    if (s[3] > 0.0) throw NotSPDError("inv_sympd(): matrix is singular or not positive definite");
+    if (S) {
+        check(cudaMemsetAsync(S, 0, sizeof(double) * (size_t)n * n, stream_), "memset S");
+        check(launch_tile_far_thr(n, kTile, geographic_, thrPtr(adaptive), bw, tile_thr16_.get(), stream_),
+              "tile thr");
+        check(launch_hat_pass(points(), geographic_, tb16_.get(), tile_thr16_.get(), x_.get(), p, vvec_.get(),
+                              thrPtr(adaptive), bw, kernel, true, qdiag_.get(), S, -1, nullptr, stream_),
+              "hat pass");
+        stats_.kernel_launches += 2;
+    }
+}
+
+void Engine::hatAll(double bw, bool adaptive, int kernel, const double* ainv, double* S0, double* SA)
+{
+    check(cudaSetDevice(device_), "cudaSetDevice");
+    computeThresholds(bw, adaptive);
+    check(launch_mgwr_hat_all(points(), geographic_, x_.get(), p_, ainv, thrPtr(adaptive), bw, kernel, S0, SA,
+                              num_sms_, stream_),
+          "hat all");
+    stats_.kernel_launches += 1;
+}
+
+void Engine::copyOut(const double* dev, int cols, std::vector<double>& out)
+{
+    const int n = n_;
+    std::vector<double> h((size_t)n * cols);
+    check(cudaMemcpyAsync(h.data(), dev, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, stream_), "D2H");
+    synchronize();
+    out.assign((size_t)n * cols, 0.0);
+    for (int s = 0; s < n; s++)
+        for (int k = 0; k < cols; k++) out[(size_t)perm_[s] + (size_t)k * n] = h[(size_t)s * cols + k];
+}
+
+void Engine::betas(std::vector<double>& out) { copyOut(beta_.get(), p_, out); }
+void Engine::betasSE(std::vector<double>& out) { copyOut(bse_.get(), p_, out); }
+
 // FP32 proxy coordinates and 32-point tile bounds shared by the select and the
 // mixed path.
 void Engine::buildProxy()
@@ -742,6 +839,7 @@ void Engine::solve(int mode, double bw, bool adaptive, int kernel, double out[4]
     a.tvec = (mixed && intercept_col_ >= 0) ? tvec_.get() : nullptr;
     a.tcol = mixed ? intercept_col_ : -1;
     a.rvec = rvec_.get();
+    a.ainv = mode == kSolveFit ? ainv_out_ : nullptr;
     int nb = 0;
     check(launch_solve(a, &nb, stream_), "solve");
     check(launch_reduce_partials(partials_.get(), nb, sums_.get(), stream_), "reduce");

@@ -105,6 +105,20 @@ public:
     // Copies X (n x p column-major), y and coords (n x 2 column-major) to the
     // device in Hilbert order.
     void setData(int n, int p, const double* x, const double* y, const double* coords, bool geographic);
+    // Replaces X (n x p column-major) and y, keeping the coordinates, their
+    // order and every distance cache (thresholds, order statistics,
+    // histograms): the per-variable problems of GWRMultiscale share one geometry.
+    void setVariables(int p, const double* x, const double* y);
+    // FP64 fit that leaves its results on the device: beta, with se the
+    // diagonal of C C^T (C = A_i^-1 X^T W_i, GWRMultiscale.cpp:216-224), and,
+    // when the pointers are set, S (n x n row-major, sorted order) and the
+    // local inverses A_i^-1 (n x p x p).  Throws NotSPDError.
+    void fitDevice(double bw, bool adaptive, int kernel, bool se, double* S, double* ainv);
+    // SA_k and S0 of the initial all-variable fit from fitDevice's inverses.
+    void hatAll(double bw, bool adaptive, int kernel, const double* ainv, double* S0, double* SA);
+    // beta / betasSE of the last fitDevice, n x p column-major in the original order.
+    void betas(std::vector<double>& out);
+    void betasSE(std::vector<double>& out);
     void setPrecision(int precision) { precision_ = precision; }
     // Tiles per FP32 accumulation chunk of the tensor-core contraction (>= 2).
     void setFlushTiles(int tiles) { flush_tiles_ = tiles; }
@@ -181,6 +195,8 @@ private:
     void solve(int mode, double bw, bool adaptive, int kernel, double out[4]);
     void refine(double bw, bool adaptive, int kernel, double out[4]);
     DevPoints points() const;
+    void copyOut(const double* dev, int cols, std::vector<double>& out);
+    double* ainv_out_ = nullptr;  // fit-mode solve: where to store A_i^-1 (fitDevice)
 
     int device_ = 0;
     int num_sms_ = 0;

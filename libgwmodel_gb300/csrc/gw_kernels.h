@@ -108,6 +108,8 @@ struct SolveArgs {
     int tcol;
     // Refine mode: beta += A^-1 rvec (n x p), then the residuals are recomputed.
     const double* rvec;
+    // Fit mode, optional: A_i^-1 (n x p x p, row-major per row).
+    double* ainv;
 };
 cudaError_t launch_solve(const SolveArgs& a, int* nblocks, cudaStream_t stream);
 // Criterion solves (kSolveAIC / kSolveCV) of many segments in one launch:
@@ -216,5 +218,24 @@ cudaError_t launch_tile_far_thr(int n, int tile, bool geographic, const double* 
 // Maximum pairwise distance (CRSDistance::maxDistance), as an ordered key in *key_out.
 cudaError_t launch_max_distance(const DevPoints& P, bool geographic, unsigned long long* key_out, int num_sms,
                                 cudaStream_t stream);
+
+
+// GWRMultiscale hat matrix (k_mgwr.cu).  Matrices are n x n row-major in the
+// sorted order; SA holds p of them back to back.
+size_t mgwr_hat_all_smem(int p);
+// SA_k(i, j) = w_ij x_ik (A_i^-1 x_j)_k and S0(i, j) = sum_k SA_k(i, j) for
+// every pair (ainv: n x p x p from the fit's solve).
+cudaError_t launch_mgwr_hat_all(const DevPoints& P, bool geographic, const double* X, int p, const double* ainv,
+                                const double* thr, double bw, int kernel, double* S0, double* SA, int num_sms,
+                                cudaStream_t stream);
+// T = SA - S0 over count elements.
+cudaError_t launch_mgwr_sub(size_t count, const double* SA, const double* S0, double* T, cudaStream_t stream);
+// SA += S; S0 = SA - T over count elements.
+cudaError_t launch_mgwr_post(size_t count, double* SA, const double* S, const double* T, double* S0,
+                             cudaStream_t stream);
+// partials[4 b + 0] / [4 b + 1]: block b's share of tr(S0) and of sum S0_ij^2;
+// *nblocks receives the block count (at most max_blocks).
+cudaError_t launch_mgwr_traces(int n, const double* S0, double* partials, int max_blocks, int* nblocks,
+                               cudaStream_t stream);
 
 }  // namespace gwgpu

@@ -170,6 +170,8 @@ __global__ void __launch_bounds__(SV_WARPS * 32)
                     e = bwd_solve(L, ld, p, lane, e);
                     if (lane < p) Ainv[lane * ld + k] = e;
                 }
+                if (a.ainv && lane < p)
+                    for (int k = 0; k < p; k++) a.ainv[((size_t)row * p + lane) * p + k] = Ainv[lane * ld + k];
                 const double* g2 = a.G2 + (size_t)row * a.ldg2;
                 if (lane < p)
                     for (int c = 0; c < p; c++)

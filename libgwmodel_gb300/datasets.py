@@ -15,6 +15,9 @@ seed, so every run and every machine sees the same inputs.
 * ``config4``  a Poisson request stream: 70% fits at a given adaptive bandwidth,
                30% AICc bandwidth searches; n log-uniform [1,000, 100,000], p
                uniform {3..20}, planar or geographic 50/50, data as config 0
+* ``multiscale`` n points planar U[0,24]^2, p=3: a global intercept, a
+               coefficient that varies over the whole region and one that varies
+               locally (the standard multiscale GWR simulation), sigma=0.5
 """
 from __future__ import annotations
 
@@ -155,3 +158,20 @@ def config4(rate, count, seed=4, pool=48, n_min=1000, n_max=100000):
         bw = float(rng.integers(max(pb.p + 10, 30), min(300, pb.n - 1) + 1))
         reqs.append(StreamRequest(t, pb, kind, bw))
     return reqs
+
+
+def multiscale(n=1000, seed=5, geographic=False):
+    """Multiscale GWR problem: beta0 = 3 everywhere, beta1 = 1 + (u + v) / 12
+    (regional), beta2 = 1 + (36 - (6 - u/2)^2)(36 - (6 - v/2)^2) / 324 (local);
+    x1, x2 standard normal.  Geographic: the square mapped onto 24 x 24 degrees
+    around lon 10, lat 45."""
+    rng = np.random.default_rng(seed)
+    uv = rng.uniform(0, 24, (n, 2))
+    u, v = uv[:, 0], uv[:, 1]
+    beta = np.column_stack([np.full(n, 3.0), 1 + (u + v) / 12,
+                            1 + (36 - (6 - u / 2) ** 2) * (36 - (6 - v / 2) ** 2) / 324])
+    x = np.column_stack([np.ones(n), rng.standard_normal((n, 2))])
+    y = (x * beta).sum(axis=1) + rng.normal(0, 0.5, n)
+    coords = np.column_stack([u - 2.0, v + 33.0]) if geographic else uv
+    return Problem("multiscale", np.asfortranarray(x), y, np.asfortranarray(coords), geographic, True,
+                   KERNELS["bisquare"], 0, beta)

@@ -127,6 +127,25 @@ class Logger:
         return False
 
 
+def telegram_struct(telegram: Logger) -> Telegram:
+    """The C callbacks (gwgpu_telegram) of a Logger; keep the result alive while it is set."""
+
+    def _print(_u, msg, level, fun, file):
+        telegram.print(msg.decode(), level, fun.decode(), file.decode())
+
+    def _progress(_u, cur, tot, fun, file):
+        telegram.progress(int(cur), int(tot), fun.decode(), file.decode())
+
+    def _percent(_u, pct, fun, file):
+        telegram.progress_percent(float(pct), fun.decode(), file.decode())
+
+    def _stop(_u):
+        return 1 if telegram.stop() else 0
+
+    return Telegram(None, Telegram.PRINT(_print), Telegram.PROGRESS(_progress), Telegram.PERCENT(_percent),
+                    Telegram.STOP(_stop))
+
+
 def _f64(a, shape=None):
     a = np.asarray(a, dtype=np.float64)
     if shape is not None:
@@ -237,20 +256,7 @@ class GWRBasic:
             self._telegram = None
             return
 
-        def _print(_u, msg, level, fun, file):
-            telegram.print(msg.decode(), level, fun.decode(), file.decode())
-
-        def _progress(_u, cur, tot, fun, file):
-            telegram.progress(int(cur), int(tot), fun.decode(), file.decode())
-
-        def _percent(_u, pct, fun, file):
-            telegram.progress_percent(float(pct), fun.decode(), file.decode())
-
-        def _stop(_u):
-            return 1 if telegram.stop() else 0
-
-        t = Telegram(None, Telegram.PRINT(_print), Telegram.PROGRESS(_progress), Telegram.PERCENT(_percent),
-                     Telegram.STOP(_stop))
+        t = telegram_struct(telegram)
         self._telegram = (telegram, t)
         check(lib().gwgpu_gwr_set_telegram(self._h, ctypes.byref(t)))
 

@@ -760,9 +760,14 @@ int orc_mgwr_fit(const orc_problem* pb0, const orc_mgwr_opts* o, orc_mgwr_out* o
         const double lo = o->has_lower ? o->lower : (ad ? o->adaptive_lower : maxd / 5000.0);
         const double hi = o->has_upper ? o->upper : (ad ? n : maxd);
         double b;
+        /* BandwidthSelector::optimize throws "Invalid initial values." (BandwidthSelector.cpp:26-29) */
         if (orc_golden(&pb1, bws[k], ad, o->kernel[k], o->approach[k] == ORC_MGWR_CV ? ORC_CV : ORC_AIC, lo, hi, &b,
-                       NULL, NULL, 0) == 0)
-            bws[k] = b;
+                       NULL, NULL, 0) < 0)
+        {
+            rc = -2;
+            goto done;
+        }
+        bws[k] = b;
     }
     /* initial all-variable bandwidth (:135-155) with the first variable's weight */
     {
@@ -770,7 +775,7 @@ int orc_mgwr_fit(const orc_problem* pb0, const orc_mgwr_opts* o, orc_mgwr_out* o
         const double lo = o->has_lower ? o->lower : (ad ? o->adaptive_lower : maxd / 5000.0);
         const double hi = o->has_upper ? o->upper : (ad ? n : maxd);
         if (orc_golden(&pb, bws[0], ad, o->kernel[0], o->approach[0] == ORC_MGWR_CV ? ORC_CV : ORC_AIC, lo, hi,
-                       &out->init_bw, NULL, NULL, 0) != 0)
+                       &out->init_bw, NULL, NULL, 0) < 0)
         {
             rc = -2; /* "Cannot select initial bandwidth." */
             goto done;
@@ -810,11 +815,18 @@ int orc_mgwr_fit(const orc_problem* pb0, const orc_mgwr_opts* o, orc_mgwr_out* o
                 if (init[k] != ORC_MGWR_INIT_SPECIFIED)
                 {
                     const int ad = o->adaptive[k];
-                    const double lo = o->has_lower ? o->lower : (ad ? o->adaptive_lower : maxd / 5000.0);
-                    const double hi = o->has_upper ? o->upper : (ad ? n : maxd);
+                    /* mMaxDistances[k] is only filled for Null-initialised variables (:117); it
+                       stays 0 for the others */
+                    const double mdk = o->init_type[k] == ORC_MGWR_INIT_NULL ? maxd : 0.0;
+                    const double lo = o->has_lower ? o->lower : (ad ? o->adaptive_lower : mdk / 5000.0);
+                    const double hi = o->has_upper ? o->upper : (ad ? n : mdk);
                     double b = bws[k];
-                    orc_golden(&pb1, bws[k], ad, o->kernel[k], o->approach[k] == ORC_MGWR_CV ? ORC_CV : ORC_AIC, lo,
-                               hi, &b, NULL, NULL, 0);
+                    if (orc_golden(&pb1, bws[k], ad, o->kernel[k], o->approach[k] == ORC_MGWR_CV ? ORC_CV : ORC_AIC,
+                                   lo, hi, &b, NULL, NULL, 0) < 0)
+                    {
+                        rc = -2;
+                        goto done2;
+                    }
                     if (fabs(b - bws[k]) > o->select_threshold[k])
                         same[k] = 0;
                     else if (++same[k] >= o->retry_times)
