@@ -50,6 +50,10 @@ def parse():
     ap.add_argument("--batch", action="store_true", help="config-3 batched evaluation instead of the config-2 line")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--config1", action="store_true", help="config-1 FP64 drop-in line instead of the config-2 line")
+    ap.add_argument("--mgwr", action="store_true", help="GWRMultiscale back-fitting line instead of the config-2 line")
+    ap.add_argument("--mgwr-n", type=int, default=20000)
+    ap.add_argument("--mgwr-hat-n", type=int, default=4000)
+    ap.add_argument("--mgwr-iterations", type=int, default=10)
     ap.add_argument("--rates", default="5,20,50,200")
     ap.add_argument("--requests", type=int, default=60)
     ap.add_argument("--slots", type=int, default=8)
@@ -309,6 +313,111 @@ def run_config1(args):
     return 0
 
 
+def mgwr_fit(pb, hat, iterations, precision=0):
+    """One GWRMultiscale fit through the public C ABI from host buffers:
+    p = 3, adaptive bisquare, AICc searches, Null initialisation, the last two
+    predictors centred, back-fitting capped at `iterations`."""
+    from libgwmodel_gb300 import BandwidthWeight, CRSDistance, SpatialWeight
+    from libgwmodel_gb300.mgwr import GWRMultiscale
+    alg = GWRMultiscale()
+    alg.setCoords(pb.coords)
+    alg.setDependentVariable(pb.y)
+    alg.setIndependentVariables(pb.x)
+    alg.setSpatialWeights([SpatialWeight(BandwidthWeight(0, True, BandwidthWeight.Bisquare),
+                                         CRSDistance(pb.geographic)) for _ in range(pb.p)])
+    alg.setHasHatMatrix(hat)
+    alg.setPreditorCentered([False] + [True] * (pb.p - 1))
+    alg.setBandwidthInitilize([GWRMultiscale.Null] * pb.p)
+    alg.setBandwidthSelectionApproach([GWRMultiscale.AIC] * pb.p)
+    alg.setBandwidthSelectThreshold([1e-5] * pb.p)
+    alg.setMaxIteration(iterations)
+    alg.setPrecision(precision)
+    t0 = time.perf_counter()
+    alg.fit()
+    dt = time.perf_counter() - t0
+    return alg, dt
+
+
+def run_mgwr(args):
+    """GWRMultiscale (GWRMultiscale.cpp:68-317) on the seeded multiscale problem:
+    the whole fit (initial searches, all-variable search and fit, back-fitting
+    with a golden search and a fit per variable per iteration) timed through
+    the C ABI, beside the oracle's per-variable criterion on the host cores."""
+    rank, _, _ = dist_env()
+    if rank != 0:
+        return 0
+    from libgwmodel_gb300 import datasets
+    pb = datasets.multiscale(args.mgwr_n, seed=13)
+    for _ in range(max(args.warmup, 1)):
+        mgwr_fit(datasets.multiscale(2000, seed=14), False, 2)
+    clocks = Clocks(0)
+    clocks.start()
+    times, alg = [], None
+    for _ in range(args.steps):
+        alg, dt = mgwr_fit(pb, False, args.mgwr_iterations)
+        times.append(dt)
+    clk = clocks.stop()
+    c = alg.counters()
+    sec = float(np.median(times))
+    value = pb.n * (c["criterion_evals"] + c["fits"]) / sec
+    bws = alg.bandwidths().tolist()
+    line = {"metric": "GWRMultiscale local fits/s (n=20k planar, p=3, adaptive bisquare, AICc searches)",
+            "value": value, "unit": UNIT, "higher_is_better": True, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sec * 1e3, "dtype": "f64", "scaling": "weak", "vs_baseline": None,
+            "data": "synthetic (seeded multiscale generator, numpy PCG64 seed 13)",
+            "config": {"workload": f"multiscale: n={pb.n} planar U[0,24]^2, p=3 (global, regional, local "
+                                   f"coefficients), adaptive bisquare, AICc golden searches, Null initial "
+                                   f"bandwidths, back-fitting capped at {args.mgwr_iterations} iterations, "
+                                   f"no hat matrix",
+                       "bandwidths": bws, "initial_bandwidth": alg.initialBandwidth(),
+                       "iterations": alg.iterations(), "criterion_evals": c["criterion_evals"], "fits": c["fits"],
+                       "phase_seconds": {"search": c["search_s"], "fit": c["fit_s"]},
+                       "timing": "host wall clock around fit() (a synchronous call)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": int(pb.n * (pb.p + 3) * 8),
+                    "d2h_bytes_per_step": int(pb.n * pb.p * 8 * (c["fits"]))},
+            "gpu_launches": c["kernel_launches"], "clocks": clk}
+    # the same fit with the tensor-core criterion in the searches (fits stay FP64)
+    am, dtm = mgwr_fit(pb, False, args.mgwr_iterations, precision=1)
+    cm = am.counters()
+    line["mixed"] = {"seconds": dtm, "value": pb.n * (cm["criterion_evals"] + cm["fits"]) / dtm,
+                     "bandwidths": am.bandwidths().tolist(), "iterations": am.iterations(),
+                     "criterion_evals": cm["criterion_evals"],
+                     "max_abs_beta_diff_vs_fp64": float(np.abs(am.betas() - alg.betas()).max())}
+    # hat-matrix form on a smaller n: (p + 3) n^2 doubles resident, one DGEMM per variable update
+    if args.mgwr_hat_n > 0:
+        ph = datasets.multiscale(args.mgwr_hat_n, seed=15)
+        ah, dth = mgwr_fit(ph, True, args.mgwr_iterations)
+        ch = ah.counters()
+        nn = float(ph.n) ** 3
+        line["hat"] = {"n": ph.n, "seconds": dth, "iterations": ah.iterations(), "bandwidths": ah.bandwidths().tolist(),
+                       "hat_updates": ch["hat_updates"], "hat_seconds": ch["hat_s"],
+                       "dgemm_tflops": 2 * nn * ch["hat_updates"] / ch["hat_s"] / 1e12 if ch["hat_s"] else None,
+                       "AICc": ah.diagnostic().AICc, "phase_seconds": {"search": ch["search_s"], "fit": ch["fit_s"],
+                                                                       "hat": ch["hat_s"]}}
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        threads = os.cpu_count() or 1
+        # the reference's per-variable criterion (GWRMultiscale.cpp:560-638) on variable 2 at its selected bandwidth
+        k = 2
+        xk = np.asfortranarray(pb.x[:, k:k + 1] - pb.x[:, k].mean())
+        prob = O.Problem(xk, pb.y, pb.coords, geographic=False, threads=threads)
+        bw = float(bws[k])
+        rows = threads * 8
+        t0 = time.perf_counter()
+        prob.criterion_rows(bw, True, 2, 0, 0, rows)
+        dt = time.perf_counter() - t0
+        rows = min(pb.n, max(rows, int(rows * min(args.cpu_seconds, 20.0) / max(dt, 1e-6))))
+        t0 = time.perf_counter()
+        prob.criterion_rows(bw, True, 2, 0, 0, rows)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": rows / dt, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"{rows} local fits of the per-variable AICc criterion (p=1, bandwidth "
+                                          f"{int(bw)} of n={pb.n}) in {dt:.1f}s with {threads} OpenMP threads"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_serve(args):
     rank, _, _ = dist_env()
     if rank != 0:
@@ -521,6 +630,8 @@ def main():
         return run_batch(args)
     if args.config1:
         return run_config1(args)
+    if args.mgwr:
+        return run_mgwr(args)
     return run_ours(args)
 
 

@@ -185,6 +185,10 @@ int gwgpu_mgwr_bandwidths(gwgpu_mgwr* g, double* out /* p */);
 int gwgpu_mgwr_diagnostic(gwgpu_mgwr* g, double* out /* 7 */);
 /* the initial all-variable bandwidth and the back-fitting iterations run */
 int gwgpu_mgwr_info(gwgpu_mgwr* g, double* initial_bandwidth, int* iterations);
+/* Work of the last fit: criterion evaluations, fits, hat updates, this library's kernel
+   launches, and host seconds in the searches, the fits and the hat updates (any may be NULL). */
+int gwgpu_mgwr_counters(gwgpu_mgwr* g, long long* criterion_evals, long long* fits, long long* hat_updates,
+                        long long* kernel_launches, double* seconds /* 3 */);
 
 /* --------------------------------------------------------- engine layer */
 

@@ -100,6 +100,14 @@ public:
     double initialBandwidth() const { return mInitBandwidth; }
     // Back-fitting iterations run.
     std::size_t iterations() const { return mIterations; }
+    // Work and host wall time of the last fit() by phase: the bandwidth
+    // searches, the fits (fitAll / fitVar), and the hat-matrix updates.
+    struct Counters {
+        std::size_t criterionEvals = 0, fits = 0, hatUpdates = 0;
+        long long kernelLaunches = 0;
+        double searchSeconds = 0.0, fitSeconds = 0.0, hatSeconds = 0.0;
+    };
+    const Counters& counters() const { return mCounters; }
     // GWRMultiscale::CalcDiagnostic (GWRMultiscale.cpp:41-66); AIC, which it
     // leaves unset, is 0.
     static RegressionDiagnostic CalcDiagnostic(const mat& x, const vec& y, double trS, double trStS, double RSS);
@@ -128,6 +136,7 @@ private:
     Precision mPrecision = Precision::FP64;
     double mBandwidthLastCriterion = DBL_MAX, mInitBandwidth = 0.0, mRSS0 = 0.0;
     RegressionDiagnostic mDiagnostic{};
+    Counters mCounters;
     std::unique_ptr<ITelegram> mTelegram;
     Status mStatus = Status::Success;
     std::unique_ptr<Impl> mImpl;

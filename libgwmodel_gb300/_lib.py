@@ -147,6 +147,8 @@ SIGNATURES = [
     ("gwgpu_mgwr_bandwidths", _i, [_vp, _dp]),
     ("gwgpu_mgwr_diagnostic", _i, [_vp, _dp]),
     ("gwgpu_mgwr_info", _i, [_vp, _dp, _ip]),
+    ("gwgpu_mgwr_counters", _i, [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
+                                 ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong), _dp]),
     ("gwgpu_engine_create", _i, [_i, ctypes.POINTER(_vp)]),
     ("gwgpu_engine_destroy", None, [_vp]),
     ("gwgpu_engine_set_data", _i, [_vp, _i, _i, _dp, _dp, _dp, _i]),

@@ -853,4 +853,21 @@ int gwgpu_mgwr_info(gwgpu_mgwr* g, double* initial_bandwidth, int* iterations)
     return GWGPU_OK;
 }
 
+int gwgpu_mgwr_counters(gwgpu_mgwr* g, long long* criterion_evals, long long* fits, long long* hat_updates,
+                        long long* kernel_launches, double* seconds)
+{
+    MGWR_CHECK(g);
+    const auto& c = g->alg.counters();
+    if (criterion_evals) *criterion_evals = (long long)c.criterionEvals;
+    if (fits) *fits = (long long)c.fits;
+    if (hat_updates) *hat_updates = (long long)c.hatUpdates;
+    if (kernel_launches) *kernel_launches = c.kernelLaunches;
+    if (seconds) {
+        seconds[0] = c.searchSeconds;
+        seconds[1] = c.fitSeconds;
+        seconds[2] = c.hatSeconds;
+    }
+    return GWGPU_OK;
+}
+
 }  // extern "C"

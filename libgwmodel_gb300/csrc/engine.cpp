@@ -410,6 +410,24 @@ void Engine::hatAll(double bw, bool adaptive, int kernel, const double* ainv, do
     stats_.kernel_launches += 1;
 }
 
+void Engine::hatUpdate(double bw, bool adaptive, int kernel, const double* T, double* SA)
+{
+    if (p_ != 1) throw std::logic_error("hatUpdate needs the one-variable problem");
+    check(cudaSetDevice(device_), "cudaSetDevice");
+    const int saved = precision_;
+    precision_ = kFP64;
+    struct Restore {
+        int& slot;
+        int value;
+        ~Restore() { slot = value; }
+    } restore{precision_, saved};
+    computeThresholds(bw, adaptive);
+    check(launch_mgwr_hat_update(points(), geographic_, tb16_.get(), x_.get(), vvec_.get(), thrPtr(adaptive), bw,
+                                 kernel, T, SA, stream_),
+          "hat update");
+    stats_.kernel_launches += 1;
+}
+
 void Engine::copyOut(const double* dev, int cols, std::vector<double>& out)
 {
     const int n = n_;

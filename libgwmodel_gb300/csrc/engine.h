@@ -116,6 +116,9 @@ public:
     void fitDevice(double bw, bool adaptive, int kernel, bool se, double* S, double* ainv);
     // SA_k and S0 of the initial all-variable fit from fitDevice's inverses.
     void hatAll(double bw, bool adaptive, int kernel, const double* ainv, double* S0, double* SA);
+    // SA = S (T + I) with S the hat matrix of the last one-variable fitDevice
+    // at this bandwidth (a compact kernel), over neighbouring tiles only.
+    void hatUpdate(double bw, bool adaptive, int kernel, const double* T, double* SA);
     // beta / betasSE of the last fitDevice, n x p column-major in the original order.
     void betas(std::vector<double>& out);
     void betasSE(std::vector<double>& out);

@@ -230,7 +230,13 @@ cudaError_t launch_mgwr_hat_all(const DevPoints& P, bool geographic, const doubl
                                 cudaStream_t stream);
 // T = SA - S0 over count elements.
 cudaError_t launch_mgwr_sub(size_t count, const double* SA, const double* S0, double* T, cudaStream_t stream);
-// SA += S; S0 = SA - T over count elements.
+// SA = S (T + I) for the one-variable hat matrix S(i, j) = w_ij v_i x_j of a
+// compact kernel (bisquare, tricube, boxcar), over neighbouring data tiles only
+// (X: the variable, v: A_i^-1 x_i from the fit, both n sorted).
+cudaError_t launch_mgwr_hat_update(const DevPoints& P, bool geographic, const float4* tb16, const double* X,
+                                   const double* v, const double* thr, double bw, int kernel, const double* T,
+                                   double* SA, cudaStream_t stream);
+// SA += S (S may be null: no addition); S0 = SA - T over count elements.
 cudaError_t launch_mgwr_post(size_t count, double* SA, const double* S, const double* T, double* S0,
                              cudaStream_t stream);
 // partials[4 b + 0] / [4 b + 1]: block b's share of tr(S0) and of sum S0_ij^2;

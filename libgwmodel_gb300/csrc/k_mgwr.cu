@@ -87,6 +87,130 @@ __global__ void __launch_bounds__(HA_THREADS)
     }
 }
 
+// SA(i, c0 + c) = v_i sum_j w_ij x_j (T(j, c0 + c) + [j == c0 + c]) for the 64
+// rows of this CTA and HU_COLS columns from c0: the variable's hat matrix
+// S(i, j) = w_ij v_i x_j (v_i = x_i / sum_j w_ij x_j^2) applied to T + I, over
+// the data tiles that can hold a neighbour of a row of the CTA (compact
+// kernels only).  The weight tile is computed in shared memory, the T tile is
+// staged with the identity and the x_j scale folded in, and each thread
+// accumulates 4 rows x HU_NC columns in FP64.
+constexpr int HU_THREADS = 256;
+constexpr int HU_BM = kRowBlock;  // 64 rows
+constexpr int HU_BK = kTile;      // 16 data points
+constexpr int HU_NC = 8;
+constexpr int HU_COLS = 16 * HU_NC;  // 128 columns per CTA
+
+template <bool GEO>
+__global__ void __launch_bounds__(HU_THREADS)
+    k_mgwr_hat_update(DevPoints P, const float4* __restrict__ tb16, const double* __restrict__ X,
+                      const double* __restrict__ v, const double* __restrict__ thr, double bw, int kernel,
+                      const double* __restrict__ T, double* __restrict__ SA)
+{
+    __shared__ double sW[HU_BM][HU_BK + 1];
+    __shared__ double sT[HU_BK][HU_COLS];
+    __shared__ double sfu[HU_BM], sfv[HU_BM], sfuR[HU_BM], sfvR[HU_BM], sthr[HU_BM];
+    __shared__ double sred[HU_THREADS / 32];
+    __shared__ float4 sbound;
+    const int n = P.n;
+    const int t = threadIdx.x, tx = t & 15, ty = t >> 4;
+    const int row0 = blockIdx.x * HU_BM;
+    const int c0 = blockIdx.y * HU_COLS;
+    if (t < HU_BM) {
+        const int i = row0 + t;
+        const bool ok = i < n;
+        sfu[t] = ok ? P.u[i] : 0.0;
+        sfv[t] = ok ? P.v[i] : 0.0;
+        sfuR[t] = (GEO && ok) ? P.uR[i] : 0.0;
+        sfvR[t] = (GEO && ok) ? P.vR[i] : 0.0;
+        sthr[t] = ok ? (thr ? thr[i] : bw) : 0.0;
+    }
+    double rmax = bw;
+    if (thr) {
+        double r = (t < HU_BM && row0 + t < n) ? thr[row0 + t] : -1.0;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) r = fmax(r, __shfl_xor_sync(0xffffffffu, r, off));
+        if ((t & 31) == 0) sred[t >> 5] = r;
+    }
+    if (t == 0) sbound = tb_union<GEO>(tb16, row0 / HU_BK, (min(row0 + HU_BM, n) - 1) / HU_BK);
+    __syncthreads();
+    if (thr) {
+        rmax = sred[0];
+        for (int q = 1; q < HU_THREADS / 32; q++) rmax = fmax(rmax, sred[q]);
+    }
+    const float4 fbound = sbound;
+    const float far_thr = tb_far_threshold<GEO>(rmax);
+
+    double acc[4][HU_NC];
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+#pragma unroll
+        for (int c = 0; c < HU_NC; c++) acc[q][c] = 0.0;
+
+    const int ntiles = (n + HU_BK - 1) / HU_BK;
+    for (int tile = 0; tile < ntiles; tile++) {
+        if (tb_far<GEO>(fbound, tb16[tile], far_thr)) continue;  // uniform over the CTA
+        const int j0 = tile * HU_BK;
+        for (int e = t; e < HU_BK * HU_COLS; e += HU_THREADS) {
+            const int k = e / HU_COLS, c = e - k * HU_COLS;
+            const int j = j0 + k, col = c0 + c;
+            double val = 0.0;
+            if (j < n && col < n) val = X[j] * (T[(size_t)j * n + col] + (j == col ? 1.0 : 0.0));
+            sT[k][c] = val;
+        }
+        {
+            const int j = j0 + tx;
+            double du = 0.0, dv = 0.0, duR = 0.0, dvR = 0.0;
+            if (j < n) {
+                du = P.u[j];
+                dv = P.v[j];
+                if (GEO) {
+                    duR = P.uR[j];
+                    dvR = P.vR[j];
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int r = ty + 16 * q;
+                double w = 0.0;
+                if (j < n && row0 + r < n) {
+                    double d;
+                    if constexpr (GEO)
+                        d = gw_gc_dist(du, sfu[r], dv, sfv[r], duR, sfuR[r], dvR, sfvR[r]);
+                    else
+                        d = gw_planar_dist(du, dv, sfu[r], sfv[r]);
+                    w = gw_kernel_weight(kernel, d, sthr[r]);
+                }
+                sW[r][tx] = w;
+            }
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int k = 0; k < HU_BK; k++) {
+            double a[4], b[HU_NC];
+#pragma unroll
+            for (int q = 0; q < 4; q++) a[q] = sW[ty + 16 * q][k];
+#pragma unroll
+            for (int c = 0; c < HU_NC; c++) b[c] = sT[k][tx + 16 * c];
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+#pragma unroll
+                for (int c = 0; c < HU_NC; c++) acc[q][c] = fma(a[q], b[c], acc[q][c]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int i = row0 + ty + 16 * q;
+        if (i >= n) continue;
+        const double vi = v[i];
+#pragma unroll
+        for (int c = 0; c < HU_NC; c++) {
+            const int col = c0 + tx + 16 * c;
+            if (col < n) SA[(size_t)i * n + col] = vi * acc[q][c];
+        }
+    }
+}
+
 __global__ void k_mgwr_sub(size_t count, const double* __restrict__ SA, const double* __restrict__ S0,
                            double* __restrict__ T)
 {
@@ -98,8 +222,8 @@ __global__ void k_mgwr_post(size_t count, double* __restrict__ SA, const double*
                             const double* __restrict__ T, double* __restrict__ S0)
 {
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x) {
-        const double a = SA[e] + S[e];
-        SA[e] = a;
+        const double a = S ? SA[e] + S[e] : SA[e];
+        if (S) SA[e] = a;
         S0[e] = a - T[e];
     }
 }
@@ -166,6 +290,19 @@ cudaError_t launch_mgwr_hat_all(const DevPoints& P, bool geographic, const doubl
         raise_smem_limit((const void*)k_mgwr_hat_all<false>, smem);
         k_mgwr_hat_all<false><<<grid, HA_THREADS, smem, stream>>>(P, X, p, ainv, thr, bw, kernel, S0, SA);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mgwr_hat_update(const DevPoints& P, bool geographic, const float4* tb16, const double* X,
+                                   const double* v, const double* thr, double bw, int kernel, const double* T,
+                                   double* SA, cudaStream_t stream)
+{
+    if (kernel < GW_KERNEL_BISQUARE) return cudaErrorInvalidValue;  // compact kernels only
+    dim3 grid((P.n + HU_BM - 1) / HU_BM, (P.n + HU_COLS - 1) / HU_COLS);
+    if (geographic)
+        k_mgwr_hat_update<true><<<grid, HU_THREADS, 0, stream>>>(P, tb16, X, v, thr, bw, kernel, T, SA);
+    else
+        k_mgwr_hat_update<false><<<grid, HU_THREADS, 0, stream>>>(P, tb16, X, v, thr, bw, kernel, T, SA);
     return cudaGetLastError();
 }
 

@@ -7,16 +7,20 @@
 // and y (Engine::setVariables), so the distance caches (adaptive thresholds,
 // order statistics) built by one bandwidth search serve every later search.
 //
-// Hat matrix (GWRMultiscale.cpp:216-224, 296-301): S0, SA_k (k < p), the
-// variable's S and the scratch T = SA_k - S0 are n x n FP64 matrices resident
-// on the device in the sorted order, (p + 3) n^2 doubles in all.  The update
-// SA_k = S T + S is one DGEMM (cuBLAS) plus an elementwise pass; tr(S0) and
-// tr(S0^T S0) are reduced on the device at the end.
+// Hat matrix (GWRMultiscale.cpp:216-224, 296-301): S0, SA_k (k < p) and the
+// scratch T = SA_k - S0 are n x n FP64 matrices resident on the device in the
+// sorted order.  The update SA_k = S T + S = S (T + I) takes, for a compact
+// kernel (bisquare, tricube, boxcar), one fused kernel that forms S's entries
+// w_ij v_i x_j on the fly and visits only the rows of T within the variable's
+// bandwidth (2 n k n flops instead of 2 n^3); for gaussian and exponential
+// kernels S is materialised (one more n x n matrix) and the product is a
+// DGEMM (cuBLAS).  tr(S0) and tr(S0^T S0) are reduced on the device at the end.
 #include "../../include/gwmodel_gb300/GWRMultiscale.h"
 
 #include <cublas_v2.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <map>
 #include <stdexcept>
@@ -34,6 +38,11 @@ void cublas_check(cublasStatus_t s, const char* what)
 {
     if (s != CUBLAS_STATUS_SUCCESS)
         throw gwgpu::CudaError(std::string(what) + ": cuBLAS status " + std::to_string((int)s));
+}
+
+double now_s()
+{
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
 std::string strjoin(const std::string& sep, const std::vector<std::string>& parts)
@@ -154,6 +163,7 @@ double GWRMultiscale::bandwidthCriterion(const BandwidthWeight& w, int approach)
     }
     double value = mImpl->engine->criterion(w.bandwidth(), w.adaptive(), (int)w.kernel(),
                                             approach == CV ? gwgpu::kCV : gwgpu::kAIC);
+    mCounters.criterionEvals++;
     if (value < DBL_MAX && std::isfinite(value)) {
         if (w.adaptive())
             GW_LOG(LOG_INFO, std::string("#bandwidth-criterion ") + std::to_string(int(w.bandwidth())) + "," +
@@ -180,6 +190,12 @@ bool GWRMultiscale::selectBandwidth(std::size_t var, bool all, double lower, dou
     std::map<double, double> record;
     double xopt = w0.bandwidth();
     BandwidthWeight probe = w0;
+    const double t0 = now_s();
+    struct Clock {
+        double t0;
+        double& acc;
+        ~Clock() { acc += now_s() - t0; }
+    } clock{t0, mCounters.searchSeconds};
     bool ok = gwgpu::golden_section(
         lower, upper, w0.adaptive(),
         [&](double b) {
@@ -213,11 +229,13 @@ mat GWRMultiscale::fit()
     mStatus = Status::Success;
     mBandwidthLastCriterion = DBL_MAX;
     mIterations = 0;
+    mCounters = Counters();
     if (!mImpl->engine || mImpl->device != mGpuId) {
         mImpl->engine.reset(new gwgpu::Engine(mGpuId));
         mImpl->device = mGpuId;
     }
     gwgpu::Engine& eng = *mImpl->engine;
+    eng.resetStats();
     eng.setPrecision(mPrecision == Precision::Mixed ? gwgpu::kMixed : gwgpu::kFP64);
     GW_STOP_RETURN(mat(n, p, 0.0));
 
@@ -270,7 +288,9 @@ mat GWRMultiscale::fit()
     Impl& I = *mImpl;
     const std::size_t nn = n * n;
     if (mHasHatMatrix) {
-        const double need = 8.0 * (double)nn * (double)(p + 3) + 8.0 * (double)n * p * p;
+        bool dense = false;  // a variable with a gaussian or exponential kernel needs S materialised
+        for (const auto& sw : mSpatialWeights) dense = dense || (int)sw.weight()->kernel() < (int)BandwidthWeight::Bisquare;
+        const double need = 8.0 * (double)nn * (double)(p + 2 + (dense ? 1 : 0)) + 8.0 * (double)n * p * p;
         size_t freeb = 0, total = 0;
         gwgpu::check(cudaMemGetInfo(&freeb, &total), "cudaMemGetInfo");
         const double held = (double)(I.S0.capacityBytes() + I.SA.capacityBytes() + I.S.capacityBytes() +
@@ -281,7 +301,10 @@ mat GWRMultiscale::fit()
                                      "setHasHatMatrix(false)");
         I.S0.alloc(nn);
         I.SA.alloc(nn * p);
-        I.S.alloc(nn);
+        if (dense)
+            I.S.alloc(nn);
+        else
+            I.S.clear();
         I.T.alloc(nn);
         I.ainv.alloc(n * p * p);
         I.partials.alloc(4096 * 4);
@@ -295,15 +318,21 @@ mat GWRMultiscale::fit()
     GW_BACKFITTING("Model fitting with inital bandwidth");
     mat betas(n, p, 0.0);
     {
+        double t0 = now_s();
         eng.fitDevice(mInitBandwidth, w0.adaptive(), (int)w0.kernel(), mHasHatMatrix, nullptr,
                       mHasHatMatrix ? I.ainv.get() : nullptr);
         std::vector<double> b;
         eng.betas(b);
         std::copy(b.begin(), b.end(), betas.memptr());
+        mCounters.fits++;
+        mCounters.fitSeconds += now_s() - t0;
         if (mHasHatMatrix) {
+            t0 = now_s();
             eng.betasSE(b);
             mBetasSE = mat(n, p, b.data());
             eng.hatAll(mInitBandwidth, w0.adaptive(), (int)w0.kernel(), I.ainv.get(), I.S0.get(), I.SA.get());
+            eng.synchronize();
+            mCounters.hatSeconds += now_s() - t0;
         } else {
             mBetasSE = mat();
         }
@@ -369,20 +398,34 @@ mat GWRMultiscale::fit()
             if (mStatus != Status::Success) break;
 
             const BandwidthWeight& wk = *mSpatialWeights[k].weight();
-            eng.fitDevice(wk.bandwidth(), wk.adaptive(), (int)wk.kernel(), false, mHasHatMatrix ? I.S.get() : nullptr,
-                          nullptr);
+            const bool compact = (int)wk.kernel() >= (int)BandwidthWeight::Bisquare;
+            double t0 = now_s();
+            eng.fitDevice(wk.bandwidth(), wk.adaptive(), (int)wk.kernel(), false,
+                          (mHasHatMatrix && !compact) ? I.S.get() : nullptr, nullptr);
             std::vector<double> b;
             eng.betas(b);
             for (std::size_t i = 0; i < n; i++) betas(i, k) = b[i];
+            mCounters.fits++;
+            mCounters.fitSeconds += now_s() - t0;
             if (mHasHatMatrix) {
+                t0 = now_s();
                 double* SAk = I.SA.get() + k * nn;
                 gwgpu::check(gwgpu::launch_mgwr_sub(nn, SAk, I.S0.get(), I.T.get(), eng.stream()), "hat: T");
-                // row-major SA_k = S T  <=>  column-major SA_k^T = T^T S^T
-                cublas_check(cublasDgemm(I.blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, (int)n, (int)n, &one, I.T.get(),
-                                         (int)n, I.S.get(), (int)n, &zero, SAk, (int)n),
-                             "hat: S T");
-                gwgpu::check(gwgpu::launch_mgwr_post(nn, SAk, I.S.get(), I.T.get(), I.S0.get(), eng.stream()),
-                             "hat: S0");
+                if (compact) {
+                    eng.hatUpdate(wk.bandwidth(), wk.adaptive(), (int)wk.kernel(), I.T.get(), SAk);
+                    gwgpu::check(gwgpu::launch_mgwr_post(nn, SAk, nullptr, I.T.get(), I.S0.get(), eng.stream()),
+                                 "hat: S0");
+                } else {
+                    // row-major SA_k = S T  <=>  column-major SA_k^T = T^T S^T
+                    cublas_check(cublasDgemm(I.blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, (int)n, (int)n, &one,
+                                             I.T.get(), (int)n, I.S.get(), (int)n, &zero, SAk, (int)n),
+                                 "hat: S T");
+                    gwgpu::check(gwgpu::launch_mgwr_post(nn, SAk, I.S.get(), I.T.get(), I.S0.get(), eng.stream()),
+                                 "hat: S0");
+                }
+                eng.synchronize();
+                mCounters.hatUpdates++;
+                mCounters.hatSeconds += now_s() - t0;
             }
             fitted_resid(resid);
         }
@@ -421,6 +464,11 @@ mat GWRMultiscale::fit()
         trStS = h[1];
     }
     mDiagnostic = CalcDiagnostic(x, mY, trS, trStS, mRSS0);
+    // this library's kernels (the DGEMMs are cuBLAS's): the engine's (including
+    // the sparse hat updates), plus the two elementwise passes of each hat
+    // update and the final trace reduction
+    mCounters.kernelLaunches =
+        eng.stats().kernel_launches + (mHasHatMatrix ? 2 * (long long)mCounters.hatUpdates + 2 : 0);
     mBetas = betas;
     if (mHasHatMatrix) {
         mBetasTV = mat(n, p, 0.0);

@@ -206,5 +206,15 @@ class GWRMultiscale:
         check(lib().gwgpu_mgwr_info(self._h, ctypes.byref(b), ctypes.byref(it)))
         return it.value
 
+    def counters(self):
+        """Work of the last fit: criterion evaluations, fits, hat updates, kernel
+        launches and host seconds by phase (search, fit, hat)."""
+        ll = [ctypes.c_longlong() for _ in range(4)]
+        sec = np.zeros(3)
+        check(lib().gwgpu_mgwr_counters(self._h, *[ctypes.byref(v) for v in ll], dptr(sec)))
+        return {"criterion_evals": ll[0].value, "fits": ll[1].value, "hat_updates": ll[2].value,
+                "kernel_launches": ll[3].value, "search_s": float(sec[0]), "fit_s": float(sec[1]),
+                "hat_s": float(sec[2])}
+
 
 __all__ = ["GWRMultiscale", "CRSDistance", "BandwidthWeight", "SpatialWeight"]

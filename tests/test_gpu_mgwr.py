@@ -100,23 +100,36 @@ def assert_parity(alg, ref, hat=True, rtol=1e-8, capped=None):
     """capped: the iteration limit when it, not convergence, ends the run.  A
     convergence test at 1e-6 on dCVR compares RSS changes of 1e-12 relative,
     which FP64 summation order alone can move by a few iterations, so the count
-    is only compared when the limit ends both runs."""
+    is only compared when the limit ends both runs.
+
+    Adaptive bandwidths are integers and must be identical.  A fixed bandwidth
+    is the end point of a continuous golden search whose last steps compare
+    criteria differing by ~1e-12 relative, where the last-ulp differences of
+    any other summation order decide the branch: it is held to the search's own
+    resolution, 1e-6 relative (the reference's tests allow 0.1 absolute), and
+    the coefficients to the same."""
     if alg.spatialWeights()[0].weight().adaptive():
         np.testing.assert_array_equal(alg.bandwidths(), ref["bandwidths"])
     else:
-        np.testing.assert_allclose(alg.bandwidths(), ref["bandwidths"], rtol=1e-9)
+        np.testing.assert_allclose(alg.bandwidths(), ref["bandwidths"], rtol=1e-6)
+        rtol = max(rtol, 1e-6)
     if capped is not None:
         assert alg.iterations() == ref["iterations"] == capped
-    assert alg.initialBandwidth() == pytest.approx(ref["init_bw"], rel=1e-12)
+    adaptive = alg.spatialWeights()[0].weight().adaptive()
+    assert alg.initialBandwidth() == pytest.approx(ref["init_bw"], rel=1e-12 if adaptive else 1e-6)
     b, rb = alg.betas(), ref["betas"]
     scale = np.abs(rb).max(axis=0) + 1e-300
     assert (np.abs(b - rb) / scale).max() <= rtol
     d = alg.diagnostic()
     rd = ref["diagnostic"]
-    assert d.RSS == pytest.approx(rd["RSS"], rel=1e-9)
+    drel = 1e-9 if adaptive else 1e-7
+    assert d.RSS == pytest.approx(rd["RSS"], rel=drel)
     if hat:
         for key in ("AICc", "ENP", "EDF", "RSquare", "RSquareAdjust"):
-            assert getattr(d, key) == pytest.approx(rd[key], rel=1e-9), key
+            # ENP / EDF are traces of S0, which holds one update per variable per iteration:
+            # with a fixed bandwidth the runs may stop a few iterations apart
+            tol = drel if adaptive or key not in ("ENP", "EDF") else 1e-6
+            assert getattr(d, key) == pytest.approx(rd[key], rel=tol), key
         se, rse = alg.betasSE(), ref["betas_se"]
         assert (np.abs(se - rse) / (np.abs(rse).max(axis=0) + 1e-300)).max() <= rtol
 
