@@ -292,13 +292,12 @@ private:
         const size_t S = segs_.size();
         err_.alloc(2);
         // offsets of every per-row array
-        std::vector<size_t> off_row(S + 1, 0), off_g(S + 1, 0), off_acc(S + 1, 0), off_beta(S + 1, 0);
+        std::vector<size_t> off_row(S + 1, 0), off_g(S + 1, 0), off_acc(S + 1, 0);
         for (size_t s = 0; s < S; s++) {
             const Engine& e = *eng_[segs_[s].q];
             off_row[s + 1] = off_row[s] + e.n_;
             off_g[s + 1] = off_g[s] + (size_t)e.n_ * e.m_;
             off_acc[s + 1] = off_acc[s] + (precision_ == kMixed ? (size_t)e.n_ * e.npad_ : 0);
-            off_beta[s + 1] = off_beta[s] + (size_t)e.n_ * e.p_;
         }
         rows_total_ = off_row[S];
         seg_g_.resize(S);
@@ -307,7 +306,6 @@ private:
         G_.alloc(off_g[S]);
         for (size_t s = 0; s < S; s++) seg_g_[s] = G_.get() + off_g[s];
         acc_.alloc(std::max<size_t>(off_acc[S], 1));
-        beta_.alloc(off_beta[S]);
         sii_.alloc(off_row[S]);
         resid_.alloc(off_row[S]);
         const int R = tune_.solve_rows;
@@ -422,7 +420,7 @@ private:
             a.y = mixed ? e.ys_.get() : e.y_.get();
             a.thr = adaptive_ ? thr_.get() + off_row[s] : nullptr;
             a.bw = segs_[s].bw;
-            a.beta = beta_.get() + off_beta[s];
+            a.beta = nullptr;  // criteria only: no coefficients
             a.sii = sii_.get() + off_row[s];
             a.resid = resid_.get() + off_row[s];
             a.partials = part_.get() + (size_t)first[s] * 4;
@@ -511,7 +509,7 @@ private:
     cudaGraph_t graph_ = nullptr;
     cudaGraphExec_t exec_ = nullptr;
 
-    DevBuf<double> thr_, G_, beta_, sii_, resid_, part_, sums_;
+    DevBuf<double> thr_, G_, sii_, resid_, part_, sums_;
     DevBuf<float> thr32_;
     DevBuf<float2> acc_;
     DevBuf<int> err_, d_first_;

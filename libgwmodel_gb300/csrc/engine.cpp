@@ -847,7 +847,8 @@ void Engine::solve(int mode, double bw, bool adaptive, int kernel, double out[4]
     a.y = mixed ? ys_.get() : y_.get();
     a.thr = thrPtr(adaptive);
     a.bw = bw;
-    a.beta = beta_.get();
+    // the criteria need no coefficients (the solve then skips the backward substitution)
+    a.beta = (mode == kSolveAIC || mode == kSolveCV) ? nullptr : beta_.get();
     a.sii = sii_.get();
     a.resid = resid_.get();
     a.v = vvec_.get();
@@ -1292,7 +1293,7 @@ double Engine::globalCriterion(const std::vector<int>& cols)
     a.y = y_.get();
     a.thr = nullptr;
     a.bw = 1.0;
-    a.beta = beta_.get();
+    a.beta = nullptr;
     a.sii = sii_.get();
     a.resid = resid_.get();
     a.partials = partials_.get();

@@ -62,6 +62,25 @@ __device__ __forceinline__ double fwd_solve(const double* L, int ld, int p, int 
     return v;
 }
 
+// Two forward substitutions with the same factor in one pass (the same
+// arithmetic as two fwd_solve calls, interleaved for latency).
+__device__ __forceinline__ void fwd_solve2(const double* L, int ld, int p, int lane, double& v1, double& v2)
+{
+    for (int j = 0; j < p; j++) {
+        const double ljj = L[j * ld + j];
+        const double z1 = __shfl_sync(FULL, v1, j) * ljj;
+        const double z2 = __shfl_sync(FULL, v2, j) * ljj;
+        if (lane == j) {
+            v1 = z1;
+            v2 = z2;
+        } else if (lane > j && lane < p) {
+            const double l = L[lane * ld + j];
+            v1 -= l * z1;
+            v2 -= l * z2;
+        }
+    }
+}
+
 // Backward substitution L^T x = rhs.
 __device__ __forceinline__ double bwd_solve(const double* L, int ld, int p, int lane, double rhs)
 {
@@ -106,30 +125,64 @@ __global__ void __launch_bounds__(SV_WARPS * 32)
         const double bvec = lane < p ? g[mm + lane] : 0.0;
         const double xr = (MODE != kSolvePredict && lane < p) ? a.X[(size_t)row * p + lane] : 0.0;
         __syncwarp();
-        // Cholesky-Crout, lane r owns row r
+        // Right-looking Cholesky: after column j is scaled, the trailing
+        // triangle (j < c <= r < p) takes A_rc -= L_rj L_cj with its
+        // (p-1-j)(p-j)/2 elements spread over all 32 lanes.  Every element sees
+        // the same subtractions in the same order as a left-looking (Crout)
+        // factorisation, so the factor is the same to the bit.
         bool fail = false;
         for (int j = 0; j < p; j++) {
-            double t = 0.0;
-            if (lane >= j && lane < p) {
-                t = L[lane * ld + j];
-                for (int k = 0; k < j; k++) t -= L[lane * ld + k] * L[j * ld + k];
-            }
-            double tjj = __shfl_sync(FULL, t, j);
+            const double tjj = L[j * ld + j];
             if (!(tjj > 0.0)) { fail = true; break; }
             const double rinv = rsqrt(tjj);  // 1 / L_jj
             __syncwarp();
             if (lane == j) L[j * ld + j] = rinv;
-            else if (lane > j && lane < p) L[lane * ld + j] = t * rinv;
+            else if (lane > j && lane < p) L[lane * ld + j] *= rinv;
+            __syncwarp();
+            const int m = p - 1 - j, tri = m * (m + 1) / 2;
+            for (int e = lane; e < tri; e += 32) {
+                // e -> (rr, cc), cc <= rr: rr = floor((sqrt(8e + 1) - 1) / 2), exact for e < 528
+                const int rr = (int)((sqrtf((float)(8 * e + 1)) - 1.0f) * 0.5f);
+                const int cc = e - rr * (rr + 1) / 2;
+                const int r = j + 1 + rr, c = j + 1 + cc;
+                L[r * ld + c] -= L[r * ld + j] * L[c * ld + j];
+            }
             __syncwarp();
         }
         if (fail) {
-            if (lane < p) a.beta[(size_t)row * p + lane] = __longlong_as_double(0x7ff8000000000000ll);
+            if (a.beta && lane < p) a.beta[(size_t)row * p + lane] = __longlong_as_double(0x7ff8000000000000ll);
             if (lane == 0) {
                 acc_f += 1.0;
                 if (MODE != kSolvePredict) {
                     a.resid[row] = __longlong_as_double(0x7ff8000000000000ll);
                     a.sii[row] = 0.0;
                 }
+            }
+            __syncwarp();
+            continue;
+        }
+        if (MODE == kSolveAIC || MODE == kSolveCV) {
+            // z = L^-1 b and u = L^-1 x_i: yhat_i = x_i^T A^-1 b = u . z and
+            // x_i^T A^-1 x_i = u . u, so the criterion needs no backward
+            // substitution; beta only when the caller asks for it
+            double z = bvec, u = xr;
+            fwd_solve2(L, ld, p, lane, z, u);
+            const double yhat = warp_sum(lane < p ? u * z : 0.0);
+            const double res = a.y[row] - yhat;
+            double sii = 0.0;
+            if (MODE == kSolveAIC) {
+                const double uu = warp_sum(lane < p ? u * u : 0.0);
+                sii = gw_kernel_weight(a.kernel, 0.0, a.thr ? a.thr[row] : a.bw) * uu;
+            }
+            if (a.beta) {
+                const double beta = bwd_solve(L, ld, p, lane, z);
+                if (lane < p) a.beta[(size_t)row * p + lane] = beta;
+            }
+            if (lane == 0) {
+                a.sii[row] = sii;
+                a.resid[row] = res;
+                acc_s += sii;
+                acc_r += res * res;
             }
             __syncwarp();
             continue;
