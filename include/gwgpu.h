@@ -129,6 +129,23 @@ int gwgpu_gwr_selected_vars(gwgpu_gwr* g, int* count, int* vars);
 /* indepVarsSelectionCriterionList(): entry i has lens[i] variables starting at vars[offset]. */
 int gwgpu_gwr_var_criterion_list(gwgpu_gwr* g, int* count, int* total_vars, int* lens, int* vars, double* value);
 
+/* ------------------------------------------------------------ CSV input */
+
+/* A comma-separated file with a header row of column names (quoted or not) and
+   numeric rows, as the reference's callers load with Armadillo's csv_name
+   (test/data/londonhp100.cpp:6-26).  Rows are parsed on all host threads;
+   blank lines are skipped; an empty or non-numeric cell fails with its line
+   number in gwgpu_last_error(). */
+typedef struct gwgpu_table gwgpu_table;
+int gwgpu_csv_read(const char* path, gwgpu_table** out);
+int gwgpu_table_shape(const gwgpu_table* t, int* rows, int* cols);
+/* Name of column col (NULL when out of range). */
+const char* gwgpu_table_column_name(const gwgpu_table* t, int col);
+/* The named columns into out, rows x ncol column-major: the layout of the
+   coords / X / y setters. */
+int gwgpu_table_columns(const gwgpu_table* t, int ncol, const char* const* names, double* out);
+void gwgpu_table_destroy(gwgpu_table* t);
+
 /* -------------------------------------------------- GWRMultiscale surface */
 
 /* gwm::GWRMultiscale (include/gwmodelpp/GWRMultiscale.h:35-1040): multiscale

@@ -116,6 +116,11 @@ SIGNATURES = [
     ("gwgpu_gwr_bandwidth_criterion_list", _i, [_vp, _ip, _dp, _dp]),
     ("gwgpu_gwr_selected_vars", _i, [_vp, _ip, _ip]),
     ("gwgpu_gwr_var_criterion_list", _i, [_vp, _ip, _ip, _ip, _ip, _dp]),
+    ("gwgpu_csv_read", _i, [ctypes.c_char_p, ctypes.POINTER(_vp)]),
+    ("gwgpu_table_shape", _i, [_vp, _ip, _ip]),
+    ("gwgpu_table_column_name", ctypes.c_char_p, [_vp, _i]),
+    ("gwgpu_table_columns", _i, [_vp, _i, ctypes.POINTER(ctypes.c_char_p), _dp]),
+    ("gwgpu_table_destroy", None, [_vp]),
     ("gwgpu_mgwr_create", _i, [ctypes.POINTER(_vp)]),
     ("gwgpu_mgwr_destroy", None, [_vp]),
     ("gwgpu_mgwr_set_coords", _i, [_vp, _i, _dp]),

@@ -19,7 +19,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgwgpu.so")
 
-SOURCES = ["k_select.cu", "k_mgwr.cu", "mgwr.cpp", "k_contract64.cu", "k_contract_tc.cu", "k_refine.cu", "k_solve.cu", "engine.cpp", "gwrbasic.cpp", "capi.cpp", "task.cpp", "noalloc.cu", "server.cpp", "batch.cpp", "launch_util.cpp"]
+SOURCES = ["k_select.cu", "k_mgwr.cu", "mgwr.cpp", "k_contract64.cu", "k_contract_tc.cu", "k_refine.cu", "k_solve.cu", "engine.cpp", "gwrbasic.cpp", "capi.cpp", "task.cpp", "noalloc.cu", "server.cpp", "batch.cpp", "launch_util.cpp", "csv.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", CSRC, "-I", INCLUDE]
 
