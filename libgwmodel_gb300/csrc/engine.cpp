@@ -194,7 +194,23 @@ DevPoints Engine::points() const
     P.v = v_.get();
     P.uR = uR_.get();
     P.vR = vR_.get();
+    P.e = e_.get();
     return P;
+}
+
+// FP64 unit vectors (cos lat cos lon, cos lat sin lon, sin lat) of points given
+// in radians, as three arrays of n: the chord form of the great-circle distance.
+static std::vector<double> unit_vectors(const std::vector<double>& lonR, const std::vector<double>& latR)
+{
+    const size_t n = lonR.size();
+    std::vector<double> e(3 * n);
+    for (size_t s = 0; s < n; s++) {
+        const double cl = std::cos(latR[s]);
+        e[s] = cl * std::cos(lonR[s]);
+        e[n + s] = cl * std::sin(lonR[s]);
+        e[2 * n + s] = std::sin(latR[s]);
+    }
+    return e;
 }
 
 void Engine::setData(int n, int p, const double* x, const double* y, const double* coords, bool geographic)
@@ -298,6 +314,13 @@ void Engine::setData(int n, int p, const double* x, const double* y, const doubl
     if (geographic) {
         check(cudaMemcpyAsync(uR_.get(), huR.data(), sizeof(double) * n, cudaMemcpyHostToDevice, stream_), "H2D");
         check(cudaMemcpyAsync(vR_.get(), hvR.data(), sizeof(double) * n, cudaMemcpyHostToDevice, stream_), "H2D");
+        const std::vector<double> he = unit_vectors(huR, hvR);
+        e_.alloc(he.size());
+        check(cudaMemcpyAsync(e_.get(), he.data(), sizeof(double) * he.size(), cudaMemcpyHostToDevice, stream_),
+              "H2D unit vectors");
+        synchronize();
+    } else {
+        e_.clear();
     }
     check(cudaMemcpyAsync(x_.get(), hx.data(), sizeof(double) * hx.size(), cudaMemcpyHostToDevice, stream_),
           "H2D x");
@@ -1043,7 +1066,7 @@ size_t Engine::estimateBytes(int n, int p, bool geographic, bool mixed, bool ada
     const double npad = std::ceil(m / 64) * 64;
     const double t16 = std::ceil(N / 16), t32 = std::ceil(N / 32);
     const double g = geographic ? 1.0 : 0.0;
-    double b = 8 * N * (2 + 2 * g);                                  // u, v, uR, vR
+    double b = 8 * N * (2 + 5 * g);                                  // u, v, uR, vR, unit vectors
     b += 8 * N * (P + 1 + 2 * m + 3 + P + 2 + P);                    // x, y, z, g, thr, sel0/1, beta, sii, resid, rvec
     b += 8 * 16384 + 64;                                              // partials, sums
     b += 32 * t16 * (1 + g) + 32 * t32 * (1 + g);                     // tile boxes and caps (16 and 32 points)
@@ -1061,7 +1084,7 @@ size_t Engine::estimateBytes(int n, int p, bool geographic, bool mixed, bool ada
 
 size_t Engine::bytesHeld() const
 {
-    size_t b = u_.capacityBytes() + v_.capacityBytes() + uR_.capacityBytes() + vR_.capacityBytes() +
+    size_t b = u_.capacityBytes() + v_.capacityBytes() + uR_.capacityBytes() + vR_.capacityBytes() + e_.capacityBytes() +
                x_.capacityBytes() + y_.capacityBytes() + z_.capacityBytes() + g_.capacityBytes() +
                thr_.capacityBytes() + sel0_.capacityBytes() + sel1_.capacityBytes() + beta_.capacityBytes() +
                sii_.capacityBytes() + resid_.capacityBytes() + partials_.capacityBytes() + sums_.capacityBytes() +
@@ -1133,6 +1156,11 @@ void Engine::predict(int nr, const double* locations, double bw, bool adaptive, 
         pf_vR_.alloc(nr);
         check(cudaMemcpyAsync(pf_uR_.get(), fuR.data(), sizeof(double) * nr, cudaMemcpyHostToDevice, stream_), "H2D");
         check(cudaMemcpyAsync(pf_vR_.get(), fvR.data(), sizeof(double) * nr, cudaMemcpyHostToDevice, stream_), "H2D");
+        const std::vector<double> fe = unit_vectors(fuR, fvR);
+        pf_e_.alloc(fe.size());
+        check(cudaMemcpyAsync(pf_e_.get(), fe.data(), sizeof(double) * fe.size(), cudaMemcpyHostToDevice, stream_),
+              "H2D unit vectors");
+        synchronize();
     }
     pf_pts_.alloc(fpts.size());
     check(cudaMemcpyAsync(pf_pts_.get(), fpts.data(), sizeof(float4) * fpts.size(), cudaMemcpyHostToDevice, stream_),
@@ -1146,6 +1174,7 @@ void Engine::predict(int nr, const double* locations, double bw, bool adaptive, 
     F.v = pf_v_.get();
     F.uR = geographic_ ? pf_uR_.get() : nullptr;
     F.vR = geographic_ ? pf_vR_.get() : nullptr;
+    F.e = geographic_ ? pf_e_.get() : nullptr;
 
     // thresholds: fixbw of BandwidthWeight.cpp:40-53 over each location's distances to the data
     const double* thr = nullptr;

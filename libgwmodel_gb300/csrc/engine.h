@@ -212,7 +212,7 @@ private:
     std::vector<int> perm_;  // sorted position -> original index
     std::vector<double> hx_, hy_, hu_, hv_;  // host copies in sorted order
 
-    DevBuf<double> u_, v_, uR_, vR_, x_, y_, z_, g_, g2_;
+    DevBuf<double> u_, v_, uR_, vR_, e_, x_, y_, z_, g_, g2_;  // e_: unit vectors (geographic)
     DevBuf<double> thr_, sel0_, sel1_;
     // order statistics already computed, by rank: brackets for new ranks
     struct RankStat {
@@ -264,7 +264,7 @@ private:
     DevBuf<unsigned long long> tc_prof_;  // phase cycles of the contraction (stats)
     // prediction points (Hilbert order): FP64 coordinates, FP32 records, 16-point
     // tile bounds, thresholds, normal equations and coefficients
-    DevBuf<double> pf_u_, pf_v_, pf_uR_, pf_vR_, pf_thr_, pf_d0_, pf_d1_, pf_g_, pf_beta_;
+    DevBuf<double> pf_u_, pf_v_, pf_uR_, pf_vR_, pf_e_, pf_thr_, pf_d0_, pf_d1_, pf_g_, pf_beta_;
     DevBuf<float4> pf_pts_, pf_tb16_;
     DevBuf<float4> stb_;  // bounds of the 1024-point super-tiles (select)
     // event pairs recorded around timed launches, resolved by stats()

@@ -51,6 +51,49 @@ __device__ __forceinline__ double pair_weight64(int kernel, double du, double dv
     return gw_kernel_weight(kernel, d, r);
 }
 
+// The reference's great-circle formula (CRSDistance.cpp:15-69) from FP64 unit
+// vectors e = (cos lat cos lon, cos lat sin lon, sin lat): its haversine terms
+// are S = sin^2 G cos^2 L + cos^2 F sin^2 L = |e_i - e_j|^2 / 4 and
+// C = |e_i + e_j|^2 / 4, and sin F cos G = (sin lat_i + sin lat_j) / 2,
+// cos F sin G = (sin lat_i - sin lat_j) / 2.  One square root, two divisions
+// and one arctangent instead of three sine-cosine pairs, a square root and four
+// divisions.  The chord of two nearby points carries an absolute error of a
+// few 1e-16, i.e. ~1e-12 km in D: nothing against a bandwidth; the relative
+// error elsewhere is a few ulp (CUDA's atan, within 2 ulp).
+__device__ __forceinline__ double gc_dist_vec(double xi, double yi, double zi, double xj, double yj, double zj)
+{
+    const double a = 6378.137, f = 1.0 / 298.257223563;
+    const double dx = xi - xj, dy = yi - yj, dz = zi - zj;
+    const double sx = xi + xj, sy = yi + yj, sz = zi + zj;
+    const double S = 0.25 * fma(dx, dx, fma(dy, dy, dz * dz));
+    const double C = 0.25 * fma(sx, sx, fma(sy, sy, sz * sz));
+    if (!(S > 0.0)) return 0.0;
+    const double sc = S * C;
+    const double rsc = sqrt(sc);
+    const double inv = 1.0 / sc;             // 1/C = S inv, 1/S = C inv
+    const double w = atan(rsc * (S * inv));  // atan(sqrt(S / C))
+    const double R = rsc / w;
+    const double D = 2.0 * w * a;
+    const double H1 = (3.0 * R - 1.0) * (0.5 * S * inv);
+    const double H2 = (3.0 * R + 1.0) * (0.5 * C * inv);
+    const double sFcG = 0.5 * sz, cFsG = 0.5 * dz;
+    return D * (1.0 + f * H1 * (sFcG * sFcG) - f * H2 * (cFsG * cFsG));
+}
+
+// w_ij of a geographic pair from the unit vectors (bisquare, tricube, gaussian,
+// exponential; the boxcar step at d = r keeps the reference formula).
+__device__ __forceinline__ double pair_weight64_vec(int kernel, double xi, double yi, double zi, double xj, double yj,
+                                                    double zj, double r, double ir2)
+{
+    const double d = gc_dist_vec(xi, yi, zi, xj, yj, zj);
+    if (kernel == GW_KERNEL_BISQUARE) {
+        const double t = 1.0 - d * d * ir2;
+        return d < r ? t * t : 0.0;
+    }
+    if (kernel == GW_KERNEL_GAUSSIAN) return exp(d * d * (-0.5 * ir2));
+    return gw_kernel_weight(kernel, d, r);
+}
+
 template <bool GEO, int NC>
 __global__ void __launch_bounds__(CT_THREADS)
     k_contract64(DevPoints P, const float4* __restrict__ tb16, DevPoints F, const float4* __restrict__ ftb16,
@@ -61,12 +104,15 @@ __global__ void __launch_bounds__(CT_THREADS)
     __shared__ double sW[CT_BM][CT_BK + 1];
     __shared__ double sZ[CT_BK][NCOL];
     __shared__ double sfu[CT_BM], sfv[CT_BM], sfuR[CT_BM], sfvR[CT_BM], sthr[CT_BM], sr2[CT_BM], sir2[CT_BM];
+    __shared__ double sfe[3][CT_BM];
     __shared__ double sred[CT_THREADS / 32];
     __shared__ float4 sbound;
 
     const int n = P.n, nf = F.n;  // data points, focus rows (the data themselves, or prediction points)
     const int t = threadIdx.x, tx = t & 15, ty = t >> 4;
     const int row0 = blockIdx.x * CT_BM;
+    // unit-vector distances for geographic data unless the boxcar step needs the reference formula
+    const bool vec = GEO && P.e && F.e && kernel != GW_KERNEL_BOXCAR;
 
     double rmax = bw;
     if (t < CT_BM) {
@@ -80,6 +126,7 @@ __global__ void __launch_bounds__(CT_THREADS)
         sthr[t] = r;
         sr2[t] = r * r;
         sir2[t] = 1.0 / (r * r);
+        for (int c = 0; c < 3; c++) sfe[c][t] = (vec && ok) ? F.e[(size_t)c * nf + i] : 0.0;
     }
     if (thr) {
         double r = (t < CT_BM && row0 + t < nf) ? thr[row0 + t] : -1.0;
@@ -116,11 +163,12 @@ __global__ void __launch_bounds__(CT_THREADS)
         // weight tile: thread (tx, ty) owns data point j0 + tx for rows ty + 16q
         {
             const int j = j0 + tx;
-            double du = 0.0, dv = 0.0, duR = 0.0, dvR = 0.0;
+            double du = 0.0, dv = 0.0, duR = 0.0, dvR = 0.0, ex = 0.0, ey = 0.0, ez = 0.0;
             if (j < n) {
                 du = P.u[j];
                 dv = P.v[j];
                 if (GEO) { duR = P.uR[j]; dvR = P.vR[j]; }
+                if (vec) { ex = P.e[j]; ey = P.e[(size_t)n + j]; ez = P.e[2 * (size_t)n + j]; }
             }
 #pragma unroll
             for (int q = 0; q < CT_ROWS_PER_THREAD; q++) {
@@ -128,8 +176,9 @@ __global__ void __launch_bounds__(CT_THREADS)
                 const int i = row0 + r;
                 double w = 0.0;
                 if (j < n && i < nf) {
-                    w = pair_weight64<GEO>(kernel, du, dv, duR, dvR, sfu[r], sfv[r], sfuR[r], sfvR[r], sthr[r], sr2[r],
-                                           sir2[r]);
+                    w = vec ? pair_weight64_vec(kernel, sfe[0][r], sfe[1][r], sfe[2][r], ex, ey, ez, sthr[r], sir2[r])
+                            : pair_weight64<GEO>(kernel, du, dv, duR, dvR, sfu[r], sfv[r], sfuR[r], sfvR[r], sthr[r],
+                                                 sr2[r], sir2[r]);
                     if (exclude_self && i == j) w = 0.0;
                     if (wpow == 2) w = w * w;
                 }
@@ -177,12 +226,14 @@ __global__ void __launch_bounds__(CT_THREADS)
 {
     constexpr int BM = 16 * RPT;  // rows of this CTA
     __shared__ double sfu[BM], sfv[BM], sfuR[BM], sfvR[BM], sthr[BM], sr2[BM], sir2[BM];
+    __shared__ double sfe[3][BM];
     __shared__ double sred[CT_THREADS / 32];
     __shared__ float4 sbound;
 
     const int n = P.n, nf = F.n;
     const int t = threadIdx.x, tx = t & 15, ty = t >> 4;
     const int row0 = blockIdx.x * BM;
+    const bool vec = GEO && P.e && F.e && kernel != GW_KERNEL_BOXCAR;
 
     double rmax = bw;
     if (t < BM) {
@@ -196,6 +247,7 @@ __global__ void __launch_bounds__(CT_THREADS)
         sthr[t] = r;
         sr2[t] = r * r;
         sir2[t] = 1.0 / (r * r);
+        for (int c = 0; c < 3; c++) sfe[c][t] = (vec && ok) ? F.e[(size_t)c * nf + i] : 0.0;
     }
     if (thr) {
         double r = (t < BM && row0 + t < nf) ? thr[row0 + t] : -1.0;
@@ -212,7 +264,7 @@ __global__ void __launch_bounds__(CT_THREADS)
     const float4 fbound = sbound;
     const float far_thr = (skip_tiles && kernel >= GW_KERNEL_BISQUARE) ? tb_far_threshold<GEO>(rmax) : -1.0f;
 
-    double fu[RPT], fv[RPT], fuR[RPT], fvR[RPT];
+    double fu[RPT], fv[RPT], fuR[RPT], fvR[RPT], fex[RPT], fey[RPT], fez[RPT];
     double rr[RPT], rr2[RPT], rir2[RPT];
     int ri[RPT];
 #pragma unroll
@@ -222,6 +274,9 @@ __global__ void __launch_bounds__(CT_THREADS)
         fv[q] = sfv[r];
         fuR[q] = sfuR[r];
         fvR[q] = sfvR[r];
+        fex[q] = sfe[0][r];
+        fey[q] = sfe[1][r];
+        fez[q] = sfe[2][r];
         rr[q] = sthr[r];
         rr2[q] = sr2[r];
         rir2[q] = sir2[r];
@@ -240,14 +295,17 @@ __global__ void __launch_bounds__(CT_THREADS)
         if (j >= n) continue;
         const double du = P.u[j], dv = P.v[j];
         const double duR = GEO ? P.uR[j] : 0.0, dvR = GEO ? P.vR[j] : 0.0;
+        const double ex = vec ? P.e[j] : 0.0, ey = vec ? P.e[(size_t)n + j] : 0.0,
+                     ez = vec ? P.e[2 * (size_t)n + j] : 0.0;
         double z[M];
 #pragma unroll
         for (int c = 0; c < M; c++) z[c] = Z[(size_t)j * ldz + c];
 #pragma unroll
         for (int q = 0; q < RPT; q++) {
             if (ri[q] < 0) continue;
-            double w = pair_weight64<GEO>(kernel, du, dv, duR, dvR, fu[q], fv[q], fuR[q], fvR[q], rr[q], rr2[q],
-                                          rir2[q]);
+            double w = vec ? pair_weight64_vec(kernel, fex[q], fey[q], fez[q], ex, ey, ez, rr[q], rir2[q])
+                           : pair_weight64<GEO>(kernel, du, dv, duR, dvR, fu[q], fv[q], fuR[q], fvR[q], rr[q],
+                                                rr2[q], rir2[q]);
             if (exclude_self && ri[q] == j) w = 0.0;
             if (wpow == 2) w = w * w;
 #pragma unroll

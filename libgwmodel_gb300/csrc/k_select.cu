@@ -460,7 +460,7 @@ __global__ void __launch_bounds__(SEL_THREADS)
 // groups of 32 tiles; at step q lane l takes point q of tile l, so the 32
 // lanes land on points far apart along the curve and rarely hit the same bin.
 constexpr int HS_ROWS = 8;
-constexpr int HS_THREADS = 512;
+constexpr int HS_THREADS = 1024;  // 32 warps at <= 64 registers: the pass is latency-bound
 
 // Histograms of rows [row0, row0 + HS_ROWS) of one dataset into its cache.
 template <bool GEO>
@@ -488,12 +488,6 @@ __device__ void hist_rows(unsigned* hs, float4 (*rf)[2], const SelectArgs& a, in
         rf[r][q] = r < nrows ? fpts[NF * (size_t)(row0 + r) + q] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     __syncthreads();
-    float4 ra[HS_ROWS], rb[HS_ROWS];
-#pragma unroll
-    for (int r = 0; r < HS_ROWS; r++) {
-        ra[r] = rf[r][0];
-        rb[r] = GEO ? rf[r][1] : ra[r];
-    }
     for (int g = warp; g < ngroups; g += HS_THREADS / 32) {
         const int tile = g * 32 + lane;
         for (int q = 0; q < SEL_TILE; q++) {
@@ -501,30 +495,23 @@ __device__ void hist_rows(unsigned* hs, float4 (*rf)[2], const SelectArgs& a, in
             const int j = tile < a.ntiles ? tile * SEL_TILE + q : 0;  // records are padded to whole tiles
             const float4 pa = a.pts[NF * (size_t)j];
             const float4 pb = GEO ? a.pts[2 * (size_t)j + 1] : pa;
-            float d32r[HS_ROWS];
-            if (GEO) {
-                GeoChord g[HS_ROWS];
-                float smax = 0.0f;
-#pragma unroll
-                for (int r = 0; r < HS_ROWS; r++) {
-                    g[r] = geo_chord32(ra[r], rb[r], ra[r].z + rb[r].z, pa, pb);
-                    smax = fmaxf(smax, g[r].S);
-                }
-                const bool near = __all_sync(0xffffffffu, smax <= 0.25f);
-#pragma unroll
-                for (int r = 0; r < HS_ROWS; r++) {
-                    const float d2 = near ? geo_d2_near(g[r]) : geo_d2_from_chord(g[r]);
-                    d32r[r] = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
-                }
-            } else {
-#pragma unroll
-                for (int r = 0; r < HS_ROWS; r++) d32r[r] = sqrtf(planar_d2_32(ra[r], pa));
-            }
-            if (!valid) continue;
+            // one row at a time (its record from shared memory), so the registers
+            // stay within the 64 that 32 warps per SM leave; the near-angle form
+            // is voted per row (it equals the general form wherever S <= 0.25)
 #pragma unroll
             for (int r = 0; r < HS_ROWS; r++) {
-                if (r >= nrows) break;
-                const float d32 = d32r[r];
+                const float4 ra = rf[r][0];
+                float d32;
+                if (GEO) {
+                    const float4 rb = rf[r][1];
+                    const GeoChord gc = geo_chord32(ra, rb, ra.z + rb.z, pa, pb);
+                    const bool near = __all_sync(0xffffffffu, gc.S <= 0.25f);
+                    const float d2 = near ? geo_d2_near(gc) : geo_d2_from_chord(gc);
+                    d32 = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
+                } else {
+                    d32 = sqrtf(planar_d2_32(ra, pa));
+                }
+                if (!valid || r >= nrows) continue;
                 if (d32 == d32) {
                     const uint32_t fb = __float_as_uint(d32);
                     unsigned bin;
