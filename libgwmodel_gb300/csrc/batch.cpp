@@ -240,6 +240,7 @@ private:
             for (auto& e : eng_) {
                 if (e->geographic_ != (geo == 1)) continue;
                 e->hist_.alloc((size_t)e->n_ * 4096);
+                e->hcoarse_.alloc((size_t)e->n_ * 64);
                 e->hist_tried_ = true;
                 SelectArgs a = selectArgs(*e, 1, nullptr);
                 args.push_back(a);
@@ -269,6 +270,7 @@ private:
         a.stb = e.stb_.get();
         a.hist_cache = e.hist_.get();
         a.cache_valid = 1;
+        a.hist_coarse = e.hcoarse_.get();
         a.rank = rank;
         a.dlo = e.dlo_;
         a.dhi = e.dhi_;

@@ -753,16 +753,19 @@ const double* Engine::orderStatistic(unsigned rank)
     if (ranks_.size() >= 64) recycleRanks();
     if (!hist_tried_) {
         hist_tried_ = true;
-        const size_t bytes = (size_t)n_ * 4096 * sizeof(unsigned);
+        const size_t bytes = (size_t)n_ * (4096 + 64) * sizeof(unsigned);
         bool fits;
         if (hist_limit_bytes_ >= 0) {
             fits = bytes <= (size_t)hist_limit_bytes_;
         } else {
             size_t free_b = 0, total_b = 0;
             cudaMemGetInfo(&free_b, &total_b);
-            fits = bytes < free_b / 4 || bytes <= hist_.capacityBytes();
+            fits = bytes < free_b / 4 || bytes <= hist_.capacityBytes() + hcoarse_.capacityBytes();
         }
-        if (fits) hist_.alloc((size_t)n_ * 4096);
+        if (fits) {
+            hist_.alloc((size_t)n_ * 4096);
+            hcoarse_.alloc((size_t)n_ * 64);
+        }
         hist_valid_ = false;
     }
     std::unique_ptr<RankStat> r;
@@ -784,6 +787,7 @@ const double* Engine::orderStatistic(unsigned rank)
     a.stb = stb_.get();
     a.hist_cache = hist_.get();
     a.cache_valid = hist_valid_ ? 1 : 0;
+    a.hist_coarse = hist_.get() ? hcoarse_.get() : nullptr;
     a.rank = rank;
     a.dlo = dlo_;
     a.dhi = dhi_;
@@ -1075,7 +1079,7 @@ size_t Engine::estimateBytes(int n, int p, bool geographic, bool mixed, bool ada
     if (mixed) b += 8 * N * (P + 1 + m) + t32 * 2 * npad * 128 + 8 * N * npad + 4 * N;
     b += 8 * N * (mm + 2 * P + 2);                                    // fit: G2, v, betasSE, qDiag, S row
     if (adaptive) {
-        const double h = 4.0 * 4096 * N;
+        const double h = 4.0 * (4096 + 64) * N;  // histograms and their segment counts
         if (hist_limit < 0 || h <= (double)hist_limit) b += h;
         b += 64 * 8 * N;                                              // cached order statistics
     }
@@ -1093,7 +1097,7 @@ size_t Engine::bytesHeld() const
                tile_thr16_.capacityBytes() + xs_.capacityBytes() + ys_.capacityBytes() + zs_.capacityBytes() +
                zimg_.capacityBytes() + acc_.capacityBytes() + thr32_.capacityBytes() + g2_.capacityBytes() +
                vvec_.capacityBytes() + bse_.capacityBytes() + qdiag_.capacityBytes() + S_.capacityBytes() +
-               hist_.capacityBytes() + xsub_.capacityBytes() + gsub_.capacityBytes() + stb_.capacityBytes();
+               hist_.capacityBytes() + hcoarse_.capacityBytes() + xsub_.capacityBytes() + gsub_.capacityBytes() + stb_.capacityBytes();
     for (auto& r : ranks_) b += r->v.capacityBytes();
     for (auto& r : rank_pool_) b += r->v.capacityBytes();
     return b;

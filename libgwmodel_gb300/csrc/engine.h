@@ -229,6 +229,7 @@ private:
     }
     long long hist_limit_bytes_ = -1;  // histogram cache limit; -1: a quarter of the free memory
     DevBuf<unsigned> hist_;    // per-row histograms of proxy distances (n x 4096)
+    DevBuf<unsigned> hcoarse_; // their cumulative counts per 64-bin segment (n x 64)
     bool hist_tried_ = false, hist_valid_ = false;
     const double* orderStatistic(unsigned rank);
     DevBuf<float4> tbsel_;     // FP32 bounds of the 32-point tiles (select, mixed kernels)

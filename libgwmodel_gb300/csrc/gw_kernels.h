@@ -24,6 +24,9 @@ struct SelectArgs {
     const float4* stb;             // per super-tile of 32 tiles (1024 points): the same bound, or null
     unsigned* hist_cache;          // n x 4096 proxy histograms of whole rows, or null
     int cache_valid;               // 1: hist_cache holds every row's histogram
+    // n x 64: cumulative counts of hist_cache at the end of each 64-bin segment
+    // (written by the histogram pass; used with cache_valid), or null
+    unsigned* hist_coarse;
     unsigned rank;
     double dlo, dhi;               // expected range of positive distances (first histogram only)
     double eps, delta;             // proxy band: d in [p (1 - eps) - delta, p (1 + eps) + delta]

@@ -36,6 +36,7 @@ constexpr int SEL_CAP = 2048;
 constexpr int SEL_BINS_PER_THREAD = SEL_BINS / SEL_THREADS;
 constexpr int SEL_MAX_PASSES = 10;
 constexpr int SEL_TILE = 32;
+constexpr int SEL_SEGS = 64;  // coarse segments of the cached histogram (64 bins each)
 
 struct SelShared {
     unsigned int hist[SEL_BINS];
@@ -371,9 +372,56 @@ __device__ void select_one(SelShared& sh, const SelectArgs& a, int row, const Wi
     Window w = wlog;
     bool ok = true;
     if (cache_row && a.cache_valid) {
-        for (int b = t; b < SEL_BINS; b += SEL_THREADS) sh.hist[b] = cache_row[b];
-        __syncthreads();
-        scan_pick(sh, a.rank);
+        if (a.hist_coarse) {
+            // the same bin as scan_pick (the first whose inclusive count reaches the
+            // rank) from the row's 64 segment counts and one segment's 64 bins: 512 B
+            // of the cache instead of 16 KB, and no block-wide scan
+            if (t < 32) {
+                const unsigned k = a.rank;
+                const unsigned* cp = a.hist_coarse + (size_t)row * SEL_SEGS;
+                const unsigned c0 = cp[t], c1 = cp[32 + t];
+                const unsigned m0 = __ballot_sync(0xffffffffu, c0 >= k), m1 = __ballot_sync(0xffffffffu, c1 >= k);
+                const int seg = m0 ? __ffs(m0) - 1 : (m1 ? 32 + __ffs(m1) - 1 : -1);
+                const unsigned prev0 = __shfl_sync(0xffffffffu, c0, (seg - 1) & 31);
+                const unsigned prev1 = __shfl_sync(0xffffffffu, c1, (seg - 33) & 31);
+                const unsigned base = seg <= 0 ? 0u : (seg <= 32 ? prev0 : prev1);
+                unsigned h0 = 0, h1 = 0;
+                if (seg >= 0) {
+                    h0 = cache_row[seg * 64 + t];
+                    h1 = cache_row[seg * 64 + 32 + t];
+                }
+                unsigned s0 = h0, s1 = h1;
+#pragma unroll
+                for (int off = 1; off < 32; off <<= 1) {
+                    const unsigned v0 = __shfl_up_sync(0xffffffffu, s0, off);
+                    const unsigned v1 = __shfl_up_sync(0xffffffffu, s1, off);
+                    if (t >= off) {
+                        s0 += v0;
+                        s1 += v1;
+                    }
+                }
+                s1 += __shfl_sync(0xffffffffu, s0, 31);
+                const unsigned f0 = __ballot_sync(0xffffffffu, seg >= 0 && base + s0 >= k);
+                const unsigned f1 = __ballot_sync(0xffffffffu, seg >= 0 && base + s1 >= k);
+                const int b = f0 ? __ffs(f0) - 1 : (f1 ? 32 + __ffs(f1) - 1 : -1);
+                const unsigned hb0 = __shfl_sync(0xffffffffu, h0, b & 31);
+                const unsigned hb1 = __shfl_sync(0xffffffffu, h1, b & 31);
+                if (t == 0) {
+                    if (seg >= 0 && b >= 0) {
+                        sh.chosen_bin = (unsigned)(seg * 64 + b);
+                        sh.count = b < 32 ? hb0 : hb1;
+                    } else {
+                        sh.chosen_bin = SEL_BINS - 1;
+                        sh.count = 0;
+                    }
+                }
+            }
+            __syncthreads();
+        } else {
+            for (int b = t; b < SEL_BINS; b += SEL_THREADS) sh.hist[b] = cache_row[b];
+            __syncthreads();
+            scan_pick(sh, a.rank);
+        }
         uint64_t lo, hi;
         bin_range(wlog, sh.chosen_bin, lo, hi);
         ok = sh.count > 0;
@@ -528,6 +576,31 @@ __device__ void hist_rows(unsigned* hs, float4 (*rf)[2], const SelectArgs& a, in
     }
     __syncthreads();
     for (int e = t; e < nrows * SEL_BINS; e += HS_THREADS) a.hist_cache[(size_t)row0 * SEL_BINS + e] = hs[e];
+    if (a.hist_coarse) {
+        // cumulative counts at the end of every 64-bin segment: one warp per row
+        for (int r = warp; r < nrows; r += HS_THREADS / 32) {
+            const unsigned* hr = hs + r * SEL_BINS;
+            unsigned s0 = 0, s1 = 0;
+            for (int b = 0; b < 64; b++) {  // rotated start: the 32 lanes hit 32 different banks
+                const int q = (b + lane) & 63;
+                s0 += hr[lane * 64 + q];
+                s1 += hr[(32 + lane) * 64 + q];
+            }
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const unsigned v0 = __shfl_up_sync(0xffffffffu, s0, off);
+                const unsigned v1 = __shfl_up_sync(0xffffffffu, s1, off);
+                if (lane >= off) {
+                    s0 += v0;
+                    s1 += v1;
+                }
+            }
+            s1 += __shfl_sync(0xffffffffu, s0, 31);
+            unsigned* cp = a.hist_coarse + (size_t)(row0 + r) * SEL_SEGS;
+            cp[lane] = s0;
+            cp[32 + lane] = s1;
+        }
+    }
     __syncthreads();
 }
 
