@@ -13,11 +13,11 @@
 //  * one thread of the control warp issues 3 x 4 tcgen05.mma.kind::tf32
 //    (hi.hi + hi.lo + lo.hi, K = 8 each) into a 128 x N FP32 accumulator in
 //    TMEM and commits to an mbarrier;
-//  * chunks of flush_tiles tiles alternate between two TMEM accumulators; the
-//    producers read a finished chunk back with tcgen05.ld one tile later and
-//    add it into double-float (hi, lo) sums in global memory, so FP32 rounding
-//    never sums more than a chunk of points and the tensor core never waits
-//    for a drain.
+//  * chunks of flush_tiles tiles alternate between two TMEM accumulators; four
+//    drain warps (one per TMEM lane quadrant) read a finished chunk back with
+//    tcgen05.ld and add it into double-float (hi, lo) sums in global memory,
+//    so FP32 rounding never sums more than a chunk of points, the tensor core
+//    never waits for a drain and the producers never drain.
 // Compactly supported kernels skip data tiles farther than the block's
 // largest threshold (FP32 tile bounds) and, for great-circle distances, pairs
 // beyond the row's haversine cut-off.  Every wait is bounded and reports
@@ -35,7 +35,9 @@ using namespace tc05;
 
 constexpr int TC_PROD_WARPS = 16;
 constexpr int TC_PROD = TC_PROD_WARPS * 32;   // producer threads
-constexpr int TC_THREADS = TC_PROD + 32;       // plus one control warp
+constexpr int TC_DRAIN_WARPS = 4;             // one per TMEM lane quadrant
+constexpr int TC_CTRL_WARP = TC_PROD_WARPS + TC_DRAIN_WARPS;
+constexpr int TC_THREADS = TC_PROD + TC_DRAIN_WARPS * 32 + 32;  // plus one control warp
 constexpr int TC_M = 128;
 constexpr int TC_BK = 32;  // points per stage (128 bytes of TF32 per row)
 constexpr uint32_t TC_A_BYTES = TC_M * 128;  // one split part of the weight tile
@@ -49,9 +51,11 @@ struct Smem {
     uint64_t mma_done[2];        // tcgen05.commit of tile k (every earlier MMA is done too)
     uint64_t full_b[TC_MAX_NB];  // Z tile landed (bulk copy)
     uint64_t full_p[2];          // point records landed (bulk copy)
-    uint64_t tmem_free[2];       // accumulator drained: one arrival per producer warp
+    uint64_t tmem_free[2];       // accumulator drained: one arrival per drain warp
+    uint64_t acc_full[2];        // tcgen05.commit after the last MMA of a chunk into accumulator c % 2
     uint32_t tmem_base;
     int abort;
+    int ktotal;                  // tiles this CTA visits
     float4 fbound;
     float red[TC_PROD_WARPS];
 };
@@ -95,11 +99,13 @@ __device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity)
 }
 
 // Warp roles: warps 0-15 produce the weight tiles (thread (r, quarter) fills
-// points [8 quarter, 8 quarter + 8) of row r) and drain the accumulators;
-// lane 0 of warp 16 issues the bulk copies and the MMAs.  Tile k uses weight
+// points [8 quarter, 8 quarter + 8) of row r); warps 16-19 drain the
+// accumulators (warp 16 + q owns TMEM lanes 32 q .. 32 q + 31, all columns);
+// lane 0 of warp 20 issues the bulk copies and the MMAs.  Tile k uses weight
 // stage k % 2, Z stage k % nb and point buffer k % 2; chunk c = k / F of F
-// tiles accumulates in TMEM accumulator c % 2, which the producers drain into
-// the double-float sums one tile after the chunk's last MMA was issued.
+// tiles accumulates in TMEM accumulator c % 2, whose last MMA commits to
+// acc_full[c % 2]; the drain warps then add it into the double-float sums and
+// release it through tmem_free[c % 2].
 // KERN: the weight kernel when fixed at compile time, -1 to read it from the arguments.
 // BATCH: CTA b works on segment work[b].x (arguments segs[work[b].x]) at row
 // block work[b].y, so one launch covers many datasets and bandwidths.
@@ -125,12 +131,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     const long long kstart = (a.prof && t == 0) ? clock64() : 0;
     const bool producer = warp < TC_PROD_WARPS;
+    const bool drainer = warp >= TC_PROD_WARPS && warp < TC_CTRL_WARP;
     const int r = t & (TC_M - 1), quarter = (t >> 7) & 3;
     const int row0 = BATCH ? work[blockIdx.x].y : blockIdx.x * TC_M;
     const int i = row0 + r;
     const bool row_ok = producer && i < a.n;
 
-    if (warp == TC_PROD_WARPS) {
+    if (warp == TC_CTRL_WARP) {
         tmem_alloc(&ctl.tmem_base, 512);
         tmem_relinquish();
     }
@@ -139,7 +146,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             mbar_init(&ctl.full_a[s], TC_PROD_WARPS);
             mbar_init(&ctl.mma_done[s], 1);
             mbar_init(&ctl.full_p[s], 1);
-            mbar_init(&ctl.tmem_free[s], TC_PROD_WARPS);
+            mbar_init(&ctl.tmem_free[s], TC_DRAIN_WARPS);
+            mbar_init(&ctl.acc_full[s], 1);
         }
         for (int s = 0; s < TC_MAX_NB; s++) mbar_init(&ctl.full_b[s], 1);
         ctl.abort = 0;
@@ -184,48 +192,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         tmask[wd] = bits;
     }
     __syncthreads();
+    if (warp == 0) {
+        int cnt = 0;
+        for (int wd = lane; wd < nwords; wd += 32) cnt += __popc(tmask[wd]);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
+        if (lane == 0) ctl.ktotal = cnt;
+    }
+    __syncthreads();
+    const int ktotal = ctl.ktotal;
 
     const int F = a.flush_tiles;
     int k = 0;  // tiles done by this thread's role
     if (producer) {
-        bool first_flush = true;
-        // drain accumulator c % 2 (its last MMA is tile `last`) into the double-float sums
-        auto flush = [&](int c, int last) -> bool {
-            if (!warp_wait(&ctl.mma_done[last & 1], (uint32_t)((last >> 1) & 1))) {
-                if (lane == 0) atomicExch(&ctl.abort, 1);
-                return false;
-            }
-            fence_after_sync();
-            const int quad = warp & 3, part = warp >> 2;
-            const int grow = row0 + quad * 32 + lane;
-            const int ncol_part = a.npad / 4;
-            const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(c & 1) * TC_ACC_COLS;
-            for (int c0 = part * ncol_part; c0 < (part + 1) * ncol_part; c0 += 16) {
-                uint32_t v[16];
-                tmem_ld16(tbase + (uint32_t)c0, v);
-                tmem_wait_ld();
-                if (grow < a.n) {
-                    float4* acc = reinterpret_cast<float4*>(a.acc + (size_t)grow * a.npad + c0);
-                    float4 o[8];
-#pragma unroll
-                    for (int q = 0; q < 8; q++) o[q] = first_flush ? make_float4(0.f, 0.f, 0.f, 0.f) : acc[q];
-#pragma unroll
-                    for (int q = 0; q < 8; q++) {
-                        const float2 h0 = df_add(make_float2(o[q].x, o[q].y), __uint_as_float(v[2 * q]));
-                        const float2 h1 = df_add(make_float2(o[q].z, o[q].w), __uint_as_float(v[2 * q + 1]));
-                        acc[q] = make_float4(h0.x, h0.y, h1.x, h1.y);
-                    }
-                }
-            }
-            fence_before_sync();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&ctl.tmem_free[c & 1]);
-            first_flush = false;
-            return true;
-        };
         TileWalker walk;
         walk.init(tmask, nwords);
-        int pending = -1;  // complete chunk not drained yet
         bool ok = true;
         const bool prof = a.prof && t == 0;
         unsigned long long pc[kTcProfSlots] = {};
@@ -238,15 +219,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 break;
             }
             const int s = k & 1;
-            if (pending >= 0 && k >= (pending + 1) * F + 1) {
-                if (prof) c0 = clock64();
-                if (!flush(pending, (pending + 1) * F - 1)) {
-                    ok = false;
-                    break;
-                }
-                pending = -1;
-                if (prof) pc[kTcProfFlush] += clock64() - c0;
-            }
             if (prof) c0 = clock64();
             // weight stage s is free once the MMAs of tile k - 2 are done
             const bool stage_ok = k < 2 || warp_wait(&ctl.mma_done[s], (uint32_t)(((k >> 1) - 1) & 1));
@@ -314,21 +286,57 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             fence_proxy_async_smem();
             __syncwarp();
             if (lane == 0) mbar_arrive(&ctl.full_a[s]);
-            if (k % F == F - 1) pending = k / F;
             if (prof) pc[kTcProfWeights] += clock64() - c0;
         }
-        if (prof) c0 = clock64();
-        if (ok && pending >= 0) ok = flush(pending, (pending + 1) * F - 1);
-        if (ok && k % F != 0) ok = flush(k / F, k - 1);
+        (void)ok;
         if (prof) {
             c1 = clock64();
-            pc[kTcProfFlush] += c1 - c0;
             pc[kTcProfLoop] += c1 - loop0;
             for (int q = 0; q < kTcProfSlots; q++)
                 if (q < kTcProfAWait || q == kTcProfLoop || q == kTcProfPrologue) atomicAdd(a.prof + q, pc[q]);
             atomicMax(a.prof + kTcProfLoopMax, (unsigned long long)(c1 - loop0));
             atomicMax(a.prof + kTcProfTilesMax, (unsigned long long)k);
         }
+    } else if (drainer) {
+        // chunk c: wait for its last MMA, add accumulator c % 2 (this warp's TMEM
+        // lane quadrant, every column) into the double-float sums, release it
+        const int quad = warp - TC_PROD_WARPS;
+        const int grow = row0 + quad * 32 + lane;
+        const int nchunks = (ktotal + F - 1) / F;
+        const bool prof = a.prof && lane == 0 && quad == 0;
+        unsigned long long pflush = 0;
+        for (int c = 0; c < nchunks; c++) {
+            if (__any_sync(0xffffffffu, *(volatile int*)&ctl.abort != 0)) break;
+            if (!warp_wait(&ctl.acc_full[c & 1], (uint32_t)((c >> 1) & 1))) {
+                if (lane == 0) atomicExch(&ctl.abort, 1);
+                break;
+            }
+            const long long c0 = prof ? clock64() : 0;
+            fence_after_sync();
+            const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(c & 1) * TC_ACC_COLS;
+            for (int col0 = 0; col0 < a.npad; col0 += 16) {
+                uint32_t v[16];
+                tmem_ld16(tbase + (uint32_t)col0, v);
+                tmem_wait_ld();
+                if (grow < a.n) {
+                    float4* acc = reinterpret_cast<float4*>(a.acc + (size_t)grow * a.npad + col0);
+                    float4 o[8];
+#pragma unroll
+                    for (int q = 0; q < 8; q++) o[q] = c == 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : acc[q];
+#pragma unroll
+                    for (int q = 0; q < 8; q++) {
+                        const float2 h0 = df_add(make_float2(o[q].x, o[q].y), __uint_as_float(v[2 * q]));
+                        const float2 h1 = df_add(make_float2(o[q].z, o[q].w), __uint_as_float(v[2 * q + 1]));
+                        acc[q] = make_float4(h0.x, h0.y, h1.x, h1.y);
+                    }
+                }
+            }
+            fence_before_sync();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&ctl.tmem_free[c & 1]);
+            if (prof) pflush += clock64() - c0;
+        }
+        if (prof) atomicAdd(a.prof + kTcProfFlush, pflush);
     } else if (lane == 0) {
         TileWalker wz, wp, wm;  // Z copies (nb ahead), point copies (2 ahead), MMAs
         wz.init(tmask, nwords);
@@ -409,6 +417,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 mma_tf32(d, alo + dk, bhi + dk, idesc, 1u);
             }
             mma_commit(&ctl.mma_done[s]);
+            if (k % F == F - 1 || k == ktotal - 1) mma_commit(&ctl.acc_full[c & 1]);  // chunk c complete
             last_mma = k;
             // Z stage of tile k - 1 is free once its MMAs are done: fetch tile k - 1 + nb
             if (k >= 1 && kz == k - 1 + nb) {
@@ -463,7 +472,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (t == 0 && a.prof) atomicAdd(a.prof + kTcProfEpilogue, (unsigned long long)(clock64() - kstart));
     fence_before_sync();
     __syncthreads();
-    if (warp == TC_PROD_WARPS) tmem_dealloc(tmem, 512);
+    if (warp == TC_CTRL_WARP) tmem_dealloc(tmem, 512);
 }
 
 // D[128 x N] = A[128 x 32] * B[N x 32]^T through the same layouts (TF32 in, FP32 out).
