@@ -55,8 +55,11 @@ __device__ __forceinline__ GeoChord geo_chord32(const float4& fa, const float4& 
 //   cos^2F sin^2G = ((sin phi_a - sin phi_b) / 2)^2,
 // so with R = sqrt(S C) / w = sqrt(C) / A (C = 1 - S) the formula
 // D = 2 a w (1 + f (H1 sin^2F cos^2G - H2 cos^2F sin^2G)), H1 = (3R - 1)/(2C),
-// H2 = (3R + 1)/(2S), becomes D^2 = (2a)^2 S (A (1 + c))^2 with
-//   c = (f / 8) [(3 sqrt C - A) zs^2 S - (3 sqrt C + A) dz^2 C] / (A S C).
+// H2 = (3R + 1)/(2S), becomes D^2 = (2a)^2 S Q^2 with Q = A (1 + c),
+//   c = (f / 8) [(3 sqrt C - A) zs^2 S - (3 sqrt C + A) dz^2 C] / (A S C),
+// so Q = A + (f / 8) num / (S C): A cancels from the correction.  num is
+// O(S) (|dz| <= 2 sqrt S), so clamping S C below at 1e-30 only keeps the
+// reciprocal finite: S = 0 gives Q = A and D = 0.
 __device__ __forceinline__ float geo_lambert_d2(const GeoChord& g, float A)
 {
     const float S = g.S;
@@ -64,10 +67,8 @@ __device__ __forceinline__ float geo_lambert_d2(const GeoChord& g, float A)
     const float cq = C * rsqrtf(C);
     const float t1 = fmaf(3.0f, cq, -A), t2 = fmaf(3.0f, cq, A);
     const float num = fmaf(t1 * (g.zs * g.zs), S, -(t2 * (g.dz * g.dz)) * C);
-    const float c = (0.125f * kGeoF) * __fdividef(num, A * S * C);
-    const float Q = fmaf(A, c, A);
-    const float d2 = kGeoK * S * (Q * Q);
-    return S > 1e-30f ? d2 : kGeoK * fmaxf(S, 0.0f);
+    const float Q = fmaf((0.125f * kGeoF) * num, __fdividef(1.0f, fmaxf(S * C, 1e-30f)), A);
+    return kGeoK * S * (Q * Q);
 }
 
 // Half angles up to 60 degrees (S <= 0.25): A from the polynomial directly.
