@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstring>
 #include <numeric>
+#include <thread>
 
 #include "gw_kernels.h"
 #include "golden.h"
@@ -45,39 +46,95 @@ uint64_t hilbert_index(uint32_t x, uint32_t y)
     return d;
 }
 
-// Geographic bounds of consecutive tiles of `size` points (sorted order).
-std::vector<TileCap> make_caps(const std::vector<double>& lon, const std::vector<double>& lat, int size)
+// fn(begin, end) over [0, n) in contiguous chunks on the host's threads (at
+// least `grain` items per chunk); the calling thread takes the first chunk.
+template <class F>
+void parallel_for(size_t n, size_t grain, F&& fn)
 {
-    const int n = (int)lon.size(), nt = (n + size - 1) / size;
-    const double DE2RA = M_PI / 180;
-    std::vector<TileCap> caps(nt);
-    for (int t = 0; t < nt; t++) {
-        const int s0 = t * size, s1 = std::min(n, s0 + size);
-        double sx = 0, sy = 0, sz = 0;
-        std::vector<double> P((size_t)3 * (s1 - s0));
-        for (int s = s0; s < s1; s++) {
-            const double la = lat[s] * DE2RA, lo = lon[s] * DE2RA;
-            double* q = &P[(size_t)3 * (s - s0)];
-            q[0] = std::cos(la) * std::cos(lo);
-            q[1] = std::cos(la) * std::sin(lo);
-            q[2] = std::sin(la);
-            sx += q[0];
-            sy += q[1];
-            sz += q[2];
-        }
-        double nrm = std::sqrt(sx * sx + sy * sy + sz * sz);
-        TileCap c{1.0, 0.0, 0.0, 2.0};  // degenerate tile: no bound
-        if (nrm > 1e-12) {
-            c = TileCap{sx / nrm, sy / nrm, sz / nrm, 0.0};
-            for (int s = s0; s < s1; s++) {
-                const double* q = &P[(size_t)3 * (s - s0)];
-                const double dx = q[0] - c.cx, dy = q[1] - c.cy, dz = q[2] - c.cz;
-                c.rho = std::max(c.rho, std::sqrt(dx * dx + dy * dy + dz * dz));
-            }
-            c.rho = c.rho * (1.0 + 1e-12) + 1e-15;
-        }
-        caps[t] = c;
+    const size_t T = std::max<size_t>(1, std::min<size_t>(std::thread::hardware_concurrency(), 64));
+    const size_t chunks = std::min(T, (n + grain - 1) / std::max<size_t>(grain, 1));
+    if (chunks <= 1) {
+        fn((size_t)0, n);
+        return;
     }
+    const size_t step = (n + chunks - 1) / chunks;
+    std::vector<std::thread> pool;
+    for (size_t c = 1; c < chunks; c++) {
+        const size_t b = c * step, e = std::min(n, b + step);
+        if (b < e) pool.emplace_back([&fn, b, e] { fn(b, e); });
+    }
+    fn((size_t)0, std::min(n, step));
+    for (auto& t : pool) t.join();
+}
+
+// Stable LSD radix sort of (key, index) pairs by key, 8 bits a pass (passes
+// whose byte is the same for every key are skipped): for input in index
+// order, the same permutation std::sort gives the pairs.
+void radix_sort(std::vector<std::pair<uint64_t, int>>& a)
+{
+    const size_t n = a.size();
+    std::vector<std::pair<uint64_t, int>> b(n);
+    uint64_t all_or = 0, all_and = ~0ull;
+    for (const auto& x : a) {
+        all_or |= x.first;
+        all_and &= x.first;
+    }
+    for (int shift = 0; shift < 64; shift += 8) {
+        if ((((all_or ^ all_and) >> shift) & 0xff) == 0) continue;
+        size_t cnt[257] = {};
+        for (const auto& x : a) cnt[((x.first >> shift) & 0xff) + 1]++;
+        for (int q = 0; q < 256; q++) cnt[q + 1] += cnt[q];
+        for (const auto& x : a) b[cnt[(x.first >> shift) & 0xff]++] = x;
+        a.swap(b);
+    }
+}
+
+// FP64 unit vectors (cos lat cos lon, cos lat sin lon, sin lat) of points given
+// in radians, as three arrays of n: the chord form of the great-circle
+// distance, and the source of every geographic record and bound below.
+std::vector<double> unit_vectors(const std::vector<double>& lonR, const std::vector<double>& latR)
+{
+    const size_t n = lonR.size();
+    std::vector<double> e(3 * n);
+    parallel_for(n, 4096, [&](size_t b, size_t en) {
+        for (size_t s = b; s < en; s++) {
+            const double cl = std::cos(latR[s]);
+            e[s] = cl * std::cos(lonR[s]);
+            e[n + s] = cl * std::sin(lonR[s]);
+            e[2 * n + s] = std::sin(latR[s]);
+        }
+    });
+    return e;
+}
+
+// Geographic bounds of consecutive tiles of `size` points (sorted order), from
+// the points' unit vectors (3 x n).
+std::vector<TileCap> make_caps(const std::vector<double>& e, int size)
+{
+    const int n = (int)(e.size() / 3), nt = (n + size - 1) / size;
+    std::vector<TileCap> caps(nt);
+    parallel_for((size_t)nt, 256, [&](size_t tb, size_t te) {
+        for (int t = (int)tb; t < (int)te; t++) {
+            const int s0 = t * size, s1 = std::min(n, s0 + size);
+            double sx = 0, sy = 0, sz = 0;
+            for (int s = s0; s < s1; s++) {
+                sx += e[s];
+                sy += e[(size_t)n + s];
+                sz += e[2 * (size_t)n + s];
+            }
+            double nrm = std::sqrt(sx * sx + sy * sy + sz * sz);
+            TileCap c{1.0, 0.0, 0.0, 2.0};  // degenerate tile: no bound
+            if (nrm > 1e-12) {
+                c = TileCap{sx / nrm, sy / nrm, sz / nrm, 0.0};
+                for (int s = s0; s < s1; s++) {
+                    const double dx = e[s] - c.cx, dy = e[(size_t)n + s] - c.cy, dz = e[2 * (size_t)n + s] - c.cz;
+                    c.rho = std::max(c.rho, std::sqrt(dx * dx + dy * dy + dz * dz));
+                }
+                c.rho = c.rho * (1.0 + 1e-12) + 1e-15;
+            }
+            caps[t] = c;
+        }
+    });
     return caps;
 }
 
@@ -90,33 +147,35 @@ void split_fp32(double v, float& hi, float& lo)
 // FP32 records of the points (hu, hv), padded to whole 32-point tiles: planar
 // (u - uc, v - vc) split hi/lo in one float4; geographic the unit vector split
 // hi/lo in two float4 (its z is sin(lat)).
+// e: the points' unit vectors (3 x n), geographic only.
 std::vector<float4> point_records(const std::vector<double>& hu, const std::vector<double>& hv, bool geographic,
-                                  double uc, double vc)
+                                  double uc, double vc, const std::vector<double>& e)
 {
     const int n = (int)hu.size();
     const size_t nt32 = (size_t)(n + 31) / 32;
     std::vector<float4> pts;
     if (!geographic) {
         pts.assign(nt32 * 32, make_float4(0.f, 0.f, 0.f, 0.f));
-        for (int s = 0; s < n; s++) {
-            float a, b, c, d;
-            split_fp32(hu[s] - uc, a, b);
-            split_fp32(hv[s] - vc, c, d);
-            pts[s] = make_float4(a, b, c, d);
-        }
+        parallel_for((size_t)n, 8192, [&](size_t b, size_t en) {
+            for (size_t s = b; s < en; s++) {
+                float a, bb, c, d;
+                split_fp32(hu[s] - uc, a, bb);
+                split_fp32(hv[s] - vc, c, d);
+                pts[s] = make_float4(a, bb, c, d);
+            }
+        });
     } else {
         pts.assign(2 * nt32 * 32, make_float4(0.f, 0.f, 0.f, 0.f));
-        const double DE2RA = M_PI / 180;
-        for (int s = 0; s < n; s++) {
-            const double lat = hv[s] * DE2RA, lon = hu[s] * DE2RA;
-            const double px = std::cos(lat) * std::cos(lon), py = std::cos(lat) * std::sin(lon), pz = std::sin(lat);
-            float xh, xl, yh, yl, zh, zl;
-            split_fp32(px, xh, xl);
-            split_fp32(py, yh, yl);
-            split_fp32(pz, zh, zl);
-            pts[2 * (size_t)s] = make_float4(xh, yh, zh, 0.f);
-            pts[2 * (size_t)s + 1] = make_float4(xl, yl, zl, 0.f);
-        }
+        parallel_for((size_t)n, 8192, [&](size_t b, size_t en) {
+            for (size_t s = b; s < en; s++) {
+                float xh, xl, yh, yl, zh, zl;
+                split_fp32(e[s], xh, xl);
+                split_fp32(e[(size_t)n + s], yh, yl);
+                split_fp32(e[2 * (size_t)n + s], zh, zl);
+                pts[2 * s] = make_float4(xh, yh, zh, 0.f);
+                pts[2 * s + 1] = make_float4(xl, yl, zl, 0.f);
+            }
+        });
     }
     return pts;
 }
@@ -125,7 +184,7 @@ std::vector<float4> point_records(const std::vector<double>& hu, const std::vect
 // boxes relative to (uc, vc) widened by `slack`, geographic 3-D caps.
 
 std::vector<float4> tile_bounds(const std::vector<double>& hu, const std::vector<double>& hv, bool geographic,
-                                int size, double uc, double vc, double slack)
+                                int size, double uc, double vc, double slack, const std::vector<double>& e)
 {
     const int n = (int)hu.size();
     const int nt = (n + size - 1) / size;
@@ -145,7 +204,7 @@ std::vector<float4> tile_bounds(const std::vector<double>& hu, const std::vector
                                 nextafterf((float)(vhi - vc + slack), INFINITY));
         }
     } else {
-        std::vector<TileCap> cp = make_caps(hu, hv, size);
+        std::vector<TileCap> cp = make_caps(e, size);
         for (int t = 0; t < nt; t++)
             tb[t] = make_float4((float)cp[t].cx, (float)cp[t].cy, (float)cp[t].cz,
                                 nextafterf((float)cp[t].rho, INFINITY) * (1.0f + 1e-6f) + 1e-7f);
@@ -198,20 +257,6 @@ DevPoints Engine::points() const
     return P;
 }
 
-// FP64 unit vectors (cos lat cos lon, cos lat sin lon, sin lat) of points given
-// in radians, as three arrays of n: the chord form of the great-circle distance.
-static std::vector<double> unit_vectors(const std::vector<double>& lonR, const std::vector<double>& latR)
-{
-    const size_t n = lonR.size();
-    std::vector<double> e(3 * n);
-    for (size_t s = 0; s < n; s++) {
-        const double cl = std::cos(latR[s]);
-        e[s] = cl * std::cos(lonR[s]);
-        e[n + s] = cl * std::sin(lonR[s]);
-        e[2 * n + s] = std::sin(latR[s]);
-    }
-    return e;
-}
 
 void Engine::setData(int n, int p, const double* x, const double* y, const double* coords, bool geographic)
 {
@@ -238,13 +283,15 @@ void Engine::setData(int n, int p, const double* x, const double* y, const doubl
     const double su = umax > umin ? 2147483647.0 / (umax - umin) : 0.0;
     const double sv = vmax > vmin ? 2147483647.0 / (vmax - vmin) : 0.0;
     std::vector<std::pair<uint64_t, int>> keyed(n);
-    for (int i = 0; i < n; i++) {
-        double fu = (coords[i] - umin) * su, fv = (coords[n + i] - vmin) * sv;
-        uint32_t qu = std::isfinite(fu) ? (uint32_t)std::min(std::max(fu, 0.0), 2147483647.0) : 0u;
-        uint32_t qv = std::isfinite(fv) ? (uint32_t)std::min(std::max(fv, 0.0), 2147483647.0) : 0u;
-        keyed[i] = {hilbert_index(qu, qv), i};
-    }
-    std::sort(keyed.begin(), keyed.end());
+    parallel_for((size_t)n, 4096, [&](size_t b, size_t e) {
+        for (size_t i = b; i < e; i++) {
+            double fu = (coords[i] - umin) * su, fv = (coords[n + i] - vmin) * sv;
+            uint32_t qu = std::isfinite(fu) ? (uint32_t)std::min(std::max(fu, 0.0), 2147483647.0) : 0u;
+            uint32_t qv = std::isfinite(fv) ? (uint32_t)std::min(std::max(fv, 0.0), 2147483647.0) : 0u;
+            keyed[i] = {hilbert_index(qu, qv), (int)i};
+        }
+    });
+    radix_sort(keyed);
     perm_.resize(n);
     for (int s = 0; s < n; s++) perm_[s] = keyed[s].second;
 
@@ -254,17 +301,19 @@ void Engine::setData(int n, int p, const double* x, const double* y, const doubl
         huR.resize(n);
         hvR.resize(n);
     }
-    for (int s = 0; s < n; s++) {
-        int i = perm_[s];
-        hu[s] = coords[i];
-        hv[s] = coords[n + i];
-        if (geographic) {
-            huR[s] = hu[s] * DE2RA;
-            hvR[s] = hv[s] * DE2RA;
+    parallel_for((size_t)n, 4096, [&](size_t b, size_t e) {
+        for (size_t s = b; s < e; s++) {
+            const int i = perm_[s];
+            hu[s] = coords[i];
+            hv[s] = coords[n + i];
+            if (geographic) {
+                huR[s] = hu[s] * DE2RA;
+                hvR[s] = hv[s] * DE2RA;
+            }
+            for (int k = 0; k < p; k++) hx[s * p + k] = x[(size_t)i + (size_t)k * n];
+            hy[s] = y[i];
         }
-        for (int k = 0; k < p; k++) hx[(size_t)s * p + k] = x[(size_t)i + (size_t)k * n];
-        hy[s] = y[i];
-    }
+    });
     const int ntiles = (n + kTile - 1) / kTile;
     std::vector<TileBox> ht(ntiles);
     for (int t = 0; t < ntiles; t++) {
@@ -314,12 +363,12 @@ void Engine::setData(int n, int p, const double* x, const double* y, const doubl
     if (geographic) {
         check(cudaMemcpyAsync(uR_.get(), huR.data(), sizeof(double) * n, cudaMemcpyHostToDevice, stream_), "H2D");
         check(cudaMemcpyAsync(vR_.get(), hvR.data(), sizeof(double) * n, cudaMemcpyHostToDevice, stream_), "H2D");
-        const std::vector<double> he = unit_vectors(huR, hvR);
-        e_.alloc(he.size());
-        check(cudaMemcpyAsync(e_.get(), he.data(), sizeof(double) * he.size(), cudaMemcpyHostToDevice, stream_),
+        he_ = unit_vectors(huR, hvR);
+        e_.alloc(he_.size());
+        check(cudaMemcpyAsync(e_.get(), he_.data(), sizeof(double) * he_.size(), cudaMemcpyHostToDevice, stream_),
               "H2D unit vectors");
-        synchronize();
     } else {
+        he_.clear();
         e_.clear();
     }
     check(cudaMemcpyAsync(x_.get(), hx.data(), sizeof(double) * hx.size(), cudaMemcpyHostToDevice, stream_),
@@ -328,7 +377,7 @@ void Engine::setData(int n, int p, const double* x, const double* y, const doubl
     check(cudaMemcpyAsync(tiles_.get(), ht.data(), sizeof(TileBox) * ntiles, cudaMemcpyHostToDevice, stream_),
           "H2D tiles");
     if (geographic) {
-        std::vector<TileCap> hc = make_caps(hu, hv, kTile);
+        std::vector<TileCap> hc = make_caps(he_, kTile);
         caps_.alloc(hc.size());
         check(cudaMemcpyAsync(caps_.get(), hc.data(), sizeof(TileCap) * hc.size(), cudaMemcpyHostToDevice, stream_),
               "H2D caps");
@@ -497,9 +546,9 @@ void Engine::buildProxy()
         for (int s = 0; s < n; s++) maxabs = std::max(maxabs, std::max(std::fabs(hu_[s] - uc_), std::fabs(hv_[s] - vc_)));
     }
     slack_ = std::ldexp(maxabs, -20);
-    std::vector<float4> pts = point_records(hu_, hv_, geographic_, uc_, vc_);
+    std::vector<float4> pts = point_records(hu_, hv_, geographic_, uc_, vc_, he_);
     if (geographic_) {
-        std::vector<TileCap> c32 = make_caps(hu_, hv_, 32);
+        std::vector<TileCap> c32 = make_caps(he_, 32);
         caps32_.alloc(c32.size());
         check(cudaMemcpyAsync(caps32_.get(), c32.data(), sizeof(TileCap) * c32.size(), cudaMemcpyHostToDevice,
                               stream_),
@@ -514,9 +563,9 @@ void Engine::buildProxy()
           "H2D pts32");
     check(cudaMemcpyAsync(boxes32_.get(), bx.data(), sizeof(TileBox) * bx.size(), cudaMemcpyHostToDevice, stream_),
           "H2D boxes");
-    std::vector<float4> tb = tile_bounds(hu_, hv_, geographic_, 32, uc_, vc_, slack_);
-    std::vector<float4> t16 = tile_bounds(hu_, hv_, geographic_, 16, uc_, vc_, slack_);
-    std::vector<float4> t1024 = tile_bounds(hu_, hv_, geographic_, 1024, uc_, vc_, slack_);
+    std::vector<float4> tb = tile_bounds(hu_, hv_, geographic_, 32, uc_, vc_, slack_, he_);
+    std::vector<float4> t16 = tile_bounds(hu_, hv_, geographic_, 16, uc_, vc_, slack_, he_);
+    std::vector<float4> t1024 = tile_bounds(hu_, hv_, geographic_, 1024, uc_, vc_, slack_, he_);
     stb_.alloc(t1024.size());
     check(cudaMemcpyAsync(stb_.get(), t1024.data(), sizeof(float4) * t1024.size(), cudaMemcpyHostToDevice, stream_),
           "H2D super-tile bounds");
@@ -547,32 +596,56 @@ void Engine::ensureMixed()
     if (mixed_ready_) return;
     const int n = n_, p = p_;
     if (m_ > 256) throw std::invalid_argument("mixed precision supports at most 21 columns of X");
+    // column statistics in two row-major passes over fixed blocks of rows (the
+    // block partials are summed in block order, so the result does not depend
+    // on the host's thread count)
+    const size_t B = 4096, nblk = ((size_t)n + B - 1) / B;
+    std::vector<double> bsum(nblk * p, 0.0), bss(nblk * p, 0.0);
+    std::vector<char> bconst(nblk * p, 1);
+    parallel_for(nblk, 1, [&](size_t b0, size_t b1) {
+        for (size_t b = b0; b < b1; b++) {
+            double* sum = &bsum[b * p];
+            char* cst = &bconst[b * p];
+            for (size_t s = b * B; s < std::min((size_t)n, (b + 1) * B); s++)
+                for (int k = 0; k < p; k++) {
+                    const double v = hx_[s * p + k];
+                    sum[k] += v;
+                    if (v != hx_[k]) cst[k] = 0;
+                }
+        }
+    });
     intercept_col_ = -1;
     for (int k = 0; k < p && intercept_col_ < 0; k++) {
-        const double c0 = hx_[k];
-        bool constant = c0 != 0.0;
-        for (int s = 1; s < n && constant; s++) constant = hx_[(size_t)s * p + k] == c0;
+        bool constant = hx_[k] != 0.0;
+        for (size_t b = 0; b < nblk && constant; b++) constant = bconst[b * p + k] != 0;
         if (constant) intercept_col_ = k;
     }
     mu_.assign(p, 0.0);
     sc_.assign(p, 1.0);
+    if (intercept_col_ >= 0)
+        for (int k = 0; k < p; k++) {
+            double t = 0.0;
+            for (size_t b = 0; b < nblk; b++) t += bsum[b * p + k];
+            mu_[k] = k == intercept_col_ ? 0.0 : t / n;
+        }
+    parallel_for(nblk, 1, [&](size_t b0, size_t b1) {
+        for (size_t b = b0; b < b1; b++) {
+            double* ss = &bss[b * p];
+            for (size_t s = b * B; s < std::min((size_t)n, (b + 1) * B); s++)
+                for (int k = 0; k < p; k++) {
+                    const double d = hx_[s * p + k] - mu_[k];
+                    ss[k] += d * d;
+                }
+        }
+    });
     for (int k = 0; k < p; k++) {
         if (k == intercept_col_) {
             sc_[k] = hx_[k];
             continue;
         }
-        double mean = 0.0;
-        if (intercept_col_ >= 0) {
-            for (int s = 0; s < n; s++) mean += hx_[(size_t)s * p + k];
-            mean /= n;
-        }
         double ss = 0.0;
-        for (int s = 0; s < n; s++) {
-            double d = hx_[(size_t)s * p + k] - mean;
-            ss += d * d;
-        }
-        double sd = std::sqrt(ss / n);
-        mu_[k] = mean;
+        for (size_t b = 0; b < nblk; b++) ss += bss[b * p + k];
+        const double sd = std::sqrt(ss / n);
         sc_[k] = (sd > 0.0 && std::isfinite(sd)) ? sd : 1.0;
     }
     mu_y_ = 0.0;
@@ -586,10 +659,12 @@ void Engine::ensureMixed()
     if (!(s_y_ > 0.0) || !std::isfinite(s_y_)) s_y_ = 1.0;
 
     std::vector<double> xs((size_t)n * p), ys(n);
-    for (int s = 0; s < n; s++) {
-        for (int k = 0; k < p; k++) xs[(size_t)s * p + k] = (hx_[(size_t)s * p + k] - mu_[k]) / sc_[k];
-        ys[s] = (hy_[s] - mu_y_) / s_y_;
-    }
+    parallel_for((size_t)n, 4096, [&](size_t b, size_t e) {
+        for (size_t s = b; s < e; s++) {
+            for (int k = 0; k < p; k++) xs[s * p + k] = (hx_[s * p + k] - mu_[k]) / sc_[k];
+            ys[s] = (hy_[s] - mu_y_) / s_y_;
+        }
+    });
     std::vector<double> tinv(p), tvec(p, 0.0);
     for (int k = 0; k < p; k++) tinv[k] = 1.0 / sc_[k];
     if (intercept_col_ >= 0) {
@@ -1149,8 +1224,9 @@ void Engine::predict(int nr, const double* locations, double bw, bool adaptive, 
         for (int s = 0; s < nr; s++) maxabs = std::max(maxabs, std::max(std::fabs(fu[s] - uc_), std::fabs(fv[s] - vc_)));
         slack = std::max(slack, std::ldexp(maxabs, -20));
     }
-    std::vector<float4> fpts = point_records(fu, fv, geographic_, uc_, vc_);
-    std::vector<float4> ftb = tile_bounds(fu, fv, geographic_, kTile, uc_, vc_, slack);
+    const std::vector<double> fe = geographic_ ? unit_vectors(fuR, fvR) : std::vector<double>();
+    std::vector<float4> fpts = point_records(fu, fv, geographic_, uc_, vc_, fe);
+    std::vector<float4> ftb = tile_bounds(fu, fv, geographic_, kTile, uc_, vc_, slack, fe);
     pf_u_.alloc(nr);
     pf_v_.alloc(nr);
     check(cudaMemcpyAsync(pf_u_.get(), fu.data(), sizeof(double) * nr, cudaMemcpyHostToDevice, stream_), "H2D");
@@ -1160,7 +1236,6 @@ void Engine::predict(int nr, const double* locations, double bw, bool adaptive, 
         pf_vR_.alloc(nr);
         check(cudaMemcpyAsync(pf_uR_.get(), fuR.data(), sizeof(double) * nr, cudaMemcpyHostToDevice, stream_), "H2D");
         check(cudaMemcpyAsync(pf_vR_.get(), fvR.data(), sizeof(double) * nr, cudaMemcpyHostToDevice, stream_), "H2D");
-        const std::vector<double> fe = unit_vectors(fuR, fvR);
         pf_e_.alloc(fe.size());
         check(cudaMemcpyAsync(pf_e_.get(), fe.data(), sizeof(double) * fe.size(), cudaMemcpyHostToDevice, stream_),
               "H2D unit vectors");

@@ -211,6 +211,7 @@ private:
     double dlo_ = 0.0, dhi_ = 0.0;
     std::vector<int> perm_;  // sorted position -> original index
     std::vector<double> hx_, hy_, hu_, hv_;  // host copies in sorted order
+    std::vector<double> he_;                 // geographic: unit vectors in sorted order (3 x n)
 
     DevBuf<double> u_, v_, uR_, vR_, e_, x_, y_, z_, g_, g2_;  // e_: unit vectors (geographic)
     DevBuf<double> thr_, sel0_, sel1_;
