@@ -102,15 +102,28 @@ cudaError_t launch_pm(const RefineArgs& a, cudaStream_t s)
     return cudaGetLastError();
 }
 
+// The unrolled FP64 loops run PMAX iterations predicated on k < p, and every
+// predicated-off FP64 instruction still takes its issue slot on a GPU whose
+// FP64 rate is 1/64 of FP32: the bound follows p in steps of two (one above 16).
 template <bool GEO>
 cudaError_t launch_geo(const RefineArgs& a, cudaStream_t s)
 {
-    if (a.p <= 4) return launch_pm<GEO, 4>(a, s);
-    if (a.p <= 8) return launch_pm<GEO, 8>(a, s);
-    if (a.p <= 12) return launch_pm<GEO, 12>(a, s);
-    if (a.p <= 16) return launch_pm<GEO, 16>(a, s);
-    if (a.p <= 21) return launch_pm<GEO, 21>(a, s);
-    return cudaErrorInvalidValue;
+    switch (a.p) {
+    case 1: case 2: return launch_pm<GEO, 2>(a, s);
+    case 3: case 4: return launch_pm<GEO, 4>(a, s);
+    case 5: case 6: return launch_pm<GEO, 6>(a, s);
+    case 7: case 8: return launch_pm<GEO, 8>(a, s);
+    case 9: case 10: return launch_pm<GEO, 10>(a, s);
+    case 11: case 12: return launch_pm<GEO, 12>(a, s);
+    case 13: case 14: return launch_pm<GEO, 14>(a, s);
+    case 15: case 16: return launch_pm<GEO, 16>(a, s);
+    case 17: return launch_pm<GEO, 17>(a, s);
+    case 18: return launch_pm<GEO, 18>(a, s);
+    case 19: return launch_pm<GEO, 19>(a, s);
+    case 20: return launch_pm<GEO, 20>(a, s);
+    case 21: return launch_pm<GEO, 21>(a, s);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 }  // namespace

@@ -217,12 +217,30 @@ __global__ void __launch_bounds__(SV_WARPS * 32)
                     a.v[(size_t)row * p + lane] = v;
                     vsh[lane] = v;
                 }
-                // explicit inverse, column by column
-                for (int k = 0; k < p; k++) {
-                    double e = fwd_solve(L, ld, p, lane, lane == k ? 1.0 : 0.0);
-                    e = bwd_solve(L, ld, p, lane, e);
-                    if (lane < p) Ainv[lane * ld + k] = e;
+                // U = L^-1 (lower triangular), lane j computing column j by forward
+                // substitution (L keeps 1 / L_jj on its diagonal), into T
+                if (lane < p) {
+                    const int j = lane;
+                    T[j * ld + j] = L[j * ld + j];
+                    for (int r2 = j + 1; r2 < p; r2++) {
+                        double acc = 0.0;
+                        for (int k = j; k < r2; k++) acc = fma(L[r2 * ld + k], T[k * ld + j], acc);
+                        T[r2 * ld + j] = -acc * L[r2 * ld + r2];
+                    }
                 }
+                __syncwarp();
+                // A^-1 = U^T U over the p (p + 1) / 2 elements (c, r), c <= r, spread over the
+                // lanes: sum over k >= r of U_kc U_kr
+                const int tri = p * (p + 1) / 2;
+                for (int e = lane; e < tri; e += 32) {
+                    const int rr = (int)((sqrtf((float)(8 * e + 1)) - 1.0f) * 0.5f);  // exact for e < 528
+                    const int cc = e - rr * (rr + 1) / 2;
+                    double acc = 0.0;
+                    for (int k = rr; k < p; k++) acc = fma(T[k * ld + cc], T[k * ld + rr], acc);
+                    Ainv[cc * ld + rr] = acc;
+                    Ainv[rr * ld + cc] = acc;
+                }
+                __syncwarp();
                 if (a.ainv && lane < p)
                     for (int k = 0; k < p; k++) a.ainv[((size_t)row * p + lane) * p + k] = Ainv[lane * ld + k];
                 const double* g2 = a.G2 + (size_t)row * a.ldg2;
@@ -231,26 +249,37 @@ __global__ void __launch_bounds__(SV_WARPS * 32)
                         Q[lane * ld + c] = g2[lane <= c ? packed_index(lane, c, p) : packed_index(c, lane, p)];
                 if (lane < p) tsh[lane] = a.tvec ? a.tvec[lane] : 0.0;
                 __syncwarp();
-                // T = A^-1 Q (row per lane), then row `lane` of M = T A^-1
+                // W = Q A^-1 (into T; U is done) over the p^2 elements, and (Q v)_lane
+                for (int e = lane; e < p * p; e += 32) {
+                    const int ra = e / p, cb = e - ra * p;
+                    double acc = 0.0;
+                    for (int q = 0; q < p; q++) acc = fma(Q[ra * ld + q], Ainv[q * ld + cb], acc);
+                    T[ra * ld + cb] = acc;
+                }
                 double qv = 0.0;
                 if (lane < p)
-                    for (int b = 0; b < p; b++) {
-                        double tb = 0.0;
-                        for (int q = 0; q < p; q++) tb += Ainv[lane * ld + q] * Q[q * ld + b];
-                        T[lane * ld + b] = tb;
-                        qv += Q[lane * ld + b] * vsh[b];
-                    }
+                    for (int b = 0; b < p; b++) qv = fma(Q[lane * ld + b], vsh[b], qv);
                 __syncwarp();
-                double mdiag = 0.0, mt = 0.0;
+                // diag(A^-1 Q A^-1)_k = sum_a A^-1_ka W_ak
+                double mdiag = 0.0;
                 if (lane < p)
-                    for (int l = 0; l < p; l++) {
-                        double m = 0.0;
-                        for (int b = 0; b < p; b++) m += T[lane * ld + b] * Ainv[b * ld + l];
-                        if (l == lane) mdiag = m;
-                        mt += m * tsh[l];
-                    }
+                    for (int q = 0; q < p; q++) mdiag = fma(Ainv[lane * ld + q], T[q * ld + lane], mdiag);
+                // t^T A^-1 Q A^-1 t = z^T Q z with z = A^-1 t (the intercept row after centring)
+                double tmt = 0.0;
+                if (a.tvec) {
+                    double* zsh = L;  // the factor is no longer needed
+                    double z = 0.0;
+                    if (lane < p)
+                        for (int q = 0; q < p; q++) z = fma(Ainv[lane * ld + q], tsh[q], z);
+                    __syncwarp();
+                    if (lane < p) zsh[lane] = z;
+                    __syncwarp();
+                    double qz = 0.0;
+                    if (lane < p)
+                        for (int b = 0; b < p; b++) qz = fma(Q[lane * ld + b], zsh[b], qz);
+                    tmt = warp_sum(lane < p ? z * qz : 0.0);
+                }
                 const double ti = (a.tinv && lane < p) ? a.tinv[lane] : 1.0;
-                const double tmt = warp_sum(lane < p ? tsh[lane] * mt : 0.0);
                 if (lane < p) a.bse[(size_t)row * p + lane] = (a.tvec && lane == a.tcol) ? tmt : ti * ti * mdiag;
                 const double sts = warp_sum(lane < p ? vsh[lane] * qv : 0.0);
                 if (lane == 0) acc_t += sts;
