@@ -917,10 +917,14 @@ void Engine::contract(const double* Z, int mcols, double* G, int ldg, double bw,
                       bool exclude_self, int wpow)
 {
     cudaEvent_t e0 = stats_on_ ? timerBegin() : nullptr;
-    check(launch_contract64(points(), geographic_, tb16_.get(), Z, m_, mcols, G, ldg, thrPtr(adaptive), bw, kernel,
-                            exclude_self, wpow, true, stream_),
-          "contract64");
-    stats_.kernel_launches += 1;
+    // the kernel takes at most 256 columns (p <= 21); wider Z (p up to 32) in column chunks
+    for (int c0 = 0; c0 < mcols; c0 += 256) {
+        const int w = std::min(256, mcols - c0);
+        check(launch_contract64(points(), geographic_, tb16_.get(), Z + c0, m_, w, G + c0, ldg, thrPtr(adaptive), bw,
+                                kernel, exclude_self, wpow, true, stream_),
+              "contract64");
+        stats_.kernel_launches += 1;
+    }
     if (stats_on_) {
         timerEnd(e0, 0);
         stats_.contract_launches += 1;
@@ -1305,9 +1309,13 @@ void Engine::predict(int nr, const double* locations, double bw, bool adaptive, 
     }
     // X^T W_i X, X^T W_i y at every location, then beta_i = (X^T W_i X)^-1 X^T W_i y
     pf_g_.alloc((size_t)nr * m_);
-    check(launch_contract64_focus(points(), tb16_.get(), F, pf_tb16_.get(), geographic_, z_.get(), m_, m_, pf_g_.get(),
-                                  m_, thr, bw, kernel, false, 1, true, stream_),
-          "predict contraction");
+    for (int c0 = 0; c0 < m_; c0 += 256) {  // at most 256 columns a launch
+        check(launch_contract64_focus(points(), tb16_.get(), F, pf_tb16_.get(), geographic_, z_.get() + c0, m_,
+                                      std::min(256, m_ - c0), pf_g_.get() + c0, m_, thr, bw, kernel, false, 1, true,
+                                      stream_),
+              "predict contraction");
+        stats_.kernel_launches += 1;
+    }
     pf_beta_.alloc((size_t)nr * p);
     SolveArgs a{};
     a.n = nr;
@@ -1324,7 +1332,7 @@ void Engine::predict(int nr, const double* locations, double bw, bool adaptive, 
     int nb = 0;
     check(launch_solve(a, &nb, stream_), "predict solve");
     check(launch_reduce_partials(partials_.get(), nb, sums_.get(), stream_), "reduce");
-    stats_.kernel_launches += 4;
+    stats_.kernel_launches += 3;
     std::vector<double> hb((size_t)nr * p);
     check(cudaMemcpyAsync(hb.data(), pf_beta_.get(), sizeof(double) * hb.size(), cudaMemcpyDeviceToHost, stream_),
           "D2H");
