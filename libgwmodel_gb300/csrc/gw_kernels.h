@@ -171,7 +171,7 @@ enum TcProf {
     kTcProfStageWait,   // producer: waiting for a free weight stage
     kTcProfPointsWait,  // producer: waiting for the tile's point records
     kTcProfWeights,     // producer: weights, split and shared-memory stores
-    kTcProfFlush,       // producer: draining accumulators
+    kTcProfFlush,       // drain warp 0: draining accumulators
     kTcProfAWait,       // control: waiting for the weight tile
     kTcProfZWait,       // control: waiting for the Z tile and a free accumulator
     kTcProfIssue,       // control: MMA issue and Z prefetch

@@ -443,6 +443,7 @@ mat GWRMultiscale::fit()
         mIterations = iteration;
     }
     if (mStatus != Status::Success) {
+        I.releaseHat();
         mBetas = betas;
         return betas;
     }
@@ -462,6 +463,7 @@ mat GWRMultiscale::fit()
         eng.synchronize();
         trS = h[0];
         trStS = h[1];
+        I.releaseHat();  // (p + 2) n^2 doubles: not held past the fit
     }
     mDiagnostic = CalcDiagnostic(x, mY, trS, trStS, mRSS0);
     // this library's kernels (the DGEMMs are cuBLAS's): the engine's (including
