@@ -21,9 +21,9 @@ struct DevPoints {
     const double* v;
     const double* uR;
     const double* vR;
-    // geographic only, optional: FP64 unit vectors (cos lat cos lon, cos lat sin lon,
-    // sin lat) as three arrays of n, for the chord form of the distance
-    const double* e = nullptr;
+    // geographic only, optional (null: absent): FP64 unit vectors (cos lat cos lon,
+    // cos lat sin lon, sin lat) as three arrays of n, for the chord form of the distance
+    const double* e;
 };
 
 // Axis-aligned bounds of one data tile of kTile consecutive (Hilbert-ordered) points.

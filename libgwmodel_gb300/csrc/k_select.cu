@@ -33,36 +33,48 @@ constexpr int SEL_WARPS = SEL_THREADS / 32;
 constexpr int SEL_BINS = 4096;
 constexpr int SEL_LOG_BINS = 12;
 constexpr int SEL_CAP = 2048;
-constexpr int SEL_BINS_PER_THREAD = SEL_BINS / SEL_THREADS;
 constexpr int SEL_MAX_PASSES = 10;
 constexpr int SEL_TILE = 32;
 constexpr int SEL_SEGS = 64;  // coarse segments of the cached histogram (64 bins each)
 
-struct SelShared {
-    unsigned int hist[SEL_BINS];
-    uint64_t cand[SEL_CAP];
-    unsigned int warp_tot[SEL_WARPS];
-    unsigned int below_w[SEL_WARPS];
-    unsigned int chosen_bin, below, count, ncand;
+// Window histogram and candidate buffer of one select CTA.  SelWide (4096
+// bins, 2048 candidates) runs passes over whole rows with the logarithmic
+// window that the histogram cache also uses; SelNarrow (1024 bins, 1024
+// candidates, 12 KB instead of 33 KB of shared memory, so three times the
+// CTAs per SM) runs the passes inside one cached bin.
+template <int LB_, int CAP_>
+struct SelCfg {
+    static constexpr int LB = LB_, BINS = 1 << LB_, CAP = CAP_, BPT = BINS / SEL_THREADS;
+    struct Shared {
+        unsigned int hist[BINS];
+        uint64_t cand[CAP];
+        unsigned int warp_tot[SEL_WARPS];
+        unsigned int below_w[SEL_WARPS];
+        unsigned int chosen_bin, below, count, ncand;
+    };
 };
+using SelWide = SelCfg<SEL_LOG_BINS, SEL_CAP>;
+using SelNarrow = SelCfg<10, 1024>;
 
 struct Window {
-    uint64_t base;  // bucket = (key - base) >> shift, clamped to [0, SEL_BINS)
+    uint64_t base;  // bucket = (key - base) >> shift, clamped to [0, bins)
     int shift;
     uint64_t wlo, whi;  // keys of the window ends (inclusive)
 };
 
+template <class C = SelWide>
 __device__ __forceinline__ unsigned bucket_of(const Window& w, uint64_t key)
 {
     if (key < w.base) return 0;
     uint64_t q = (key - w.base) >> w.shift;
-    return q > (uint64_t)(SEL_BINS - 1) ? (unsigned)(SEL_BINS - 1) : (unsigned)q;
+    return q > (uint64_t)(C::BINS - 1) ? (unsigned)(C::BINS - 1) : (unsigned)q;
 }
 
+template <class C = SelWide>
 __device__ __forceinline__ void bin_range(const Window& w, unsigned b, uint64_t& lo, uint64_t& hi)
 {
     lo = (b == 0) ? w.wlo : w.base + ((uint64_t)b << w.shift);
-    if (b == SEL_BINS - 1) {
+    if (b == C::BINS - 1) {
         hi = w.whi;
     } else {
         uint64_t span = ((uint64_t)(b + 1) << w.shift) - 1;
@@ -70,11 +82,12 @@ __device__ __forceinline__ void bin_range(const Window& w, unsigned b, uint64_t&
     }
 }
 
+template <class C>
 __device__ __forceinline__ Window linear_window(uint64_t lo, uint64_t hi)
 {
     uint64_t span = hi - lo;
     int bits = span ? 64 - __clzll((long long)span) : 0;
-    return Window{lo, bits > SEL_LOG_BINS ? bits - SEL_LOG_BINS : 0, lo, hi};
+    return Window{lo, bits > C::LB ? bits - C::LB : 0, lo, hi};
 }
 
 // Coarse window over positive distances [dlo, dhi] for whole-row histograms.
@@ -91,12 +104,13 @@ __device__ __forceinline__ Window coarse_window(const SelectArgs& a)
 }
 
 // Finds the bin where the cumulative count reaches krem (1-based).
-__device__ void scan_pick(SelShared& sh, unsigned krem)
+template <class C>
+__device__ void scan_pick(typename C::Shared& sh, unsigned krem)
 {
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     unsigned local = 0;
 #pragma unroll
-    for (int q = 0; q < SEL_BINS_PER_THREAD; q++) local += sh.hist[t * SEL_BINS_PER_THREAD + q];
+    for (int q = 0; q < C::BPT; q++) local += sh.hist[t * C::BPT + q];
     unsigned incl = local;
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
@@ -105,7 +119,7 @@ __device__ void scan_pick(SelShared& sh, unsigned krem)
     }
     if (lane == 31) sh.warp_tot[warp] = incl;
     if (t == 0) {
-        sh.chosen_bin = SEL_BINS - 1;
+        sh.chosen_bin = C::BINS - 1;
         sh.below = 0;
         sh.count = 0;
     }
@@ -115,8 +129,8 @@ __device__ void scan_pick(SelShared& sh, unsigned krem)
     const unsigned excl = wpre + incl - local;
     if (excl < krem && excl + local >= krem) {
         unsigned c = excl;
-        for (int q = 0; q < SEL_BINS_PER_THREAD; q++) {
-            unsigned b = t * SEL_BINS_PER_THREAD + q;
+        for (int q = 0; q < C::BPT; q++) {
+            unsigned b = t * C::BPT + q;
             unsigned h = sh.hist[b];
             if (c + h >= krem) {
                 sh.chosen_bin = b;
@@ -131,7 +145,8 @@ __device__ void scan_pick(SelShared& sh, unsigned krem)
 }
 
 // Ascending bitonic sort of cand[0, count) padded with +inf keys.
-__device__ void bitonic_sort(SelShared& sh, unsigned count)
+template <class C>
+__device__ void bitonic_sort(typename C::Shared& sh, unsigned count)
 {
     unsigned len = 1;
     while (len < count) len <<= 1;
@@ -191,8 +206,8 @@ __device__ __forceinline__ int classify_tile(const float4& tb, const RowCtx& c, 
 // otherwise the FP32 proxies.  Returns false when the bracket does not hold
 // the rank or the pass limit is reached.  The first pass may store its
 // histogram (coarse log window over [0, +inf]) in cache_row.
-template <bool GEO, bool EXACT>
-__device__ bool select_row(SelShared& sh, const SelectArgs& a, const RowCtx& c, double T_lo, double T_hi, Window w,
+template <bool GEO, bool EXACT, class C>
+__device__ bool select_row(typename C::Shared& sh, const SelectArgs& a, const RowCtx& c, double T_lo, double T_hi, Window w,
                            unsigned* cache_row, double& result)
 {
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -215,7 +230,7 @@ __device__ bool select_row(SelShared& sh, const SelectArgs& a, const RowCtx& c, 
             above_thr = !(thi < 1.8e19f) ? 3e38f : thi * thi * (1.0f + 1e-5f);
         }
         const uint64_t klo = dkey(T_lo), khi = dkey(T_hi);
-        for (int b = t; b < SEL_BINS; b += SEL_THREADS) sh.hist[b] = 0;
+        for (int b = t; b < C::BINS; b += SEL_THREADS) sh.hist[b] = 0;
         if (t == 0) sh.ncand = 0;
         __syncthreads();
         unsigned below = 0;
@@ -288,7 +303,7 @@ __device__ bool select_row(SelShared& sh, const SelectArgs& a, const RowCtx& c, 
                     const unsigned act = __ballot_sync(0xffffffffu, in);
                     if (act) {
                         if (in) {
-                            const unsigned bin = bucket_of(w, key);
+                            const unsigned bin = bucket_of<C>(w, key);
                             const unsigned peers = __match_any_sync(act, bin);
                             if (lane == __ffs(peers) - 1) atomicAdd(&sh.hist[bin], (unsigned)__popc(peers));
                         }
@@ -298,7 +313,7 @@ __device__ bool select_row(SelShared& sh, const SelectArgs& a, const RowCtx& c, 
                         base = __shfl_sync(0xffffffffu, base, leader);
                         if (in) {
                             const unsigned slot = base + __popc(act & ((1u << lane) - 1u));
-                            if (slot < SEL_CAP) sh.cand[slot] = key;
+                            if (slot < C::CAP) sh.cand[slot] = key;
                         }
                     }
                 }
@@ -308,8 +323,10 @@ __device__ bool select_row(SelShared& sh, const SelectArgs& a, const RowCtx& c, 
         for (int off = 16; off > 0; off >>= 1) below += __shfl_xor_sync(0xffffffffu, below, off);
         if (lane == 0) sh.below_w[warp] = below;
         __syncthreads();
-        if (pass == 0 && cache_row)
-            for (int b = t; b < SEL_BINS; b += SEL_THREADS) cache_row[b] = sh.hist[b];
+        if constexpr (C::BINS == SEL_BINS) {  // a whole-row pass can fill the cache row
+            if (pass == 0 && cache_row)
+                for (int b = t; b < SEL_BINS; b += SEL_THREADS) cache_row[b] = sh.hist[b];
+        }
         unsigned below_all = 0;
         for (int q = 0; q < SEL_WARPS; q++) below_all += sh.below_w[q];
         const unsigned ncand = sh.ncand;
@@ -318,15 +335,15 @@ __device__ bool select_row(SelShared& sh, const SelectArgs& a, const RowCtx& c, 
             return false;
         }
         const unsigned krem = a.rank - below_all;
-        if (ncand <= (unsigned)SEL_CAP) {
-            bitonic_sort(sh, ncand);
+        if (ncand <= (unsigned)C::CAP) {
+            bitonic_sort<C>(sh, ncand);
             result = keyd(sh.cand[krem - 1]);
             __syncthreads();
             return true;
         }
-        scan_pick(sh, krem);
+        scan_pick<C>(sh, krem);
         uint64_t lo, hi;
-        bin_range(w, sh.chosen_bin, lo, hi);
+        bin_range<C>(w, sh.chosen_bin, lo, hi);
         __syncthreads();
         if (lo == hi) {
             result = keyd(lo);
@@ -334,15 +351,15 @@ __device__ bool select_row(SelShared& sh, const SelectArgs& a, const RowCtx& c, 
         }
         T_lo = keyd(lo);
         T_hi = keyd(hi);
-        w = linear_window(lo, hi);
+        w = linear_window<C>(lo, hi);
     }
     return false;
 }
 
 // The adaptive threshold of one row (stage A on the proxies from the cached
 // histogram when there is one, stage B on the reference's FP64 values).
-template <bool GEO, bool EXACT>
-__device__ void select_one(SelShared& sh, const SelectArgs& a, int row, const Window& wlog)
+template <bool GEO, bool EXACT, class C>
+__device__ void select_one(typename C::Shared& sh, const SelectArgs& a, int row, const Window& wlog)
 {
     const int t = threadIdx.x;
     const DevPoints P = a.F.u ? a.F : a.P;  // focus coordinates
@@ -417,28 +434,28 @@ __device__ void select_one(SelShared& sh, const SelectArgs& a, int row, const Wi
                 }
             }
             __syncthreads();
-        } else {
+        } else if constexpr (C::BINS == SEL_BINS) {
             for (int b = t; b < SEL_BINS; b += SEL_THREADS) sh.hist[b] = cache_row[b];
             __syncthreads();
-            scan_pick(sh, a.rank);
+            scan_pick<C>(sh, a.rank);
         }
         uint64_t lo, hi;
-        bin_range(wlog, sh.chosen_bin, lo, hi);
+        bin_range<SelWide>(wlog, sh.chosen_bin, lo, hi);
         ok = sh.count > 0;
         __syncthreads();
         T_lo = keyd(lo);
         T_hi = keyd(hi);
-        w = linear_window(lo, hi);
+        w = linear_window<C>(lo, hi);
         cache_row = nullptr;
     }
     double q = __longlong_as_double(0x7ff8000000000000ll);
-    if (ok) ok = select_row<GEO, false>(sh, a, c, T_lo, T_hi, w, a.cache_valid ? nullptr : cache_row, q);
+    if (ok) ok = select_row<GEO, false, C>(sh, a, c, T_lo, T_hi, w, a.cache_valid ? nullptr : cache_row, q);
     double result = q;
     // stage B: the reference's FP64 value, inside the proxy band around q
     if (EXACT && ok) {
         const double lo = q * (1.0 - a.eps) - a.delta, hi = q * (1.0 + a.eps) + a.delta;
         const double blo = lo > 0.0 ? lo : 0.0;
-        ok = select_row<GEO, true>(sh, a, c, blo, hi, linear_window(dkey(blo), dkey(hi)), nullptr, result);
+        ok = select_row<GEO, true, C>(sh, a, c, blo, hi, linear_window<C>(dkey(blo), dkey(hi)), nullptr, result);
     }
     if (t == 0) {
         if (!ok) {
@@ -450,15 +467,16 @@ __device__ void select_one(SelShared& sh, const SelectArgs& a, int row, const Wi
     __syncthreads();
 }
 
-template <bool GEO, bool EXACT>
+// C = SelNarrow needs a valid cache with its segment counts (hist_coarse).
+template <bool GEO, bool EXACT, class C>
 __global__ void __launch_bounds__(SEL_THREADS) k_select(SelectArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    SelShared& sh = *reinterpret_cast<SelShared*>(smem_raw);
+    typename C::Shared& sh = *reinterpret_cast<typename C::Shared*>(smem_raw);
     // coarse logarithmic window of the first pass over a whole row
     const Window wlog = coarse_window(a);
     const int nrows = a.F.u ? a.F.n : a.n;
-    for (int row = blockIdx.x; row < nrows; row += gridDim.x) select_one<GEO, EXACT>(sh, a, row, wlog);
+    for (int row = blockIdx.x; row < nrows; row += gridDim.x) select_one<GEO, EXACT, C>(sh, a, row, wlog);
 }
 
 // Index of the segment holding flattened item `item`: the last seg with start[seg] <= item.
@@ -475,12 +493,12 @@ __device__ __forceinline__ int find_segment(const long long* __restrict__ start,
 
 // Many selects in one launch: segment s (its own dataset and rank) owns the
 // flattened rows [start[s], start[s + 1]).
-template <bool GEO, bool EXACT>
+template <bool GEO, bool EXACT, class C>
 __global__ void __launch_bounds__(SEL_THREADS)
     k_select_batch(const SelectArgs* __restrict__ segs, const long long* __restrict__ start, int nseg)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    SelShared& sh = *reinterpret_cast<SelShared*>(smem_raw);
+    typename C::Shared& sh = *reinterpret_cast<typename C::Shared*>(smem_raw);
     __shared__ SelectArgs sa;
     __shared__ int cur;
     if (threadIdx.x == 0) cur = -1;
@@ -497,7 +515,7 @@ __global__ void __launch_bounds__(SEL_THREADS)
             }
             __syncthreads();
         }
-        select_one<GEO, EXACT>(sh, sa, (int)(item - start[seg]), coarse_window(sa));
+        select_one<GEO, EXACT, C>(sh, sa, (int)(item - start[seg]), coarse_window(sa));
     }
 }
 
@@ -685,19 +703,16 @@ cudaError_t launch_to_float(int n, const double* in, float* out, cudaStream_t st
     return cudaGetLastError();
 }
 
-size_t select_smem_bytes() { return sizeof(SelShared); }
+size_t select_smem_bytes() { return sizeof(SelWide::Shared); }
 
-cudaError_t launch_select(const SelectArgs& a, bool geographic, bool exact, int num_sms, cudaStream_t stream)
+template <class C>
+cudaError_t launch_select_cfg(const SelectArgs& a, bool geographic, bool exact, int grid, cudaStream_t stream)
 {
-    if (a.rank < 1 || a.rank > (unsigned)a.n) return cudaErrorInvalidValue;
-    const int nrows = a.F.u ? a.F.n : a.n;
-    int grid = num_sms * 12;
-    if (grid > nrows) grid = nrows;
-    const size_t smem = sizeof(SelShared);
-#define GW_SEL(G, E)                                                                                  \
-    do {                                                                                              \
-        raise_smem_limit((const void*)k_select<G, E>, smem); \
-        k_select<G, E><<<grid, SEL_THREADS, smem, stream>>>(a);                                       \
+    const size_t smem = sizeof(typename C::Shared);
+#define GW_SEL(G, E)                                                          \
+    do {                                                                      \
+        raise_smem_limit((const void*)k_select<G, E, C>, smem);               \
+        k_select<G, E, C><<<grid, SEL_THREADS, smem, stream>>>(a);            \
     } while (0)
     if (geographic) {
         if (exact) GW_SEL(true, true);
@@ -708,6 +723,18 @@ cudaError_t launch_select(const SelectArgs& a, bool geographic, bool exact, int 
     }
 #undef GW_SEL
     return cudaGetLastError();
+}
+
+cudaError_t launch_select(const SelectArgs& a, bool geographic, bool exact, int num_sms, cudaStream_t stream)
+{
+    if (a.rank < 1 || a.rank > (unsigned)a.n) return cudaErrorInvalidValue;
+    const int nrows = a.F.u ? a.F.n : a.n;
+    // inside a cached bin the small window buffers fit three times the CTAs per SM
+    const bool narrow = a.hist_cache && a.cache_valid && a.hist_coarse;
+    int grid = num_sms * (narrow ? 24 : 12);
+    if (grid > nrows) grid = nrows;
+    return narrow ? launch_select_cfg<SelNarrow>(a, geographic, exact, grid, stream)
+                  : launch_select_cfg<SelWide>(a, geographic, exact, grid, stream);
 }
 
 cudaError_t launch_select_hist(const SelectArgs& a, bool geographic, int num_sms, cudaStream_t stream)
@@ -743,12 +770,13 @@ cudaError_t launch_select_hist_batch(const SelectArgs* segs, const long long* st
 cudaError_t launch_select_batch(const SelectArgs* segs, const long long* start, int nseg, bool geographic, bool exact,
                                 int num_sms, cudaStream_t stream)
 {
-    const int grid = num_sms * 12;
-    const size_t smem = sizeof(SelShared);
+    // every segment carries a valid cache with its segment counts: the narrow window buffers
+    const int grid = num_sms * 24;
+    const size_t smem = sizeof(SelNarrow::Shared);
 #define GW_SELB(G, E)                                                                                       \
     do {                                                                                                    \
-        raise_smem_limit((const void*)k_select_batch<G, E>, smem); \
-        k_select_batch<G, E><<<grid, SEL_THREADS, smem, stream>>>(segs, start, nseg);                       \
+        raise_smem_limit((const void*)k_select_batch<G, E, SelNarrow>, smem);                               \
+        k_select_batch<G, E, SelNarrow><<<grid, SEL_THREADS, smem, stream>>>(segs, start, nseg);            \
     } while (0)
     if (geographic) {
         if (exact) GW_SELB(true, true);
