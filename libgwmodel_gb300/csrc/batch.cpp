@@ -257,6 +257,10 @@ private:
         }
         for (auto& e : eng_) e->hist_valid_ = true;
         hist_ready_ = true;
+        // the select argument tables were built before the caches existed (null
+        // cache pointers make every select scan whole rows): rebuild them
+        dropGraph();
+        build();
     }
 
     SelectArgs selectArgs(Engine& e, unsigned rank, double* out)
