@@ -227,6 +227,8 @@ typedef struct gwgpu_stats {
        then the largest tile loop of one CTA, prologue, kernel start to end
        (summed), and the largest tile count of one CTA */
     double contract_phase_cycles[12];
+    int d2c_fills;              /* distance cache fills (mixed geographic contraction) */
+    double d2c_fill_ms;         /* their duration */
 } gwgpu_stats;
 
 int gwgpu_engine_create(int device, gwgpu_engine** out);
@@ -254,8 +256,23 @@ int gwgpu_engine_max_distance(gwgpu_engine* e, double* out);
  * pairs sorted by bandwidth; *count receives their number. */
 int gwgpu_engine_golden(gwgpu_engine* e, int adaptive, int kernel, int criterion, double lower, double upper,
                         double* bandwidth, int* count, double* list_bw, double* list_value, int cap);
-/* Drop the dataset's cached order statistics and distance histograms. */
+/* Drop the dataset's cached order statistics, distance histograms and
+   distance cache contents. */
 int gwgpu_engine_clear_cache(gwgpu_engine* e);
+/* Distance cache of the mixed geographic contraction (no counterpart in
+ * libgwmodel, whose CRSDistance::distance recomputes a focus row's distances
+ * at every evaluation, CRSDistance.cpp:122-131): the FP32 squared distance of
+ * every pair, filled once per dataset with the arithmetic of the weight
+ * producer, so cached and uncached results are bit-identical.  It takes
+ * n^2 x 4 bytes (160 GB at n = 200,000); one buffer per device is shared by
+ * all engines on it, owned by the engine that used it last and freed with
+ * that engine or by _release_.  limit_bytes < 0: automatic (the default; used
+ * when max(16 GB, 1/8 of the device) stays free beside it), 0: never, > 0: at
+ * most that many bytes. */
+int gwgpu_engine_set_distance_cache(gwgpu_engine* e, long long limit_bytes);
+int gwgpu_engine_release_distance_cache(gwgpu_engine* e);
+/* *active = 1 when the device's distance cache holds this engine's dataset. */
+int gwgpu_engine_distance_cache_active(gwgpu_engine* e, int* active);
 /* Coefficients at nr prediction locations (nr x 2 column-major) from the
    resident data at the given bandwidth (FP64, exact thresholds); betas nr x p. */
 int gwgpu_engine_predict(gwgpu_engine* e, int nr, const double* locations, double bandwidth, int adaptive,

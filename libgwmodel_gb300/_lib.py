@@ -40,7 +40,8 @@ class Stats(ctypes.Structure):
                 ("contract_ms", ctypes.c_double), ("contract_flops", ctypes.c_double),
                 ("contract_bytes", ctypes.c_double), ("select_launches", ctypes.c_int),
                 ("select_ms", ctypes.c_double), ("kernel_launches", ctypes.c_longlong),
-                ("contract_tiles", ctypes.c_longlong), ("contract_phase_cycles", ctypes.c_double * 12)]
+                ("contract_tiles", ctypes.c_longlong), ("contract_phase_cycles", ctypes.c_double * 12),
+                ("d2c_fills", ctypes.c_int), ("d2c_fill_ms", ctypes.c_double)]
 
 
 class Request(ctypes.Structure):
@@ -166,6 +167,9 @@ SIGNATURES = [
     ("gwgpu_engine_max_distance", _i, [_vp, _dp]),
     ("gwgpu_engine_golden", _i, [_vp, _i, _i, _i, _d, _d, _dp, _ip, _dp, _dp, _i]),
     ("gwgpu_engine_clear_cache", _i, [_vp]),
+    ("gwgpu_engine_set_distance_cache", _i, [_vp, ctypes.c_longlong]),
+    ("gwgpu_engine_release_distance_cache", _i, [_vp]),
+    ("gwgpu_engine_distance_cache_active", _i, [_vp, _ip]),
     ("gwgpu_engine_predict", _i, [_vp, _i, _dp, _d, _i, _i, _dp]),
     ("gwgpu_engine_event_record", _i, [_vp, _i]),
     ("gwgpu_engine_event_elapsed", _i, [_vp, _i, _i, ctypes.POINTER(ctypes.c_float)]),

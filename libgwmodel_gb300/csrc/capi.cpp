@@ -518,6 +518,25 @@ int gwgpu_engine_clear_cache(gwgpu_engine* e)
     return guarded([&] { e->eng.clearCaches(); });
 }
 
+int gwgpu_engine_set_distance_cache(gwgpu_engine* e, long long limit_bytes)
+{
+    ENG_CHECK(e);
+    return guarded([&] { e->eng.setDistanceCacheLimit(limit_bytes); });
+}
+
+int gwgpu_engine_release_distance_cache(gwgpu_engine* e)
+{
+    ENG_CHECK(e);
+    return guarded([&] { e->eng.releaseDistanceCache(); });
+}
+
+int gwgpu_engine_distance_cache_active(gwgpu_engine* e, int* active)
+{
+    ENG_CHECK(e);
+    if (!active) return fail(GWGPU_ERR_INVALID, "null output");
+    return guarded([&] { *active = e->eng.distanceCacheActive() ? 1 : 0; });
+}
+
 int gwgpu_engine_event_record(gwgpu_engine* e, int slot)
 {
     ENG_CHECK(e);
@@ -564,6 +583,8 @@ int gwgpu_engine_get_stats(gwgpu_engine* e, gwgpu_stats* out)
     out->kernel_launches = s.kernel_launches;
     out->contract_tiles = s.contract_tiles;
     for (int q = 0; q < 12; q++) out->contract_phase_cycles[q] = s.contract_phase_cycles[q];
+    out->d2c_fills = s.d2c_fills;
+    out->d2c_fill_ms = s.d2c_fill_ms;
     return GWGPU_OK;
 }
 

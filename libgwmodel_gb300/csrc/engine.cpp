@@ -5,6 +5,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <numeric>
 #include <thread>
 
@@ -218,6 +219,36 @@ double aicc(double n, double rss, double trS)
     return n * std::log(rss / n) + n * std::log(2 * M_PI) + n * ((n + trS) / (n - 2 - trS));
 }
 
+// The distance cache of each device, shared by the engines on it (see
+// Engine::setDistanceCacheLimit).  Every launch that fills or reads it runs
+// under `mu` and records `used` on its engine's stream; a new owner's stream
+// waits for that event before it overwrites the buffer.
+struct DeviceD2Cache {
+    std::mutex mu;
+    float* ptr = nullptr;
+    size_t bytes = 0;
+    const Engine* owner = nullptr;
+    cudaEvent_t used = nullptr;
+};
+constexpr int kMaxDevices = 64;
+DeviceD2Cache g_d2c[kMaxDevices];
+
+DeviceD2Cache& device_d2c(int device)
+{
+    if (device < 0 || device >= kMaxDevices) throw std::invalid_argument("device ordinal out of range");
+    return g_d2c[device];
+}
+
+// Frees the device's cache (the caller holds its lock); waits for its last use.
+void free_d2c(DeviceD2Cache& c)
+{
+    if (c.used) cudaEventSynchronize(c.used);
+    if (c.ptr) cudaFree(c.ptr);
+    c.ptr = nullptr;
+    c.bytes = 0;
+    c.owner = nullptr;
+}
+
 }  // namespace
 
 Engine::Engine(int device) : device_(device)
@@ -233,6 +264,14 @@ Engine::Engine(int device) : device_(device)
 Engine::~Engine()
 {
     if (stream_) cudaStreamSynchronize(stream_);
+    if (device_ >= 0 && device_ < kMaxDevices) {
+        DeviceD2Cache& c = g_d2c[device_];
+        std::lock_guard<std::mutex> lk(c.mu);
+        if (c.owner == this) {
+            cudaSetDevice(device_);
+            free_d2c(c);
+        }
+    }
     for (auto& e : events_)
         if (e) cudaEventDestroy(e);
     for (auto& pt : pending_) {
@@ -395,6 +434,7 @@ void Engine::setData(int n, int p, const double* x, const double* y, const doubl
     hist_.clear();
     hist_tried_ = false;
     hist_valid_ = false;
+    d2c_valid_ = false;
     buildProxy();
 }
 
@@ -716,7 +756,7 @@ EngineStats& Engine::stats()
     for (auto& pt : pending_) {
         float ms = 0.f;
         if (cudaEventSynchronize(pt.e1) == cudaSuccess && cudaEventElapsedTime(&ms, pt.e0, pt.e1) == cudaSuccess)
-            (pt.kind == 0 ? stats_.contract_ms : stats_.select_ms) += ms;
+            (pt.kind == 0 ? stats_.contract_ms : pt.kind == 1 ? stats_.select_ms : stats_.d2c_fill_ms) += ms;
         cudaEventDestroy(pt.e0);
         cudaEventDestroy(pt.e1);
     }
@@ -753,7 +793,6 @@ void Engine::contractMixed(double* G, int ldg, int mcols, double bw, bool adapti
         check(launch_to_float(n_, thr_.get(), thr32_.get(), stream_), "thr32");
         stats_.kernel_launches += 1;
     }
-    cudaEvent_t e0 = stats_on_ ? timerBegin() : nullptr;
     TcArgs a{};
     a.n = n_;
     a.mcols = mcols;
@@ -773,6 +812,15 @@ void Engine::contractMixed(double* G, int ldg, int mcols, double bw, bool adapti
     a.G = G;
     a.ldg = ldg;
     a.err = err_.get();
+    // geographic: the pair distances come from the device's distance cache when it fits
+    DeviceD2Cache& dc = device_d2c(device_);
+    std::unique_lock<std::mutex> d2lock(dc.mu, std::defer_lock);
+    if (geographic_ && d2c_limit_bytes_ != 0) {
+        d2lock.lock();
+        a.d2c = ensureDistanceCache();
+        if (!a.d2c) d2lock.unlock();
+    }
+    cudaEvent_t e0 = stats_on_ ? timerBegin() : nullptr;
     if (stats_on_) {
         if (!tile_count_.get()) {
             tile_count_.alloc(1);
@@ -787,6 +835,10 @@ void Engine::contractMixed(double* G, int ldg, int mcols, double bw, bool adapti
     }
     check(launch_contract_tc(a, geographic_, stream_), "contract_tc");
     stats_.kernel_launches += 1;
+    if (a.d2c) {
+        check(cudaEventRecord(dc.used, stream_), "cudaEventRecord");
+        d2lock.unlock();
+    }
     if (stats_on_) {
         timerEnd(e0, 0);
         stats_.contract_launches += 1;
@@ -794,6 +846,7 @@ void Engine::contractMixed(double* G, int ldg, int mcols, double bw, bool adapti
         if (adaptive && kernel >= GW_KERNEL_BISQUARE) pairs = (double)n_ * std::max(0.0, std::min(bw, (double)n_) - 1);
         stats_.contract_flops += 2.0 * mcols * pairs;
         stats_.contract_bytes += 2.0 * npad_ * 128.0 * ntiles32_ * 2 + 8.0 * n_ * mcols + 16.0 * n_;
+        if (a.d2c) stats_.contract_bytes += 4.0 * pairs;  // the cached distances of the nonzero pairs
     }
 }
 
@@ -871,8 +924,25 @@ const double* Engine::orderStatistic(unsigned rank)
     a.out = r->v.get();
     a.err = sel_err_.get();
     if (hist_.get() && !hist_valid_) {
+        // geographic mixed data: the histogram pass fills the distance cache on the way
+        DeviceD2Cache& dc = device_d2c(device_);
+        std::unique_lock<std::mutex> lk(dc.mu, std::defer_lock);
+        float* fill = nullptr;
+        if (geographic_ && precision_ == kMixed && d2c_limit_bytes_ != 0) {
+            lk.lock();
+            if (!(dc.owner == this && d2c_valid_)) fill = acquireDistanceCache();
+            if (!fill) lk.unlock();
+        }
+        a.d2c_out = fill;
         check(launch_select_hist(a, geographic_, num_sms_, stream_), "select histograms");
+        a.d2c_out = nullptr;
         stats_.kernel_launches += 1;
+        if (fill) {
+            d2c_valid_ = true;
+            stats_.d2c_fills += 1;
+            check(cudaEventRecord(dc.used, stream_), "cudaEventRecord");
+            lk.unlock();
+        }
         hist_valid_ = true;
         a.cache_valid = 1;
     }
@@ -1350,8 +1420,80 @@ void Engine::predict(int nr, const double* locations, double bw, bool adaptive, 
     }
 }
 
+void Engine::releaseDistanceCache()
+{
+    DeviceD2Cache& c = device_d2c(device_);
+    std::lock_guard<std::mutex> lk(c.mu);
+    d2c_valid_ = false;
+    if (c.owner != this) return;
+    check(cudaSetDevice(device_), "cudaSetDevice");
+    free_d2c(c);
+}
+
+bool Engine::distanceCacheActive() const
+{
+    DeviceD2Cache& c = device_d2c(device_);
+    std::lock_guard<std::mutex> lk(c.mu);
+    return c.owner == this && d2c_valid_;
+}
+
+// The device's distance cache holding this dataset, filled now if needed, or
+// null when the cache does not apply or does not fit.  The caller holds the
+// cache's lock and records its `used` event after the launch that reads it.
+const float* Engine::ensureDistanceCache()
+{
+    DeviceD2Cache& c = g_d2c[device_];
+    if (c.owner == this && d2c_valid_ && c.ptr) return c.ptr;
+    float* d2c = acquireDistanceCache();
+    if (!d2c) return nullptr;
+    cudaEvent_t e0 = stats_on_ ? timerBegin() : nullptr;
+    check(launch_fill_d2(n_, pts32_.get(), d2c, stream_), "fill distance cache");
+    stats_.kernel_launches += 1;
+    if (stats_on_) {
+        timerEnd(e0, 2);
+        stats_.d2c_fills += 1;
+    }
+    d2c_valid_ = true;
+    return d2c;
+}
+
+// The device's distance cache, owned by this engine and large enough for its
+// dataset (contents not yet this dataset's: the caller fills it), or null.
+// The caller holds the cache's lock.
+float* Engine::acquireDistanceCache()
+{
+    if (!geographic_ || precision_ != kMixed || d2c_limit_bytes_ == 0 || n_ < 1) return nullptr;
+    DeviceD2Cache& c = g_d2c[device_];
+    d2c_valid_ = false;
+    const size_t need = d2_cache_bytes(n_);
+    if (d2c_limit_bytes_ > 0 && need > (size_t)d2c_limit_bytes_) return nullptr;
+    if (c.bytes < need) {
+        if (c.ptr) free_d2c(c);
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        const size_t reserve = std::max((size_t)16 << 30, total_b / 8);
+        if (need + reserve > free_b) return nullptr;
+        if (cudaMalloc(&c.ptr, need) != cudaSuccess) {
+            cudaGetLastError();  // too little memory after all: run without the cache
+            c.ptr = nullptr;
+            return nullptr;
+        }
+        c.bytes = need;
+        c.owner = nullptr;
+    }
+    if (!c.used) check(cudaEventCreateWithFlags(&c.used, cudaEventDisableTiming), "cudaEventCreate");
+    // the previous owner's launches that read the buffer come first
+    if (c.owner && c.owner != this) check(cudaStreamWaitEvent(stream_, c.used, 0), "cudaStreamWaitEvent");
+    c.owner = this;
+    return c.ptr;
+}
+
 void Engine::clearCaches()
 {
+    d2c_valid_ = false;
     recycleRanks();
     hist_valid_ = false;
     thr_valid_ = false;

@@ -83,6 +83,8 @@ struct EngineStats {
     double solve_ms = 0.0;
     int criterion_evals = 0;
     long long kernel_launches = 0;  // kernels launched by the engine (always counted)
+    int d2c_fills = 0;              // distance cache fills
+    double d2c_fill_ms = 0.0;       // their event-timed duration
 };
 
 struct FitOutput {
@@ -163,8 +165,19 @@ public:
     // record with (bandwidth, criterion).
     double golden(bool adaptive, int kernel, int crit, double lower, double upper, std::map<double, double>& record);
     // Forget the per-dataset caches (order statistics, distance histograms,
-    // thresholds) so the next search recomputes everything.
+    // thresholds, the distance cache's contents) so the next search
+    // recomputes everything.
     void clearCaches();
+    // Distance cache of the mixed geographic contraction (the FP32 squared
+    // distance of every pair, n^2 x 4 bytes: 160 GB at n = 200,000).  One
+    // buffer per device is shared by the engines on it: the engine that
+    // uses it last owns its contents, and it is freed with its owner or by
+    // releaseDistanceCache().  limit < 0: automatic (used when the device
+    // keeps max(16 GB, 1/8 of its memory) free beside it); 0: never; > 0: at
+    // most that many bytes.
+    void setDistanceCacheLimit(long long bytes) { d2c_limit_bytes_ = bytes; }
+    void releaseDistanceCache();
+    bool distanceCacheActive() const;
     // CUDA events on the engine stream (slots 0..7) for device timing.
     void recordEvent(int slot);
     float elapsedMs(int a, int b);
@@ -191,6 +204,8 @@ private:
     void buildProxy();
     void contractMixed(double* G, int ldg, int mcols, double bw, bool adaptive, int kernel, bool exclude_self,
                        int wpow);
+    const float* ensureDistanceCache();  // called with the device cache's lock held
+    float* acquireDistanceCache();       // likewise
     void computeThresholds(double bw, bool adaptive);
     const double* thrPtr(bool adaptive) const { return adaptive ? thr_.get() : nullptr; }
     void contract(const double* Z, int mcols, double* G, int ldg, double bw, bool adaptive, int kernel,
@@ -262,6 +277,8 @@ private:
     DevBuf<float2> acc_;
     DevBuf<float> thr32_;
     DevBuf<int> err_;
+    long long d2c_limit_bytes_ = -1;
+    bool d2c_valid_ = false;  // this engine's dataset is in the device cache (while it owns it)
     DevBuf<unsigned long long> tile_count_;
     DevBuf<unsigned long long> tc_prof_;  // phase cycles of the contraction (stats)
     // prediction points (Hilbert order): FP64 coordinates, FP32 records, 16-point

@@ -36,6 +36,9 @@ struct SelectArgs {
     // coordinates and FP32 records of F.n focus points.  Null F.u: the data.
     DevPoints F;
     const float4* fpts;
+    // Geographic data rows only (F.u null), or null: the histogram pass also
+    // fills this distance cache (layout of launch_fill_d2) from the same values.
+    float* d2c_out;
 };
 // exact: FP64 order statistics (bit-exact); otherwise the FP32 proxy's.
 cudaError_t launch_select(const SelectArgs& a, bool geographic, bool exact, int num_sms, cudaStream_t stream);
@@ -164,6 +167,7 @@ struct TcArgs {
     int* err;                     // set to 1 if a bounded wait timed out
     unsigned long long* tiles;    // if not null: += 128 x 32 weight tiles processed
     unsigned long long* prof;     // if not null: += clock64 cycles per phase (kTcProfSlots slots)
+    const float* d2c;             // geographic only, optional: the distance cache of launch_fill_d2
 };
 // Phase slots of TcArgs::prof, summed over CTAs (producer: warp 0 lane 0;
 // control: the issuing thread).
@@ -191,6 +195,16 @@ cudaError_t launch_contract_tc_batch(const TcArgs* segs, const int2* work, int n
                                      int flush_tiles, bool geographic, int kernel, cudaStream_t stream);
 cudaError_t launch_build_zimg(int n, int mcols, int npad, const double* Z, int ldz, unsigned char* img,
                               cudaStream_t stream);
+// Distance cache of the mixed geographic contraction: the FP32 squared
+// great-circle distance of every (focus row, data point) pair, exactly the
+// value the contraction's weight producer computes, for rows padded to whole
+// 128-row blocks and points padded to whole 32-point tiles.  Block (rb, tile)
+// is 4096 floats at ((rb * ntiles + tile) * 4096), ordered [quarter 4][half 2]
+// [row 128][4 points] so the producer thread of (row, quarter) reads its 8
+// points as two float4 and a warp's loads are contiguous; padded pairs hold
+// FLT_MAX.  pts: the 2 float4 records per point, padded to whole tiles.
+size_t d2_cache_bytes(int n);
+cudaError_t launch_fill_d2(int n, const float4* pts, float* d2c, cudaStream_t stream);
 // D[128 x N] = A[128 x 32] B[N x 32]^T through tcgen05 (device pointers).
 cudaError_t launch_tc_selftest(const float* A, const float* B, float* D, int N, int* err, cudaStream_t stream);
 

@@ -22,6 +22,10 @@
 // largest threshold (FP32 tile bounds) and, for great-circle distances, pairs
 // beyond the row's haversine cut-off.  Every wait is bounded and reports
 // through err.
+// With a distance cache (CACHED, geographic) the producers read each pair's
+// FP32 squared distance -- filled once per dataset by k_fill_d2 with the same
+// arithmetic -- instead of computing it: about 14 instead of 58 instructions
+// per weight, bit-identical weights, and no point records to stage.
 #include "gw_common.cuh"
 #include "gw_kernels.h"
 #include "mixed_weight.cuh"
@@ -45,6 +49,7 @@ constexpr uint32_t TC_WAIT = 1u << 22;
 constexpr uint32_t TC_ACC_COLS = 256;  // TMEM column of the second accumulator
 constexpr int TC_MAX_NB = 3;           // Z stages at most
 constexpr uint32_t TC_P_MAX = 2u * 16u * TC_BK;  // point records of one tile, geographic
+constexpr uint32_t TC_D_BYTES = TC_M * TC_BK * 4;  // one cached 128 x 32 distance block
 
 struct Smem {
     uint64_t full_a[2];          // weight tile k written: one arrival per producer warp
@@ -109,10 +114,12 @@ __device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity)
 // KERN: the weight kernel when fixed at compile time, -1 to read it from the arguments.
 // BATCH: CTA b works on segment work[b].x (arguments segs[work[b].x]) at row
 // block work[b].y, so one launch covers many datasets and bandwidths.
-template <bool GEO, int KERN, bool BATCH>
+// CACHED: weights from the distance cache a.d2c (geographic, single dataset only).
+template <bool GEO, int KERN, bool BATCH, bool CACHED = false>
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    k_contract_tc(TcArgs a0, int nb, const TcArgs* __restrict__ segs, const int2* __restrict__ work)
+    k_contract_tc(TcArgs a0, int nb, int nd, const TcArgs* __restrict__ segs, const int2* __restrict__ work)
 {
+    static_assert(!CACHED || (GEO && !BATCH), "the distance cache serves single geographic datasets");
     const TcArgs a = BATCH ? segs[work[blockIdx.x].x] : a0;
     const int kernel = KERN >= 0 ? KERN : a.kernel;
     extern __shared__ unsigned char smem_dyn[];
@@ -213,7 +220,32 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         long long c0 = prof ? clock64() : 0, c1 = 0;
         const long long loop0 = c0;
         if (prof) pc[kTcProfPrologue] = (unsigned long long)(c0 - kstart);
-        for (int tile = walk.next(); tile >= 0; tile = walk.next(), k++) {
+        // cached: this thread's 8 distances of a tile are two float4 of its row and
+        // quarter, loaded one visited tile ahead (from L2: the control thread
+        // prefetches the blocks nd tiles ahead)
+        const float4* d2row = CACHED ? reinterpret_cast<const float4*>(a.d2c) +
+                                           (size_t)blockIdx.x * a.ntiles * (TC_D_BYTES / 16) + quarter * 256 + r
+                                     : nullptr;
+        int tnext = walk.next();
+        int tpre = (CACHED && tnext >= 0) ? walk.next() : -1;
+        float4 nd0 = make_float4(0.f, 0.f, 0.f, 0.f), nd1 = nd0;
+        if (CACHED && tnext >= 0) {
+            nd0 = __ldcs(d2row + (size_t)tnext * (TC_D_BYTES / 16));
+            nd1 = __ldcs(d2row + (size_t)tnext * (TC_D_BYTES / 16) + 128);
+        }
+        for (; tnext >= 0; k++) {
+            const int tile = tnext;
+            const float4 cd0 = nd0, cd1 = nd1;
+            if (CACHED) {
+                tnext = tpre;
+                tpre = tnext >= 0 ? walk.next() : -1;
+                if (tnext >= 0) {
+                    nd0 = __ldcs(d2row + (size_t)tnext * (TC_D_BYTES / 16));
+                    nd1 = __ldcs(d2row + (size_t)tnext * (TC_D_BYTES / 16) + 128);
+                }
+            } else {
+                tnext = walk.next();
+            }
             if (__any_sync(0xffffffffu, *(volatile int*)&ctl.abort != 0)) {
                 ok = false;
                 break;
@@ -227,7 +259,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 pc[kTcProfStageWait] += c1 - c0;
                 c0 = c1;
             }
-            if (!stage_ok || !warp_wait(&ctl.full_p[s], (uint32_t)((k >> 1) & 1))) {
+            if (!stage_ok || (!CACHED && !warp_wait(&ctl.full_p[s], (uint32_t)((k >> 1) & 1)))) {
                 if (lane == 0) atomicExch(&ctl.abort, 1);
                 ok = false;
                 break;
@@ -246,6 +278,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 float w[4];
                 bool in[4];
                 GeoChord g[4];
+                if constexpr (CACHED) {
+                    const float4 dv = q4 ? cd1 : cd0;  // row r, points kbase + 4 q4 .. + 3
+                    const float dd[4] = {dv.x, dv.y, dv.z, dv.w};
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        const int j = tile * TC_BK + kbase + q4 * 4 + e;
+                        float v = weight32(kernel, dd[e], rr, inv_r2);
+                        v = (j == self_j) ? 0.0f : v;
+                        v = square ? v * v : v;
+                        w[e] = (row_ok && j < a.n) ? v : 0.0f;
+                    }
+                } else {
 #pragma unroll
                 for (int e = 0; e < 4; e++) {
                     const int kk = kbase + q4 * 4 + e;
@@ -272,6 +316,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                         v = square ? v * v : v;
                         w[e] = in[e] ? v : 0.0f;
                     }
+                }
                 }
                 float hi[4], lo[4];
 #pragma unroll
@@ -338,11 +383,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         if (prof) atomicAdd(a.prof + kTcProfFlush, pflush);
     } else if (lane == 0) {
-        TileWalker wz, wp, wm;  // Z copies (nb ahead), point copies (2 ahead), MMAs
+        TileWalker wz, wp, wm;  // Z copies (nb ahead), point copies (2 ahead) or L2 prefetches (nd ahead), MMAs
         wz.init(tmask, nwords);
         wp.init(tmask, nwords);
         wm.init(tmask, nwords);
-        int kz = 0, kp = 0;  // copies issued
+        int kz = 0, kp = 0;  // copies (or prefetches) issued
+        const float* d2blk = CACHED ? a.d2c + (size_t)blockIdx.x * a.ntiles * (TC_D_BYTES / 4) : nullptr;
+        auto issue_d = [&](int tl) {
+            bulk_prefetch_l2(d2blk + (size_t)tl * (TC_D_BYTES / 4), TC_D_BYTES);
+            kp++;
+        };
         int last_mma = -1;
         auto issue_z = [&](int tl) {
             const int sb = kz % nb;
@@ -362,10 +412,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (tl < 0) break;
             issue_z(tl);
         }
-        for (int q = 0; q < 2; q++) {
+        for (int q = 0; q < (CACHED ? nd : 2); q++) {
             const int tl = wp.next();
             if (tl < 0) break;
-            issue_p(tl);
+            if (CACHED) issue_d(tl);
+            else issue_p(tl);
         }
         const uint32_t idesc = idesc_tf32(TC_M, a.npad);
         const bool prof = a.prof != nullptr;
@@ -385,9 +436,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 c0 = c1;
             }
             // the producers are done with point buffer s: fetch the records of tile k + 2
-            if (kp == k + 2) {
+            // (cached: keep the L2 prefetch of the distance blocks nd tiles ahead)
+            if (!CACHED && kp == k + 2) {
                 const int tl = wp.next();
                 if (tl >= 0) issue_p(tl);
+            } else if (CACHED && kp == k + nd) {
+                const int tl = wp.next();
+                if (tl >= 0) issue_d(tl);
             }
             bool ok = mbar_wait(&ctl.full_b[sb], (uint32_t)((k / nb) & 1), TC_WAIT);
             if (ok && k % F == 0 && c >= 2)
@@ -440,7 +495,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (last_mma >= 0) mbar_wait(&ctl.mma_done[last_mma & 1], (uint32_t)((last_mma >> 1) & 1), TC_WAIT);
             for (int j = kz - nb > 0 ? kz - nb : 0; j < kz; j++)
                 mbar_wait(&ctl.full_b[j % nb], (uint32_t)((j / nb) & 1), TC_WAIT);
-            for (int j = kp - 2 > 0 ? kp - 2 : 0; j < kp; j++)
+            for (int j = kp - 2 > 0 ? kp - 2 : 0; j < kp && !CACHED; j++)
                 mbar_wait(&ctl.full_p[j & 1], (uint32_t)((j >> 1) & 1), TC_WAIT);
         }
     }
@@ -546,7 +601,66 @@ __global__ void k_build_zimg(int n, int mcols, int npad, const double* __restric
     }
 }
 
+// Distance cache: CTA (row block rb, group of FD_TILES tiles); thread (r,
+// quarter) computes points [8 quarter, 8 quarter + 8) of row rb * 128 + r for
+// every tile of the group with the producer's arithmetic (geo_chord32, the
+// warp-voted near-angle form) and streams them out as two float4, so each
+// warp store covers 512 contiguous bytes.
+constexpr int FD_TILES = 32;
+
+__global__ void __launch_bounds__(512) k_fill_d2(int n, int ntiles, const float4* __restrict__ pts,
+                                                  float* __restrict__ d2c)
+{
+    const int t = threadIdx.x, r = t & (TC_M - 1), quarter = t >> 7;
+    const int rb = blockIdx.x;
+    const int i = rb * TC_M + r;
+    float4 fa = make_float4(0.f, 0.f, 0.f, 0.f), fb = fa;
+    if (i < n) {
+        fa = pts[2 * (size_t)i];
+        fb = pts[2 * (size_t)i + 1];
+    }
+    const float fz = fa.z + fb.z;
+    const int t0 = blockIdx.y * FD_TILES, t1 = min(ntiles, t0 + FD_TILES);
+    float4* out = reinterpret_cast<float4*>(d2c) + (size_t)rb * ntiles * 1024 + quarter * 256 + r;
+    for (int tile = t0; tile < t1; tile++) {
+#pragma unroll
+        for (int q4 = 0; q4 < 2; q4++) {
+            GeoChord g[4];
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const size_t j = (size_t)tile * TC_BK + quarter * 8 + q4 * 4 + e;  // records padded to whole tiles
+                g[e] = geo_chord32(fa, fb, fz, pts[2 * j], pts[2 * j + 1]);
+            }
+            const bool near = __all_sync(0xffffffffu, fmaxf(fmaxf(g[0].S, g[1].S), fmaxf(g[2].S, g[3].S)) <= 0.25f);
+            float d[4];
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int j = tile * TC_BK + quarter * 8 + q4 * 4 + e;
+                const float d2 = near ? geo_d2_near(g[e]) : geo_d2_from_chord(g[e]);
+                d[e] = (i < n && j < n) ? d2 : 3.402823466e38f;
+            }
+            __stcs(out + (size_t)tile * 1024 + q4 * 128, make_float4(d[0], d[1], d[2], d[3]));
+        }
+    }
+}
+
 }  // namespace
+
+size_t d2_cache_bytes(int n)
+{
+    const size_t nrb = ((size_t)n + TC_M - 1) / TC_M, ntiles = ((size_t)n + TC_BK - 1) / TC_BK;
+    return nrb * ntiles * (size_t)TC_M * TC_BK * sizeof(float);
+}
+
+cudaError_t launch_fill_d2(int n, const float4* pts, float* d2c, cudaStream_t stream)
+{
+    if (n < 1 || !pts || !d2c) return cudaErrorInvalidValue;
+    const int nrb = (n + TC_M - 1) / TC_M, ntiles = (n + TC_BK - 1) / TC_BK;
+    const int groups = (ntiles + FD_TILES - 1) / FD_TILES;
+    if (groups > 65535) return cudaErrorInvalidValue;
+    k_fill_d2<<<dim3(nrb, groups), 512, 0, stream>>>(n, ntiles, pts, d2c);
+    return cudaGetLastError();
+}
 
 size_t contract_tc_smem_bytes(int npad, int ntiles, int nb)
 {
@@ -563,11 +677,17 @@ cudaError_t launch_contract_tc(const TcArgs& a, bool geographic, cudaStream_t st
     const size_t smem = contract_tc_smem_bytes(a.npad, a.ntiles, nb);
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
     const int grid = (a.n + TC_M - 1) / TC_M;
+    // cached: the L2 prefetch of the distance blocks runs 4 tiles ahead
+    const int nd = 4;
     auto go = [&](auto kfn) {
         raise_smem_limit((const void*)kfn, smem);
-        kfn<<<grid, TC_THREADS, smem, stream>>>(a, nb, nullptr, nullptr);
+        kfn<<<grid, TC_THREADS, smem, stream>>>(a, nb, nd, nullptr, nullptr);
     };
-    if (geographic) {
+    if (geographic && a.d2c) {
+        if (a.kernel == GW_KERNEL_BISQUARE) go(k_contract_tc<true, GW_KERNEL_BISQUARE, false, true>);
+        else if (a.kernel == GW_KERNEL_GAUSSIAN) go(k_contract_tc<true, GW_KERNEL_GAUSSIAN, false, true>);
+        else go(k_contract_tc<true, -1, false, true>);
+    } else if (geographic) {
         if (a.kernel == GW_KERNEL_BISQUARE) go(k_contract_tc<true, GW_KERNEL_BISQUARE, false>);
         else if (a.kernel == GW_KERNEL_GAUSSIAN) go(k_contract_tc<true, GW_KERNEL_GAUSSIAN, false>);
         else go(k_contract_tc<true, -1, false>);
@@ -591,7 +711,7 @@ cudaError_t launch_contract_tc_batch(const TcArgs* segs, const int2* work, int n
     TcArgs none{};
     auto go = [&](auto kfn) {
         raise_smem_limit((const void*)kfn, smem);
-        kfn<<<nwork, TC_THREADS, smem, stream>>>(none, nb, segs, work);
+        kfn<<<nwork, TC_THREADS, smem, stream>>>(none, nb, 2, segs, work);
     };
     if (geographic) {
         if (kernel == GW_KERNEL_BISQUARE) go(k_contract_tc<true, GW_KERNEL_BISQUARE, true>);

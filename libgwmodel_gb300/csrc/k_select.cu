@@ -528,6 +528,8 @@ __global__ void __launch_bounds__(SEL_THREADS)
 constexpr int HS_ROWS = 8;
 constexpr int HS_THREADS = 1024;  // 32 warps at <= 64 registers: the pass is latency-bound
 
+__device__ void hist_store(const unsigned* hs, const SelectArgs& a, int row0, int nrows);
+
 // Histograms of rows [row0, row0 + HS_ROWS) of one dataset into its cache.
 template <bool GEO>
 __device__ void hist_rows(unsigned* hs, float4 (*rf)[2], const SelectArgs& a, int row0)
@@ -593,6 +595,14 @@ __device__ void hist_rows(unsigned* hs, float4 (*rf)[2], const SelectArgs& a, in
         }
     }
     __syncthreads();
+    hist_store(hs, a, row0, nrows);
+}
+
+// Writes the histograms of rows [row0, row0 + nrows) into the cache, with
+// their cumulative segment counts.
+__device__ void hist_store(const unsigned* hs, const SelectArgs& a, int row0, int nrows)
+{
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     for (int e = t; e < nrows * SEL_BINS; e += HS_THREADS) a.hist_cache[(size_t)row0 * SEL_BINS + e] = hs[e];
     if (a.hist_coarse) {
         // cumulative counts at the end of every 64-bin segment: one warp per row
@@ -622,13 +632,92 @@ __device__ void hist_rows(unsigned* hs, float4 (*rf)[2], const SelectArgs& a, in
     __syncthreads();
 }
 
+// The histogram pass of geographic data rows that also fills the distance
+// cache a.d2c_out (block (rb, tile) of 4096 floats at (rb * ntiles + tile) *
+// 4096, ordered [quarter 4][half 2][row 128][4 points]).  Lane (r = lane % 8,
+// quarter = lane / 8) of warp w computes row row0 + r's distances to points
+// [8 quarter, 8 quarter + 8) of tiles w, w + 32, ...; the 8 rows of a group
+// are consecutive within one 128-row block, so every (quarter, half) store of
+// a warp is one whole 128-byte line.  The distances and bins are those of
+// hist_rows (the same chord, the same near/far forms, which agree wherever
+// both apply), so the counts are identical.
+__device__ void hist_rows_fill(unsigned* hs, float4 (*rf)[2], const SelectArgs& a, int row0)
+{
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int n = a.n;
+    const Window wlog = coarse_window(a);
+    const bool fastbin = wlog.shift >= 29 && wlog.shift <= 52;
+    const int s2 = fastbin ? wlog.shift - 29 : 0;
+    const long long kbin = fastbin ? (long long)((896ull << 23) >> s2) + (long long)((1ull << 63) >> wlog.shift) -
+                                         (long long)(wlog.base >> wlog.shift)
+                                   : 0;
+    const int nrows = min(HS_ROWS, n - row0);
+    for (int b = t; b < HS_ROWS * SEL_BINS; b += HS_THREADS) hs[b] = 0;
+    if (t < HS_ROWS * 2) {
+        const int r = t / 2, q = t % 2;
+        rf[r][q] = r < nrows ? a.pts[2 * (size_t)(row0 + r) + q] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    const int r = lane & 7, quarter = lane >> 3;
+    const int row = row0 + r;
+    const bool row_ok = r < nrows;
+    const float4 ra = rf[r][0], rb = rf[r][1];
+    const float fz = ra.z + rb.z;
+    unsigned* hrow = hs + r * SEL_BINS;
+    float4* out = reinterpret_cast<float4*>(a.d2c_out) + (size_t)(row / 128) * a.ntiles * 1024 + quarter * 256 +
+                  (row & 127);
+    for (int tile = warp; tile < a.ntiles; tile += HS_THREADS / 32) {
+#pragma unroll
+        for (int q4 = 0; q4 < 2; q4++) {
+            GeoChord g[4];
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const size_t j = (size_t)tile * SEL_TILE + quarter * 8 + q4 * 4 + e;  // records padded to whole tiles
+                g[e] = geo_chord32(ra, rb, fz, a.pts[2 * j], a.pts[2 * j + 1]);
+            }
+            const bool near = __all_sync(0xffffffffu, fmaxf(fmaxf(g[0].S, g[1].S), fmaxf(g[2].S, g[3].S)) <= 0.25f);
+            float d[4];
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int j = tile * SEL_TILE + quarter * 8 + q4 * 4 + e;
+                const float d2 = near ? geo_d2_near(g[e]) : geo_d2_from_chord(g[e]);
+                d[e] = (row_ok && j < n) ? d2 : 3.402823466e38f;
+            }
+            if (row_ok) __stcs(out + (size_t)tile * 1024 + q4 * 128, make_float4(d[0], d[1], d[2], d[3]));
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int j = tile * SEL_TILE + quarter * 8 + q4 * 4 + e;
+                if (!row_ok || j >= n) continue;
+                const float d32 = d[e] > 0.0f ? d[e] * rsqrtf(d[e]) : 0.0f;
+                if (d32 == d32) {
+                    const uint32_t fb = __float_as_uint(d32);
+                    unsigned bin;
+                    if (fastbin) {
+                        const long long q = (long long)(fb >> s2) + kbin;
+                        bin = fb < 0x00800000u ? 0u : (unsigned)min(max(q, 0ll), (long long)(SEL_BINS - 1));
+                    } else {
+                        bin = bucket_of(wlog, dkey_f(d32));
+                    }
+                    atomicAdd(&hrow[bin], 1u);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    hist_store(hs, a, row0, nrows);
+}
+
 template <bool GEO>
 __global__ void __launch_bounds__(HS_THREADS, 1) k_select_hist(SelectArgs a)
 {
     extern __shared__ __align__(16) unsigned hs[];  // HS_ROWS x SEL_BINS
     __shared__ float4 rf[HS_ROWS][2];
     const int nfocus = a.F.u ? a.F.n : a.n;
-    for (int row0 = blockIdx.x * HS_ROWS; row0 < nfocus; row0 += gridDim.x * HS_ROWS) hist_rows<GEO>(hs, rf, a, row0);
+    const bool fill = GEO && a.d2c_out && !a.F.u;
+    for (int row0 = blockIdx.x * HS_ROWS; row0 < nfocus; row0 += gridDim.x * HS_ROWS) {
+        if (fill) hist_rows_fill(hs, rf, a, row0);
+        else hist_rows<GEO>(hs, rf, a, row0);
+    }
 }
 
 // Histogram caches of many datasets in one launch: segment s owns the row

@@ -266,6 +266,7 @@ private:
             if (!engines_[slot]) engines_[slot].reset(new Engine(device_));
             Engine& e = *engines_[slot];
             e.setHistLimit(hist_limit(r.n));
+            e.setDistanceCacheLimit(0);  // n^2 bytes per request would break the HBM budget's admission
             e.setData(r.n, r.p, q.x.data(), q.y.data(), q.coords.data(), r.geographic != 0);
             e.setPrecision(r.precision == GWGPU_MIXED ? kMixed : kFP64);
             double bw = r.bandwidth;

@@ -434,6 +434,20 @@ class Engine:
     def clear_cache(self):
         check(lib().gwgpu_engine_clear_cache(self._h))
 
+    def set_distance_cache(self, limit_bytes=-1):
+        """Distance cache of the mixed geographic contraction: -1 automatic
+        (default), 0 never, > 0 at most that many bytes (it takes n^2 x 4)."""
+        check(lib().gwgpu_engine_set_distance_cache(self._h, int(limit_bytes)))
+
+    def release_distance_cache(self):
+        """Free the device's distance cache if this engine owns it."""
+        check(lib().gwgpu_engine_release_distance_cache(self._h))
+
+    def distance_cache_active(self):
+        v = ctypes.c_int(0)
+        check(lib().gwgpu_engine_distance_cache_active(self._h, ctypes.byref(v)))
+        return bool(v.value)
+
     def record_event(self, slot):
         check(lib().gwgpu_engine_event_record(self._h, int(slot)))
 
