@@ -712,7 +712,7 @@ void Engine::ensureMixed()
         for (int k = 0; k < p; k++) tvec[k] = (k == intercept_col_) ? 1.0 / c : -mu_[k] / (c * sc_[k]);
     }
 
-    npad_ = (m_ + 63) / 64 * 64;
+    npad_ = (m_ + 15) / 16 * 16;  // the accumulator width: the tcgen05 N of an M = 128 MMA is a multiple of 16
     xs_.alloc((size_t)n * p);
     ys_.alloc(n);
     zs_.alloc((size_t)n * m_);
@@ -1216,7 +1216,7 @@ size_t Engine::estimateBytes(int n, int p, bool geographic, bool mixed, bool ada
 {
     const double N = n, P = p;
     const double m = P * (P + 1) / 2 + P, mm = P * (P + 1) / 2;
-    const double npad = std::ceil(m / 64) * 64;
+    const double npad = std::ceil(m / 16) * 16;
     const double t16 = std::ceil(N / 16), t32 = std::ceil(N / 32);
     const double g = geographic ? 1.0 : 0.0;
     double b = 8 * N * (2 + 5 * g);                                  // u, v, uR, vR, unit vectors

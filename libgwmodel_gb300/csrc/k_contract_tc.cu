@@ -9,10 +9,13 @@
 //    K-major layout the tensor core reads (two weight stages);
 //  * the matching Z~ tile (scaled/centred products, split hi + lo, stored in
 //    global memory already in the swizzled image) arrives by one 1-D bulk copy
-//    up to three tiles ahead;
-//  * one thread of the control warp issues 3 x 4 tcgen05.mma.kind::tf32
+//    up to three tiles ahead, issued by one thread of a copy warp;
+//  * one thread of the MMA warp issues 3 x 4 tcgen05.mma.kind::tf32
 //    (hi.hi + hi.lo + lo.hi, K = 8 each) into a 128 x N FP32 accumulator in
-//    TMEM and commits to an mbarrier;
+//    TMEM and commits to mbarriers.  An MMA issue returns only when the tensor
+//    pipe accepts it (about as long as the MMA runs), so that thread issues
+//    nothing else: with the copies on the same thread the pipe idled about
+//    two thirds of the time;
 //  * chunks of flush_tiles tiles alternate between two TMEM accumulators; four
 //    drain warps (one per TMEM lane quadrant) read a finished chunk back with
 //    tcgen05.ld and add it into double-float (hi, lo) sums in global memory,
@@ -23,9 +26,10 @@
 // beyond the row's haversine cut-off.  Every wait is bounded and reports
 // through err.
 // With a distance cache (CACHED, geographic) the producers read each pair's
-// FP32 squared distance -- filled once per dataset by k_fill_d2 with the same
-// arithmetic -- instead of computing it: about 14 instead of 58 instructions
-// per weight, bit-identical weights, and no point records to stage.
+// FP32 squared distance -- filled once per dataset, by the histogram pass of
+// the select or by k_fill_d2, with the same arithmetic -- instead of computing
+// it: about 14 instead of 58 instructions per weight, bit-identical weights,
+// and no point records to stage.
 #include "gw_common.cuh"
 #include "gw_kernels.h"
 #include "mixed_weight.cuh"
@@ -40,8 +44,9 @@ using namespace tc05;
 constexpr int TC_PROD_WARPS = 16;
 constexpr int TC_PROD = TC_PROD_WARPS * 32;   // producer threads
 constexpr int TC_DRAIN_WARPS = 4;             // one per TMEM lane quadrant
-constexpr int TC_CTRL_WARP = TC_PROD_WARPS + TC_DRAIN_WARPS;
-constexpr int TC_THREADS = TC_PROD + TC_DRAIN_WARPS * 32 + 32;  // plus one control warp
+constexpr int TC_CTRL_WARP = TC_PROD_WARPS + TC_DRAIN_WARPS;  // issues the MMAs
+constexpr int TC_COPY_WARP = TC_CTRL_WARP + 1;                 // issues the bulk copies
+constexpr int TC_THREADS = TC_PROD + TC_DRAIN_WARPS * 32 + 64;
 constexpr int TC_M = 128;
 constexpr int TC_BK = 32;  // points per stage (128 bytes of TF32 per row)
 constexpr uint32_t TC_A_BYTES = TC_M * 128;  // one split part of the weight tile
@@ -56,6 +61,7 @@ struct Smem {
     uint64_t mma_done[2];        // tcgen05.commit of tile k (every earlier MMA is done too)
     uint64_t full_b[TC_MAX_NB];  // Z tile landed (bulk copy)
     uint64_t full_p[2];          // point records landed (bulk copy)
+    uint64_t z_free[TC_MAX_NB];  // tcgen05.commit after the MMAs that read Z stage s
     uint64_t tmem_free[2];       // accumulator drained: one arrival per drain warp
     uint64_t acc_full[2];        // tcgen05.commit after the last MMA of a chunk into accumulator c % 2
     uint32_t tmem_base;
@@ -156,7 +162,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             mbar_init(&ctl.tmem_free[s], TC_DRAIN_WARPS);
             mbar_init(&ctl.acc_full[s], 1);
         }
-        for (int s = 0; s < TC_MAX_NB; s++) mbar_init(&ctl.full_b[s], 1);
+        for (int s = 0; s < TC_MAX_NB; s++) {
+            mbar_init(&ctl.full_b[s], 1);
+            mbar_init(&ctl.z_free[s], 1);
+        }
         ctl.abort = 0;
         fence_mbar_init();
     }
@@ -216,10 +225,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         walk.init(tmask, nwords);
         bool ok = true;
         const bool prof = a.prof && t == 0;
-        unsigned long long pc[kTcProfSlots] = {};
+        unsigned long long p_stage = 0, p_points = 0, p_weights = 0;  // phase cycles (prof)
         long long c0 = prof ? clock64() : 0, c1 = 0;
         const long long loop0 = c0;
-        if (prof) pc[kTcProfPrologue] = (unsigned long long)(c0 - kstart);
         // cached: this thread's 8 distances of a tile are two float4 of its row and
         // quarter, loaded one visited tile ahead (from L2: the control thread
         // prefetches the blocks nd tiles ahead)
@@ -256,7 +264,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const bool stage_ok = k < 2 || warp_wait(&ctl.mma_done[s], (uint32_t)(((k >> 1) - 1) & 1));
             if (prof) {
                 c1 = clock64();
-                pc[kTcProfStageWait] += c1 - c0;
+                p_stage += c1 - c0;
                 c0 = c1;
             }
             if (!stage_ok || (!CACHED && !warp_wait(&ctl.full_p[s], (uint32_t)((k >> 1) & 1)))) {
@@ -266,7 +274,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             if (prof) {
                 c1 = clock64();
-                pc[kTcProfPointsWait] += c1 - c0;
+                p_points += c1 - c0;
                 c0 = c1;
             }
             const float4* tp = ptsbuf + (size_t)s * NF * TC_BK;
@@ -331,14 +339,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             fence_proxy_async_smem();
             __syncwarp();
             if (lane == 0) mbar_arrive(&ctl.full_a[s]);
-            if (prof) pc[kTcProfWeights] += clock64() - c0;
+            if (prof) p_weights += clock64() - c0;
         }
         (void)ok;
         if (prof) {
             c1 = clock64();
-            pc[kTcProfLoop] += c1 - loop0;
-            for (int q = 0; q < kTcProfSlots; q++)
-                if (q < kTcProfAWait || q == kTcProfLoop || q == kTcProfPrologue) atomicAdd(a.prof + q, pc[q]);
+            atomicAdd(a.prof + kTcProfStageWait, p_stage);
+            atomicAdd(a.prof + kTcProfPointsWait, p_points);
+            atomicAdd(a.prof + kTcProfWeights, p_weights);
+            atomicAdd(a.prof + kTcProfLoop, (unsigned long long)(c1 - loop0));
+            atomicAdd(a.prof + kTcProfPrologue, (unsigned long long)(loop0 - kstart));
             atomicMax(a.prof + kTcProfLoopMax, (unsigned long long)(c1 - loop0));
             atomicMax(a.prof + kTcProfTilesMax, (unsigned long long)k);
         }
@@ -382,121 +392,144 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (prof) pflush += clock64() - c0;
         }
         if (prof) atomicAdd(a.prof + kTcProfFlush, pflush);
-    } else if (lane == 0) {
-        TileWalker wz, wp, wm;  // Z copies (nb ahead), point copies (2 ahead) or L2 prefetches (nd ahead), MMAs
-        wz.init(tmask, nwords);
-        wp.init(tmask, nwords);
-        wm.init(tmask, nwords);
-        int kz = 0, kp = 0;  // copies (or prefetches) issued
-        const float* d2blk = CACHED ? a.d2c + (size_t)blockIdx.x * a.ntiles * (TC_D_BYTES / 4) : nullptr;
-        auto issue_d = [&](int tl) {
-            bulk_prefetch_l2(d2blk + (size_t)tl * (TC_D_BYTES / 4), TC_D_BYTES);
-            kp++;
-        };
-        int last_mma = -1;
-        auto issue_z = [&](int tl) {
-            const int sb = kz % nb;
-            unsigned char* B = sB + (size_t)sb * 2 * b_bytes;
-            mbar_arrive_expect_tx(&ctl.full_b[sb], 2u * b_bytes);
-            bulk_g2s(B, a.zimg + (size_t)tl * 2u * b_bytes, 2u * b_bytes, &ctl.full_b[sb]);
-            kz++;
-        };
-        auto issue_p = [&](int tl) {
-            const int sp = kp & 1;
-            mbar_arrive_expect_tx(&ctl.full_p[sp], P_BYTES);
-            bulk_g2s(ptsbuf + (size_t)sp * NF * TC_BK, a.pts + (size_t)NF * TC_BK * tl, P_BYTES, &ctl.full_p[sp]);
-            kp++;
-        };
-        for (int q = 0; q < nb; q++) {
-            const int tl = wz.next();
-            if (tl < 0) break;
-            issue_z(tl);
-        }
-        for (int q = 0; q < (CACHED ? nd : 2); q++) {
-            const int tl = wp.next();
-            if (tl < 0) break;
-            if (CACHED) issue_d(tl);
-            else issue_p(tl);
-        }
-        const uint32_t idesc = idesc_tf32(TC_M, a.npad);
-        const bool prof = a.prof != nullptr;
-        unsigned long long pc[3] = {0, 0, 0};
-        long long c0 = 0, c1 = 0;
-        for (int tile = wm.next(); tile >= 0; tile = wm.next(), k++) {
-            if (*(volatile int*)&ctl.abort) break;
-            const int s = k & 1, sb = k % nb, c = k / F;
-            if (prof) c0 = clock64();
-            if (!mbar_wait(&ctl.full_a[s], (uint32_t)((k >> 1) & 1), TC_WAIT)) {
-                atomicExch(&ctl.abort, 1);
-                break;
-            }
-            if (prof) {
-                c1 = clock64();
-                pc[0] += c1 - c0;
-                c0 = c1;
-            }
-            // the producers are done with point buffer s: fetch the records of tile k + 2
-            // (cached: keep the L2 prefetch of the distance blocks nd tiles ahead)
-            if (!CACHED && kp == k + 2) {
-                const int tl = wp.next();
-                if (tl >= 0) issue_p(tl);
-            } else if (CACHED && kp == k + nd) {
-                const int tl = wp.next();
-                if (tl >= 0) issue_d(tl);
-            }
-            bool ok = mbar_wait(&ctl.full_b[sb], (uint32_t)((k / nb) & 1), TC_WAIT);
-            if (ok && k % F == 0 && c >= 2)
-                ok = mbar_wait(&ctl.tmem_free[c & 1], (uint32_t)(((c >> 1) - 1) & 1), TC_WAIT);
-            if (!ok) {
-                atomicExch(&ctl.abort, 1);
-                break;
-            }
-            if (prof) {
-                c1 = clock64();
-                pc[1] += c1 - c0;
-                c0 = c1;
-            }
-            fence_after_sync();
-            unsigned char* A_hi = sA + (size_t)s * 2 * TC_A_BYTES;
-            unsigned char* B_hi = sB + (size_t)sb * 2 * b_bytes;
-            const uint64_t ahi = sw128_kmajor_desc(smem_u32(A_hi));
-            const uint64_t alo = sw128_kmajor_desc(smem_u32(A_hi + TC_A_BYTES));
-            const uint64_t bhi = sw128_kmajor_desc(smem_u32(B_hi));
-            const uint64_t blo = sw128_kmajor_desc(smem_u32(B_hi + b_bytes));
-            const uint32_t d = tmem + (uint32_t)(c & 1) * TC_ACC_COLS;
-#pragma unroll
-            for (int kk = 0; kk < 4; kk++) {
-                const uint64_t dk = (uint64_t)(kk * 2);  // 32 bytes = 8 TF32 along K
-                mma_tf32(d, ahi + dk, bhi + dk, idesc, (k % F != 0 || kk > 0) ? 1u : 0u);
-                mma_tf32(d, ahi + dk, blo + dk, idesc, 1u);
-                mma_tf32(d, alo + dk, bhi + dk, idesc, 1u);
-            }
-            mma_commit(&ctl.mma_done[s]);
-            if (k % F == F - 1 || k == ktotal - 1) mma_commit(&ctl.acc_full[c & 1]);  // chunk c complete
-            last_mma = k;
-            // Z stage of tile k - 1 is free once its MMAs are done: fetch tile k - 1 + nb
-            if (k >= 1 && kz == k - 1 + nb) {
-                if (!mbar_wait(&ctl.mma_done[(k - 1) & 1], (uint32_t)(((k - 1) >> 1) & 1), TC_WAIT)) {
+    } else if (warp == TC_CTRL_WARP) {
+        // MMA issue (lane 0).  An MMA issue returns only once the tensor pipe takes
+        // it, so this thread does nothing but wait for a tile's weights, its Z tile
+        // and a free accumulator and issue: every copy is the copy warp's.
+        if (lane == 0) {
+            TileWalker wm;
+            wm.init(tmask, nwords);
+            int last_mma = -1;
+            const uint32_t idesc = idesc_tf32(TC_M, a.npad);
+            const bool prof = a.prof != nullptr;
+            unsigned long long p_a = 0, p_z = 0, p_i = 0;
+            long long c0 = 0, c1 = 0;
+            for (int tile = wm.next(); tile >= 0; tile = wm.next(), k++) {
+                if (*(volatile int*)&ctl.abort) break;
+                const int s = k & 1, sb = k % nb, c = k / F;
+                if (prof) c0 = clock64();
+                if (!mbar_wait(&ctl.full_a[s], (uint32_t)((k >> 1) & 1), TC_WAIT)) {
                     atomicExch(&ctl.abort, 1);
                     break;
                 }
-                const int tl = wz.next();
-                if (tl >= 0) issue_z(tl);
+                if (prof) {
+                    c1 = clock64();
+                    p_a += c1 - c0;
+                    c0 = c1;
+                }
+                bool ok = mbar_wait(&ctl.full_b[sb], (uint32_t)((k / nb) & 1), TC_WAIT);
+                if (ok && k % F == 0 && c >= 2)
+                    ok = mbar_wait(&ctl.tmem_free[c & 1], (uint32_t)(((c >> 1) - 1) & 1), TC_WAIT);
+                if (!ok) {
+                    atomicExch(&ctl.abort, 1);
+                    break;
+                }
+                if (prof) {
+                    c1 = clock64();
+                    p_z += c1 - c0;
+                    c0 = c1;
+                }
+                fence_after_sync();
+                unsigned char* A_hi = sA + (size_t)s * 2 * TC_A_BYTES;
+                unsigned char* B_hi = sB + (size_t)sb * 2 * b_bytes;
+                const uint64_t ahi = sw128_kmajor_desc(smem_u32(A_hi));
+                const uint64_t alo = sw128_kmajor_desc(smem_u32(A_hi + TC_A_BYTES));
+                const uint64_t bhi = sw128_kmajor_desc(smem_u32(B_hi));
+                const uint64_t blo = sw128_kmajor_desc(smem_u32(B_hi + b_bytes));
+                const uint32_t d = tmem + (uint32_t)(c & 1) * TC_ACC_COLS;
+#pragma unroll
+                for (int kk = 0; kk < 4; kk++) {
+                    const uint64_t dk = (uint64_t)(kk * 2);  // 32 bytes = 8 TF32 along K
+                    mma_tf32(d, ahi + dk, bhi + dk, idesc, (k % F != 0 || kk > 0) ? 1u : 0u);
+                    mma_tf32(d, ahi + dk, blo + dk, idesc, 1u);
+                    mma_tf32(d, alo + dk, bhi + dk, idesc, 1u);
+                }
+                mma_commit(&ctl.mma_done[s]);  // weight stage s reusable (producers)
+                mma_commit(&ctl.z_free[sb]);   // Z stage sb reusable (copy warp)
+                if (k % F == F - 1 || k == ktotal - 1) mma_commit(&ctl.acc_full[c & 1]);  // chunk c complete
+                last_mma = k;
+                if (prof) p_i += clock64() - c0;
             }
-            if (prof) pc[2] += clock64() - c0;
+            if (prof) {
+                atomicAdd(a.prof + kTcProfAWait, p_a);
+                atomicAdd(a.prof + kTcProfZWait, p_z);
+                atomicAdd(a.prof + kTcProfIssue, p_i);
+            }
+            // leave no MMA in flight before TMEM and the CTA go away
+            if (*(volatile int*)&ctl.abort && last_mma >= 0)
+                mbar_wait(&ctl.mma_done[last_mma & 1], (uint32_t)((last_mma >> 1) & 1), TC_WAIT);
         }
-        if (prof) {
-            atomicAdd(a.prof + kTcProfAWait, pc[0]);
-            atomicAdd(a.prof + kTcProfZWait, pc[1]);
-            atomicAdd(a.prof + kTcProfIssue, pc[2]);
-        }
-        if (*(volatile int*)&ctl.abort) {
-            // leave no MMA and no bulk copy in flight before TMEM and the CTA go away
-            if (last_mma >= 0) mbar_wait(&ctl.mma_done[last_mma & 1], (uint32_t)((last_mma >> 1) & 1), TC_WAIT);
-            for (int j = kz - nb > 0 ? kz - nb : 0; j < kz; j++)
-                mbar_wait(&ctl.full_b[j % nb], (uint32_t)((j / nb) & 1), TC_WAIT);
-            for (int j = kp - 2 > 0 ? kp - 2 : 0; j < kp && !CACHED; j++)
-                mbar_wait(&ctl.full_p[j & 1], (uint32_t)((j >> 1) & 1), TC_WAIT);
+    } else if (warp == TC_COPY_WARP) {
+        // Copies (lane 0): the Z tiles nb ahead (a stage is refilled once the MMAs
+        // that read it are done), the point records two ahead (once the producers
+        // are done with a buffer) or, with the cache, L2 prefetches of the distance
+        // blocks nd ahead.  Each wait is for a phase whose successor needs a copy
+        // this thread has not issued yet, so it can never be two phases behind.
+        if (lane == 0) {
+            TileWalker wz, wp;
+            wz.init(tmask, nwords);
+            wp.init(tmask, nwords);
+            int kz = 0, kp = 0;  // copies (or prefetches) issued
+            const float* d2blk = CACHED ? a.d2c + (size_t)blockIdx.x * a.ntiles * (TC_D_BYTES / 4) : nullptr;
+            auto issue_d = [&](int tl) {
+                bulk_prefetch_l2(d2blk + (size_t)tl * (TC_D_BYTES / 4), TC_D_BYTES);
+                kp++;
+            };
+            auto issue_z = [&](int tl) {
+                const int sb = kz % nb;
+                unsigned char* B = sB + (size_t)sb * 2 * b_bytes;
+                mbar_arrive_expect_tx(&ctl.full_b[sb], 2u * b_bytes);
+                bulk_g2s(B, a.zimg + (size_t)tl * 2u * b_bytes, 2u * b_bytes, &ctl.full_b[sb]);
+                kz++;
+            };
+            auto issue_p = [&](int tl) {
+                const int sp = kp & 1;
+                mbar_arrive_expect_tx(&ctl.full_p[sp], P_BYTES);
+                bulk_g2s(ptsbuf + (size_t)sp * NF * TC_BK, a.pts + (size_t)NF * TC_BK * tl, P_BYTES, &ctl.full_p[sp]);
+                kp++;
+            };
+            for (int q = 0; q < nb; q++) {
+                const int tl = wz.next();
+                if (tl < 0) break;
+                issue_z(tl);
+            }
+            for (int q = 0; q < (CACHED ? nd : 2); q++) {
+                const int tl = wp.next();
+                if (tl < 0) break;
+                if (CACHED) issue_d(tl);
+                else issue_p(tl);
+            }
+            for (int j = 0; j < ktotal && (kz < ktotal || kp < ktotal); j++) {
+                if (*(volatile int*)&ctl.abort) break;
+                if (CACHED) {
+                    const int tl = wp.next();
+                    if (tl >= 0) issue_d(tl);
+                } else if (kp < ktotal) {
+                    // point buffer j % 2 is free once the producers are done with tile j
+                    if (!mbar_wait(&ctl.full_a[j & 1], (uint32_t)((j >> 1) & 1), TC_WAIT)) {
+                        atomicExch(&ctl.abort, 1);
+                        break;
+                    }
+                    const int tl = wp.next();
+                    if (tl >= 0) issue_p(tl);
+                }
+                if (kz < ktotal) {
+                    // Z stage j % nb is free once the MMAs of tile j are done
+                    if (!mbar_wait(&ctl.z_free[j % nb], (uint32_t)((j / nb) & 1), TC_WAIT)) {
+                        atomicExch(&ctl.abort, 1);
+                        break;
+                    }
+                    const int tl = wz.next();
+                    if (tl >= 0) issue_z(tl);
+                }
+            }
+            if (*(volatile int*)&ctl.abort) {
+                // leave no bulk copy in flight before the CTA goes away
+                for (int j = kz - nb > 0 ? kz - nb : 0; j < kz; j++)
+                    mbar_wait(&ctl.full_b[j % nb], (uint32_t)((j / nb) & 1), TC_WAIT);
+                for (int j = kp - 2 > 0 ? kp - 2 : 0; j < kp && !CACHED; j++)
+                    mbar_wait(&ctl.full_p[j & 1], (uint32_t)((j >> 1) & 1), TC_WAIT);
+            }
         }
     }
     __syncwarp();
@@ -670,7 +703,7 @@ size_t contract_tc_smem_bytes(int npad, int ntiles, int nb)
 
 cudaError_t launch_contract_tc(const TcArgs& a, bool geographic, cudaStream_t stream)
 {
-    if (a.npad % 64 != 0 || a.npad < 64 || a.npad > 256 || a.mcols > a.npad) return cudaErrorInvalidValue;
+    if (a.npad % 16 != 0 || a.npad < 16 || a.npad > 256 || a.mcols > a.npad) return cudaErrorInvalidValue;
     if (a.flush_tiles < 2) return cudaErrorInvalidValue;
     int nb = TC_MAX_NB;
     while (nb > 2 && contract_tc_smem_bytes(a.npad, a.ntiles, nb) > 227 * 1024) nb--;
@@ -702,7 +735,7 @@ cudaError_t launch_contract_tc(const TcArgs& a, bool geographic, cudaStream_t st
 cudaError_t launch_contract_tc_batch(const TcArgs* segs, const int2* work, int nwork, int max_npad, int max_ntiles,
                                      int flush_tiles, bool geographic, int kernel, cudaStream_t stream)
 {
-    if (max_npad % 64 != 0 || max_npad < 64 || max_npad > 256 || flush_tiles < 2 || nwork < 1)
+    if (max_npad % 16 != 0 || max_npad < 16 || max_npad > 256 || flush_tiles < 2 || nwork < 1)
         return cudaErrorInvalidValue;
     int nb = TC_MAX_NB;
     while (nb > 2 && contract_tc_smem_bytes(max_npad, max_ntiles, nb) > 227 * 1024) nb--;
