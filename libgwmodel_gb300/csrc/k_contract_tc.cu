@@ -52,7 +52,11 @@ constexpr int TC_BK = 32;  // points per stage (128 bytes of TF32 per row)
 constexpr uint32_t TC_A_BYTES = TC_M * 128;  // one split part of the weight tile
 constexpr uint32_t TC_WAIT = 1u << 22;
 constexpr uint32_t TC_ACC_COLS = 256;  // TMEM column of the second accumulator
-constexpr int TC_MAX_NB = 3;           // Z stages at most
+// Weights in tensor memory (npad <= 192): accumulators at columns 0 and 192,
+// weight stage s at 384 + 64 s (hi: 32 columns, then lo: 32 columns)
+constexpr uint32_t TC_ATM_ACC_COLS = 192;
+constexpr uint32_t TC_ATM_A_COL = 384;
+constexpr int TC_MAX_NB = 4;           // Z stages at most
 constexpr uint32_t TC_P_MAX = 2u * 16u * TC_BK;  // point records of one tile, geographic
 constexpr uint32_t TC_D_BYTES = TC_M * TC_BK * 4;  // one cached 128 x 32 distance block
 
@@ -121,11 +125,16 @@ __device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity)
 // BATCH: CTA b works on segment work[b].x (arguments segs[work[b].x]) at row
 // block work[b].y, so one launch covers many datasets and bandwidths.
 // CACHED: weights from the distance cache a.d2c (geographic, single dataset only).
-template <bool GEO, int KERN, bool BATCH, bool CACHED = false>
+// ATM: the weight tiles live in tensor memory (written with tcgen05.st, read by
+// the MMA as its A operand), which frees their 64 KB of shared memory for a
+// fourth Z stage and takes their traffic off shared memory; npad <= 192.
+template <bool GEO, int KERN, bool BATCH, bool CACHED = false, bool ATM = false>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_contract_tc(TcArgs a0, int nb, int nd, const TcArgs* __restrict__ segs, const int2* __restrict__ work)
 {
     static_assert(!CACHED || (GEO && !BATCH), "the distance cache serves single geographic datasets");
+    static_assert(!ATM || !BATCH, "tensor-memory weights serve single datasets");
+    constexpr uint32_t ACC_COLS = ATM ? TC_ATM_ACC_COLS : TC_ACC_COLS;
     const TcArgs a = BATCH ? segs[work[blockIdx.x].x] : a0;
     const int kernel = KERN >= 0 ? KERN : a.kernel;
     extern __shared__ unsigned char smem_dyn[];
@@ -134,7 +143,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const uint32_t pad = (1024u - (base_u32 & 1023u)) & 1023u;
     unsigned char* sA = smem_dyn + pad;  // 2 stages x [A_hi | A_lo]
     const uint32_t b_bytes = (uint32_t)a.npad * 128u;
-    unsigned char* sB = sA + 4 * (size_t)TC_A_BYTES;  // nb stages x [B_hi | B_lo]
+    unsigned char* sB = sA + (ATM ? 0 : 4 * (size_t)TC_A_BYTES);  // nb stages x [B_hi | B_lo]
     constexpr int NF = GEO ? 2 : 1;                    // float4 per point record
     constexpr uint32_t P_BYTES = NF * 16u * TC_BK;     // point records of one tile
     float4* ptsbuf = reinterpret_cast<float4*>(sB + (size_t)nb * 2 * b_bytes);  // 2 x P_BYTES
@@ -277,10 +286,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 p_points += c1 - c0;
                 c0 = c1;
             }
+            if constexpr (ATM) fence_after_sync();  // the MMAs that read stage s are done
             const float4* tp = ptsbuf + (size_t)s * NF * TC_BK;
             unsigned char* A_hi = sA + (size_t)s * 2 * TC_A_BYTES;
             unsigned char* A_lo = A_hi + TC_A_BYTES;
             const int kbase = quarter * 8;
+            uint32_t hv[8], lv[8];  // ATM: this thread's 8 columns of the hi and lo tiles
 #pragma unroll
             for (int q4 = 0; q4 < 2; q4++) {
                 float w[4];
@@ -332,11 +343,29 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     hi[e] = to_tf32(w[e]);
                     lo[e] = to_tf32(w[e] - hi[e]);
                 }
-                const uint32_t off = sw128_offset((uint32_t)r, (uint32_t)(kbase + q4 * 4));
-                *reinterpret_cast<float4*>(A_hi + off) = make_float4(hi[0], hi[1], hi[2], hi[3]);
-                *reinterpret_cast<float4*>(A_lo + off) = make_float4(lo[0], lo[1], lo[2], lo[3]);
+                if constexpr (ATM) {
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        hv[q4 * 4 + e] = __float_as_uint(hi[e]);
+                        lv[q4 * 4 + e] = __float_as_uint(lo[e]);
+                    }
+                } else {
+                    const uint32_t off = sw128_offset((uint32_t)r, (uint32_t)(kbase + q4 * 4));
+                    *reinterpret_cast<float4*>(A_hi + off) = make_float4(hi[0], hi[1], hi[2], hi[3]);
+                    *reinterpret_cast<float4*>(A_lo + off) = make_float4(lo[0], lo[1], lo[2], lo[3]);
+                }
             }
-            fence_proxy_async_smem();
+            if constexpr (ATM) {
+                // row r is lane r of tensor memory: this warp's lane quadrant is (warp % 4)
+                const uint32_t acol = tmem + ((uint32_t)((warp & 3) * 32) << 16) + TC_ATM_A_COL +
+                                      (uint32_t)s * 64u + (uint32_t)kbase;
+                tmem_st8(acol, hv);
+                tmem_st8(acol + 32u, lv);
+                tmem_wait_st();
+                fence_before_sync();
+            } else {
+                fence_proxy_async_smem();
+            }
             __syncwarp();
             if (lane == 0) mbar_arrive(&ctl.full_a[s]);
             if (prof) p_weights += clock64() - c0;
@@ -368,7 +397,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             const long long c0 = prof ? clock64() : 0;
             fence_after_sync();
-            const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(c & 1) * TC_ACC_COLS;
+            const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(c & 1) * ACC_COLS;
             for (int col0 = 0; col0 < a.npad; col0 += 16) {
                 uint32_t v[16];
                 tmem_ld16(tbase + (uint32_t)col0, v);
@@ -408,7 +437,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 if (*(volatile int*)&ctl.abort) break;
                 const int s = k & 1, sb = k % nb, c = k / F;
                 if (prof) c0 = clock64();
-                if (!mbar_wait(&ctl.full_a[s], (uint32_t)((k >> 1) & 1), TC_WAIT)) {
+                if (!mbar_wait_spin(&ctl.full_a[s], (uint32_t)((k >> 1) & 1), TC_WAIT)) {
                     atomicExch(&ctl.abort, 1);
                     break;
                 }
@@ -417,9 +446,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     p_a += c1 - c0;
                     c0 = c1;
                 }
-                bool ok = mbar_wait(&ctl.full_b[sb], (uint32_t)((k / nb) & 1), TC_WAIT);
+                bool ok = mbar_wait_spin(&ctl.full_b[sb], (uint32_t)((k / nb) & 1), TC_WAIT);
                 if (ok && k % F == 0 && c >= 2)
-                    ok = mbar_wait(&ctl.tmem_free[c & 1], (uint32_t)(((c >> 1) - 1) & 1), TC_WAIT);
+                    ok = mbar_wait_spin(&ctl.tmem_free[c & 1], (uint32_t)(((c >> 1) - 1) & 1), TC_WAIT);
                 if (!ok) {
                     atomicExch(&ctl.abort, 1);
                     break;
@@ -436,13 +465,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const uint64_t alo = sw128_kmajor_desc(smem_u32(A_hi + TC_A_BYTES));
                 const uint64_t bhi = sw128_kmajor_desc(smem_u32(B_hi));
                 const uint64_t blo = sw128_kmajor_desc(smem_u32(B_hi + b_bytes));
-                const uint32_t d = tmem + (uint32_t)(c & 1) * TC_ACC_COLS;
+                const uint32_t d = tmem + (uint32_t)(c & 1) * ACC_COLS;
+                if constexpr (ATM) {
+                    const uint32_t ta = tmem + TC_ATM_A_COL + (uint32_t)s * 64u;  // hi; lo 32 columns on
 #pragma unroll
-                for (int kk = 0; kk < 4; kk++) {
-                    const uint64_t dk = (uint64_t)(kk * 2);  // 32 bytes = 8 TF32 along K
-                    mma_tf32(d, ahi + dk, bhi + dk, idesc, (k % F != 0 || kk > 0) ? 1u : 0u);
-                    mma_tf32(d, ahi + dk, blo + dk, idesc, 1u);
-                    mma_tf32(d, alo + dk, bhi + dk, idesc, 1u);
+                    for (int kk = 0; kk < 4; kk++) {
+                        const uint64_t dk = (uint64_t)(kk * 2);  // 32 bytes = 8 TF32 along K
+                        const uint32_t tk = ta + (uint32_t)(kk * 8);
+                        mma_tf32_ts(d, tk, bhi + dk, idesc, (k % F != 0 || kk > 0) ? 1u : 0u);
+                        mma_tf32_ts(d, tk, blo + dk, idesc, 1u);
+                        mma_tf32_ts(d, tk + 32u, bhi + dk, idesc, 1u);
+                    }
+                } else {
+#pragma unroll
+                    for (int kk = 0; kk < 4; kk++) {
+                        const uint64_t dk = (uint64_t)(kk * 2);  // 32 bytes = 8 TF32 along K
+                        mma_tf32(d, ahi + dk, bhi + dk, idesc, (k % F != 0 || kk > 0) ? 1u : 0u);
+                        mma_tf32(d, ahi + dk, blo + dk, idesc, 1u);
+                        mma_tf32(d, alo + dk, bhi + dk, idesc, 1u);
+                    }
                 }
                 mma_commit(&ctl.mma_done[s]);  // weight stage s reusable (producers)
                 mma_commit(&ctl.z_free[sb]);   // Z stage sb reusable (copy warp)
@@ -478,8 +519,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             auto issue_z = [&](int tl) {
                 const int sb = kz % nb;
                 unsigned char* B = sB + (size_t)sb * 2 * b_bytes;
+                const unsigned char* src = a.zimg + (size_t)tl * 2u * b_bytes;
                 mbar_arrive_expect_tx(&ctl.full_b[sb], 2u * b_bytes);
-                bulk_g2s(B, a.zimg + (size_t)tl * 2u * b_bytes, 2u * b_bytes, &ctl.full_b[sb]);
+                // four pieces of npad x 64 bytes (multiples of 16): the copy engine overlaps them
+                const uint32_t piece = b_bytes / 2;
+                for (int q = 0; q < 4; q++) bulk_g2s(B + q * piece, src + q * piece, piece, &ctl.full_b[sb]);
                 kz++;
             };
             auto issue_p = [&](int tl) {
@@ -499,14 +543,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 if (CACHED) issue_d(tl);
                 else issue_p(tl);
             }
-            for (int j = 0; j < ktotal && (kz < ktotal || kp < ktotal); j++) {
+            for (int j = 0; j < ktotal && (kz < ktotal || (kp < ktotal && (!CACHED || nd > 0))); j++) {
                 if (*(volatile int*)&ctl.abort) break;
                 if (CACHED) {
-                    const int tl = wp.next();
-                    if (tl >= 0) issue_d(tl);
+                    if (nd > 0) {
+                        const int tl = wp.next();
+                        if (tl >= 0) issue_d(tl);
+                    }
                 } else if (kp < ktotal) {
                     // point buffer j % 2 is free once the producers are done with tile j
-                    if (!mbar_wait(&ctl.full_a[j & 1], (uint32_t)((j >> 1) & 1), TC_WAIT)) {
+                    if (!mbar_wait_spin(&ctl.full_a[j & 1], (uint32_t)((j >> 1) & 1), TC_WAIT)) {
                         atomicExch(&ctl.abort, 1);
                         break;
                     }
@@ -515,7 +561,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 }
                 if (kz < ktotal) {
                     // Z stage j % nb is free once the MMAs of tile j are done
-                    if (!mbar_wait(&ctl.z_free[j % nb], (uint32_t)((j / nb) & 1), TC_WAIT)) {
+                    if (!mbar_wait_spin(&ctl.z_free[j % nb], (uint32_t)((j / nb) & 1), TC_WAIT)) {
                         atomicExch(&ctl.abort, 1);
                         break;
                     }
@@ -705,30 +751,48 @@ cudaError_t launch_contract_tc(const TcArgs& a, bool geographic, cudaStream_t st
 {
     if (a.npad % 16 != 0 || a.npad < 16 || a.npad > 256 || a.mcols > a.npad) return cudaErrorInvalidValue;
     if (a.flush_tiles < 2) return cudaErrorInvalidValue;
+    const int grid = (a.n + TC_M - 1) / TC_M;
+    // cached: the L2 prefetch of the distance blocks runs nd tiles ahead
+    const int nd = 4;
+    const size_t mask = (size_t)((a.ntiles + 31) / 32) * 4;
+    if ((uint32_t)a.npad <= TC_ATM_ACC_COLS) {
+        // weights in tensor memory: the shared memory holds only the Z stages
+        auto bytes = [&](int b) { return 1024 + (size_t)b * 2 * a.npad * 128 + 2 * TC_P_MAX + mask; };
+        int nb = TC_MAX_NB;
+        while (nb > 2 && bytes(nb) > 227 * 1024) nb--;
+        const size_t smem = bytes(nb);
+        if (smem > 227 * 1024) return cudaErrorInvalidValue;
+        auto go = [&](auto kfn) {
+            raise_smem_limit((const void*)kfn, smem);
+            kfn<<<grid, TC_THREADS, smem, stream>>>(a, nb, nd, nullptr, nullptr);
+        };
+        if (geographic && a.d2c) {
+            if (a.kernel == GW_KERNEL_BISQUARE) go(k_contract_tc<true, GW_KERNEL_BISQUARE, false, true, true>);
+            else if (a.kernel == GW_KERNEL_GAUSSIAN) go(k_contract_tc<true, GW_KERNEL_GAUSSIAN, false, true, true>);
+            else go(k_contract_tc<true, -1, false, true, true>);
+        } else if (geographic) {
+            if (a.kernel == GW_KERNEL_BISQUARE) go(k_contract_tc<true, GW_KERNEL_BISQUARE, false, false, true>);
+            else if (a.kernel == GW_KERNEL_GAUSSIAN) go(k_contract_tc<true, GW_KERNEL_GAUSSIAN, false, false, true>);
+            else go(k_contract_tc<true, -1, false, false, true>);
+        } else {
+            if (a.kernel == GW_KERNEL_BISQUARE) go(k_contract_tc<false, GW_KERNEL_BISQUARE, false, false, true>);
+            else if (a.kernel == GW_KERNEL_GAUSSIAN) go(k_contract_tc<false, GW_KERNEL_GAUSSIAN, false, false, true>);
+            else go(k_contract_tc<false, -1, false, false, true>);
+        }
+        return cudaGetLastError();
+    }
+    // wider Z (npad 208 .. 256): weights in shared memory, the kernel read at run time
     int nb = TC_MAX_NB;
     while (nb > 2 && contract_tc_smem_bytes(a.npad, a.ntiles, nb) > 227 * 1024) nb--;
     const size_t smem = contract_tc_smem_bytes(a.npad, a.ntiles, nb);
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
-    const int grid = (a.n + TC_M - 1) / TC_M;
-    // cached: the L2 prefetch of the distance blocks runs 4 tiles ahead
-    const int nd = 4;
     auto go = [&](auto kfn) {
         raise_smem_limit((const void*)kfn, smem);
         kfn<<<grid, TC_THREADS, smem, stream>>>(a, nb, nd, nullptr, nullptr);
     };
-    if (geographic && a.d2c) {
-        if (a.kernel == GW_KERNEL_BISQUARE) go(k_contract_tc<true, GW_KERNEL_BISQUARE, false, true>);
-        else if (a.kernel == GW_KERNEL_GAUSSIAN) go(k_contract_tc<true, GW_KERNEL_GAUSSIAN, false, true>);
-        else go(k_contract_tc<true, -1, false, true>);
-    } else if (geographic) {
-        if (a.kernel == GW_KERNEL_BISQUARE) go(k_contract_tc<true, GW_KERNEL_BISQUARE, false>);
-        else if (a.kernel == GW_KERNEL_GAUSSIAN) go(k_contract_tc<true, GW_KERNEL_GAUSSIAN, false>);
-        else go(k_contract_tc<true, -1, false>);
-    } else {
-        if (a.kernel == GW_KERNEL_BISQUARE) go(k_contract_tc<false, GW_KERNEL_BISQUARE, false>);
-        else if (a.kernel == GW_KERNEL_GAUSSIAN) go(k_contract_tc<false, GW_KERNEL_GAUSSIAN, false>);
-        else go(k_contract_tc<false, -1, false>);
-    }
+    if (geographic && a.d2c) go(k_contract_tc<true, -1, false, true>);
+    else if (geographic) go(k_contract_tc<true, -1, false>);
+    else go(k_contract_tc<false, -1, false>);
     return cudaGetLastError();
 }
 
