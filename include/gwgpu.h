@@ -281,6 +281,8 @@ int gwgpu_engine_predict(gwgpu_engine* e, int nr, const double* locations, doubl
 int gwgpu_engine_event_record(gwgpu_engine* e, int slot);
 int gwgpu_engine_event_elapsed(gwgpu_engine* e, int first, int second, float* ms);
 int gwgpu_engine_thresholds(gwgpu_engine* e, double bandwidth, int adaptive, double* out /* n */);
+/* on: 0 off, 1 event timings and counters, 2 also the mixed contraction's
+   clock64 phase counters (contract_phase_cycles; instrumented kernels). */
 int gwgpu_engine_enable_stats(gwgpu_engine* e, int on);
 int gwgpu_engine_get_stats(gwgpu_engine* e, gwgpu_stats* out);
 int gwgpu_engine_reset_stats(gwgpu_engine* e);

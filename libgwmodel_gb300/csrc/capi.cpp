@@ -564,7 +564,7 @@ int gwgpu_engine_thresholds(gwgpu_engine* e, double bandwidth, int adaptive, dou
 int gwgpu_engine_enable_stats(gwgpu_engine* e, int on)
 {
     ENG_CHECK(e);
-    e->eng.enableStats(on != 0);
+    e->eng.enableStats(on != 0, on == 2);
     return GWGPU_OK;
 }
 

@@ -830,7 +830,7 @@ void Engine::contractMixed(double* G, int ldg, int mcols, double bw, bool adapti
                   "memset prof");
         }
         a.tiles = tile_count_.get();
-        a.prof = tc_prof_.get();
+        a.prof = phases_on_ ? tc_prof_.get() : nullptr;
         counters_dirty_ = true;
     }
     check(launch_contract_tc(a, geographic_, stream_), "contract_tc");

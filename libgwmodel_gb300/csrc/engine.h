@@ -187,7 +187,13 @@ public:
     // Per-row adaptive thresholds (fixbw) in original order, for tests.
     void thresholds(double bw, bool adaptive, std::vector<double>& out);
 
-    void enableStats(bool on) { stats_on_ = on; }
+    // Event timings and counters; `phases` adds the contraction's clock64 phase
+    // counters (instrumented kernels, for profiling only).
+    void enableStats(bool on, bool phases = false)
+    {
+        stats_on_ = on;
+        phases_on_ = on && phases;
+    }
     // Counters and event timings; resolving them waits for the recorded
     // events, never for anything during a fit.
     EngineStats& stats();
@@ -303,7 +309,7 @@ private:
     double thr_bw_ = 0.0;
     int thr_prec_ = -1;
 
-    bool stats_on_ = false;
+    bool stats_on_ = false, phases_on_ = false;
     EngineStats stats_;
     cudaEvent_t events_[8] = {};
 };

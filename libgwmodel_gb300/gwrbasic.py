@@ -461,8 +461,10 @@ class Engine:
         check(lib().gwgpu_engine_thresholds(self._h, float(bw), int(bool(adaptive)), dptr(out)))
         return out
 
-    def enable_stats(self, on=True):
-        check(lib().gwgpu_engine_enable_stats(self._h, int(bool(on))))
+    def enable_stats(self, on=True, phases=False):
+        """Event timings and counters; phases=True adds the contraction's
+        clock64 phase counters (instrumented kernels, profiling only)."""
+        check(lib().gwgpu_engine_enable_stats(self._h, (2 if phases else 1) if on else 0))
 
     def stats(self):
         s = Stats()
