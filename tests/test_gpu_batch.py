@@ -79,3 +79,28 @@ def test_batch_rejects_bad_candidates():
     with pytest.raises(GwgpuError):
         b.set_candidates([np.array([pbs[0].n + 1.0]), np.array([20.0])])
     b.close()
+
+
+def test_first_graph_reads_the_histogram_caches():
+    """The graph captured at the first evaluation must carry the histogram
+    caches made for it (null cache pointers leave every select scanning whole
+    rows: the same values, several times slower).  The replay of the first
+    graph is timed against a replay after a rebuild of the same schedule."""
+    pbs, cands = datasets.config3()
+    b = Batch(pbs, precision=Precision.Mixed)
+    b.set_candidates(cands, adaptive=True, kernel=2, criterion=0)
+    first = None
+    for _ in range(3):
+        v0 = b.evaluate(use_graph=True)
+        t = b.info()["last_ms"]
+        first = t if first is None else min(first, t)
+    info = b.info()
+    b.set_tuning(info["flush_tiles"], info["order"], info["solve_rows"], info["select_ctas"])
+    rebuilt = None
+    for _ in range(3):
+        v1 = b.evaluate(use_graph=True)
+        t = b.info()["last_ms"]
+        rebuilt = t if rebuilt is None else min(rebuilt, t)
+    for a, c in zip(v0, v1):
+        np.testing.assert_array_equal(a, c)
+    assert first < 2.0 * rebuilt + 20.0, (first, rebuilt)
