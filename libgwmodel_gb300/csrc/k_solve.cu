@@ -307,6 +307,138 @@ __global__ void __launch_bounds__(SV_WARPS * 32)
     }
 }
 
+constexpr int ST_THREADS = 32;  // locations (lanes) per block of k_solve_crit_t
+
+// Criterion solves (AICc / CV, no beta) with one location per thread.  GB300
+// runs FP64 at about two lanes per clock per SM, so an FP64 warp instruction
+// costs the same whatever its active lanes: the warp-per-location form above
+// spends most of its instructions on a few lanes (the tail of each trailing
+// update, the pivots, the substitutions).  Here every lane has its own p x p
+// factor in shared memory (element e of lane t at e * ST_THREADS + t, so a
+// warp's accesses hit 32 consecutive doubles), and each operation is the one
+// the warp form applies to that element, in the same order, down to the
+// butterfly order of its warp sums (where the compiler fuses a product into a
+// sum differently the two can differ by an ulp).  Only the grouping of the
+// block partials of the criterion sums differs.
+__device__ __forceinline__ int tri_index(int r, int c) { return r * (r + 1) / 2 + c; }  // c <= r
+
+// Lane 0's value of warp_sum over x[i] y[i], i < p, padded with zeros to 32
+// (x, y: one lane's column of a shared-memory block, stride ST_THREADS).
+__device__ __forceinline__ double butterfly_dot(const double* x, const double* y, int p)
+{
+    double a[32];
+#pragma unroll
+    for (int i = 0; i < 32; i++) a[i] = i < p ? x[(size_t)i * ST_THREADS] * y[(size_t)i * ST_THREADS] : 0.0;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+        for (int i = 0; i < off; i++) a[i] = a[i] + a[i + off];
+    }
+    return a[0];
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(ST_THREADS) k_solve_crit_t(SolveArgs a)
+{
+    extern __shared__ double smem[];
+    const int p = a.p, mm = p * (p + 1) / 2, m = mm + p;
+    const int t = threadIdx.x;
+    double* L = smem;                      // mm elements (lower, packed by rows) x ST_THREADS
+    double* zv = smem + (size_t)mm * ST_THREADS;  // p elements
+    double* uv = zv + (size_t)p * ST_THREADS;     // p elements
+    double acc_s = 0.0, acc_r = 0.0, acc_f = 0.0;
+    for (int row0 = blockIdx.x * ST_THREADS; row0 < a.n; row0 += gridDim.x * ST_THREADS) {
+        const int nrow = min(ST_THREADS, a.n - row0);
+        __syncwarp();
+        // coalesced loads of the block's rows of G: column q of G is A[c][r]
+        // (upper, packed by rows) for q < mm, else b
+        for (int e = t; e < nrow * m; e += ST_THREADS) {
+            const int lr = e / m, q = e - lr * m;
+            const double v = a.G[(size_t)(row0 + lr) * a.ldg + q];
+            if (q < mm) {
+                int c = 0, base = 0;
+                while (base + (p - c) <= q) {
+                    base += p - c;
+                    c++;
+                }
+                const int r = c + (q - base);
+                L[(size_t)tri_index(r, c) * ST_THREADS + lr] = v;
+            } else {
+                zv[(size_t)(q - mm) * ST_THREADS + lr] = v;
+            }
+        }
+        __syncwarp();
+        const int row = row0 + t;
+        if (t < nrow) {
+            double* Lt = L + t;
+            double* zt = zv + t;
+            double* ut = uv + t;
+            for (int r = 0; r < p; r++) ut[(size_t)r * ST_THREADS] = a.X[(size_t)row * p + r];
+            bool fail = false;
+            for (int j = 0; j < p; j++) {
+                const double tjj = Lt[(size_t)tri_index(j, j) * ST_THREADS];
+                if (!(tjj > 0.0)) {
+                    fail = true;
+                    break;
+                }
+                const double rinv = rsqrt(tjj);
+                Lt[(size_t)tri_index(j, j) * ST_THREADS] = rinv;
+                for (int r = j + 1; r < p; r++) Lt[(size_t)tri_index(r, j) * ST_THREADS] *= rinv;
+                for (int r = j + 1; r < p; r++) {
+                    const double lrj = Lt[(size_t)tri_index(r, j) * ST_THREADS];
+                    for (int c = j + 1; c <= r; c++) {
+                        double* lrc = Lt + (size_t)tri_index(r, c) * ST_THREADS;
+                        *lrc -= lrj * Lt[(size_t)tri_index(c, j) * ST_THREADS];
+                    }
+                }
+            }
+            if (fail) {
+                acc_f += 1.0;
+                if (a.beta) for (int r = 0; r < p; r++) a.beta[(size_t)row * p + r] = __longlong_as_double(0x7ff8000000000000ll);
+                a.resid[row] = __longlong_as_double(0x7ff8000000000000ll);
+                a.sii[row] = 0.0;
+            } else {
+                // z = L^-1 b and u = L^-1 x_i (fwd_solve2)
+                for (int j = 0; j < p; j++) {
+                    const double ljj = Lt[(size_t)tri_index(j, j) * ST_THREADS];
+                    const double z1 = zt[(size_t)j * ST_THREADS] * ljj;
+                    const double z2 = ut[(size_t)j * ST_THREADS] * ljj;
+                    zt[(size_t)j * ST_THREADS] = z1;
+                    ut[(size_t)j * ST_THREADS] = z2;
+                    for (int r = j + 1; r < p; r++) {
+                        const double l = Lt[(size_t)tri_index(r, j) * ST_THREADS];
+                        zt[(size_t)r * ST_THREADS] -= l * z1;
+                        ut[(size_t)r * ST_THREADS] -= l * z2;
+                    }
+                }
+                const double yhat = butterfly_dot(ut, zt, p);
+                const double res = a.y[row] - yhat;
+                double sii = 0.0;
+                if (MODE == kSolveAIC) {
+                    const double uu = butterfly_dot(ut, ut, p);
+                    sii = gw_kernel_weight(a.kernel, 0.0, a.thr ? a.thr[row] : a.bw) * uu;
+                }
+                a.sii[row] = sii;
+                a.resid[row] = res;
+                acc_s += sii;
+                acc_r += res * res;
+            }
+        }
+    }
+    // the block's partial sums (lane order)
+    __shared__ double part[ST_THREADS][3];
+    part[t][0] = acc_s;
+    part[t][1] = acc_r;
+    part[t][2] = acc_f;
+    __syncwarp();
+    if (t < 4) {
+        double v = 0.0;
+        if (t != 2)
+            for (int q = 0; q < ST_THREADS; q++) v += part[q][t == 3 ? 2 : t];
+        a.partials[blockIdx.x * 4 + t] = v;
+    }
+}
+
 __global__ void k_reduce(const double* __restrict__ partials, int nblocks, double* __restrict__ out)
 {
     __shared__ double sh[256][4];
@@ -571,6 +703,22 @@ cudaError_t launch_build_z(int n, int p, const double* X, const double* y, doubl
 cudaError_t launch_solve(const SolveArgs& a, int* nblocks, cudaStream_t stream)
 {
     if (a.p < 1 || a.p > kMaxP) return cudaErrorInvalidValue;
+    if ((a.mode == kSolveAIC || a.mode == kSolveCV) && !a.beta && a.p <= 20) {
+        // criterion without beta: one location per thread (k_solve_crit_t)
+        const int mm = a.p * (a.p + 1) / 2;
+        const size_t smem = (size_t)(mm + 2 * a.p) * ST_THREADS * sizeof(double);
+        int grid = (a.n + ST_THREADS - 1) / ST_THREADS;
+        if (grid > 4096) grid = 4096;  // the callers' partials hold 4096 blocks (as for k_solve)
+        *nblocks = grid;
+        if (a.mode == kSolveAIC) {
+            raise_smem_limit((const void*)k_solve_crit_t<kSolveAIC>, smem);
+            k_solve_crit_t<kSolveAIC><<<grid, ST_THREADS, smem, stream>>>(a);
+        } else {
+            raise_smem_limit((const void*)k_solve_crit_t<kSolveCV>, smem);
+            k_solve_crit_t<kSolveCV><<<grid, ST_THREADS, smem, stream>>>(a);
+        }
+        return cudaGetLastError();
+    }
     int grid = (a.n + SV_WARPS - 1) / SV_WARPS;
     if (grid > 4096) grid = 4096;
     const int ld = a.p + 1;
