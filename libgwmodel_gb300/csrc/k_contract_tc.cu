@@ -433,9 +433,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const bool prof = a.prof != nullptr;
             unsigned long long p_a = 0, p_z = 0, p_i = 0;
             long long c0 = 0, c1 = 0;
+            // k % nb, (k / nb) & 1, k % F and k / F kept as counters: divisions by
+            // run-time values are long dependent chains on this critical thread
+            int sb = 0, zpar = 0, kf = 0, c = 0;
             for (int tile = wm.next(); tile >= 0; tile = wm.next(), k++) {
                 if (*(volatile int*)&ctl.abort) break;
-                const int s = k & 1, sb = k % nb, c = k / F;
+                const int s = k & 1;
                 if (prof) c0 = clock64();
                 if (!mbar_wait_spin(&ctl.full_a[s], (uint32_t)((k >> 1) & 1), TC_WAIT)) {
                     atomicExch(&ctl.abort, 1);
@@ -446,8 +449,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     p_a += c1 - c0;
                     c0 = c1;
                 }
-                bool ok = mbar_wait_spin(&ctl.full_b[sb], (uint32_t)((k / nb) & 1), TC_WAIT);
-                if (ok && k % F == 0 && c >= 2)
+                bool ok = mbar_wait_spin(&ctl.full_b[sb], (uint32_t)zpar, TC_WAIT);
+                if (ok && kf == 0 && c >= 2)
                     ok = mbar_wait_spin(&ctl.tmem_free[c & 1], (uint32_t)(((c >> 1) - 1) & 1), TC_WAIT);
                 if (!ok) {
                     atomicExch(&ctl.abort, 1);
@@ -472,7 +475,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     for (int kk = 0; kk < 4; kk++) {
                         const uint64_t dk = (uint64_t)(kk * 2);  // 32 bytes = 8 TF32 along K
                         const uint32_t tk = ta + (uint32_t)(kk * 8);
-                        mma_tf32_ts(d, tk, bhi + dk, idesc, (k % F != 0 || kk > 0) ? 1u : 0u);
+                        mma_tf32_ts(d, tk, bhi + dk, idesc, (kf != 0 || kk > 0) ? 1u : 0u);
                         mma_tf32_ts(d, tk, blo + dk, idesc, 1u);
                         mma_tf32_ts(d, tk + 32u, bhi + dk, idesc, 1u);
                     }
@@ -480,15 +483,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
                     for (int kk = 0; kk < 4; kk++) {
                         const uint64_t dk = (uint64_t)(kk * 2);  // 32 bytes = 8 TF32 along K
-                        mma_tf32(d, ahi + dk, bhi + dk, idesc, (k % F != 0 || kk > 0) ? 1u : 0u);
+                        mma_tf32(d, ahi + dk, bhi + dk, idesc, (kf != 0 || kk > 0) ? 1u : 0u);
                         mma_tf32(d, ahi + dk, blo + dk, idesc, 1u);
                         mma_tf32(d, alo + dk, bhi + dk, idesc, 1u);
                     }
                 }
                 mma_commit(&ctl.mma_done[s]);  // weight stage s reusable (producers)
                 mma_commit(&ctl.z_free[sb]);   // Z stage sb reusable (copy warp)
-                if (k % F == F - 1 || k == ktotal - 1) mma_commit(&ctl.acc_full[c & 1]);  // chunk c complete
+                if (kf == F - 1 || k == ktotal - 1) mma_commit(&ctl.acc_full[c & 1]);  // chunk c complete
                 last_mma = k;
+                if (++sb == nb) {
+                    sb = 0;
+                    zpar ^= 1;
+                }
+                if (++kf == F) {
+                    kf = 0;
+                    c++;
+                }
                 if (prof) p_i += clock64() - c0;
             }
             if (prof) {
@@ -516,8 +527,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 bulk_prefetch_l2(d2blk + (size_t)tl * (TC_D_BYTES / 4), TC_D_BYTES);
                 kp++;
             };
+            int zsb = 0;  // kz % nb, kept as a counter (no run-time divisions on this thread)
             auto issue_z = [&](int tl) {
-                const int sb = kz % nb;
+                const int sb = zsb;
+                if (++zsb == nb) zsb = 0;
                 unsigned char* B = sB + (size_t)sb * 2 * b_bytes;
                 const unsigned char* src = a.zimg + (size_t)tl * 2u * b_bytes;
                 mbar_arrive_expect_tx(&ctl.full_b[sb], 2u * b_bytes);
@@ -543,6 +556,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 if (CACHED) issue_d(tl);
                 else issue_p(tl);
             }
+            int jsb = 0, jpar = 0;  // j % nb and (j / nb) & 1
             for (int j = 0; j < ktotal && (kz < ktotal || (kp < ktotal && (!CACHED || nd > 0))); j++) {
                 if (*(volatile int*)&ctl.abort) break;
                 if (CACHED) {
@@ -561,12 +575,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 }
                 if (kz < ktotal) {
                     // Z stage j % nb is free once the MMAs of tile j are done
-                    if (!mbar_wait_spin(&ctl.z_free[j % nb], (uint32_t)((j / nb) & 1), TC_WAIT)) {
+                    if (!mbar_wait_spin(&ctl.z_free[jsb], (uint32_t)jpar, TC_WAIT)) {
                         atomicExch(&ctl.abort, 1);
                         break;
                     }
                     const int tl = wz.next();
                     if (tl >= 0) issue_z(tl);
+                }
+                if (++jsb == nb) {
+                    jsb = 0;
+                    jpar ^= 1;
                 }
             }
             if (*(volatile int*)&ctl.abort) {
