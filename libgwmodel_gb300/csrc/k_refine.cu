@@ -61,14 +61,27 @@ __global__ void __launch_bounds__(RF_THREADS) k_refine(RefineArgs a)
     const float4 fbound = fbound_s;
     const float far_thr =
         (a.skip && a.kernel >= GW_KERNEL_BISQUARE) ? tb_far_threshold<GEO>((double)rmax) : -1.0f;
+    // this thread's elements of a tile's staging block (point q, column c), once:
+    // no division by the run-time p + 1 inside the tile loop
+    constexpr int RF_LOADS = (RF_TILE * (PMAX + 1) + RF_THREADS - 1) / RF_THREADS;
+    int lq[RF_LOADS], lc[RF_LOADS];
+#pragma unroll
+    for (int u = 0; u < RF_LOADS; u++) {
+        const int e = t + u * RF_THREADS;
+        lq[u] = e / pp;
+        lc[u] = e - lq[u] * pp;
+    }
 
     for (int tile = 0; tile < a.ntiles; tile++) {
         if (tb_far<GEO>(fbound, a.tb[tile], far_thr)) continue;
         const int j0 = tile * RF_TILE;
-        for (int e = t; e < RF_TILE * pp; e += RF_THREADS) {
-            const int q = e / pp, c = e - q * pp;
-            const int j = j0 + q;
-            rsm[e] = (j < a.n) ? (c < p ? a.X[(size_t)j * p + c] : a.y[j]) : 0.0;
+#pragma unroll
+        for (int u = 0; u < RF_LOADS; u++) {
+            const int e = t + u * RF_THREADS;
+            if (e < RF_TILE * pp) {
+                const int j = j0 + lq[u], c = lc[u];
+                rsm[e] = (j < a.n) ? (c < p ? a.X[(size_t)j * p + c] : a.y[j]) : 0.0;
+            }
         }
         __syncthreads();
         if (ok) {

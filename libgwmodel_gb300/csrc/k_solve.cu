@@ -346,26 +346,30 @@ __global__ void __launch_bounds__(ST_THREADS) k_solve_crit_t(SolveArgs a)
     double* L = smem;                      // mm elements (lower, packed by rows) x ST_THREADS
     double* zv = smem + (size_t)mm * ST_THREADS;  // p elements
     double* uv = zv + (size_t)p * ST_THREADS;     // p elements
+    // element of column q of G in the shared block: A[c][r] (upper, packed by
+    // rows) goes to the lower factor's tri_index(r, c), b right after it; built
+    // once, so the loads below need no division or search per element
+    __shared__ short slot[20 * 21 / 2 + 20];
+    for (int q = t; q < m; q += ST_THREADS) {
+        if (q < mm) {
+            int c = 0, base = 0;
+            while (base + (p - c) <= q) {
+                base += p - c;
+                c++;
+            }
+            slot[q] = (short)tri_index(c + (q - base), c);
+        } else {
+            slot[q] = (short)q;  // zv follows L: element mm + (q - mm)
+        }
+    }
     double acc_s = 0.0, acc_r = 0.0, acc_f = 0.0;
     for (int row0 = blockIdx.x * ST_THREADS; row0 < a.n; row0 += gridDim.x * ST_THREADS) {
         const int nrow = min(ST_THREADS, a.n - row0);
         __syncwarp();
-        // coalesced loads of the block's rows of G: column q of G is A[c][r]
-        // (upper, packed by rows) for q < mm, else b
-        for (int e = t; e < nrow * m; e += ST_THREADS) {
-            const int lr = e / m, q = e - lr * m;
-            const double v = a.G[(size_t)(row0 + lr) * a.ldg + q];
-            if (q < mm) {
-                int c = 0, base = 0;
-                while (base + (p - c) <= q) {
-                    base += p - c;
-                    c++;
-                }
-                const int r = c + (q - base);
-                L[(size_t)tri_index(r, c) * ST_THREADS + lr] = v;
-            } else {
-                zv[(size_t)(q - mm) * ST_THREADS + lr] = v;
-            }
+        // coalesced loads of the block's rows of G
+        for (int lr = 0; lr < nrow; lr++) {
+            const double* g = a.G + (size_t)(row0 + lr) * a.ldg;
+            for (int q = t; q < m; q += ST_THREADS) L[(size_t)slot[q] * ST_THREADS + lr] = g[q];
         }
         __syncwarp();
         const int row = row0 + t;
