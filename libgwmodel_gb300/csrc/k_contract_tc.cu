@@ -440,7 +440,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 if (*(volatile int*)&ctl.abort) break;
                 const int s = k & 1;
                 if (prof) c0 = clock64();
-                if (!mbar_wait_spin(&ctl.full_a[s], (uint32_t)((k >> 1) & 1), TC_WAIT)) {
+                if (!mbar_wait(&ctl.full_a[s], (uint32_t)((k >> 1) & 1), TC_WAIT)) {
                     atomicExch(&ctl.abort, 1);
                     break;
                 }
@@ -449,9 +449,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     p_a += c1 - c0;
                     c0 = c1;
                 }
-                bool ok = mbar_wait_spin(&ctl.full_b[sb], (uint32_t)zpar, TC_WAIT);
+                bool ok = mbar_wait(&ctl.full_b[sb], (uint32_t)zpar, TC_WAIT);
                 if (ok && kf == 0 && c >= 2)
-                    ok = mbar_wait_spin(&ctl.tmem_free[c & 1], (uint32_t)(((c >> 1) - 1) & 1), TC_WAIT);
+                    ok = mbar_wait(&ctl.tmem_free[c & 1], (uint32_t)(((c >> 1) - 1) & 1), TC_WAIT);
                 if (!ok) {
                     atomicExch(&ctl.abort, 1);
                     break;
@@ -566,7 +566,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     }
                 } else if (kp < ktotal) {
                     // point buffer j % 2 is free once the producers are done with tile j
-                    if (!mbar_wait_spin(&ctl.full_a[j & 1], (uint32_t)((j >> 1) & 1), TC_WAIT)) {
+                    if (!mbar_wait(&ctl.full_a[j & 1], (uint32_t)((j >> 1) & 1), TC_WAIT)) {
                         atomicExch(&ctl.abort, 1);
                         break;
                     }
@@ -575,7 +575,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 }
                 if (kz < ktotal) {
                     // Z stage j % nb is free once the MMAs of tile j are done
-                    if (!mbar_wait_spin(&ctl.z_free[jsb], (uint32_t)jpar, TC_WAIT)) {
+                    if (!mbar_wait(&ctl.z_free[jsb], (uint32_t)jpar, TC_WAIT)) {
                         atomicExch(&ctl.abort, 1);
                         break;
                     }

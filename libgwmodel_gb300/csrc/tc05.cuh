@@ -60,33 +60,6 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
     return false;
 }
 
-// Non-blocking test of the phase with the given parity.
-__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// mbar_wait by polling with test_wait, for a single thread on the critical path
-// (no suspension, so it sees the phase complete at once); the same bounds.
-__device__ __forceinline__ bool mbar_wait_spin(uint64_t* bar, uint32_t parity, uint32_t max_iters)
-{
-    if (mbar_test_wait(bar, parity)) return true;
-    const uint64_t t0 = globaltimer_ns();
-    for (uint32_t it = 1; it < max_iters; ++it) {
-        if (mbar_test_wait(bar, parity)) return true;
-        if ((it & 255u) == 0 && globaltimer_ns() - t0 > 2000000000ull) return false;
-    }
-    return false;
-}
-
 // Plain arrive (release at CTA scope) by the calling thread.
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
 {
