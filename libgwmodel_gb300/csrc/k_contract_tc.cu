@@ -4,18 +4,22 @@
 // warp-specialised pipeline synchronised by mbarriers only:
 //  * 16 producer warps compute the 128 x 32 weight tile of each 32-point
 //    data tile in FP32 from the point records (planar or WGS-84 great-circle,
-//    prefetched into shared memory by a bulk copy two tiles ahead), split
-//    every weight into TF32 hi + lo and store both in the 128-byte-swizzled
-//    K-major layout the tensor core reads (two weight stages);
+//    prefetched into shared memory by a bulk copy two tiles ahead) or from
+//    the distance cache, split every weight into TF32 hi + lo and write both
+//    into tensor memory (tcgen05.st; two weight stages) or, for npad > 192,
+//    into shared memory in the 128-byte-swizzled K-major layout;
 //  * the matching Z~ tile (scaled/centred products, split hi + lo, stored in
-//    global memory already in the swizzled image) arrives by one 1-D bulk copy
-//    up to three tiles ahead, issued by one thread of a copy warp;
+//    global memory already in the swizzled image) arrives by 1-D bulk copies
+//    issued by one thread of a copy warp, up to four stages ahead (three with
+//    weights in shared memory);
 //  * one thread of the MMA warp issues 3 x 4 tcgen05.mma.kind::tf32
 //    (hi.hi + hi.lo + lo.hi, K = 8 each) into a 128 x N FP32 accumulator in
 //    TMEM and commits to mbarriers.  An MMA issue returns only when the tensor
 //    pipe accepts it (about as long as the MMA runs), so that thread issues
 //    nothing else: with the copies on the same thread the pipe idled about
-//    two thirds of the time;
+//    two thirds of the time.  Both single-thread loops keep their stage and
+//    chunk positions as counters: a division by a run-time value there costs
+//    a dependent chain on the thread that gates the whole CTA;
 //  * chunks of flush_tiles tiles alternate between two TMEM accumulators; four
 //    drain warps (one per TMEM lane quadrant) read a finished chunk back with
 //    tcgen05.ld and add it into double-float (hi, lo) sums in global memory,
@@ -116,7 +120,8 @@ __device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity)
 // Warp roles: warps 0-15 produce the weight tiles (thread (r, quarter) fills
 // points [8 quarter, 8 quarter + 8) of row r); warps 16-19 drain the
 // accumulators (warp 16 + q owns TMEM lanes 32 q .. 32 q + 31, all columns);
-// lane 0 of warp 20 issues the bulk copies and the MMAs.  Tile k uses weight
+// lane 0 of warp 20 issues the MMAs and lane 0 of warp 21 the bulk copies
+// (Z stage j is refilled once z_free[j % nb] reports its MMAs done).  Tile k uses weight
 // stage k % 2, Z stage k % nb and point buffer k % 2; chunk c = k / F of F
 // tiles accumulates in TMEM accumulator c % 2, whose last MMA commits to
 // acc_full[c % 2]; the drain warps then add it into the double-float sums and
