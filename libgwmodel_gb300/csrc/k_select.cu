@@ -820,7 +820,7 @@ cudaError_t launch_select(const SelectArgs& a, bool geographic, bool exact, int 
     const int nrows = a.F.u ? a.F.n : a.n;
     // inside a cached bin the small window buffers fit three times the CTAs per SM
     const bool narrow = a.hist_cache && a.cache_valid && a.hist_coarse;
-    int grid = num_sms * (narrow ? 24 : 12);
+    int grid = num_sms * (narrow ? 32 : 12);
     if (grid > nrows) grid = nrows;
     return narrow ? launch_select_cfg<SelNarrow>(a, geographic, exact, grid, stream)
                   : launch_select_cfg<SelWide>(a, geographic, exact, grid, stream);
