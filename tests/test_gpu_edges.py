@@ -81,3 +81,22 @@ def test_smallest_problems(n):
     if n > 3:
         check_against_oracle(x, y, c, False, n, True, O.BOXCAR)  # every nearer neighbour at weight 1
     check_against_oracle(x, y, c, False, 50.0, False, O.GAUSSIAN)
+
+
+@pytest.mark.parametrize("p", [1, 2, 19, 20, 21])
+@pytest.mark.parametrize("criterion", [O.AIC, O.CV])
+def test_criterion_solve_forms_at_their_column_limits(p, criterion):
+    """The criterion without beta runs one location per thread up to p = 20 and
+    one warp per location beyond; both agree with the oracle at the edges
+    (p = 1 has no off-diagonal work, p = 20 fills the per-thread factor)."""
+    rng = np.random.default_rng(100 + p)
+    n = 700
+    c = rng.uniform(0, 100, (n, 2))
+    x, y, c = problem(n, p, c, 200 + p)
+    e = Engine(0)
+    e.set_data(x, y, c, False)
+    pb = O.Problem(x, y, c, geographic=False)
+    for bw, adaptive, kernel in ((max(3 * p, 60), True, O.BISQUARE), (40.0, False, O.GAUSSIAN)):
+        got = e.criterion(bw, adaptive, kernel, criterion)
+        want = pb.criterion(bw, adaptive, kernel, criterion)[0]
+        assert abs(got - want) <= 1e-9 * abs(want), (p, bw, got, want)
