@@ -118,3 +118,31 @@ def test_cache_off_for_planar_and_fp64():
     g.set_data(x, y, coords * 0.5, True)
     g.criterion(100, True, 2, 0)  # FP64 drop-in
     assert not g.distance_cache_active()
+
+
+@pytest.mark.parametrize("geographic", [True, False])
+def test_wide_x_keeps_shared_memory_weights(geographic):
+    """p = 20 (Z 230 columns, npad 240 > 192): the contraction keeps its weight
+    tiles in shared memory.  Cached and uncached agree bit for bit, and the
+    mixed criterion stays within 1e-5 of the FP64 engine."""
+    n, p = 1500, 20
+    rng = np.random.default_rng(21)
+    if geographic:
+        x, y, coords = sphere_problem(n, p, 22)
+        coords = np.column_stack([rng.uniform(-10, 30, n), rng.uniform(35, 60, n)])
+    else:
+        coords = rng.uniform(0, 100, (n, 2))
+        x = np.column_stack([np.ones(n)] + [rng.standard_normal(n) for _ in range(p - 1)])
+        y = x @ rng.uniform(-1, 1, p) + 0.3 * rng.standard_normal(n)
+    cached, plain = engines(x, y, coords) if geographic else (None, None)
+    e64 = Engine(0)
+    e64.set_data(x, y, coords, geographic)
+    emx = Engine(0)
+    emx.set_data(x, y, coords, geographic)
+    emx.set_precision(1)
+    for bw in (120, 600):
+        c64 = e64.criterion(bw, True, 2, 0)
+        cmx = emx.criterion(bw, True, 2, 0)
+        assert abs(cmx - c64) <= 1e-5 * abs(c64), (bw, cmx, c64)
+        if geographic:
+            assert cached.criterion(bw, True, 2, 0) == plain.criterion(bw, True, 2, 0)
