@@ -231,7 +231,9 @@ struct DeviceD2Cache {
     cudaEvent_t used = nullptr;
 };
 constexpr int kMaxDevices = 64;
-DeviceD2Cache g_d2c[kMaxDevices];
+// Allocated once and never destroyed, so engines that outlive static
+// destruction at process exit still find their device's entry and mutex.
+DeviceD2Cache* const g_d2c = new DeviceD2Cache[kMaxDevices];
 
 DeviceD2Cache& device_d2c(int device)
 {
