@@ -21,7 +21,7 @@ public:
 
 constexpr int kCRSDistance = 0;  // Distance::DistanceType::CRSDistance (Distance.h:50-57)
 
-class GWRBasicGpuTask : public IGWRBasicGpuTask {
+class GWRBasicGpuTask final : public IGWRBasicGpuTask {
 public:
     GWRBasicGpuTask(int nDp, int nVar, int distanceType, int nPredict = 0)
         : mX(nDp, nVar), mY(nDp, 1), mCoords(nDp, 2), mPredictLocations(nPredict, 2), mDistanceType(distanceType)
