@@ -398,7 +398,7 @@ void Engine::setData(int n, int p, const double* x, const double* y, const doubl
     partials_.alloc(4096 * 4);
     sums_.alloc(8);
     tiles_.alloc(ntiles);
-    key_.alloc(1);
+    key_.alloc(2);
     check(cudaMemcpyAsync(u_.get(), hu.data(), sizeof(double) * n, cudaMemcpyHostToDevice, stream_), "H2D u");
     check(cudaMemcpyAsync(v_.get(), hv.data(), sizeof(double) * n, cudaMemcpyHostToDevice, stream_), "H2D v");
     if (geographic) {
@@ -611,11 +611,16 @@ void Engine::buildProxy()
     stb_.alloc(t1024.size());
     check(cudaMemcpyAsync(stb_.get(), t1024.data(), sizeof(float4) * t1024.size(), cudaMemcpyHostToDevice, stream_),
           "H2D super-tile bounds");
+    // proxy error bands of the exact select.  The FP32 great-circle proxy is within
+    // 5.3e-7 relative of the reference's distance wherever it is trusted (d < 15,000 km;
+    // measured over near, regional and global pairs), 1e-10 km absolute for nearly
+    // coincident points: 2^-16 (1.5e-5) and 1e-6 km leave a margin of 25x over it.
+    // Every point inside the band is evaluated with the correctly rounded formula.
     if (!geographic_) {
         sel_eps_ = std::ldexp(1.0, -18);
         sel_delta_ = std::ldexp(dhi_, -36);
     } else {
-        sel_eps_ = std::ldexp(1.0, -12);
+        sel_eps_ = std::ldexp(1.0, -16);
         sel_delta_ = 1e-6;
     }
     tbsel_.alloc(tb.size());
@@ -1570,10 +1575,12 @@ double Engine::globalCriterion(const std::vector<int>& cols)
 double Engine::maxDistance()
 {
     check(cudaSetDevice(device_), "cudaSetDevice");
-    check(cudaMemsetAsync(key_.get(), 0, sizeof(unsigned long long), stream_), "memset");
-    check(launch_max_distance(points(), geographic_, key_.get(), num_sms_, stream_), "maxdist");
+    check(cudaMemsetAsync(key_.get(), 0, 2 * sizeof(unsigned long long), stream_), "memset");
+    if (geographic_) rowmax_.alloc(n_);
+    check(launch_max_distance(points(), geographic_, key_.get(), rowmax_.get(), num_sms_, stream_), "maxdist");
     unsigned long long k = 0;
-    check(cudaMemcpyAsync(&k, key_.get(), sizeof(k), cudaMemcpyDeviceToHost, stream_), "D2H");
+    check(cudaMemcpyAsync(&k, key_.get() + (geographic_ ? 1 : 0), sizeof(k), cudaMemcpyDeviceToHost, stream_),
+          "D2H");
     synchronize();
     uint64_t b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
     double d;

@@ -302,7 +302,8 @@ private:
     cudaEvent_t timerBegin();
     void timerEnd(cudaEvent_t e0, int kind);  // processed-tile counter of the contraction (stats)
     DevBuf<double> tinv_, tvec_;   // transform of the fit's covariance diagonal
-    DevBuf<unsigned long long> key_;
+    DevBuf<unsigned long long> key_;  // maxDistance: fast and exact maxima as ordered keys
+    DevBuf<double> rowmax_;           // maxDistance: per-row maxima of the fast pass (geographic)
     double* host_sums_ = nullptr;  // pinned
 
     bool thr_valid_ = false;

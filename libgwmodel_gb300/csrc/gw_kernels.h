@@ -117,6 +117,8 @@ struct SolveArgs {
     // Fit mode, optional: A_i^-1 (n x p x p, row-major per row).
     double* ainv;
 };
+// Largest grid launch_solve uses; callers size `partials` (4 doubles per block) for it.
+constexpr int kSolveMaxBlocks = 4096;
 cudaError_t launch_solve(const SolveArgs& a, int* nblocks, cudaStream_t stream);
 // Criterion solves (kSolveAIC / kSolveCV) of many segments in one launch:
 // block b solves rows [work[b].y, work[b].z) of segment work[b].x and writes
@@ -232,9 +234,12 @@ cudaError_t launch_hat_mixed(int n, bool geographic, const float4* pts, const fl
 cudaError_t launch_tile_far_thr(int n, int tile, bool geographic, const double* thr, double bw, float* tile_thr,
                                 cudaStream_t stream);
 
-// Maximum pairwise distance (CRSDistance::maxDistance), as an ordered key in *key_out.
-cudaError_t launch_max_distance(const DevPoints& P, bool geographic, unsigned long long* key_out, int num_sms,
-                                cudaStream_t stream);
+// Maximum pairwise distance (CRSDistance::maxDistance) as an ordered key: key_out[0]
+// for planar data, key_out[1] for geographic data (key_out[0] then holds the
+// unit-vector form's maximum).  Both keys start at 0; rowmax (geographic only)
+// holds n doubles of scratch.
+cudaError_t launch_max_distance(const DevPoints& P, bool geographic, unsigned long long* key_out, double* rowmax,
+                                int num_sms, cudaStream_t stream);
 
 
 // GWRMultiscale hat matrix (k_mgwr.cu).  Matrices are n x n row-major in the

@@ -45,39 +45,11 @@ __device__ __forceinline__ double pair_weight64(int kernel, double du, double dv
     }
     double d;
     if constexpr (GEO)
-        d = gw_gc_dist(du, fu, dv, fv, duR, fuR, dvR, fvR);
+        d = kernel == GW_KERNEL_BOXCAR ? gw_gc_dist(du, fu, dv, fv, duR, fuR, dvR, fvR)
+                                       : gw_gc_dist_fast(du, fu, dv, fv, duR, fuR, dvR, fvR);
     else
         d = gw_planar_dist(du, dv, fu, fv);
     return gw_kernel_weight(kernel, d, r);
-}
-
-// The reference's great-circle formula (CRSDistance.cpp:15-69) from FP64 unit
-// vectors e = (cos lat cos lon, cos lat sin lon, sin lat): its haversine terms
-// are S = sin^2 G cos^2 L + cos^2 F sin^2 L = |e_i - e_j|^2 / 4 and
-// C = |e_i + e_j|^2 / 4, and sin F cos G = (sin lat_i + sin lat_j) / 2,
-// cos F sin G = (sin lat_i - sin lat_j) / 2.  One square root, two divisions
-// and one arctangent instead of three sine-cosine pairs, a square root and four
-// divisions.  The chord of two nearby points carries an absolute error of a
-// few 1e-16, i.e. ~1e-12 km in D: nothing against a bandwidth; the relative
-// error elsewhere is a few ulp (CUDA's atan, within 2 ulp).
-__device__ __forceinline__ double gc_dist_vec(double xi, double yi, double zi, double xj, double yj, double zj)
-{
-    const double a = 6378.137, f = 1.0 / 298.257223563;
-    const double dx = xi - xj, dy = yi - yj, dz = zi - zj;
-    const double sx = xi + xj, sy = yi + yj, sz = zi + zj;
-    const double S = 0.25 * fma(dx, dx, fma(dy, dy, dz * dz));
-    const double C = 0.25 * fma(sx, sx, fma(sy, sy, sz * sz));
-    if (!(S > 0.0)) return 0.0;
-    const double sc = S * C;
-    const double rsc = sqrt(sc);
-    const double inv = 1.0 / sc;             // 1/C = S inv, 1/S = C inv
-    const double w = atan(rsc * (S * inv));  // atan(sqrt(S / C))
-    const double R = rsc / w;
-    const double D = 2.0 * w * a;
-    const double H1 = (3.0 * R - 1.0) * (0.5 * S * inv);
-    const double H2 = (3.0 * R + 1.0) * (0.5 * C * inv);
-    const double sFcG = 0.5 * sz, cFsG = 0.5 * dz;
-    return D * (1.0 + f * H1 * (sFcG * sFcG) - f * H2 * (cFsG * cFsG));
 }
 
 // w_ij of a geographic pair from the unit vectors (bisquare, tricube, gaussian,

@@ -513,7 +513,8 @@ __global__ void __launch_bounds__(HAT_THREADS)
             for (int q = 0; q < iend; q++) {
                 double d;
                 if constexpr (GEO)
-                    d = gw_gc_dist(du, su[q], dv, sv[q], duR, suR[q], dvR, svR[q]);
+                    d = kernel == GW_KERNEL_BOXCAR ? gw_gc_dist(du, su[q], dv, sv[q], duR, suR[q], dvR, svR[q])
+                                                   : gw_gc_dist_fast(du, su[q], dv, sv[q], duR, suR[q], dvR, svR[q]);
                 else
                     d = gw_planar_dist(du, dv, su[q], sv[q]);
                 double w = gw_kernel_weight(kernel, d, sr[q]);
@@ -602,23 +603,67 @@ __global__ void __launch_bounds__(HAT_THREADS)
     if (j < n) qdiag[j] = acc;
 }
 
+// CRSDistance::maxDistance (CRSDistance.cpp:133-143).  Planar distances are
+// exact, so one pass takes the maximum.  Great-circle distances take two: the
+// first finds every row's maximum with the unit-vector form of the formula
+// (a few ulp, ~100 FP64 operations per pair instead of the ~3,000 of the
+// correctly rounded one); the second evaluates the reference's double only
+// for the pairs of the rows that come within kMaxdistMargin of the largest
+// row maximum, so the result is the reference's maximum.
+constexpr double kMaxdistMargin = 1e-9;
+
 template <bool GEO>
-__global__ void k_maxdist(DevPoints P, unsigned long long* __restrict__ key)
+__global__ void k_maxdist(DevPoints P, unsigned long long* __restrict__ key, double* __restrict__ rowmax)
 {
     const int lane = threadIdx.x & 31;
     const int warps = gridDim.x * (blockDim.x / 32);
     double best = 0.0;
     for (int i = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); i < P.n; i += warps) {
         const double fu = P.u[i], fv = P.v[i];
-        const double fuR = GEO ? P.uR[i] : 0.0, fvR = GEO ? P.vR[i] : 0.0;
+        double rm = 0.0;
+        if constexpr (GEO) {
+            const double fuR = P.uR[i], fvR = P.vR[i];
+            if (P.e) {
+                const double xi = P.e[i], yi = P.e[(size_t)P.n + i], zi = P.e[2 * (size_t)P.n + i];
+                for (int j = lane; j < P.n; j += 32)
+                    rm = fmax(rm, gc_dist_vec(xi, yi, zi, P.e[j], P.e[(size_t)P.n + j], P.e[2 * (size_t)P.n + j]));
+            } else {
+                for (int j = lane; j < P.n; j += 32)
+                    rm = fmax(rm, gw_gc_dist_fast(P.u[j], fu, P.v[j], fv, P.uR[j], fuR, P.vR[j], fvR));
+            }
+        } else {
+            for (int j = lane; j < P.n; j += 32) rm = fmax(rm, gw_planar_dist(P.u[j], P.v[j], fu, fv));
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) rm = fmax(rm, __shfl_xor_sync(FULL, rm, off));
+        if (GEO && lane == 0) rowmax[i] = rm;
+        best = fmax(best, rm);
+    }
+    if (lane == 0) atomicMax(key, (unsigned long long)dkey(best));
+}
+
+// Second pass of the great-circle maximum: key[0] holds the first pass's
+// maximum M; rows whose maximum reaches M (1 - margin) evaluate the
+// reference's double for their pairs within the margin into key[1].
+__global__ void k_maxdist_exact(DevPoints P, unsigned long long* __restrict__ key, const double* __restrict__ rowmax)
+{
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (blockDim.x / 32);
+    const double cut = keyd(key[0]) * (1.0 - kMaxdistMargin);
+    double best = 0.0;
+    for (int i = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); i < P.n; i += warps) {
+        if (!(rowmax[i] >= cut)) continue;  // warp-uniform
+        const double fu = P.u[i], fv = P.v[i], fuR = P.uR[i], fvR = P.vR[i];
         for (int j = lane; j < P.n; j += 32) {
-            double d = pair_dist<GEO>(P, j, fu, fv, fuR, fvR);
-            best = fmax(best, d);
+            const double df = P.e ? gc_dist_vec(P.e[i], P.e[(size_t)P.n + i], P.e[2 * (size_t)P.n + i], P.e[j],
+                                                P.e[(size_t)P.n + j], P.e[2 * (size_t)P.n + j])
+                                  : gw_gc_dist_fast(P.u[j], fu, P.v[j], fv, P.uR[j], fuR, P.vR[j], fvR);
+            if (df >= cut) best = fmax(best, gw_gc_dist(P.u[j], fu, P.v[j], fv, P.uR[j], fuR, P.vR[j], fvR));
         }
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) best = fmax(best, __shfl_xor_sync(FULL, best, off));
-    if (lane == 0) atomicMax(key, (unsigned long long)dkey(best));
+    if (lane == 0) atomicMax(key + 1, (unsigned long long)dkey(best));
 }
 
 __global__ void k_colsum_partial(int n, int m, const double* __restrict__ Z, double* __restrict__ part)
@@ -712,7 +757,7 @@ cudaError_t launch_solve(const SolveArgs& a, int* nblocks, cudaStream_t stream)
         const int mm = a.p * (a.p + 1) / 2;
         const size_t smem = (size_t)(mm + 2 * a.p) * ST_THREADS * sizeof(double);
         int grid = (a.n + ST_THREADS - 1) / ST_THREADS;
-        if (grid > 4096) grid = 4096;  // the callers' partials hold 4096 blocks (as for k_solve)
+        if (grid > kSolveMaxBlocks) grid = kSolveMaxBlocks;  // the callers' partials hold this many blocks
         *nblocks = grid;
         if (a.mode == kSolveAIC) {
             raise_smem_limit((const void*)k_solve_crit_t<kSolveAIC>, smem);
@@ -724,7 +769,7 @@ cudaError_t launch_solve(const SolveArgs& a, int* nblocks, cudaStream_t stream)
         return cudaGetLastError();
     }
     int grid = (a.n + SV_WARPS - 1) / SV_WARPS;
-    if (grid > 4096) grid = 4096;
+    if (grid > kSolveMaxBlocks) grid = kSolveMaxBlocks;
     const int ld = a.p + 1;
     size_t per_warp = (a.mode == kSolveFit) ? 4 * a.p * ld + 2 * a.p : a.p * ld + a.p;
     size_t smem = per_warp * SV_WARPS * sizeof(double);
@@ -831,14 +876,16 @@ cudaError_t launch_hat_mixed(int n, bool geographic, const float4* pts, const fl
     return cudaGetLastError();
 }
 
-cudaError_t launch_max_distance(const DevPoints& P, bool geographic, unsigned long long* key_out, int num_sms,
-                                cudaStream_t stream)
+cudaError_t launch_max_distance(const DevPoints& P, bool geographic, unsigned long long* key_out, double* rowmax,
+                                int num_sms, cudaStream_t stream)
 {
-    int grid = num_sms * 8;
-    if (geographic)
-        k_maxdist<true><<<grid, 256, 0, stream>>>(P, key_out);
-    else
-        k_maxdist<false><<<grid, 256, 0, stream>>>(P, key_out);
+    const int grid = num_sms * 8;
+    if (geographic) {
+        k_maxdist<true><<<grid, 256, 0, stream>>>(P, key_out, rowmax);
+        k_maxdist_exact<<<grid, 256, 0, stream>>>(P, key_out, rowmax);
+    } else {
+        k_maxdist<false><<<grid, 256, 0, stream>>>(P, key_out, rowmax);
+    }
     return cudaGetLastError();
 }
 

@@ -2,7 +2,9 @@
  * gwr_oracle.c -- TEST INFRASTRUCTURE ONLY: the CPU oracle for the GWRBasic
  * hot path.  Every function restates the reference line range it cites
  * (paths inside libgwmodel).  Build with -ffp-contract=off so that distances
- * and weights round exactly as the reference's expressions do.
+ * and weights round exactly as the reference's expressions do.  Nothing of
+ * the engine is compiled in: distances, kernels and the great-circle formula
+ * (with the platform libm) are restated here from the reference alone.
  */
 #include "gwr_oracle.h"
 
@@ -14,7 +16,8 @@
 #include <omp.h>
 #endif
 
-#include "../libgwmodel_gb300/csrc/gw_arith.h"
+/* DOUBLE_EPS compile definition of the reference (src/CMakeLists.txt:33-36). */
+#define ORC_DOUBLE_EPS 1e-8
 
 #define X_(pb, i, k) ((pb)->x[(size_t)(i) + (size_t)(k) * (size_t)(pb)->n])
 #define U_(pb, i) ((pb)->coords[(size_t)(i)])
@@ -45,11 +48,11 @@ double orc_gcdist_libm(double lon1, double lon2, double lat1, double lat2)
     DE2RA = M_PI / 180;
     a = 6378.137;
     f = 1.0 / 298.257223563;
-    if (fabs(lat1 - lat2) < GW_DOUBLE_EPS)
+    if (fabs(lat1 - lat2) < ORC_DOUBLE_EPS)
     {
-        if (fabs(lon1 - lon2) < GW_DOUBLE_EPS)
+        if (fabs(lon1 - lon2) < ORC_DOUBLE_EPS)
             return 0.0;
-        else if (fabs((fabs(lon1) + fabs(lon2)) - 360.0) < GW_DOUBLE_EPS)
+        else if (fabs((fabs(lon1) + fabs(lon2)) - 360.0) < ORC_DOUBLE_EPS)
             return 0.0;
     }
     lat1R = lat1 * DE2RA;
@@ -75,11 +78,37 @@ double orc_gcdist_libm(double lon1, double lon2, double lat1, double lat2)
     return D * (1 + f * H1 * sinF2 * cosG2 - f * H2 * cosF2 * sinG2);
 }
 
-/* The same formula evaluated with the engine's portable sin/cos/atan. */
-double orc_gcdist_portable(double lon1, double lon2, double lat1, double lat2)
+/* CRSDistance::EuclideanDistance (CRSDistance.h:95-99): diff = data - focus,
+ * sqrt(sum(diff % diff, 1)). */
+static double orc_planar_dist(double ud, double vd, double uf, double vf)
 {
-    const double DE2RA = M_PI / 180;
-    return gw_gc_dist(lon1, lon2, lat1, lat2, lon1 * DE2RA, lon2 * DE2RA, lat1 * DE2RA, lat2 * DE2RA);
+    double dx = ud - uf, dy = vd - vf;
+    return sqrt(dx * dx + dy * dy);
+}
+
+/* The five kernel functions (BandwidthWeight.h:68-121) for one element: the
+ * indicator (dist < bw) multiplies the polynomial as a 0/1 double. */
+static double orc_kernel_weight(int kernel, double d, double bw)
+{
+    switch (kernel)
+    {
+    case 0: /* Gaussian */
+        return exp((d * d) / ((-2.0) * (bw * bw)));
+    case 1: /* Exponential */
+        return exp(-d / bw);
+    case 2: /* Bisquare */
+    {
+        double t = 1.0 - (d * d) / (bw * bw);
+        return (d < bw ? 1.0 : 0.0) * (t * t);
+    }
+    case 3: /* Tricube */
+    {
+        double t = 1.0 - (d * d * d) / (bw * bw * bw);
+        return (d < bw ? 1.0 : 0.0) * (t * t * t);
+    }
+    default: /* Boxcar */
+        return (d < bw ? 1.0 : 0.0) * 1.0;
+    }
 }
 
 /* CRSDistance::distance(focus) (CRSDistance.cpp:122-131) with focus points ==
@@ -92,9 +121,7 @@ void orc_distance_row(const orc_problem* pb, int focus, double* out)
     for (int j = 0; j < pb->n; j++)
     {
         if (!pb->geographic)
-            out[j] = gw_planar_dist(U_(pb, j), V_(pb, j), uf, vf);
-        else if (pb->gc_mode == ORC_GC_PORTABLE)
-            out[j] = orc_gcdist_portable(U_(pb, j), uf, V_(pb, j), vf);
+            out[j] = orc_planar_dist(U_(pb, j), V_(pb, j), uf, vf);
         else
             out[j] = orc_gcdist_libm(U_(pb, j), uf, V_(pb, j), vf);
     }
@@ -160,7 +187,7 @@ int orc_weight(const double* dist, int n, double bw, int adaptive, int kernel, d
     double b = bw;
     if (adaptive && orc_adaptive_threshold(dist, n, bw, &b) != 0) return -1;
     for (int j = 0; j < n; j++)
-        w[j] = gw_kernel_weight(kernel, dist[j], b);
+        w[j] = orc_kernel_weight(kernel, dist[j], b);
     return 0;
 }
 
@@ -507,9 +534,7 @@ int orc_predict(const orc_problem* pb, int nr, const double* loc, double bw, int
         for (int j = 0; j < n; j++)
         {
             if (!pb->geographic)
-                w->d[j] = gw_planar_dist(U_(pb, j), V_(pb, j), uf, vf);
-            else if (pb->gc_mode == ORC_GC_PORTABLE)
-                w->d[j] = orc_gcdist_portable(U_(pb, j), uf, V_(pb, j), vf);
+                w->d[j] = orc_planar_dist(U_(pb, j), V_(pb, j), uf, vf);
             else
                 w->d[j] = orc_gcdist_libm(U_(pb, j), uf, V_(pb, j), vf);
         }

@@ -23,8 +23,6 @@ extern "C" {
 #define ORC_AIC 0 /* GWRBasic::BandwidthSelectionCriterionType::AIC */
 #define ORC_CV 1  /* GWRBasic::BandwidthSelectionCriterionType::CV */
 
-#define ORC_GC_LIBM 0     /* great-circle with the platform libm, as the reference */
-#define ORC_GC_PORTABLE 1 /* great-circle with the engine's portable sin/cos/atan */
 
 typedef struct orc_problem
 {
@@ -33,14 +31,11 @@ typedef struct orc_problem
     const double* y;      /* n */
     const double* coords; /* n x 2: column 0 = x or longitude, column 1 = y or latitude */
     int geographic;       /* CRSDistance(isGeographic) */
-    int gc_mode;          /* ORC_GC_LIBM or ORC_GC_PORTABLE */
     int threads;          /* OpenMP threads (mOmpThreadNum) */
 } orc_problem;
 
 /* CRSDistance::SpGcdist with libm (CRSDistance.cpp:15-69). */
 double orc_gcdist_libm(double lon1, double lon2, double lat1, double lat2);
-/* The same formula with the engine's portable arithmetic. */
-double orc_gcdist_portable(double lon1, double lon2, double lat1, double lat2);
 
 /* CRSDistance::distance(focus) for focus points == data points (CRSDistance.cpp:122-131). */
 void orc_distance_row(const orc_problem* pb, int focus, double* out);

@@ -23,13 +23,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libgwr_oracle.so")
 SOURCES = [os.path.join(HERE, "gwr_oracle.c")]
-DEPS = SOURCES + [os.path.join(HERE, "gwr_oracle.h"),
-                  os.path.join(HERE, "..", "libgwmodel_gb300", "csrc", "gw_arith.h")]
+DEPS = SOURCES + [os.path.join(HERE, "gwr_oracle.h")]
 
 DBL_MAX = np.finfo(np.float64).max
 AIC, CV = 0, 1
 GAUSSIAN, EXPONENTIAL, BISQUARE, TRICUBE, BOXCAR = range(5)
-GC_LIBM, GC_PORTABLE = 0, 1
 
 _lock = threading.Lock()
 _lib = None
@@ -52,7 +50,7 @@ def build(force: bool = False) -> str:
 class _Problem(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int), ("p", ctypes.c_int),
                 ("x", ctypes.c_void_p), ("y", ctypes.c_void_p), ("coords", ctypes.c_void_p),
-                ("geographic", ctypes.c_int), ("gc_mode", ctypes.c_int), ("threads", ctypes.c_int)]
+                ("geographic", ctypes.c_int), ("threads", ctypes.c_int)]
 
 
 class _MgwrOpts(ctypes.Structure):
@@ -83,8 +81,6 @@ def lib():
             d, i = ctypes.c_double, ctypes.c_int
             L.orc_gcdist_libm.restype = d
             L.orc_gcdist_libm.argtypes = [d, d, d, d]
-            L.orc_gcdist_portable.restype = d
-            L.orc_gcdist_portable.argtypes = [d, d, d, d]
             L.orc_distance_row.argtypes = [P, i, dp]
             L.orc_max_distance.restype = d
             L.orc_max_distance.argtypes = [P]
@@ -120,7 +116,7 @@ def _dp(a: np.ndarray):
 class Problem:
     """Column-major copies of X, y and coords, like GWRBase/SpatialAlgorithm keep."""
 
-    def __init__(self, x, y, coords, geographic=False, gc_mode=GC_PORTABLE, threads=None):
+    def __init__(self, x, y, coords, geographic=False, threads=None):
         self.x = np.asfortranarray(np.asarray(x, dtype=np.float64))
         self.y = np.ascontiguousarray(np.asarray(y, dtype=np.float64).reshape(-1))
         self.coords = np.asfortranarray(np.asarray(coords, dtype=np.float64))
@@ -130,11 +126,10 @@ class Problem:
         self.geographic = bool(geographic)
         self.threads = int(threads or os.cpu_count() or 1)
         self._s = _Problem(n, p, self.x.ctypes.data, self.y.ctypes.data, self.coords.ctypes.data,
-                           int(geographic), int(gc_mode), self.threads)
+                           int(geographic), self.threads)
 
     def with_columns(self, cols):
-        return Problem(self.x[:, cols], self.y, self.coords, self.geographic,
-                       self._s.gc_mode, self.threads)
+        return Problem(self.x[:, cols], self.y, self.coords, self.geographic, self.threads)
 
     @property
     def ref(self):
@@ -246,9 +241,9 @@ def weight(dist, bw, adaptive, kernel):
     return w
 
 
-def gcdist(lon1, lon2, lat1, lat2, mode=GC_PORTABLE):
-    f = lib().orc_gcdist_portable if mode == GC_PORTABLE else lib().orc_gcdist_libm
-    return f(float(lon1), float(lon2), float(lat1), float(lat2))
+def gcdist(lon1, lon2, lat1, lat2):
+    """CRSDistance::SpGcdist (CRSDistance.cpp:15-69) with the platform libm."""
+    return lib().orc_gcdist_libm(float(lon1), float(lon2), float(lat1), float(lat2))
 
 
 def forward_select(pb: Problem, has_intercept: bool, threshold: float):
@@ -292,14 +287,14 @@ def forward_select(pb: Problem, has_intercept: bool, threshold: float):
 def gwr_fit(x, y, coords, *, geographic=False, bandwidth=0.0, adaptive=True, kernel=GAUSSIAN,
             autoselect_bandwidth=False, criterion=CV, golden_lower=None, golden_upper=None,
             has_hat_matrix=True, autoselect_vars=False, var_threshold=3.0, has_intercept=True,
-            gc_mode=GC_PORTABLE, threads=None):
+            threads=None):
     """GWRBasic::fit (GWRBasic.cpp:36-128) with the OpenMP kernels.
 
     ``criterion`` follows the reference quirk that the criterion function
     pointer is CV until setBandwidthSelectionCriterion/setParallelType runs
     (GWRBasic.h:738-739); callers that never set it pass CV here.
     """
-    pb = Problem(x, y, coords, geographic, gc_mode, threads)
+    pb = Problem(x, y, coords, geographic, threads)
     n = pb.n
     out = {}
     if autoselect_vars:

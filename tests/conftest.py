@@ -1,5 +1,7 @@
+import ctypes
 import json
 import os
+import subprocess
 import sys
 
 import numpy as np
@@ -55,3 +57,48 @@ def londonhp_mgwr():
     y = data[:, 0].copy()
     x = np.column_stack([np.ones(len(y)), data[:, 1], data[:, 3]])
     return {"coords": coords, "x": x, "y": y, "cases": g["mgwr"], "tol": g["mgwr_tolerance_abs"]}
+
+
+class GcHost:
+    """The engine's great-circle arithmetic (gw_arith.h) built for the host by
+    tests/arith/gc_host.c: correctly rounded sin/cos/atan and exact distance rows."""
+
+    def __init__(self, path):
+        self.lib = ctypes.CDLL(path)
+        self._dp = ctypes.POINTER(ctypes.c_double)
+
+    def _p(self, a):
+        return a.ctypes.data_as(self._dp)
+
+    def sincos(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        s, c = np.empty_like(x), np.empty_like(x)
+        self.lib.gc_sincos_cr(self._p(x), self._p(s), self._p(c), len(x))
+        return s, c
+
+    def atan(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        a = np.empty_like(x)
+        self.lib.gc_atan_cr(self._p(x), self._p(a), len(x))
+        return a
+
+    def rows(self, coords):
+        """Distance rows (focus i against every point) for geographic coords."""
+        lon = np.ascontiguousarray(coords[:, 0], dtype=np.float64)
+        lat = np.ascontiguousarray(coords[:, 1], dtype=np.float64)
+        n = len(lon)
+
+        def row(i):
+            out = np.empty(n)
+            self.lib.gc_row_cr(self._p(lon), self._p(lat), n, int(i), self._p(out))
+            return out
+        return row
+
+
+@pytest.fixture(scope="session")
+def gc_host(tmp_path_factory):
+    src = os.path.join(ROOT, "tests", "arith", "gc_host.c")
+    out = str(tmp_path_factory.mktemp("gc_host") / "libgc_host.so")
+    subprocess.check_call(["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-ffp-contract=off", "-fPIC", "-shared",
+                           "-o", out, src, "-lm"])
+    return GcHost(out)

@@ -1,13 +1,15 @@
 """Edge inputs of the FP64 drop-in against the oracle: the widest X the engine
 takes (p = 25: Z has 350 columns, more than one contraction launch covers),
 geographic data across the antimeridian and at high latitude, and the smallest
-problems.  Bars as in test_gpu_parity: thresholds bit-exact, beta within 1e-10
-of each column's scale, criteria within 1e-9 relative."""
+problems.  Bars as in test_gpu_parity: thresholds bit-exact (great-circle
+ones as parity_util states), beta within 1e-10 of each column's scale,
+criteria within 1e-9 relative."""
 import numpy as np
 import pytest
 
 import oracle as O
 from libgwmodel_gb300 import Engine, Precision
+from parity_util import check_geo_thresholds, geo_rows
 
 pytestmark = pytest.mark.gpu
 
@@ -54,7 +56,7 @@ def test_widest_x_takes_several_contraction_launches():
 
 
 @pytest.mark.parametrize("bw", [25, 180.5])
-def test_antimeridian_and_high_latitude(bw):
+def test_antimeridian_and_high_latitude(bw, gc_host):
     """Longitudes on both sides of +-180 and latitudes up to 89.9 degrees."""
     rng = np.random.default_rng(42)
     n = 700
@@ -63,8 +65,7 @@ def test_antimeridian_and_high_latitude(bw):
     lat = rng.uniform(60, 89.9, n)
     x, y, c = problem(n, 4, np.column_stack([lon, lat]), 43)
     e, pb = check_against_oracle(x, y, c, True, bw, True, O.BISQUARE)
-    want = np.array([O.adaptive_threshold(pb.distance_row(i), bw) for i in range(n)])
-    assert np.array_equal(e.thresholds(bw), want)
+    check_geo_thresholds(e.thresholds(bw), *geo_rows(c, range(n), gc_host), bw)
     # the mixed path on the same data: within its tolerance of FP64
     e.set_precision(Precision.Mixed)
     got = e.criterion(bw, True, O.BISQUARE, O.AIC)

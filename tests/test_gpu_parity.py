@@ -3,25 +3,20 @@
 Tolerances (FP64 drop-in): adaptive thresholds and the selected bandwidth
 bit-exact; beta relative error <= 1e-10 (against the column's largest
 |beta|); AICc and CV within 1e-9 relative; tr(S), tr(S^T S), qDiag, S and
-betasSE within 1e-9 relative."""
+betasSE within 1e-9 relative.
+
+Geographic thresholds: see parity_util (bit-exact to the engine's correctly
+rounded distances, libm's within the stated bar, identical neighbour sets)."""
 import numpy as np
 import pytest
 
 import oracle as O
+from parity_util import GEO_THR_ULP, check_geo_thresholds, col_rel, geo_rows as rows_of, rel, ulps
 from libgwmodel_gb300 import BandwidthWeight, CRSDistance, Engine, GWRBasic, SpatialWeight, datasets
 
 pytestmark = pytest.mark.gpu
 
 KERNELS = [O.GAUSSIAN, O.EXPONENTIAL, O.BISQUARE, O.TRICUBE, O.BOXCAR]
-
-
-def rel(a, b):
-    a, b = np.asarray(a), np.asarray(b)
-    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
-
-
-def col_rel(a, b):
-    return max(rel(a[:, k], b[:, k]) for k in range(b.shape[1]))
 
 
 @pytest.fixture(scope="module")
@@ -31,7 +26,13 @@ def planar():
 
 @pytest.fixture(scope="module")
 def geo():
-    return datasets.config2(n=700, seed=12, k=4)
+    return datasets.config2(n=2000, seed=12, k=16)
+
+
+@pytest.fixture(scope="module")
+def geo_rows(geo, gc_host):
+    """Distance rows of `geo`: (libm oracle, engine arithmetic on the host)."""
+    return rows_of(geo.coords, range(geo.n), gc_host)
 
 
 @pytest.fixture(scope="module")
@@ -64,13 +65,10 @@ def test_adaptive_thresholds_bit_exact_planar(planar, bw):
     assert np.array_equal(got, want), np.flatnonzero(got != want)[:10]
 
 
-@pytest.mark.parametrize("bw", [20, 141, 350.5, 699])
-def test_adaptive_thresholds_bit_exact_geographic(geo, bw):
+@pytest.mark.parametrize("bw", [20, 141, 350.5, 1351, 1999])
+def test_adaptive_thresholds_geographic(geo, geo_rows, bw):
     e = engine_for(geo.x, geo.y, geo.coords, True)
-    pb = O.Problem(geo.x, geo.y, geo.coords, geographic=True, gc_mode=O.GC_PORTABLE)
-    got = e.thresholds(bw)
-    want = oracle_thresholds(pb, bw)
-    assert np.array_equal(got, want), np.flatnonzero(got != want)[:10]
+    check_geo_thresholds(e.thresholds(bw), *geo_rows, bw)
 
 
 @pytest.mark.parametrize("bw", [5, 33, 200, 450.5])
@@ -81,11 +79,13 @@ def test_adaptive_thresholds_with_ties(ties, bw):
     assert np.array_equal(e.thresholds(bw), oracle_thresholds(pb, bw))
 
 
-def test_max_distance(planar, geo):
+def test_max_distance(planar, geo, geo_rows):
     e = engine_for(planar.x, planar.y, planar.coords)
     assert e.max_distance() == O.Problem(planar.x, planar.y, planar.coords).max_distance()
     g = engine_for(geo.x, geo.y, geo.coords, True)
-    assert g.max_distance() == O.Problem(geo.x, geo.y, geo.coords, geographic=True).max_distance()
+    got = g.max_distance()
+    assert got == max(d.max() for d in geo_rows[1])
+    assert ulps(got, O.Problem(geo.x, geo.y, geo.coords, geographic=True).max_distance()) <= GEO_THR_ULP
 
 
 @pytest.mark.parametrize("kernel", KERNELS)
@@ -191,17 +191,20 @@ def test_not_spd_is_dbl_max():
         e.fit(50, True, O.BISQUARE, True)
 
 
-def test_thresholds_reuse_cached_histograms(planar, geo):
+def test_thresholds_reuse_cached_histograms(planar, geo, geo_rows):
     """Many bandwidths on one engine: later selects start from the cached
     per-row histograms and must stay bit-exact."""
-    for pbm, geographic in ((planar, False), (geo, True)):
-        e = engine_for(pbm.x, pbm.y, pbm.coords, geographic)
-        pb = O.Problem(pbm.x, pbm.y, pbm.coords, geographic=geographic)
-        dists = [pb.distance_row(i) for i in range(pb.n)]
-        for bw in (pb.n // 2, 25, pb.n // 5, 120.5, pb.n - 1, 64, pb.n + 10):
-            got = e.thresholds(bw)
-            want = np.array([O.adaptive_threshold(d, bw) for d in dists])
-            assert np.array_equal(got, want), (geographic, bw, np.flatnonzero(got != want)[:5])
+    e = engine_for(planar.x, planar.y, planar.coords)
+    pb = O.Problem(planar.x, planar.y, planar.coords)
+    dists = [pb.distance_row(i) for i in range(pb.n)]
+    for bw in (pb.n // 2, 25, pb.n // 5, 120.5, pb.n - 1, 64, pb.n + 10):
+        got = e.thresholds(bw)
+        want = np.array([O.adaptive_threshold(d, bw) for d in dists])
+        assert np.array_equal(got, want), (bw, np.flatnonzero(got != want)[:5])
+    g = engine_for(geo.x, geo.y, geo.coords, True)
+    n = geo.n
+    for bw in (n // 2, 25, n // 5, 120.5, n - 1, 64, n + 10):
+        check_geo_thresholds(g.thresholds(bw), *geo_rows, bw)
 
 
 def test_mixed_thresholds_close_to_exact(geo):

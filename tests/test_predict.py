@@ -52,7 +52,7 @@ def test_engine_predict_matches_oracle(name, geo, adaptive, kernel, bw):
     from libgwmodel_gb300 import Engine
     pb = problem(1500, 5, geo, 3)
     loc = locations(pb, 400, 4)
-    prob = O.Problem(pb.x, pb.y, pb.coords, geographic=geo, gc_mode=O.GC_PORTABLE)
+    prob = O.Problem(pb.x, pb.y, pb.coords, geographic=geo)
     want = prob.predict(loc, bw, adaptive, kernel)
     e = Engine(0)
     e.set_data(pb.x, pb.y, pb.coords, geo)
