@@ -296,8 +296,8 @@ int gwgpu_engine_tc_selftest(gwgpu_engine* e, int N, const float* A, const float
 /* Criterion of one bandwidth from normal equations the caller already holds
  * on the device, without allocating any device memory.  No counterpart in
  * libgwmodel.  For callers that cannot let a library call cudaMalloc: code
- * that owns all device memory through its own pool, must not allocate after
- * start-up, or is about to be recorded into a CUDA graph.
+ * that owns all device memory through its own pool, or must not allocate
+ * after start-up (cudaMalloc and cudaFree synchronise the whole device).
  *
  * Inputs (device pointers): G, n x (p(p+1)/2 + p) row-major -- per location
  * the upper triangle of X^T W_i X packed by rows, then X^T W_i y (for CV with

@@ -1,9 +1,9 @@
 // noalloc.cu -- a criterion entry point that never allocates device memory.
 //
 // Some callers cannot let a library call cudaMalloc: an application that owns
-// all device memory through its own pool or budget, a process that must not
-// allocate after start-up (real-time serving), or code that is about to be
-// recorded into a CUDA graph, where an allocation would break the capture.
+// all device memory through its own pool or budget, or a process that must not
+// allocate after start-up (real-time serving, where cudaMalloc and cudaFree
+// synchronise the device and stall every stream).
 // gwgpu_criterion_noalloc serves them: the caller passes every input and
 // output as device pointers, and the only scratch -- per-row hat diagonals and
 // residuals and the per-block partial sums of the warp-per-location solve --
@@ -33,7 +33,7 @@ void set_last_error(const char* msg);
 namespace {
 
 constexpr int kNoAllocMaxRows = 65536;    // largest n accepted
-constexpr int kNoAllocMaxBlocks = 4096;   // launch_solve uses at most this many blocks
+constexpr int kNoAllocMaxBlocks = gwgpu::kSolveMaxBlocks;  // the largest grid launch_solve uses
 constexpr int kNoAllocMaxDevices = 64;
 
 struct NoAllocScratch {
@@ -41,6 +41,8 @@ struct NoAllocScratch {
     double resid[kNoAllocMaxRows];
     double partials[kNoAllocMaxBlocks * 4];
 };
+static_assert(sizeof(NoAllocScratch::partials) >= sizeof(double) * 4 * gwgpu::kSolveMaxBlocks,
+              "the partial sums must hold every block launch_solve can use");
 
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 
@@ -117,9 +119,8 @@ extern "C" int gwgpu_criterion_noalloc(int n, int p, int criterion, int kernel, 
     a.partials = reinterpret_cast<double*>(b + offsetof(NoAllocScratch, partials));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     int nblocks = 0;
-    rc = gwgpu::launch_solve(a, &nblocks, s);
+    rc = gwgpu::launch_solve(a, &nblocks, s);  // at most kSolveMaxBlocks blocks (static_assert above)
     if (rc != cudaSuccess) return fail(GWGPU_ERR_CUDA, cudaGetErrorString(rc));
-    if (nblocks > kNoAllocMaxBlocks) return fail(GWGPU_ERR_INVALID, "gwgpu_criterion_noalloc: too many blocks");
     rc = gwgpu::launch_reduce_partials(a.partials, nblocks, sums, s);
     if (rc != cudaSuccess) return fail(GWGPU_ERR_CUDA, cudaGetErrorString(rc));
     k_noalloc_value<<<1, 32, 0, s>>>(n, criterion, sums);
