@@ -58,21 +58,15 @@ def _compile(src: str, force: bool, headers, extra) -> str:
     return obj
 
 
-def cuda_lib() -> str:
-    """The toolkit's library folder (libcublas.so lives there)."""
-    return os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))), "lib64")
-
-
 def build(force: bool = False, verbose: bool = False, extra=None) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    CUDA_LIB = cuda_lib()
     headers = _headers()
     extra = list(extra or [])
     with cf.ThreadPoolExecutor(max_workers=min(len(SOURCES), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, force, headers, extra), SOURCES))
     if force or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
         tmp = LIB + f".tmp{os.getpid()}"
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread", "-lcublas", "-Xlinker", "-rpath=" + CUDA_LIB]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

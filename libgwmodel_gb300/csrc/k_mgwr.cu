@@ -69,7 +69,8 @@ __global__ void __launch_bounds__(HA_THREADS)
         for (int q = 0; q < iend; q++) {
             double d;
             if constexpr (GEO)
-                d = gw_gc_dist(du, su[q], dv, sv[q], duR, suR[q], dvR, svR[q]);
+                d = kernel == GW_KERNEL_BOXCAR ? gw_gc_dist(du, su[q], dv, sv[q], duR, suR[q], dvR, svR[q])
+                                               : gw_gc_dist_fast(du, su[q], dv, sv[q], duR, suR[q], dvR, svR[q]);
             else
                 d = gw_planar_dist(du, dv, su[q], sv[q]);
             const double w = gw_kernel_weight(kernel, d, sr[q]);
@@ -91,7 +92,8 @@ __global__ void __launch_bounds__(HA_THREADS)
 // rows of this CTA and HU_COLS columns from c0: the variable's hat matrix
 // S(i, j) = w_ij v_i x_j (v_i = x_i / sum_j w_ij x_j^2) applied to T + I, over
 // the data tiles that can hold a neighbour of a row of the CTA (compact
-// kernels only).  The weight tile is computed in shared memory, the T tile is
+// kernels; gaussian and exponential weights visit every tile: the dense
+// product).  The weight tile is computed in shared memory, the T tile is
 // staged with the identity and the x_j scale folded in, and each thread
 // accumulates 4 rows x HU_NC columns in FP64.
 constexpr int HU_THREADS = 256;
@@ -138,7 +140,8 @@ __global__ void __launch_bounds__(HU_THREADS)
         for (int q = 1; q < HU_THREADS / 32; q++) rmax = fmax(rmax, sred[q]);
     }
     const float4 fbound = sbound;
-    const float far_thr = tb_far_threshold<GEO>(rmax);
+    // compact kernels skip the tiles beyond every row's bandwidth; gaussian and exponential weights never vanish
+    const float far_thr = kernel >= GW_KERNEL_BISQUARE ? tb_far_threshold<GEO>(rmax) : -1.0f;
 
     double acc[4][HU_NC];
 #pragma unroll
@@ -175,7 +178,8 @@ __global__ void __launch_bounds__(HU_THREADS)
                 if (j < n && row0 + r < n) {
                     double d;
                     if constexpr (GEO)
-                        d = gw_gc_dist(du, sfu[r], dv, sfv[r], duR, sfuR[r], dvR, sfvR[r]);
+                        d = kernel == GW_KERNEL_BOXCAR ? gw_gc_dist(du, sfu[r], dv, sfv[r], duR, sfuR[r], dvR, sfvR[r])
+                                                       : gw_gc_dist_fast(du, sfu[r], dv, sfv[r], duR, sfuR[r], dvR, sfvR[r]);
                     else
                         d = gw_planar_dist(du, dv, sfu[r], sfv[r]);
                     w = gw_kernel_weight(kernel, d, sthr[r]);
@@ -297,7 +301,6 @@ cudaError_t launch_mgwr_hat_update(const DevPoints& P, bool geographic, const fl
                                    const double* v, const double* thr, double bw, int kernel, const double* T,
                                    double* SA, cudaStream_t stream)
 {
-    if (kernel < GW_KERNEL_BISQUARE) return cudaErrorInvalidValue;  // compact kernels only
     dim3 grid((P.n + HU_BM - 1) / HU_BM, (P.n + HU_COLS - 1) / HU_COLS);
     if (geographic)
         k_mgwr_hat_update<true><<<grid, HU_THREADS, 0, stream>>>(P, tb16, X, v, thr, bw, kernel, T, SA);

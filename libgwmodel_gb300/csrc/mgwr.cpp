@@ -9,15 +9,13 @@
 //
 // Hat matrix (GWRMultiscale.cpp:216-224, 296-301): S0, SA_k (k < p) and the
 // scratch T = SA_k - S0 are n x n FP64 matrices resident on the device in the
-// sorted order.  The update SA_k = S T + S = S (T + I) takes, for a compact
-// kernel (bisquare, tricube, boxcar), one fused kernel that forms S's entries
-// w_ij v_i x_j on the fly and visits only the rows of T within the variable's
-// bandwidth (2 n k n flops instead of 2 n^3); for gaussian and exponential
-// kernels S is materialised (one more n x n matrix) and the product is a
-// DGEMM (cuBLAS).  tr(S0) and tr(S0^T S0) are reduced on the device at the end.
+// sorted order.  The update SA_k = S T + S = S (T + I) is one fused kernel that
+// forms S's entries w_ij v_i x_j on the fly (S is never stored): for a compact
+// kernel (bisquare, tricube, boxcar) it visits only the rows of T within the
+// variable's bandwidth (2 n k n flops instead of 2 n^3); gaussian and
+// exponential kernels visit every row (the dense 2 n^3 product).  tr(S0) and
+// tr(S0^T S0) are reduced on the device at the end.
 #include "../../include/gwmodel_gb300/GWRMultiscale.h"
-
-#include <cublas_v2.h>
 
 #include <algorithm>
 #include <chrono>
@@ -33,12 +31,6 @@ namespace gwm {
 
 namespace {
 const char* kFile = "mgwr.cpp";
-
-void cublas_check(cublasStatus_t s, const char* what)
-{
-    if (s != CUBLAS_STATUS_SUCCESS)
-        throw gwgpu::CudaError(std::string(what) + ": cuBLAS status " + std::to_string((int)s));
-}
 
 double now_s()
 {
@@ -57,17 +49,11 @@ struct GWRMultiscale::Impl {
     std::unique_ptr<gwgpu::Engine> engine;
     int device = -1;
     // hat-matrix state
-    gwgpu::DevBuf<double> S0, SA, S, T, ainv, partials, sums;
-    cublasHandle_t blas = nullptr;
-    ~Impl()
-    {
-        if (blas) cublasDestroy(blas);
-    }
+    gwgpu::DevBuf<double> S0, SA, T, ainv, partials, sums;
     void releaseHat()
     {
         S0.release();
         SA.release();
-        S.release();
         T.release();
         ainv.release();
     }
@@ -288,29 +274,21 @@ mat GWRMultiscale::fit()
     Impl& I = *mImpl;
     const std::size_t nn = n * n;
     if (mHasHatMatrix) {
-        bool dense = false;  // a variable with a gaussian or exponential kernel needs S materialised
-        for (const auto& sw : mSpatialWeights) dense = dense || (int)sw.weight()->kernel() < (int)BandwidthWeight::Bisquare;
-        const double need = 8.0 * (double)nn * (double)(p + 2 + (dense ? 1 : 0)) + 8.0 * (double)n * p * p;
+        const double need = 8.0 * (double)nn * (double)(p + 2) + 8.0 * (double)n * p * p;
         size_t freeb = 0, total = 0;
         gwgpu::check(cudaMemGetInfo(&freeb, &total), "cudaMemGetInfo");
-        const double held = (double)(I.S0.capacityBytes() + I.SA.capacityBytes() + I.S.capacityBytes() +
-                                     I.T.capacityBytes() + I.ainv.capacityBytes());
+        const double held = (double)(I.S0.capacityBytes() + I.SA.capacityBytes() + I.T.capacityBytes() +
+                                     I.ainv.capacityBytes());
         if (need > (double)freeb + held)
             throw std::runtime_error("the hat matrix needs " + std::to_string(need / 1e9) +
-                                     " GB of device memory ((p + 3) n x n doubles); disable it with "
+                                     " GB of device memory ((p + 2) n x n doubles); disable it with "
                                      "setHasHatMatrix(false)");
         I.S0.alloc(nn);
         I.SA.alloc(nn * p);
-        if (dense)
-            I.S.alloc(nn);
-        else
-            I.S.clear();
         I.T.alloc(nn);
         I.ainv.alloc(n * p * p);
         I.partials.alloc(4096 * 4);
         I.sums.alloc(4);
-        if (!I.blas) cublas_check(cublasCreate(&I.blas), "cublasCreate");
-        cublas_check(cublasSetStream(I.blas, eng.stream()), "cublasSetStream");
     }
 
     // backfitting (:192-317)
@@ -352,7 +330,6 @@ mat GWRMultiscale::fit()
     fitted_resid(resid);
     double RSS0 = 0.0, RSS1 = DBL_MAX, criterion = DBL_MAX;
     for (std::size_t i = 0; i < n; i++) RSS0 += resid(i) * resid(i);
-    const double one = 1.0, zero = 0.0;
     for (std::size_t iteration = 1; iteration <= mMaxIteration && criterion > mCriterionThreshold; iteration++) {
         if (mTelegram->stop()) {
             mStatus = Status::Terminated;
@@ -398,10 +375,8 @@ mat GWRMultiscale::fit()
             if (mStatus != Status::Success) break;
 
             const BandwidthWeight& wk = *mSpatialWeights[k].weight();
-            const bool compact = (int)wk.kernel() >= (int)BandwidthWeight::Bisquare;
             double t0 = now_s();
-            eng.fitDevice(wk.bandwidth(), wk.adaptive(), (int)wk.kernel(), false,
-                          (mHasHatMatrix && !compact) ? I.S.get() : nullptr, nullptr);
+            eng.fitDevice(wk.bandwidth(), wk.adaptive(), (int)wk.kernel(), false, nullptr, nullptr);
             std::vector<double> b;
             eng.betas(b);
             for (std::size_t i = 0; i < n; i++) betas(i, k) = b[i];
@@ -411,18 +386,9 @@ mat GWRMultiscale::fit()
                 t0 = now_s();
                 double* SAk = I.SA.get() + k * nn;
                 gwgpu::check(gwgpu::launch_mgwr_sub(nn, SAk, I.S0.get(), I.T.get(), eng.stream()), "hat: T");
-                if (compact) {
-                    eng.hatUpdate(wk.bandwidth(), wk.adaptive(), (int)wk.kernel(), I.T.get(), SAk);
-                    gwgpu::check(gwgpu::launch_mgwr_post(nn, SAk, nullptr, I.T.get(), I.S0.get(), eng.stream()),
-                                 "hat: S0");
-                } else {
-                    // row-major SA_k = S T  <=>  column-major SA_k^T = T^T S^T
-                    cublas_check(cublasDgemm(I.blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, (int)n, (int)n, &one,
-                                             I.T.get(), (int)n, I.S.get(), (int)n, &zero, SAk, (int)n),
-                                 "hat: S T");
-                    gwgpu::check(gwgpu::launch_mgwr_post(nn, SAk, I.S.get(), I.T.get(), I.S0.get(), eng.stream()),
-                                 "hat: S0");
-                }
+                eng.hatUpdate(wk.bandwidth(), wk.adaptive(), (int)wk.kernel(), I.T.get(), SAk);
+                gwgpu::check(gwgpu::launch_mgwr_post(nn, SAk, nullptr, I.T.get(), I.S0.get(), eng.stream()),
+                             "hat: S0");
                 eng.synchronize();
                 mCounters.hatUpdates++;
                 mCounters.hatSeconds += now_s() - t0;
