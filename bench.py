@@ -12,6 +12,12 @@ public GWRBasic C ABI from host buffers (the upload of coordinates, X, y and
 the download of the outputs inside the timed region).  The unit is local
 fits/s = n x (criterion evaluations + 1) / seconds.
 
+The same line carries, measured in the same run: one step of the FP64
+drop-in on the same data (``fp64``, ``speedup_vs_fp64``) and the mixed path's
+errors against it; the config-4 serving stream at 5, 50 and 200 requests/s in
+both forms (``serve``); the config-3 batched evaluation (``batch``); the CPU
+baseline (the oracle on a bounded sample of rows).
+
     python bench.py [--steps K] [--warmup W] [--precision mixed|fp64] [--impl reference]
 """
 from __future__ import annotations
@@ -45,7 +51,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
-    ap.add_argument("--no-serve", action="store_true", help="skip the short serving run of the main line")
+    ap.add_argument("--no-serve", action="store_true", help="skip the config-4 serving block of the main line")
+    ap.add_argument("--no-batch", action="store_true", help="skip the config-3 batch block of the main line")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the live FP64 drop-in step of the main line")
     ap.add_argument("--serve", action="store_true", help="config-4 serving sweep instead of the config-2 line")
     ap.add_argument("--batch", action="store_true", help="config-3 batched evaluation instead of the config-2 line")
     ap.add_argument("--no-autotune", action="store_true")
@@ -54,10 +62,11 @@ def parse():
     ap.add_argument("--mgwr-n", type=int, default=20000)
     ap.add_argument("--mgwr-hat-n", type=int, default=4000)
     ap.add_argument("--mgwr-iterations", type=int, default=10)
-    ap.add_argument("--rates", default="5,20,50,200")
-    ap.add_argument("--requests", type=int, default=60)
+    ap.add_argument("--rates", default="5,50,200")
+    ap.add_argument("--requests", type=int, default=200, help="requests per rate (mixed form)")
+    ap.add_argument("--requests-fp64", type=int, default=100, help="requests per rate (FP64 form)")
     ap.add_argument("--slots", type=int, default=8)
-    ap.add_argument("--precision-serve", choices=["mixed", "fp64", "both"], default="mixed")
+    ap.add_argument("--precision-serve", choices=["mixed", "fp64", "both"], default="both")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     return ap.parse_args()
 
@@ -135,17 +144,6 @@ def ncu_traffic(name):
     return float(m.group(1)) if m else None
 
 
-def fp64_search_ms():
-    """FP64 drop-in time per step of this workload from the committed measurement
-    (profiles/fp64_config2.md); the FP64 search takes minutes, so it is not rerun."""
-    path = os.path.join(ROOT, "profiles", "fp64_config2.md")
-    if not os.path.exists(path):
-        return None
-    with open(path) as f:
-        m = re.search(r"fp64_ms_per_step:\s*([0-9.eE+]+)", f.read())
-    return float(m.group(1)) if m else None
-
-
 def rel_err(a, b):
     """Largest absolute difference over the largest magnitude, per column."""
     a = np.asarray(a, dtype=np.float64)
@@ -155,21 +153,59 @@ def rel_err(a, b):
     return max(float(np.abs(a[:, k] - b[:, k]).max() / max(np.abs(b[:, k]).max(), 1e-300)) for k in range(a.shape[1]))
 
 
-def accuracy_vs_fp64(engine, pb, bw, local):
-    """Errors of the mixed path against the FP64 path at the selected bandwidth:
-    beta, betasSE, tr(S), tr(S^T S), qDiag and the AICc value."""
-    from libgwmodel_gb300 import Engine, Precision
-    e64 = Engine(local)
-    e64.set_data(pb.x, pb.y, pb.coords, pb.geographic)
-    e64.set_precision(Precision.FP64)
-    b64, se64, sh64, q64, _ = e64.fit(bw, True, pb.kernel, store_s=False)
+def elem_rel(a, b, floor=1e-3):
+    """Per-element relative error |a - b| / |b| over the elements of each column
+    with |b| >= floor x the column's largest |b|: quantiles and maximum."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    if a.ndim == 1:
+        a, b = a[:, None], b[:, None]
+    r = []
+    for k in range(b.shape[1]):
+        m = np.abs(b[:, k]) >= floor * np.abs(b[:, k]).max()
+        r.append(np.abs(a[m, k] - b[m, k]) / np.abs(b[m, k]))
+    r = np.concatenate(r)
+    return {"p50": float(np.quantile(r, 0.5)), "p99": float(np.quantile(r, 0.99)),
+            "p999": float(np.quantile(r, 0.999)), "max": float(r.max()), "elements": int(r.size),
+            "floor": floor}
+
+
+def accuracy_vs_fp64(engine, e64, pb, bw, out64):
+    """Errors of the mixed path against the FP64 drop-in at the FP64 search's
+    bandwidth: beta, betasSE, tr(S), tr(S^T S), qDiag and the AICc value."""
+    b64, se64, sh64, q64, _ = out64
     c64 = e64.criterion(bw, True, pb.kernel, 0)
     bmx, semx, shmx, qmx, _ = engine.fit(bw, True, pb.kernel, store_s=False)
     cmx = engine.criterion(bw, True, pb.kernel, 0)
     return {"bandwidth": bw, "beta_rel": rel_err(bmx, b64), "betasSE_rel": rel_err(semx, se64),
             "trS_rel": abs(shmx[0] - sh64[0]) / abs(sh64[0]), "trStS_rel": abs(shmx[1] - sh64[1]) / abs(sh64[1]),
             "qdiag_rel": rel_err(qmx, q64), "aicc_rel": abs(cmx - c64) / abs(c64), "beta_tolerance": 1e-6,
-            "note": "max |mixed - fp64| / max |fp64| per column; same bandwidth, FP64 drop-in as the reference"}
+            "beta_elementwise": elem_rel(bmx, b64), "betasSE_elementwise": elem_rel(semx, se64),
+            "note": "*_rel: max |mixed - fp64| / max |fp64| per column; *_elementwise: |mixed - fp64| / |fp64| "
+                    "per element with |fp64| >= 1e-3 of its column's largest; same bandwidth (the FP64 "
+                    "search's), FP64 drop-in as the reference"}
+
+
+def fp64_step(pb, local):
+    """One step of the FP64 drop-in on the same workload (golden search + fit),
+    timed with CUDA events on its engine's stream, clocks sampled."""
+    from libgwmodel_gb300 import Engine, Precision
+    e64 = Engine(local)
+    e64.set_data(pb.x, pb.y, pb.coords, pb.geographic)
+    e64.set_precision(Precision.FP64)
+    e64.enable_stats(True)
+    clocks = Clocks(local)
+    clocks.start()
+    e64.record_event(0)
+    bw, crit, out = one_fit(e64, pb)
+    e64.record_event(1)
+    ms = e64.elapsed_ms(0, 1)
+    clk = clocks.stop()
+    st = e64.stats()
+    info = {"ms_per_step": ms, "selected_bandwidth": bw, "criterion_evals": st["criterion_evals"],
+            "contract_ms": st["contract_ms"], "select_ms": st["select_ms"], "clocks": clk,
+            "timing": "one step, CUDA events on the FP64 engine's stream (data resident)"}
+    return info, e64, out
 
 
 def serve_stream(rate, count, precision, slots=8, budget_gb=150.0, seed=4):
@@ -198,6 +234,58 @@ def serve_stream(rate, count, precision, slots=8, budget_gb=150.0, seed=4):
             "wall_s": wall, "requests_per_s": len(ok) / wall, "local_fits_per_s": fits / wall,
             "max_concurrent": st["max_concurrent"], "peak_reserved_gb": st["peak_reserved_bytes"] / 1e9,
             "warmup_requests": int(warm["completed"])}
+
+
+def serve_block(rates, requests, precisions):
+    """Config 4 inside the main line: the request stream at each rate, per form."""
+    from libgwmodel_gb300 import Precision
+    out = {}
+    for pr in precisions:
+        prec = Precision.Mixed if pr == "mixed" else Precision.FP64
+        out[pr] = [serve_stream(r, requests[pr], prec) for r in rates]
+    return out
+
+
+def batch_block(precision, steps, warmup, autotune=True):
+    """Config 3 inside the main line: evaluations/s of the batched launch and its
+    largest relative difference against the one-problem-at-a-time engine."""
+    from libgwmodel_gb300 import Engine, Precision, datasets
+    from libgwmodel_gb300.batch import Batch
+    prec = Precision.Mixed if precision == "mixed" else Precision.FP64
+    pbs, cands = datasets.config3()
+    b = Batch(pbs, precision=prec)
+    b.set_candidates(cands, adaptive=True, kernel=2, criterion=0)
+    t0 = time.perf_counter()
+    if autotune:
+        b.autotune(repeats=2)
+    tune_s = time.perf_counter() - t0
+    for _ in range(warmup):
+        b.evaluate(use_graph=True)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        vals = b.evaluate(use_graph=True)  # replays the graph and reads the values back
+    dt = (time.perf_counter() - t0) / steps
+    info = b.info()
+    seq = []
+    for pb, cs in zip(pbs, cands):
+        e = Engine(0)
+        e.set_data(pb.x, pb.y, pb.coords, pb.geographic)
+        e.set_precision(prec)
+        e.criterion(cs[0], True, 2, 0)
+        seq.append((e, cs))
+    t0 = time.perf_counter()
+    ref = [np.array([e.criterion(bw, True, 2, 0) for bw in cs]) for e, cs in seq]
+    seq_s = time.perf_counter() - t0
+    err = max(float(np.max(np.abs(v - r) / np.abs(r))) for v, r in zip(vals, ref))
+    return {"evaluations_per_s": info["segments"] / dt, "ms_per_step": dt * 1e3, "evaluations": info["segments"],
+            "local_fits_per_s": info["rows_total"] / dt, "precision": precision, "graph": info["graph"],
+            "launches_per_step": info["launches_per_evaluate"], "autotune_s": tune_s,
+            "schedule": {k: info[k] for k in ("flush_tiles", "order", "solve_rows", "select_ctas", "tuned")},
+            "sequential_ms": seq_s * 1e3, "speedup_vs_sequential": seq_s / dt, "max_rel_diff_vs_sequential": err,
+            "workload": "config3: 64 problems, n log-uniform [500, 20000], p in 3..12, 5 Gaussian clusters, "
+                        "32 adaptive bisquare candidates each, AICc; one evaluation of every (problem, candidate) "
+                        "per step under a captured CUDA graph",
+            "timing": "host wall clock around evaluate(), which replays the graph and copies the values back"}
 
 
 def run_batch(args):
@@ -427,7 +515,8 @@ def run_serve(args):
     rates = [float(r) for r in args.rates.split(",")]
     for pr in precs:
         prec = Precision.Mixed if pr == "mixed" else Precision.FP64
-        rows = [serve_stream(r, args.requests, prec, slots=args.slots) for r in rates]
+        count = args.requests if pr == "mixed" else args.requests_fp64
+        rows = [serve_stream(r, count, prec, slots=args.slots) for r in rates]
         line = {"metric": "GWR serving latency, config-4 request stream (70% fits, 30% AICc searches)",
                 "value": rows[0]["p99_ms"], "unit": "ms (p99, first rate)", "higher_is_better": False,
                 "n_gpus": 1, "precision": pr, "slots": args.slots, "hbm_budget_gb": 150.0,
@@ -486,7 +575,7 @@ def cpu_baseline(pb, seconds, threads=None):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     threads = threads or os.cpu_count() or 1
-    prob = O.Problem(pb.x, pb.y, pb.coords, geographic=pb.geographic, gc_mode=O.GC_LIBM, threads=threads)
+    prob = O.Problem(pb.x, pb.y, pb.coords, geographic=pb.geographic, threads=threads)
     bw = float(np.floor(20 + (np.sqrt(5) - 1) / 2 * (pb.n - 20)))
     rows = threads
     t0 = time.perf_counter()
@@ -613,16 +702,28 @@ def run_ours(args):
         line["e2e"] = e2e
     if clk:
         line["clocks"] = clk
-    if prec == Precision.Mixed and rank == 0 and not args.no_accuracy:
-        line["accuracy_vs_fp64"] = accuracy_vs_fp64(engine, pb, bw, local)
-        f64 = fp64_search_ms() if args.n == 200000 else None
-        if f64:
-            line["fp64_ms_per_step"] = f64
-            line["speedup_vs_fp64"] = f64 / (ms / args.steps)
+    if prec == Precision.Mixed and rank == 0 and not args.no_fp64:
+        # the FP64 drop-in on the same workload, measured in this run: the >= 5x target's denominator
+        engine.release_distance_cache()
+        f64, e64, out64 = fp64_step(pb, local)
+        line["fp64"] = f64
+        line["fp64_ms_per_step"] = f64["ms_per_step"]
+        line["speedup_vs_fp64"] = f64["ms_per_step"] / (ms / args.steps)
+        line["same_bandwidth_as_fp64"] = f64["selected_bandwidth"] == bw
+        if not args.no_accuracy:
+            line["accuracy_vs_fp64"] = accuracy_vs_fp64(engine, e64, pb, f64["selected_bandwidth"], out64)
+        e64 = out64 = None
     engine.release_distance_cache()
-    if rank == 0 and not args.no_serve and args.n == 200000:
-        from libgwmodel_gb300 import Precision as _P
-        line["serve"] = serve_stream(20.0, 48, _P.Mixed)
+    engine = None
+    if rank == 0 and not args.no_serve:
+        rates = [float(r) for r in args.rates.split(",")]
+        line["serve"] = serve_block(rates, {"mixed": args.requests, "fp64": args.requests_fp64},
+                                    ["mixed", "fp64"] if args.precision_serve == "both" else [args.precision_serve])
+        line["serve"]["note"] = ("config 4: Poisson arrivals, 70% fits at a given adaptive bandwidth / 30% AICc "
+                                 "searches, n log-uniform [1e3, 1e5], p 3..20, planar/geographic 50/50, 150 GB "
+                                 "budget, 8 slots; latency = submit to result")
+    if rank == 0 and not args.no_batch:
+        line["batch"] = batch_block("mixed", steps=5, warmup=2)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(pb, args.cpu_seconds)
     if rank == 0:
