@@ -1,13 +1,13 @@
 """Generate tests/golden/londonhp100.json from the reference's own test fixture.
 
-Reads the reference checkout (argument 1, default /root/reference) -- the
-londonhp100 coordinates and data that test/testGWRBasic.cpp loads through
+Reads the reference checkout (argument 1, or the GWMODEL_REFERENCE environment
+variable) -- the londonhp100 coordinates and data that test/testGWRBasic.cpp loads through
 test/data/londonhp100.cpp:6-26 -- and records the known answers that
 test/testGWRBasic.cpp asserts (absolute tolerance 1e-8), with the line each
 comes from.  The GPU machine has no reference checkout, so the tests read this
 JSON instead.
 
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py /path/to/libgwmodel
 """
 import csv
 import json
@@ -23,7 +23,10 @@ def read_csv(path, fields):
     return [[float(r[k]) for k in fields] for r in rows]
 
 
-def main(ref="/root/reference"):
+def main(ref=None):
+    ref = ref or os.environ.get("GWMODEL_REFERENCE")
+    if not ref:
+        sys.exit("usage: make_golden.py /path/to/libgwmodel (or set GWMODEL_REFERENCE)")
     data_dir = os.path.join(ref, "test", "data")
     coords = read_csv(os.path.join(data_dir, "londonhp100coords.csv"), ["x", "y"])
     data = read_csv(os.path.join(data_dir, "londonhp100data.csv"),
