@@ -239,6 +239,12 @@ int gwgpu_engine_set_precision(gwgpu_engine* e, int precision);
 /* Mixed path: 32-point data tiles summed in FP32 on the tensor core before
    each double-float drain (default 64, at least 2). */
 int gwgpu_engine_set_flush_tiles(gwgpu_engine* e, int tiles);
+/* Mixed path: polls of each pipeline wait of the tensor-core contraction before
+   it times out (0 = the default, about two seconds).  A timeout makes the
+   kernel wait for its own MMAs and copies, free its tensor memory and report;
+   the call then fails with GWGPU_ERR_CUDA and the engine stays usable.  Small
+   values are for testing that path (no counterpart in libgwmodel). */
+int gwgpu_engine_set_tc_wait_limit(gwgpu_engine* e, unsigned polls);
 /* Mixed path: FP64 refinement steps of the final fit (default 1), and
    whether each AICc criterion of the search is refined too (default 0). */
 int gwgpu_engine_set_refinement(gwgpu_engine* e, int steps, int refine_search);

@@ -160,6 +160,7 @@ SIGNATURES = [
     ("gwgpu_engine_set_data", _i, [_vp, _i, _i, _dp, _dp, _dp, _i]),
     ("gwgpu_engine_set_precision", _i, [_vp, _i]),
     ("gwgpu_engine_set_flush_tiles", _i, [_vp, _i]),
+    ("gwgpu_engine_set_tc_wait_limit", _i, [_vp, ctypes.c_uint]),
     ("gwgpu_engine_set_refinement", _i, [_vp, _i, _i]),
     ("gwgpu_engine_criterion", _i, [_vp, _d, _i, _i, _i, _dp]),
     ("gwgpu_engine_global_criterion", _i, [_vp, _i, _ip, _dp]),

@@ -437,6 +437,13 @@ int gwgpu_engine_set_flush_tiles(gwgpu_engine* e, int tiles)
     return GWGPU_OK;
 }
 
+int gwgpu_engine_set_tc_wait_limit(gwgpu_engine* e, unsigned polls)
+{
+    ENG_CHECK(e);
+    e->eng.setTcWaitLimit(polls);
+    return GWGPU_OK;
+}
+
 int gwgpu_engine_criterion(gwgpu_engine* e, double bandwidth, int adaptive, int kernel, int criterion, double* value)
 {
     ENG_CHECK(e);

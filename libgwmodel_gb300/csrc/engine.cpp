@@ -814,6 +814,7 @@ void Engine::contractMixed(double* G, int ldg, int mcols, double bw, bool adapti
     a.exclude_self = exclude_self ? 1 : 0;
     a.skip = 1;
     a.flush_tiles = flush_tiles_;
+    a.wait_limit = tc_wait_limit_;
     a.wpow = wpow;
     a.acc = acc_.get();
     a.G = G;
@@ -1058,7 +1059,12 @@ void Engine::solve(int mode, double bw, bool adaptive, int kernel, double out[4]
     if (mixed) {
         int err = 0;
         std::memcpy(&err, host_sums_ + 4, sizeof(int));
-        if (err) throw CudaError("tensor-core contraction: a bounded wait timed out");
+        if (err) {
+            // clear the flag so that the engine's next call starts clean
+            check(cudaMemsetAsync(err_.get(), 0, sizeof(int), stream_), "memset err");
+            synchronize();
+            throw CudaError("tensor-core contraction: a bounded wait timed out");
+        }
         out[1] *= s_y_ * s_y_;  // RSS / CV in the units of y
     }
 }

@@ -127,6 +127,9 @@ public:
     void setPrecision(int precision) { precision_ = precision; }
     // Tiles per FP32 accumulation chunk of the tensor-core contraction (>= 2).
     void setFlushTiles(int tiles) { flush_tiles_ = tiles; }
+    // Polls of the tensor-core contraction's pipeline waits before they time out
+    // (0: the default, about two seconds); small values exercise the timeout path.
+    void setTcWaitLimit(unsigned polls) { tc_wait_limit_ = polls; }
     int flushTiles() const { return flush_tiles_; }
     // Refinement steps of the mixed final fit (and of each search criterion when refine_search).
     void setRefinement(int steps, bool refine_search)
@@ -229,6 +232,7 @@ private:
     bool geographic_ = false;
     int precision_ = kFP64;
     int flush_tiles_ = 64;
+    unsigned tc_wait_limit_ = 0;
     double dlo_ = 0.0, dhi_ = 0.0;
     std::vector<int> perm_;  // sorted position -> original index
     std::vector<double> hx_, hy_, hu_, hv_;  // host copies in sorted order

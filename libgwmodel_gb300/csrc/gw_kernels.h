@@ -170,6 +170,7 @@ struct TcArgs {
     unsigned long long* tiles;    // if not null: += 128 x 32 weight tiles processed
     unsigned long long* prof;     // if not null: += clock64 cycles per phase (kTcProfSlots slots)
     const float* d2c;             // geographic only, optional: the distance cache of launch_fill_d2
+    unsigned wait_limit;          // polls of a pipeline wait before it times out (0: the default)
 };
 // Phase slots of TcArgs::prof, summed over CTAs (producer: warp 0 lane 0;
 // control: the issuing thread).

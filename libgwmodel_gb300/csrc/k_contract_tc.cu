@@ -112,9 +112,9 @@ __device__ __forceinline__ float2 df_add(float2 a, float v)
     return make_float2(hi, lo - (hi - s));
 }
 
-__device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity)
+__device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity, uint32_t lim)
 {
-    return __all_sync(0xffffffffu, mbar_wait(bar, parity, TC_WAIT));
+    return __all_sync(0xffffffffu, mbar_wait(bar, parity, lim));
 }
 
 // Warp roles: warps 0-15 produce the weight tiles (thread (r, quarter) fills
@@ -142,6 +142,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     constexpr uint32_t ACC_COLS = ATM ? TC_ATM_ACC_COLS : TC_ACC_COLS;
     const TcArgs a = BATCH ? segs[work[blockIdx.x].x] : a0;
     const int kernel = KERN >= 0 ? KERN : a.kernel;
+    // polls of a pipeline wait before it gives up; the waits of the clean-up after
+    // a timeout (MMAs and copies in flight) always use TC_WAIT
+    const uint32_t lim = a.wait_limit ? a.wait_limit : TC_WAIT;
     extern __shared__ unsigned char smem_dyn[];
     __shared__ Smem ctl;
     const uint32_t base_u32 = smem_u32(smem_dyn);
@@ -275,13 +278,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const int s = k & 1;
             if (prof) c0 = clock64();
             // weight stage s is free once the MMAs of tile k - 2 are done
-            const bool stage_ok = k < 2 || warp_wait(&ctl.mma_done[s], (uint32_t)(((k >> 1) - 1) & 1));
+            const bool stage_ok = k < 2 || warp_wait(&ctl.mma_done[s], (uint32_t)(((k >> 1) - 1) & 1), lim);
             if (prof) {
                 c1 = clock64();
                 p_stage += c1 - c0;
                 c0 = c1;
             }
-            if (!stage_ok || (!CACHED && !warp_wait(&ctl.full_p[s], (uint32_t)((k >> 1) & 1)))) {
+            if (!stage_ok || (!CACHED && !warp_wait(&ctl.full_p[s], (uint32_t)((k >> 1) & 1), lim))) {
                 if (lane == 0) atomicExch(&ctl.abort, 1);
                 ok = false;
                 break;
@@ -396,7 +399,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         unsigned long long pflush = 0;
         for (int c = 0; c < nchunks; c++) {
             if (__any_sync(0xffffffffu, *(volatile int*)&ctl.abort != 0)) break;
-            if (!warp_wait(&ctl.acc_full[c & 1], (uint32_t)((c >> 1) & 1))) {
+            if (!warp_wait(&ctl.acc_full[c & 1], (uint32_t)((c >> 1) & 1), lim)) {
                 if (lane == 0) atomicExch(&ctl.abort, 1);
                 break;
             }
@@ -445,7 +448,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 if (*(volatile int*)&ctl.abort) break;
                 const int s = k & 1;
                 if (prof) c0 = clock64();
-                if (!mbar_wait(&ctl.full_a[s], (uint32_t)((k >> 1) & 1), TC_WAIT)) {
+                if (!mbar_wait(&ctl.full_a[s], (uint32_t)((k >> 1) & 1), lim)) {
                     atomicExch(&ctl.abort, 1);
                     break;
                 }
@@ -454,9 +457,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     p_a += c1 - c0;
                     c0 = c1;
                 }
-                bool ok = mbar_wait(&ctl.full_b[sb], (uint32_t)zpar, TC_WAIT);
+                bool ok = mbar_wait(&ctl.full_b[sb], (uint32_t)zpar, lim);
                 if (ok && kf == 0 && c >= 2)
-                    ok = mbar_wait(&ctl.tmem_free[c & 1], (uint32_t)(((c >> 1) - 1) & 1), TC_WAIT);
+                    ok = mbar_wait(&ctl.tmem_free[c & 1], (uint32_t)(((c >> 1) - 1) & 1), lim);
                 if (!ok) {
                     atomicExch(&ctl.abort, 1);
                     break;
@@ -571,7 +574,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     }
                 } else if (kp < ktotal) {
                     // point buffer j % 2 is free once the producers are done with tile j
-                    if (!mbar_wait(&ctl.full_a[j & 1], (uint32_t)((j >> 1) & 1), TC_WAIT)) {
+                    if (!mbar_wait(&ctl.full_a[j & 1], (uint32_t)((j >> 1) & 1), lim)) {
                         atomicExch(&ctl.abort, 1);
                         break;
                     }
@@ -580,7 +583,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 }
                 if (kz < ktotal) {
                     // Z stage j % nb is free once the MMAs of tile j are done
-                    if (!mbar_wait(&ctl.z_free[jsb], (uint32_t)jpar, TC_WAIT)) {
+                    if (!mbar_wait(&ctl.z_free[jsb], (uint32_t)jpar, lim)) {
                         atomicExch(&ctl.abort, 1);
                         break;
                     }

@@ -527,6 +527,10 @@ __global__ void __launch_bounds__(SEL_THREADS)
 // lanes land on points far apart along the curve and rarely hit the same bin.
 constexpr int HS_ROWS = 8;
 constexpr int HS_THREADS = 1024;  // 32 warps at <= 64 registers: the pass is latency-bound
+// Row stride of the shared-memory histograms: one word more than the bins, so
+// the same bin of different rows falls in different banks (neighbouring rows
+// see nearly the same distances, so their lanes hit the same bins at once).
+constexpr int HS_STRIDE = SEL_BINS + 1;
 
 __device__ void hist_store(const unsigned* hs, const SelectArgs& a, int row0, int nrows);
 
@@ -550,7 +554,7 @@ __device__ void hist_rows(unsigned* hs, float4 (*rf)[2], const SelectArgs& a, in
     const long long kbin = fastbin ? (long long)((896ull << 23) >> s2) + (long long)((1ull << 63) >> wlog.shift) -
                                          (long long)(wlog.base >> wlog.shift)
                                    : 0;
-    for (int b = t; b < HS_ROWS * SEL_BINS; b += HS_THREADS) hs[b] = 0;
+    for (int b = t; b < HS_ROWS * HS_STRIDE; b += HS_THREADS) hs[b] = 0;
     if (t < HS_ROWS * NF) {
         const int r = t / NF, q = t % NF;
         rf[r][q] = r < nrows ? fpts[NF * (size_t)(row0 + r) + q] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -589,7 +593,7 @@ __device__ void hist_rows(unsigned* hs, float4 (*rf)[2], const SelectArgs& a, in
                     } else {
                         bin = bucket_of(wlog, dkey_f(d32));
                     }
-                    atomicAdd(&hs[r * SEL_BINS + bin], 1u);
+                    atomicAdd(&hs[r * HS_STRIDE + bin], 1u);
                 }
             }
         }
@@ -603,11 +607,12 @@ __device__ void hist_rows(unsigned* hs, float4 (*rf)[2], const SelectArgs& a, in
 __device__ void hist_store(const unsigned* hs, const SelectArgs& a, int row0, int nrows)
 {
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    for (int e = t; e < nrows * SEL_BINS; e += HS_THREADS) a.hist_cache[(size_t)row0 * SEL_BINS + e] = hs[e];
+    for (int e = t; e < nrows * SEL_BINS; e += HS_THREADS)
+        a.hist_cache[(size_t)row0 * SEL_BINS + e] = hs[(e / SEL_BINS) * HS_STRIDE + e % SEL_BINS];
     if (a.hist_coarse) {
         // cumulative counts at the end of every 64-bin segment: one warp per row
         for (int r = warp; r < nrows; r += HS_THREADS / 32) {
-            const unsigned* hr = hs + r * SEL_BINS;
+            const unsigned* hr = hs + r * HS_STRIDE;
             unsigned s0 = 0, s1 = 0;
             for (int b = 0; b < 64; b++) {  // rotated start: the 32 lanes hit 32 different banks
                 const int q = (b + lane) & 63;
@@ -652,7 +657,7 @@ __device__ void hist_rows_fill(unsigned* hs, float4 (*rf)[2], const SelectArgs& 
                                          (long long)(wlog.base >> wlog.shift)
                                    : 0;
     const int nrows = min(HS_ROWS, n - row0);
-    for (int b = t; b < HS_ROWS * SEL_BINS; b += HS_THREADS) hs[b] = 0;
+    for (int b = t; b < HS_ROWS * HS_STRIDE; b += HS_THREADS) hs[b] = 0;
     if (t < HS_ROWS * 2) {
         const int r = t / 2, q = t % 2;
         rf[r][q] = r < nrows ? a.pts[2 * (size_t)(row0 + r) + q] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -663,7 +668,7 @@ __device__ void hist_rows_fill(unsigned* hs, float4 (*rf)[2], const SelectArgs& 
     const bool row_ok = r < nrows;
     const float4 ra = rf[r][0], rb = rf[r][1];
     const float fz = ra.z + rb.z;
-    unsigned* hrow = hs + r * SEL_BINS;
+    unsigned* hrow = hs + r * HS_STRIDE;
     float4* out = reinterpret_cast<float4*>(a.d2c_out) + (size_t)(row / 128) * a.ntiles * 1024 + quarter * 256 +
                   (row & 127);
     for (int tile = warp; tile < a.ntiles; tile += HS_THREADS / 32) {
@@ -710,7 +715,7 @@ __device__ void hist_rows_fill(unsigned* hs, float4 (*rf)[2], const SelectArgs& 
 template <bool GEO>
 __global__ void __launch_bounds__(HS_THREADS, 1) k_select_hist(SelectArgs a)
 {
-    extern __shared__ __align__(16) unsigned hs[];  // HS_ROWS x SEL_BINS
+    extern __shared__ __align__(16) unsigned hs[];  // HS_ROWS x HS_STRIDE
     __shared__ float4 rf[HS_ROWS][2];
     const int nfocus = a.F.u ? a.F.n : a.n;
     const bool fill = GEO && a.d2c_out && !a.F.u;
@@ -829,7 +834,7 @@ cudaError_t launch_select(const SelectArgs& a, bool geographic, bool exact, int 
 cudaError_t launch_select_hist(const SelectArgs& a, bool geographic, int num_sms, cudaStream_t stream)
 {
     if (!a.hist_cache || a.n < 1) return cudaErrorInvalidValue;
-    const size_t smem = (size_t)HS_ROWS * SEL_BINS * sizeof(unsigned);
+    const size_t smem = (size_t)HS_ROWS * HS_STRIDE * sizeof(unsigned);
     int grid = (a.n + HS_ROWS - 1) / HS_ROWS;
     if (grid > num_sms) grid = num_sms;
     if (geographic) {
@@ -845,7 +850,7 @@ cudaError_t launch_select_hist(const SelectArgs& a, bool geographic, int num_sms
 cudaError_t launch_select_hist_batch(const SelectArgs* segs, const long long* start, int nseg, bool geographic,
                                      int num_sms, cudaStream_t stream)
 {
-    const size_t smem = (size_t)HS_ROWS * SEL_BINS * sizeof(unsigned);
+    const size_t smem = (size_t)HS_ROWS * HS_STRIDE * sizeof(unsigned);
     if (geographic) {
         raise_smem_limit((const void*)k_select_hist_batch<true>, smem);
         k_select_hist_batch<true><<<num_sms, HS_THREADS, smem, stream>>>(segs, start, nseg);

@@ -385,6 +385,11 @@ class Engine:
     def set_flush_tiles(self, tiles):
         check(lib().gwgpu_engine_set_flush_tiles(self._h, int(tiles)))
 
+    def set_tc_wait_limit(self, polls):
+        """Polls of each pipeline wait of the tensor-core contraction (0: default);
+        small values exercise the timeout path."""
+        check(lib().gwgpu_engine_set_tc_wait_limit(self._h, int(polls)))
+
     def criterion(self, bw, adaptive, kernel, criterion):
         v = ctypes.c_double()
         check(lib().gwgpu_engine_criterion(self._h, float(bw), int(bool(adaptive)), int(kernel), int(criterion),

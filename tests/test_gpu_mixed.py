@@ -68,3 +68,20 @@ def test_mixed_fit_close_to_fp64(name, kw, bws):
     assert max(rel(semx[:, k], se64[:, k]) for k in range(pb.p)) <= 1e-4
     assert rel(shmx, sh64) <= 1e-5
     assert rel(qmx, q64) <= 1e-5
+
+
+@pytest.mark.parametrize("name,kw,bw", [("config2", dict(n=3000, k=8), 900), ("config0", dict(n=2000), 400)])
+def test_contraction_timeout_is_reported_and_engine_recovers(name, kw, bw):
+    """With a limit of one poll the contraction's pipeline waits run out: the
+    kernel waits for its own MMAs and bulk copies, frees its tensor memory and
+    sets the error flag; the call fails with that error, and the next call on
+    the same engine (default limit) returns the value it returned before."""
+    from libgwmodel_gb300 import GwgpuError
+    pb = datasets.CONFIGS[name](**kw)
+    _, emx = pair(pb)
+    want = emx.criterion(bw, pb.adaptive, pb.kernel, pb.criterion)
+    emx.set_tc_wait_limit(1)
+    with pytest.raises(GwgpuError, match="timed out"):
+        emx.criterion(bw, pb.adaptive, pb.kernel, pb.criterion)
+    emx.set_tc_wait_limit(0)
+    assert emx.criterion(bw, pb.adaptive, pb.kernel, pb.criterion) == want
