@@ -189,7 +189,7 @@ enum TcProf {
     kTcProfTilesMax,    // largest number of tiles one CTA processed (maximum, not cycles)
     kTcProfSlots
 };
-size_t contract_tc_smem_bytes(int npad, int ntiles, int nb);
+size_t contract_tc_smem_bytes(int npad, int ntiles, int nb, bool cached);
 cudaError_t launch_contract_tc(const TcArgs& a, bool geographic, cudaStream_t stream);
 // Many contractions in one launch: CTA b computes row block work[b].y of
 // segment work[b].x (device arrays; every segment's npad <= max_npad and

@@ -14,7 +14,8 @@
 //    weights in shared memory);
 //  * one thread of the MMA warp issues 3 x 4 tcgen05.mma.kind::tf32
 //    (hi.hi + hi.lo + lo.hi, K = 8 each) into a 128 x N FP32 accumulator in
-//    TMEM and commits to mbarriers.  An MMA issue returns only when the tensor
+//    TMEM and commits once per tile (tile_done frees both the weight stage
+//    and the Z stage of that tile).  An MMA issue returns only when the tensor
 //    pipe accepts it (about as long as the MMA runs), so that thread issues
 //    nothing else: with the copies on the same thread the pipe idled about
 //    two thirds of the time.  Both single-thread loops keep their stage and
@@ -32,8 +33,11 @@
 // With a distance cache (CACHED, geographic) the producers read each pair's
 // FP32 squared distance -- filled once per dataset, by the histogram pass of
 // the select or by k_fill_d2, with the same arithmetic -- instead of computing
-// it: about 14 instead of 58 instructions per weight, bit-identical weights,
-// and no point records to stage.
+// it: about 14 instead of 58 instructions per weight, bit-identical weights.
+// The tile's 16 KB distance block takes the place of its point records: a
+// bulk copy two tiles ahead into shared memory (after an L2 prefetch nd tiles
+// ahead), so the producers never wait on global loads (reading the block with
+// per-thread global loads one tile ahead cost 3.6% more time per launch).
 #include "gw_common.cuh"
 #include "gw_kernels.h"
 #include "mixed_weight.cuh"
@@ -66,10 +70,9 @@ constexpr uint32_t TC_D_BYTES = TC_M * TC_BK * 4;  // one cached 128 x 32 distan
 
 struct Smem {
     uint64_t full_a[2];          // weight tile k written: one arrival per producer warp
-    uint64_t mma_done[2];        // tcgen05.commit of tile k (every earlier MMA is done too)
+    uint64_t tile_done[4];       // tcgen05.commit after the MMAs of tile k (slot k % 4; every earlier MMA too)
     uint64_t full_b[TC_MAX_NB];  // Z tile landed (bulk copy)
-    uint64_t full_p[2];          // point records landed (bulk copy)
-    uint64_t z_free[TC_MAX_NB];  // tcgen05.commit after the MMAs that read Z stage s
+    uint64_t full_p[2];          // point records or cached distances of a tile landed (bulk copy)
     uint64_t tmem_free[2];       // accumulator drained: one arrival per drain warp
     uint64_t acc_full[2];        // tcgen05.commit after the last MMA of a chunk into accumulator c % 2
     uint32_t tmem_base;
@@ -121,7 +124,8 @@ __device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity, uint32
 // points [8 quarter, 8 quarter + 8) of row r); warps 16-19 drain the
 // accumulators (warp 16 + q owns TMEM lanes 32 q .. 32 q + 31, all columns);
 // lane 0 of warp 20 issues the MMAs and lane 0 of warp 21 the bulk copies
-// (Z stage j is refilled once z_free[j % nb] reports its MMAs done).  Tile k uses weight
+// (Z stage j % nb is refilled once tile_done[j % 4] reports the MMAs of tile j done;
+// the same commit frees weight stage j % 2 for the producers).  Tile k uses weight
 // stage k % 2, Z stage k % nb and point buffer k % 2; chunk c = k / F of F
 // tiles accumulates in TMEM accumulator c % 2, whose last MMA commits to
 // acc_full[c % 2]; the drain warps then add it into the double-float sums and
@@ -153,9 +157,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const uint32_t b_bytes = (uint32_t)a.npad * 128u;
     unsigned char* sB = sA + (ATM ? 0 : 4 * (size_t)TC_A_BYTES);  // nb stages x [B_hi | B_lo]
     constexpr int NF = GEO ? 2 : 1;                    // float4 per point record
-    constexpr uint32_t P_BYTES = NF * 16u * TC_BK;     // point records of one tile
-    float4* ptsbuf = reinterpret_cast<float4*>(sB + (size_t)nb * 2 * b_bytes);  // 2 x P_BYTES
-    uint32_t* tmask = reinterpret_cast<uint32_t*>(sB + (size_t)nb * 2 * b_bytes + 2 * TC_P_MAX);
+    // per tile: the point records, or with the cache the tile's 128 x 32 distance block
+    constexpr uint32_t P_BYTES = CACHED ? TC_D_BYTES : NF * 16u * TC_BK;
+    constexpr uint32_t P_SLOT = CACHED ? TC_D_BYTES : TC_P_MAX;  // bytes per buffer (two buffers)
+    float4* ptsbuf = reinterpret_cast<float4*>(sB + (size_t)nb * 2 * b_bytes);  // 2 x P_SLOT
+    uint32_t* tmask = reinterpret_cast<uint32_t*>(sB + (size_t)nb * 2 * b_bytes + 2 * P_SLOT);
     const int nwords = (a.ntiles + 31) / 32;
 
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
@@ -172,16 +178,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         tmem_relinquish();
     }
     if (t == 0) {
+        for (int s = 0; s < 4; s++) mbar_init(&ctl.tile_done[s], 1);
         for (int s = 0; s < 2; s++) {
             mbar_init(&ctl.full_a[s], TC_PROD_WARPS);
-            mbar_init(&ctl.mma_done[s], 1);
             mbar_init(&ctl.full_p[s], 1);
             mbar_init(&ctl.tmem_free[s], TC_DRAIN_WARPS);
             mbar_init(&ctl.acc_full[s], 1);
         }
         for (int s = 0; s < TC_MAX_NB; s++) {
             mbar_init(&ctl.full_b[s], 1);
-            mbar_init(&ctl.z_free[s], 1);
         }
         ctl.abort = 0;
         fence_mbar_init();
@@ -245,32 +250,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         unsigned long long p_stage = 0, p_points = 0, p_weights = 0;  // phase cycles (prof)
         long long c0 = prof ? clock64() : 0, c1 = 0;
         const long long loop0 = c0;
-        // cached: this thread's 8 distances of a tile are two float4 of its row and
-        // quarter, loaded one visited tile ahead (from L2: the control thread
-        // prefetches the blocks nd tiles ahead)
-        const float4* d2row = CACHED ? reinterpret_cast<const float4*>(a.d2c) +
-                                           (size_t)blockIdx.x * a.ntiles * (TC_D_BYTES / 16) + quarter * 256 + r
-                                     : nullptr;
-        int tnext = walk.next();
-        int tpre = (CACHED && tnext >= 0) ? walk.next() : -1;
-        float4 nd0 = make_float4(0.f, 0.f, 0.f, 0.f), nd1 = nd0;
-        if (CACHED && tnext >= 0) {
-            nd0 = __ldcs(d2row + (size_t)tnext * (TC_D_BYTES / 16));
-            nd1 = __ldcs(d2row + (size_t)tnext * (TC_D_BYTES / 16) + 128);
-        }
-        for (; tnext >= 0; k++) {
+        for (int tnext = walk.next(); tnext >= 0; k++) {
             const int tile = tnext;
-            const float4 cd0 = nd0, cd1 = nd1;
-            if (CACHED) {
-                tnext = tpre;
-                tpre = tnext >= 0 ? walk.next() : -1;
-                if (tnext >= 0) {
-                    nd0 = __ldcs(d2row + (size_t)tnext * (TC_D_BYTES / 16));
-                    nd1 = __ldcs(d2row + (size_t)tnext * (TC_D_BYTES / 16) + 128);
-                }
-            } else {
-                tnext = walk.next();
-            }
+            tnext = walk.next();
             if (__any_sync(0xffffffffu, *(volatile int*)&ctl.abort != 0)) {
                 ok = false;
                 break;
@@ -278,13 +260,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const int s = k & 1;
             if (prof) c0 = clock64();
             // weight stage s is free once the MMAs of tile k - 2 are done
-            const bool stage_ok = k < 2 || warp_wait(&ctl.mma_done[s], (uint32_t)(((k >> 1) - 1) & 1), lim);
+            const bool stage_ok =
+                k < 2 || warp_wait(&ctl.tile_done[(k - 2) & 3], (uint32_t)(((k - 2) >> 2) & 1), lim);
             if (prof) {
                 c1 = clock64();
                 p_stage += c1 - c0;
                 c0 = c1;
             }
-            if (!stage_ok || (!CACHED && !warp_wait(&ctl.full_p[s], (uint32_t)((k >> 1) & 1), lim))) {
+            // the tile's point records (or, cached, its distance block) in buffer s
+            if (!stage_ok || !warp_wait(&ctl.full_p[s], (uint32_t)((k >> 1) & 1), lim)) {
                 if (lane == 0) atomicExch(&ctl.abort, 1);
                 ok = false;
                 break;
@@ -295,7 +279,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 c0 = c1;
             }
             if constexpr (ATM) fence_after_sync();  // the MMAs that read stage s are done
-            const float4* tp = ptsbuf + (size_t)s * NF * TC_BK;
+            const float4* tp = ptsbuf + (size_t)s * (P_SLOT / 16);
             unsigned char* A_hi = sA + (size_t)s * 2 * TC_A_BYTES;
             unsigned char* A_lo = A_hi + TC_A_BYTES;
             const int kbase = quarter * 8;
@@ -306,7 +290,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 bool in[4];
                 GeoChord g[4];
                 if constexpr (CACHED) {
-                    const float4 dv = q4 ? cd1 : cd0;  // row r, points kbase + 4 q4 .. + 3
+                    // the block is [quarter 4][half 2][row 128][4 points]: row r, points kbase + 4 q4 .. + 3
+                    const float4 dv = tp[(2 * quarter + q4) * TC_M + r];
                     const float dd[4] = {dv.x, dv.y, dv.z, dv.w};
 #pragma unroll
                     for (int e = 0; e < 4; e++) {
@@ -496,8 +481,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                         mma_tf32(d, alo + dk, bhi + dk, idesc, 1u);
                     }
                 }
-                mma_commit(&ctl.mma_done[s]);  // weight stage s reusable (producers)
-                mma_commit(&ctl.z_free[sb]);   // Z stage sb reusable (copy warp)
+                // one commit frees weight stage s (producers) and Z stage sb (copy warp)
+                mma_commit(&ctl.tile_done[k & 3]);
                 if (kf == F - 1 || k == ktotal - 1) mma_commit(&ctl.acc_full[c & 1]);  // chunk c complete
                 last_mma = k;
                 if (++sb == nb) {
@@ -517,23 +502,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             // leave no MMA in flight before TMEM and the CTA go away
             if (*(volatile int*)&ctl.abort && last_mma >= 0)
-                mbar_wait(&ctl.mma_done[last_mma & 1], (uint32_t)((last_mma >> 1) & 1), TC_WAIT);
+                mbar_wait(&ctl.tile_done[last_mma & 3], (uint32_t)((last_mma >> 2) & 1), TC_WAIT);
         }
     } else if (warp == TC_COPY_WARP) {
         // Copies (lane 0): the Z tiles nb ahead (a stage is refilled once the MMAs
-        // that read it are done), the point records two ahead (once the producers
-        // are done with a buffer) or, with the cache, L2 prefetches of the distance
-        // blocks nd ahead.  Each wait is for a phase whose successor needs a copy
-        // this thread has not issued yet, so it can never be two phases behind.
+        // of the tile that read it are done), the point records or, with the
+        // cache, the 16 KB distance block of a tile two ahead (once the producers
+        // are done with a buffer), and with the cache an L2 prefetch of the
+        // distance blocks nd ahead.  Each wait is for a phase whose successor
+        // needs a copy this thread has not issued yet, so it can never be two
+        // phases behind.
         if (lane == 0) {
-            TileWalker wz, wp;
+            TileWalker wz, wp, wl;
             wz.init(tmask, nwords);
             wp.init(tmask, nwords);
-            int kz = 0, kp = 0;  // copies (or prefetches) issued
+            wl.init(tmask, nwords);
+            int kz = 0, kp = 0, kl = 0;  // copies and prefetches issued
             const float* d2blk = CACHED ? a.d2c + (size_t)blockIdx.x * a.ntiles * (TC_D_BYTES / 4) : nullptr;
-            auto issue_d = [&](int tl) {
+            auto issue_l = [&](int tl) {
                 bulk_prefetch_l2(d2blk + (size_t)tl * (TC_D_BYTES / 4), TC_D_BYTES);
-                kp++;
+                kl++;
             };
             int zsb = 0;  // kz % nb, kept as a counter (no run-time divisions on this thread)
             auto issue_z = [&](int tl) {
@@ -549,8 +537,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             };
             auto issue_p = [&](int tl) {
                 const int sp = kp & 1;
+                const void* src = CACHED ? static_cast<const void*>(d2blk + (size_t)tl * (TC_D_BYTES / 4))
+                                         : static_cast<const void*>(a.pts + (size_t)NF * TC_BK * tl);
                 mbar_arrive_expect_tx(&ctl.full_p[sp], P_BYTES);
-                bulk_g2s(ptsbuf + (size_t)sp * NF * TC_BK, a.pts + (size_t)NF * TC_BK * tl, P_BYTES, &ctl.full_p[sp]);
+                bulk_g2s(ptsbuf + (size_t)sp * (P_SLOT / 16), src, P_BYTES, &ctl.full_p[sp]);
                 kp++;
             };
             for (int q = 0; q < nb; q++) {
@@ -558,22 +548,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 if (tl < 0) break;
                 issue_z(tl);
             }
-            for (int q = 0; q < (CACHED ? nd : 2); q++) {
+            for (int q = 0; CACHED && q < nd; q++) {
+                const int tl = wl.next();
+                if (tl < 0) break;
+                issue_l(tl);
+            }
+            for (int q = 0; q < 2; q++) {
                 const int tl = wp.next();
                 if (tl < 0) break;
-                if (CACHED) issue_d(tl);
-                else issue_p(tl);
+                issue_p(tl);
             }
-            int jsb = 0, jpar = 0;  // j % nb and (j / nb) & 1
-            for (int j = 0; j < ktotal && (kz < ktotal || (kp < ktotal && (!CACHED || nd > 0))); j++) {
+            for (int j = 0; j < ktotal && (kz < ktotal || kp < ktotal || (CACHED && kl < ktotal)); j++) {
                 if (*(volatile int*)&ctl.abort) break;
-                if (CACHED) {
-                    if (nd > 0) {
-                        const int tl = wp.next();
-                        if (tl >= 0) issue_d(tl);
-                    }
-                } else if (kp < ktotal) {
-                    // point buffer j % 2 is free once the producers are done with tile j
+                if (CACHED && kl < ktotal) {
+                    const int tl = wl.next();
+                    if (tl >= 0) issue_l(tl);
+                }
+                if (kp < ktotal) {
+                    // buffer j % 2 is free once the producers are done with tile j
                     if (!mbar_wait(&ctl.full_a[j & 1], (uint32_t)((j >> 1) & 1), lim)) {
                         atomicExch(&ctl.abort, 1);
                         break;
@@ -583,23 +575,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 }
                 if (kz < ktotal) {
                     // Z stage j % nb is free once the MMAs of tile j are done
-                    if (!mbar_wait(&ctl.z_free[jsb], (uint32_t)jpar, lim)) {
+                    if (!mbar_wait(&ctl.tile_done[j & 3], (uint32_t)((j >> 2) & 1), lim)) {
                         atomicExch(&ctl.abort, 1);
                         break;
                     }
                     const int tl = wz.next();
                     if (tl >= 0) issue_z(tl);
                 }
-                if (++jsb == nb) {
-                    jsb = 0;
-                    jpar ^= 1;
-                }
             }
             if (*(volatile int*)&ctl.abort) {
                 // leave no bulk copy in flight before the CTA goes away
                 for (int j = kz - nb > 0 ? kz - nb : 0; j < kz; j++)
                     mbar_wait(&ctl.full_b[j % nb], (uint32_t)((j / nb) & 1), TC_WAIT);
-                for (int j = kp - 2 > 0 ? kp - 2 : 0; j < kp && !CACHED; j++)
+                for (int j = kp - 2 > 0 ? kp - 2 : 0; j < kp; j++)
                     mbar_wait(&ctl.full_p[j & 1], (uint32_t)((j >> 1) & 1), TC_WAIT);
             }
         }
@@ -767,10 +755,11 @@ cudaError_t launch_fill_d2(int n, const float4* pts, float* d2c, cudaStream_t st
     return cudaGetLastError();
 }
 
-size_t contract_tc_smem_bytes(int npad, int ntiles, int nb)
+size_t contract_tc_smem_bytes(int npad, int ntiles, int nb, bool cached)
 {
     const size_t mask = (size_t)((ntiles + 31) / 32) * 4;
-    return 1024 + 4 * (size_t)TC_A_BYTES + (size_t)nb * 2 * npad * 128 + 2 * TC_P_MAX + mask;
+    return 1024 + 4 * (size_t)TC_A_BYTES + (size_t)nb * 2 * npad * 128 + 2 * (size_t)(cached ? TC_D_BYTES : TC_P_MAX) +
+           mask;
 }
 
 cudaError_t launch_contract_tc(const TcArgs& a, bool geographic, cudaStream_t stream)
@@ -783,7 +772,9 @@ cudaError_t launch_contract_tc(const TcArgs& a, bool geographic, cudaStream_t st
     const size_t mask = (size_t)((a.ntiles + 31) / 32) * 4;
     if ((uint32_t)a.npad <= TC_ATM_ACC_COLS) {
         // weights in tensor memory: the shared memory holds only the Z stages
-        auto bytes = [&](int b) { return 1024 + (size_t)b * 2 * a.npad * 128 + 2 * TC_P_MAX + mask; };
+        // (two buffers of point records, or of 16 KB distance blocks with the cache)
+        const size_t pbuf = a.d2c && geographic ? TC_D_BYTES : TC_P_MAX;
+        auto bytes = [&](int b) { return 1024 + (size_t)b * 2 * a.npad * 128 + 2 * pbuf + mask; };
         int nb = TC_MAX_NB;
         while (nb > 2 && bytes(nb) > 227 * 1024) nb--;
         const size_t smem = bytes(nb);
@@ -809,8 +800,9 @@ cudaError_t launch_contract_tc(const TcArgs& a, bool geographic, cudaStream_t st
     }
     // wider Z (npad 208 .. 256): weights in shared memory, the kernel read at run time
     int nb = TC_MAX_NB;
-    while (nb > 2 && contract_tc_smem_bytes(a.npad, a.ntiles, nb) > 227 * 1024) nb--;
-    const size_t smem = contract_tc_smem_bytes(a.npad, a.ntiles, nb);
+    const bool cached = geographic && a.d2c;
+    while (nb > 2 && contract_tc_smem_bytes(a.npad, a.ntiles, nb, cached) > 227 * 1024) nb--;
+    const size_t smem = contract_tc_smem_bytes(a.npad, a.ntiles, nb, cached);
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
     auto go = [&](auto kfn) {
         raise_smem_limit((const void*)kfn, smem);
@@ -828,8 +820,8 @@ cudaError_t launch_contract_tc_batch(const TcArgs* segs, const int2* work, int n
     if (max_npad % 16 != 0 || max_npad < 16 || max_npad > 256 || flush_tiles < 2 || nwork < 1)
         return cudaErrorInvalidValue;
     int nb = TC_MAX_NB;
-    while (nb > 2 && contract_tc_smem_bytes(max_npad, max_ntiles, nb) > 227 * 1024) nb--;
-    const size_t smem = contract_tc_smem_bytes(max_npad, max_ntiles, nb);
+    while (nb > 2 && contract_tc_smem_bytes(max_npad, max_ntiles, nb, false) > 227 * 1024) nb--;
+    const size_t smem = contract_tc_smem_bytes(max_npad, max_ntiles, nb, false);
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
     TcArgs none{};
     auto go = [&](auto kfn) {
