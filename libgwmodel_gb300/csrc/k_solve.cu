@@ -533,7 +533,8 @@ __global__ void __launch_bounds__(HAT_THREADS)
 }
 
 // Mixed-precision hat pass: the weights are the FP32 weights of the tensor-core
-// contraction (FP32 proxy distance, FP32 threshold); dot products and sums in FP64.
+// contraction (FP32 proxy distance, FP32 threshold); the hat entries
+// s_ij = w_ij v_i^T x_j in FP32, the sums of squares in FP64.
 template <bool GEO>
 __global__ void __launch_bounds__(HAT_THREADS)
     k_hat_mixed(int n, const float4* __restrict__ pts, const float4* __restrict__ tb16,
@@ -541,9 +542,13 @@ __global__ void __launch_bounds__(HAT_THREADS)
                 const double* __restrict__ v, const float* __restrict__ thr32, float bw, int kernel,
                 double* __restrict__ qdiag, double* __restrict__ S, int row_target, double* __restrict__ s_row)
 {
-    extern __shared__ double hsm[];
-    double* sX = hsm;                       // HAT_THREADS x p
-    double* sV = sX + HAT_THREADS * p;      // HAT_TILE x p
+    // FP32 copies of x_j and v_i: the FP32 weights already give s_ij a ~1e-7
+    // relative error, and an FP32 dot product of p terms adds one of the same
+    // order at 1/64 of the FP64 cost per pair; qDiag_j = sum_i (delta_ij - s_ij)^2
+    // is dominated by (1 - s_jj)^2 with s_jj ~ p / b, so it moves by far less
+    extern __shared__ float hsmf[];
+    float* sX = hsmf;                      // HAT_THREADS x p
+    float* sV = sX + HAT_THREADS * p;      // HAT_TILE x p
     constexpr int NF = GEO ? 2 : 1;
     __shared__ float4 sf[HAT_TILE][NF];
     __shared__ float sr[HAT_TILE], sinv[HAT_TILE];
@@ -552,7 +557,7 @@ __global__ void __launch_bounds__(HAT_THREADS)
     const int j0 = blockIdx.x * HAT_THREADS, j = j0 + t;
     for (int e = t; e < HAT_THREADS * p; e += HAT_THREADS) {
         int jj = j0 + e / p;
-        sX[e] = jj < n ? X[(size_t)j0 * p + e] : 0.0;
+        sX[e] = jj < n ? (float)X[(size_t)j0 * p + e] : 0.0f;
     }
     if (t == 0) sbound = tb_union<GEO>(tb16, j0 / HAT_TILE, (min(j0 + HAT_THREADS, n) - 1) / HAT_TILE);
     __syncthreads();
@@ -578,19 +583,19 @@ __global__ void __launch_bounds__(HAT_THREADS)
         }
         for (int e = t; e < HAT_TILE * p; e += HAT_THREADS) {
             int i = i0 + e / p;
-            sV[e] = i < n ? v[(size_t)i0 * p + e] : 0.0;
+            sV[e] = i < n ? (float)v[(size_t)i0 * p + e] : 0.0f;
         }
         __syncthreads();
         if (j < n) {
             const int iend = min(HAT_TILE, n - i0);
             for (int q = 0; q < iend; q++) {
                 const float d2 = GEO ? geo_d2_32(sf[q][0], sf[q][1], pa, pb) : planar_d2_32(sf[q][0], pa);
-                const double w = (double)weight32(kernel, d2, sr[q], sinv[q]);
+                const float w = weight32(kernel, d2, sr[q], sinv[q]);
                 double s = 0.0;
-                if (w != 0.0) {
-                    double dot = 0.0;
-                    for (int r = 0; r < p; r++) dot += sV[q * p + r] * sX[t * p + r];
-                    s = w * dot;
+                if (w != 0.0f) {
+                    float dot = 0.0f;
+                    for (int r = 0; r < p; r++) dot = fmaf(sV[q * p + r], sX[t * p + r], dot);
+                    s = (double)(w * dot);
                 }
                 const double e = (i0 + q == j) ? 1.0 - s : -s;
                 acc += e * e;
@@ -866,7 +871,7 @@ cudaError_t launch_hat_mixed(int n, bool geographic, const float4* pts, const fl
                              double* qdiag, double* S, int row_target, double* s_row, cudaStream_t stream)
 {
     int grid = (n + HAT_THREADS - 1) / HAT_THREADS;
-    size_t smem = (size_t)(HAT_THREADS + HAT_TILE) * p * sizeof(double);
+    size_t smem = (size_t)(HAT_THREADS + HAT_TILE) * p * sizeof(float);
     if (geographic)
         k_hat_mixed<true><<<grid, HAT_THREADS, smem, stream>>>(n, pts, tb16, tile_thr, X, p, v, thr32, bw, kernel,
                                                                qdiag, S, row_target, s_row);
