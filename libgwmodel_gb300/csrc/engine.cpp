@@ -1087,8 +1087,20 @@ void Engine::refine(double bw, bool adaptive, int kernel, double out[4])
     r.thr = adaptive ? thr32_.get() : nullptr;
     r.bw = (float)bw;
     r.r = rvec_.get();
+    // geographic: the contraction's distances from the device's distance cache, as the contraction read them
+    DeviceD2Cache& dc = device_d2c(device_);
+    std::unique_lock<std::mutex> d2lock(dc.mu, std::defer_lock);
+    if (geographic_ && d2c_limit_bytes_ != 0) {
+        d2lock.lock();
+        r.d2c = ensureDistanceCache();
+        if (!r.d2c) d2lock.unlock();
+    }
     check(launch_refine_residual(r, geographic_, stream_), "refine residual");
     stats_.kernel_launches += 1;
+    if (r.d2c) {
+        check(cudaEventRecord(dc.used, stream_), "cudaEventRecord");
+        d2lock.unlock();
+    }
     solve(kSolveRefine, bw, adaptive, kernel, out);
 }
 

@@ -223,6 +223,7 @@ struct RefineArgs {
     const float* thr;
     float bw;
     double* r;            // n x p
+    const float* d2c;     // geographic only, optional: the distance cache (the contraction's FP32 d^2)
 };
 cudaError_t launch_refine_residual(const RefineArgs& a, bool geographic, cudaStream_t stream);
 

@@ -13,7 +13,10 @@
 // error-free products (fma) and sums (TwoSum), ~44 bits, about five times
 // faster than FP64 on a GPU whose FP64 rate is 1/64 of FP32.
 // One thread owns one focus row; data tiles beyond the block's largest
-// threshold are skipped exactly as in the contraction.
+// threshold are skipped exactly as in the contraction.  With the distance
+// cache the 128 rows of a CTA are one row block of the cache, so a tile's
+// squared distances are read coalesced instead of recomputed (the same FP32
+// values the contraction weighted).
 #include "gw_common.cuh"
 #include "gw_kernels.h"
 #include "mixed_weight.cuh"
@@ -120,6 +123,10 @@ __global__ void __launch_bounds__(RF_THREADS) k_refine(RefineArgs a)
         lc[u] = e - lq[u] * pp;
     }
 
+    // cache block (row block, tile): [quarter 4][half 2][row 128][4 points], so point q of
+    // this thread's row is component q % 4 of float4 (q / 4) * 128 + row
+    static_assert(RF_THREADS == 128 && RF_TILE == 32, "one CTA is one row block of the distance cache");
+    const float* d2base = (GEO && a.d2c) ? a.d2c + (size_t)blockIdx.x * a.ntiles * 4096 + 4 * t : nullptr;
     for (int tile = 0; tile < a.ntiles; tile++) {
         if (tb_far<GEO>(fbound, a.tb[tile], far_thr)) continue;
         const int j0 = tile * RF_TILE;
@@ -135,7 +142,9 @@ __global__ void __launch_bounds__(RF_THREADS) k_refine(RefineArgs a)
         if (ok) {
             const int qend = min(RF_TILE, a.n - j0);
             for (int q = 0; q < qend; q++) {
-                const float w = mixed_weight<GEO>(a.pts, j0 + q, fa, fb, a.kernel, rr, inv_r2);
+                const float w = d2base ? weight32(a.kernel, d2base[(size_t)tile * 4096 + (q >> 2) * 512 + (q & 3)], rr,
+                                                  inv_r2)
+                                       : mixed_weight<GEO>(a.pts, j0 + q, fa, fb, a.kernel, rr, inv_r2);
                 if (w == 0.0f) continue;
                 const DF* xj = rsm + q * pp;
                 DF e = xj[p];

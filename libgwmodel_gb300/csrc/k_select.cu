@@ -656,6 +656,10 @@ __device__ void hist_rows_fill(unsigned* hs, float4 (*rf)[2], const SelectArgs& 
     const long long kbin = fastbin ? (long long)((896ull << 23) >> s2) + (long long)((1ull << 63) >> wlog.shift) -
                                          (long long)(wlog.base >> wlog.shift)
                                    : 0;
+    // the same bins in 32-bit integer steps when the window's constants allow it (they do
+    // for distances in km): (bits >> s2) + kbin then stays inside int32 for every positive float
+    const bool bin32 = fastbin && kbin > -(1ll << 30) && kbin + (long long)(0x7f800000u >> s2) < (1ll << 30);
+    const int kbin32 = bin32 ? (int)kbin : 0;
     const int nrows = min(HS_ROWS, n - row0);
     for (int b = t; b < HS_ROWS * HS_STRIDE; b += HS_THREADS) hs[b] = 0;
     if (t < HS_ROWS * 2) {
@@ -672,32 +676,33 @@ __device__ void hist_rows_fill(unsigned* hs, float4 (*rf)[2], const SelectArgs& 
     float4* out = reinterpret_cast<float4*>(a.d2c_out) + (size_t)(row / 128) * a.ntiles * 1024 + quarter * 256 +
                   (row & 127);
     for (int tile = warp; tile < a.ntiles; tile += HS_THREADS / 32) {
+        const int jl = tile * SEL_TILE + quarter * 8;                 // this lane's first point
+        const float4* tp = a.pts + 2 * (size_t)jl;                    // its 8 records (padded to whole tiles)
+        const int nv = row_ok ? min(8, n - jl) : 0;                   // how many of them are points
 #pragma unroll
         for (int q4 = 0; q4 < 2; q4++) {
             GeoChord g[4];
 #pragma unroll
-            for (int e = 0; e < 4; e++) {
-                const size_t j = (size_t)tile * SEL_TILE + quarter * 8 + q4 * 4 + e;  // records padded to whole tiles
-                g[e] = geo_chord32(ra, rb, fz, a.pts[2 * j], a.pts[2 * j + 1]);
-            }
+            for (int e = 0; e < 4; e++) g[e] = geo_chord32(ra, rb, fz, tp[2 * (q4 * 4 + e)], tp[2 * (q4 * 4 + e) + 1]);
             const bool near = __all_sync(0xffffffffu, fmaxf(fmaxf(g[0].S, g[1].S), fmaxf(g[2].S, g[3].S)) <= 0.25f);
             float d[4];
 #pragma unroll
             for (int e = 0; e < 4; e++) {
-                const int j = tile * SEL_TILE + quarter * 8 + q4 * 4 + e;
                 const float d2 = near ? geo_d2_near(g[e]) : geo_d2_from_chord(g[e]);
-                d[e] = (row_ok && j < n) ? d2 : 3.402823466e38f;
+                d[e] = q4 * 4 + e < nv ? d2 : 3.402823466e38f;
             }
             if (row_ok) __stcs(out + (size_t)tile * 1024 + q4 * 128, make_float4(d[0], d[1], d[2], d[3]));
 #pragma unroll
             for (int e = 0; e < 4; e++) {
-                const int j = tile * SEL_TILE + quarter * 8 + q4 * 4 + e;
-                if (!row_ok || j >= n) continue;
+                if (q4 * 4 + e >= nv) continue;
                 const float d32 = d[e] > 0.0f ? d[e] * rsqrtf(d[e]) : 0.0f;
                 if (d32 == d32) {
                     const uint32_t fb = __float_as_uint(d32);
                     unsigned bin;
-                    if (fastbin) {
+                    if (bin32) {
+                        const int q = (int)(fb >> s2) + kbin32;
+                        bin = fb < 0x00800000u ? 0u : (unsigned)min(max(q, 0), SEL_BINS - 1);
+                    } else if (fastbin) {
                         const long long q = (long long)(fb >> s2) + kbin;
                         bin = fb < 0x00800000u ? 0u : (unsigned)min(max(q, 0ll), (long long)(SEL_BINS - 1));
                     } else {

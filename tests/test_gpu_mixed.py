@@ -65,6 +65,12 @@ def test_mixed_fit_close_to_fp64(name, kw, bws):
     bmx, semx, shmx, qmx, _ = emx.fit(bw, pb.adaptive, pb.kernel, False)
     beta_err = max(rel(bmx[:, k], b64[:, k]) for k in range(pb.p))
     assert beta_err <= 1e-6, beta_err
+    # element by element, over the coefficients at least 1e-3 of their column's largest:
+    # median <= 1e-7, 99th percentile <= 1e-5, none above 1e-3
+    e = np.concatenate([np.abs(bmx[m, k] - b64[m, k]) / np.abs(b64[m, k]) for k in range(pb.p)
+                        for m in [np.abs(b64[:, k]) >= 1e-3 * np.abs(b64[:, k]).max()]])
+    assert np.median(e) <= 1e-7 and np.quantile(e, 0.99) <= 1e-5 and e.max() <= 1e-3, \
+        (np.median(e), np.quantile(e, 0.99), e.max())
     assert max(rel(semx[:, k], se64[:, k]) for k in range(pb.p)) <= 1e-4
     assert rel(shmx, sh64) <= 1e-5
     assert rel(qmx, q64) <= 1e-5
