@@ -64,7 +64,7 @@ def parse():
     ap.add_argument("--mgwr-iterations", type=int, default=10)
     ap.add_argument("--rates", default="5,50,200")
     ap.add_argument("--requests", type=int, default=200, help="requests per rate (mixed form)")
-    ap.add_argument("--requests-fp64", type=int, default=100, help="requests per rate (FP64 form)")
+    ap.add_argument("--requests-fp64", type=int, default=200, help="requests per rate (FP64 form)")
     ap.add_argument("--slots", type=int, default=8)
     ap.add_argument("--precision-serve", choices=["mixed", "fp64", "both"], default="both")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -134,13 +134,14 @@ def peaks():
     return 6800.0, 1900.0, "fallback"
 
 
-def ncu_traffic(name):
-    """DRAM bytes per launch of the contraction kernel from the committed ncu summary."""
+def ncu_traffic_per_tile(name):
+    """DRAM bytes per processed 32-point tile of the contraction, from the committed
+    ncu summary (a small-case capture; the traffic grows with the tiles processed)."""
     path = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(path):
         return None
     with open(path) as f:
-        m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", f.read())
+        m = re.search(r"traffic_bytes_per_tile:\s*([0-9.eE+]+)", f.read())
     return float(m.group(1)) if m else None
 
 
@@ -670,10 +671,15 @@ def run_ours(args):
     hbm, bf16, src = peaks()
     tf32_peak = bf16 / 2.0
     achieved = stats["contract_flops"] / (stats["contract_ms"] / 1e3) / 1e12 if stats["contract_ms"] else 0.0
-    traffic = ncu_traffic("contract_tc_config2.md") if prec == Precision.Mixed else None
+    per_tile = ncu_traffic_per_tile("contract_tc_config2.md") if prec == Precision.Mixed else None
+    tiles_per_launch = stats["contract_tiles"] / max(stats["contract_launches"], 1)
+    traffic = per_tile * tiles_per_launch if per_tile else None
     if prec == Precision.Mixed:
         roof = {"bound": "tensor", "achieved": achieved, "peak": tf32_peak, "unit": "TFLOP/s",
                 "frac": achieved / tf32_peak, "traffic": traffic,
+                "traffic_note": "DRAM bytes per processed tile from the small-case ncu capture "
+                                "(profiles/contract_tc_config2.md) x mean tiles per launch of this step",
+                "tiles_per_launch": tiles_per_launch,
                 "kernel": "k_contract_tc (tcgen05 TF32x3 W.Z)",
                 "note": f"useful 2*m*P FLOPs (m=170, P=nonzero-weight pairs) / event-timed launch; peak = {src} "
                         f"bf16 burst {bf16:.0f} TF/s halved for dense TF32"}
