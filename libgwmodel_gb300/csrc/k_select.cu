@@ -42,19 +42,24 @@ constexpr int SEL_SEGS = 64;  // coarse segments of the cached histogram (64 bin
 // window that the histogram cache also uses; SelNarrow (1024 bins, 1024
 // candidates, 12 KB instead of 33 KB of shared memory, so three times the
 // CTAs per SM) runs the passes inside one cached bin.
-template <int LB_, int CAP_>
+template <int LB_, int CAP_, int THREADS_>
 struct SelCfg {
-    static constexpr int LB = LB_, BINS = 1 << LB_, CAP = CAP_, BPT = BINS / SEL_THREADS;
+    static constexpr int LB = LB_, BINS = 1 << LB_, CAP = CAP_, THREADS = THREADS_, WARPS = THREADS_ / 32,
+                         BPT = BINS / THREADS_;
     struct Shared {
         unsigned int hist[BINS];
         uint64_t cand[CAP];
-        unsigned int warp_tot[SEL_WARPS];
-        unsigned int below_w[SEL_WARPS];
+        unsigned int warp_tot[WARPS];
+        unsigned int below_w[WARPS];
         unsigned int chosen_bin, below, count, ncand;
     };
 };
-using SelWide = SelCfg<SEL_LOG_BINS, SEL_CAP>;
-using SelNarrow = SelCfg<10, 1024>;
+using SelWide = SelCfg<SEL_LOG_BINS, SEL_CAP, SEL_THREADS>;
+// Two warps per row: inside a cached bin a row's work is mostly a chain of
+// dependent loads (segment counts, bins, tile bounds, point records), so more
+// rows in flight per SM (18 CTAs resident instead of 12) matter more than more
+// lanes per row.
+using SelNarrow = SelCfg<10, 1024, 64>;
 
 struct Window {
     uint64_t base;  // bucket = (key - base) >> shift, clamped to [0, bins)
@@ -150,11 +155,11 @@ __device__ void bitonic_sort(typename C::Shared& sh, unsigned count)
 {
     unsigned len = 1;
     while (len < count) len <<= 1;
-    for (unsigned q = count + threadIdx.x; q < len; q += SEL_THREADS) sh.cand[q] = ~0ull;
+    for (unsigned q = count + threadIdx.x; q < len; q += C::THREADS) sh.cand[q] = ~0ull;
     __syncthreads();
     for (unsigned size = 2; size <= len; size <<= 1) {
         for (unsigned stride = size >> 1; stride > 0; stride >>= 1) {
-            for (unsigned t = threadIdx.x; t < len / 2; t += SEL_THREADS) {
+            for (unsigned t = threadIdx.x; t < len / 2; t += C::THREADS) {
                 unsigned i = 2 * t - (t & (stride - 1));
                 unsigned j = i + stride;
                 bool up = (i & size) == 0;
@@ -230,7 +235,7 @@ __device__ bool select_row(typename C::Shared& sh, const SelectArgs& a, const Ro
             above_thr = !(thi < 1.8e19f) ? 3e38f : thi * thi * (1.0f + 1e-5f);
         }
         const uint64_t klo = dkey(T_lo), khi = dkey(T_hi);
-        for (int b = t; b < C::BINS; b += SEL_THREADS) sh.hist[b] = 0;
+        for (int b = t; b < C::BINS; b += C::THREADS) sh.hist[b] = 0;
         if (t == 0) sh.ncand = 0;
         __syncthreads();
         unsigned below = 0;
@@ -239,8 +244,8 @@ __device__ bool select_row(typename C::Shared& sh, const SelectArgs& a, const Ro
         // a straddling super-tile is walked tile by tile, a straddling tile
         // point by point
         const int nst = (a.ntiles + 31) / 32;
-        for (int sgrp = 0; sgrp * SEL_WARPS * 32 < nst; sgrp++) {
-            const int mys = warp + SEL_WARPS * (lane + 32 * sgrp);
+        for (int sgrp = 0; sgrp * C::WARPS * 32 < nst; sgrp++) {
+            const int mys = warp + C::WARPS * (lane + 32 * sgrp);
             int scls = 1;
             if (mys < nst) scls = a.stb ? classify_tile<GEO>(a.stb[mys], c, below_thr, above_thr) : 0;
             if (scls < 0) below += (unsigned)min(32 * SEL_TILE, n - mys * 32 * SEL_TILE);
@@ -248,7 +253,7 @@ __device__ bool select_row(typename C::Shared& sh, const SelectArgs& a, const Ro
             while (sstr) {
                 const int ks = __ffs(sstr) - 1;
                 sstr &= sstr - 1;
-                const int tbase = (warp + SEL_WARPS * (ks + 32 * sgrp)) * 32;
+                const int tbase = (warp + C::WARPS * (ks + 32 * sgrp)) * 32;
                 const int mytile = tbase + lane;
                 int cls = 1;
                 if (mytile < a.ntiles) cls = classify_tile<GEO>(a.tb[mytile], c, below_thr, above_thr);
@@ -325,10 +330,10 @@ __device__ bool select_row(typename C::Shared& sh, const SelectArgs& a, const Ro
         __syncthreads();
         if constexpr (C::BINS == SEL_BINS) {  // a whole-row pass can fill the cache row
             if (pass == 0 && cache_row)
-                for (int b = t; b < SEL_BINS; b += SEL_THREADS) cache_row[b] = sh.hist[b];
+                for (int b = t; b < SEL_BINS; b += C::THREADS) cache_row[b] = sh.hist[b];
         }
         unsigned below_all = 0;
-        for (int q = 0; q < SEL_WARPS; q++) below_all += sh.below_w[q];
+        for (int q = 0; q < C::WARPS; q++) below_all += sh.below_w[q];
         const unsigned ncand = sh.ncand;
         if (a.rank <= below_all || a.rank > below_all + ncand) {
             __syncthreads();
@@ -435,7 +440,7 @@ __device__ void select_one(typename C::Shared& sh, const SelectArgs& a, int row,
             }
             __syncthreads();
         } else if constexpr (C::BINS == SEL_BINS) {
-            for (int b = t; b < SEL_BINS; b += SEL_THREADS) sh.hist[b] = cache_row[b];
+            for (int b = t; b < SEL_BINS; b += C::THREADS) sh.hist[b] = cache_row[b];
             __syncthreads();
             scan_pick<C>(sh, a.rank);
         }
@@ -469,7 +474,7 @@ __device__ void select_one(typename C::Shared& sh, const SelectArgs& a, int row,
 
 // C = SelNarrow needs a valid cache with its segment counts (hist_coarse).
 template <bool GEO, bool EXACT, class C>
-__global__ void __launch_bounds__(SEL_THREADS) k_select(SelectArgs a)
+__global__ void __launch_bounds__(C::THREADS) k_select(SelectArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     typename C::Shared& sh = *reinterpret_cast<typename C::Shared*>(smem_raw);
@@ -494,7 +499,7 @@ __device__ __forceinline__ int find_segment(const long long* __restrict__ start,
 // Many selects in one launch: segment s (its own dataset and rank) owns the
 // flattened rows [start[s], start[s + 1]).
 template <bool GEO, bool EXACT, class C>
-__global__ void __launch_bounds__(SEL_THREADS)
+__global__ void __launch_bounds__(C::THREADS)
     k_select_batch(const SelectArgs* __restrict__ segs, const long long* __restrict__ start, int nseg)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -811,7 +816,7 @@ cudaError_t launch_select_cfg(const SelectArgs& a, bool geographic, bool exact, 
 #define GW_SEL(G, E)                                                          \
     do {                                                                      \
         raise_smem_limit((const void*)k_select<G, E, C>, smem);               \
-        k_select<G, E, C><<<grid, SEL_THREADS, smem, stream>>>(a);            \
+        k_select<G, E, C><<<grid, C::THREADS, smem, stream>>>(a);             \
     } while (0)
     if (geographic) {
         if (exact) GW_SEL(true, true);
@@ -830,7 +835,7 @@ cudaError_t launch_select(const SelectArgs& a, bool geographic, bool exact, int 
     const int nrows = a.F.u ? a.F.n : a.n;
     // inside a cached bin the small window buffers fit three times the CTAs per SM
     const bool narrow = a.hist_cache && a.cache_valid && a.hist_coarse;
-    int grid = num_sms * (narrow ? 32 : 12);
+    int grid = num_sms * (narrow ? 48 : 12);
     if (grid > nrows) grid = nrows;
     return narrow ? launch_select_cfg<SelNarrow>(a, geographic, exact, grid, stream)
                   : launch_select_cfg<SelWide>(a, geographic, exact, grid, stream);
@@ -870,12 +875,12 @@ cudaError_t launch_select_batch(const SelectArgs* segs, const long long* start, 
                                 int num_sms, cudaStream_t stream)
 {
     // every segment carries a valid cache with its segment counts: the narrow window buffers
-    const int grid = num_sms * 24;
+    const int grid = num_sms * 36;
     const size_t smem = sizeof(SelNarrow::Shared);
 #define GW_SELB(G, E)                                                                                       \
     do {                                                                                                    \
         raise_smem_limit((const void*)k_select_batch<G, E, SelNarrow>, smem);                               \
-        k_select_batch<G, E, SelNarrow><<<grid, SEL_THREADS, smem, stream>>>(segs, start, nseg);            \
+        k_select_batch<G, E, SelNarrow><<<grid, SelNarrow::THREADS, smem, stream>>>(segs, start, nseg);     \
     } while (0)
     if (geographic) {
         if (exact) GW_SELB(true, true);

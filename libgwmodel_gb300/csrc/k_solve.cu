@@ -366,10 +366,28 @@ __global__ void __launch_bounds__(ST_THREADS) k_solve_crit_t(SolveArgs a)
     for (int row0 = blockIdx.x * ST_THREADS; row0 < a.n; row0 += gridDim.x * ST_THREADS) {
         const int nrow = min(ST_THREADS, a.n - row0);
         __syncwarp();
-        // coalesced loads of the block's rows of G
-        for (int lr = 0; lr < nrow; lr++) {
-            const double* g = a.G + (size_t)(row0 + lr) * a.ldg;
-            for (int q = t; q < m; q += ST_THREADS) L[(size_t)slot[q] * ST_THREADS + lr] = g[q];
+        // coalesced loads of the block's rows of G, four rows (up to 32 loads per lane) in
+        // flight before their stores: G streams from DRAM, and one row at a time left
+        // the loads waiting on each other
+        for (int lr0 = 0; lr0 < nrow; lr0 += 4) {
+            double v[4][8];  // m <= 230 columns: at most 8 per lane
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const double* g = a.G + (size_t)(row0 + lr0 + u) * a.ldg;
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    const int q = t + k * ST_THREADS;
+                    v[u][k] = (lr0 + u < nrow && q < m) ? g[q] : 0.0;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    const int q = t + k * ST_THREADS;
+                    if (lr0 + u < nrow && q < m) L[(size_t)slot[q] * ST_THREADS + lr0 + u] = v[u][k];
+                }
+            }
         }
         __syncwarp();
         const int row = row0 + t;
