@@ -55,11 +55,14 @@ struct SelCfg {
     };
 };
 using SelWide = SelCfg<SEL_LOG_BINS, SEL_CAP, SEL_THREADS>;
-// Two warps per row: inside a cached bin a row's work is mostly a chain of
-// dependent loads (segment counts, bins, tile bounds, point records), so more
-// rows in flight per SM (18 CTAs resident instead of 12) matter more than more
-// lanes per row.
+// Inside a cached bin a row's work is mostly a chain of dependent loads
+// (segment counts, bins, tile bounds, point records): for small ranks more rows
+// in flight per SM (two warps per row, 18 CTAs resident instead of 12) matter
+// more than more lanes per row; large ranks walk long rings of tiles, where
+// four warps per row are faster.
 using SelNarrow = SelCfg<10, 1024, 64>;
+using SelNarrow4 = SelCfg<10, 1024, 128>;
+constexpr unsigned kNarrow4Rank = 20000;  // ranks above this take four warps per row
 
 struct Window {
     uint64_t base;  // bucket = (key - base) >> shift, clamped to [0, bins)
@@ -835,10 +838,12 @@ cudaError_t launch_select(const SelectArgs& a, bool geographic, bool exact, int 
     const int nrows = a.F.u ? a.F.n : a.n;
     // inside a cached bin the small window buffers fit three times the CTAs per SM
     const bool narrow = a.hist_cache && a.cache_valid && a.hist_coarse;
-    int grid = num_sms * (narrow ? 48 : 12);
+    const bool wide_rows = a.rank > kNarrow4Rank;
+    int grid = num_sms * (narrow ? (wide_rows ? 32 : 48) : 12);
     if (grid > nrows) grid = nrows;
-    return narrow ? launch_select_cfg<SelNarrow>(a, geographic, exact, grid, stream)
-                  : launch_select_cfg<SelWide>(a, geographic, exact, grid, stream);
+    if (!narrow) return launch_select_cfg<SelWide>(a, geographic, exact, grid, stream);
+    return wide_rows ? launch_select_cfg<SelNarrow4>(a, geographic, exact, grid, stream)
+                     : launch_select_cfg<SelNarrow>(a, geographic, exact, grid, stream);
 }
 
 cudaError_t launch_select_hist(const SelectArgs& a, bool geographic, int num_sms, cudaStream_t stream)
