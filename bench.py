@@ -209,12 +209,21 @@ def fp64_step(pb, local):
     return info, e64, out
 
 
-def serve_stream(rate, count, precision, slots=8, budget_gb=150.0, seed=4):
+def serve_stream(rate, count, precision, slots=8, budget_gb=150.0, seed=4, budget_x_largest=None):
     """Config 4: replay a Poisson request stream through the serving loop and
-    report latency percentiles (submit to result) and throughput."""
+    report latency percentiles (submit to result) and throughput.  With
+    budget_x_largest the HBM budget is that multiple of the largest request's
+    admission estimate (admission under memory pressure)."""
     from libgwmodel_gb300 import datasets
     from libgwmodel_gb300.serve import Server, percentile, run_stream
     reqs = datasets.config4(rate, count, seed=seed)
+    if budget_x_largest:
+        probe = Server(0, hbm_budget_gb=budget_gb, slots=slots)
+        largest = max(probe.estimate(r.problem, kind=r.kind, bandwidth=r.bandwidth, precision=precision) for r in reqs)
+        big = max((r.problem for r in reqs), key=lambda pb: pb.n * pb.p)
+        largest = max(largest, probe.estimate(big, kind=0, bandwidth=50.0, precision=precision))  # the warm-up's
+        probe.close()
+        budget_gb = budget_x_largest * largest / 1e9
     srv = Server(0, hbm_budget_gb=budget_gb, slots=slots)
     # warm-up: every slot grows its buffers to the largest dataset of the pool once
     big = max((r.problem for r in reqs), key=lambda pb: pb.n * pb.p)
@@ -234,7 +243,7 @@ def serve_stream(rate, count, precision, slots=8, budget_gb=150.0, seed=4):
             "search_p50_ms": percentile(searches, 50), "search_p99_ms": percentile(searches, 99),
             "wall_s": wall, "requests_per_s": len(ok) / wall, "local_fits_per_s": fits / wall,
             "max_concurrent": st["max_concurrent"], "peak_reserved_gb": st["peak_reserved_bytes"] / 1e9,
-            "warmup_requests": int(warm["completed"])}
+            "budget_gb": budget_gb, "rejected": int(st["rejected"]), "warmup_requests": int(warm["completed"])}
 
 
 def serve_block(rates, requests, precisions):
@@ -725,9 +734,13 @@ def run_ours(args):
         rates = [float(r) for r in args.rates.split(",")]
         line["serve"] = serve_block(rates, {"mixed": args.requests, "fp64": args.requests_fp64},
                                     ["mixed", "fp64"] if args.precision_serve == "both" else [args.precision_serve])
+        from libgwmodel_gb300 import Precision as _P
+        # the same stream at 50 req/s under memory pressure: budget = 2.5 x the largest request's estimate
+        line["serve"]["mixed_budget_pressure"] = serve_stream(50.0, args.requests, _P.Mixed, budget_x_largest=2.5)
         line["serve"]["note"] = ("config 4: Poisson arrivals, 70% fits at a given adaptive bandwidth / 30% AICc "
                                  "searches, n log-uniform [1e3, 1e5], p 3..20, planar/geographic 50/50, 150 GB "
-                                 "budget, 8 slots; latency = submit to result")
+                                 "budget (mixed_budget_pressure: 2.5 x the largest request's estimate), 8 slots; "
+                                 "latency = submit to result")
     if rank == 0 and not args.no_batch:
         line["batch"] = batch_block("mixed", steps=5, warmup=2)
     if rank == 0 and not args.no_cpu:
