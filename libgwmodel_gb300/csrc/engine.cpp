@@ -954,8 +954,21 @@ const double* Engine::orderStatistic(unsigned rank)
         hist_valid_ = true;
         a.cache_valid = 1;
     }
+    // geographic mixed data whose distance cache is filled: the select reads the
+    // histogram pass's proxy values from it instead of recomputing them
+    DeviceD2Cache& dc = device_d2c(device_);
+    std::unique_lock<std::mutex> lk(dc.mu, std::defer_lock);
+    if (geographic_ && precision_ == kMixed && d2c_valid_) {
+        lk.lock();
+        if (dc.owner == this && d2c_valid_ && dc.ptr) a.d2c = dc.ptr;
+        else lk.unlock();
+    }
     check(launch_select(a, geographic_, exact, num_sms_, stream_), "select");
     stats_.kernel_launches += 1;
+    if (a.d2c) {
+        check(cudaEventRecord(dc.used, stream_), "cudaEventRecord");
+        lk.unlock();
+    }
     if (hist_.get()) hist_valid_ = true;
     ranks_.push_back(std::move(r));
     return ranks_.back()->v.get();

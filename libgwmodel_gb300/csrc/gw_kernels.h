@@ -39,6 +39,9 @@ struct SelectArgs {
     // Geographic data rows only (F.u null), or null: the histogram pass also
     // fills this distance cache (layout of launch_fill_d2) from the same values.
     float* d2c_out;
+    // Geographic data rows only, or null: the distance cache that histogram pass
+    // filled; the selects read their proxy values from it instead of recomputing them.
+    const float* d2c;
 };
 // exact: FP64 order statistics (bit-exact); otherwise the FP32 proxy's.
 cudaError_t launch_select(const SelectArgs& a, bool geographic, bool exact, int num_sms, cudaStream_t stream);

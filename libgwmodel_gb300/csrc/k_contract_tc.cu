@@ -203,6 +203,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const float s_cut = (GEO && kernel >= GW_KERNEL_BISQUARE) ? geo_s_cut(rr) : __int_as_float(0x7f800000);
     const float fz = fa.z + fb.z;  // sin(lat) of the focus
     const int self_j = a.exclude_self ? i : -1;
+    // tiles that may hold a self pair of this block's rows (none without exclude_self)
+    const int self_t0 = a.exclude_self ? row0 / TC_BK : a.ntiles, self_t1 = (row0 + TC_M - 1) / TC_BK;
     const bool square = a.wpow == 2;
 
     // block bound and largest threshold for tile skipping
@@ -253,11 +255,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         for (int tnext = walk.next(); tnext >= 0; k++) {
             const int tile = tnext;
             tnext = walk.next();
-            if (__any_sync(0xffffffffu, *(volatile int*)&ctl.abort != 0)) {
+            // another role's timeout: every wait is bounded too, so a look every 16 tiles is enough
+            if ((k & 15) == 0 && __any_sync(0xffffffffu, *(volatile int*)&ctl.abort != 0)) {
                 ok = false;
                 break;
             }
             const int s = k & 1;
+            // no self pair and no padding point in this tile: the per-pair checks drop out
+            const bool plain = (tile + 1) * TC_BK <= a.n && (self_j < 0 || tile < self_t0 || tile > self_t1);
             if (prof) c0 = clock64();
             // weight stage s is free once the MMAs of tile k - 2 are done
             const bool stage_ok =
@@ -293,13 +298,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     // the block is [quarter 4][half 2][row 128][4 points]: row r, points kbase + 4 q4 .. + 3
                     const float4 dv = tp[(2 * quarter + q4) * TC_M + r];
                     const float dd[4] = {dv.x, dv.y, dv.z, dv.w};
+                    if (plain) {
 #pragma unroll
-                    for (int e = 0; e < 4; e++) {
-                        const int j = tile * TC_BK + kbase + q4 * 4 + e;
-                        float v = weight32(kernel, dd[e], rr, inv_r2);
-                        v = (j == self_j) ? 0.0f : v;
-                        v = square ? v * v : v;
-                        w[e] = (row_ok && j < a.n) ? v : 0.0f;
+                        for (int e = 0; e < 4; e++) {
+                            float v = weight32(kernel, dd[e], rr, inv_r2);
+                            v = square ? v * v : v;
+                            w[e] = row_ok ? v : 0.0f;
+                        }
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < 4; e++) {
+                            const int j = tile * TC_BK + kbase + q4 * 4 + e;
+                            float v = weight32(kernel, dd[e], rr, inv_r2);
+                            v = (j == self_j) ? 0.0f : v;
+                            v = square ? v * v : v;
+                            w[e] = (row_ok && j < a.n) ? v : 0.0f;
+                        }
                     }
                 } else {
 #pragma unroll
@@ -321,7 +335,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     for (int e = 0; e < 4; e++) {
                         const int kk = kbase + q4 * 4 + e;
                         float d2;
-                        if (GEO) d2 = near ? geo_d2_near(g[e]) : geo_d2_from_chord(g[e]);
+                        if (GEO) d2 = near ? geo_d2_near(g[e]) : geo_d2_far(g[e], fa, fb, tp[2 * kk], tp[2 * kk + 1]);
                         else d2 = planar_d2_32(fa, tp[kk]);
                         float v = weight32(kernel, d2, rr, inv_r2);
                         v = (tile * TC_BK + kk == self_j) ? 0.0f : v;
@@ -430,7 +444,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             // run-time values are long dependent chains on this critical thread
             int sb = 0, zpar = 0, kf = 0, c = 0;
             for (int tile = wm.next(); tile >= 0; tile = wm.next(), k++) {
-                if (*(volatile int*)&ctl.abort) break;
+                if ((k & 15) == 0 && *(volatile int*)&ctl.abort) break;
                 const int s = k & 1;
                 if (prof) c0 = clock64();
                 if (!mbar_wait(&ctl.full_a[s], (uint32_t)((k >> 1) & 1), lim)) {
@@ -729,7 +743,8 @@ __global__ void __launch_bounds__(512) k_fill_d2(int n, int ntiles, const float4
 #pragma unroll
             for (int e = 0; e < 4; e++) {
                 const int j = tile * TC_BK + quarter * 8 + q4 * 4 + e;
-                const float d2 = near ? geo_d2_near(g[e]) : geo_d2_from_chord(g[e]);
+                const size_t jr = (size_t)j;
+                const float d2 = near ? geo_d2_near(g[e]) : geo_d2_far(g[e], fa, fb, pts[2 * jr], pts[2 * jr + 1]);
                 d[e] = (i < n && j < n) ? d2 : 3.402823466e38f;
             }
             __stcs(out + (size_t)tile * 1024 + q4 * 128, make_float4(d[0], d[1], d[2], d[3]));

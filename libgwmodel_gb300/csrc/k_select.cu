@@ -216,7 +216,7 @@ __device__ __forceinline__ int classify_tile(const float4& tb, const RowCtx& c, 
 // histogram (coarse log window over [0, +inf]) in cache_row.
 template <bool GEO, bool EXACT, class C>
 __device__ bool select_row(typename C::Shared& sh, const SelectArgs& a, const RowCtx& c, double T_lo, double T_hi, Window w,
-                           unsigned* cache_row, double& result)
+                           unsigned* cache_row, const float* d2r, double& result)
 {
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const int n = a.n;
@@ -230,7 +230,8 @@ __device__ bool select_row(typename C::Shared& sh, const SelectArgs& a, const Ro
             const float a2 = 2.0f * 6378.137f;
             const float f = 1.0f / 298.257223563f;
             const float wl = tlo / (a2 * (1.0f + f));
-            below_thr = !(wl > 0.0f) ? -1.0f : (wl >= 1.5f ? 1e30f : 2.0f * sinf(wl) * (1.0f - 1e-5f));
+            // D <= 2 a w (1 + f) for every half angle w <= pi/2: beyond pi/2 every point is below
+            below_thr = !(wl > 0.0f) ? -1.0f : (wl >= 1.5708f ? 1e30f : 2.0f * sinf(wl) * (1.0f - 1e-5f));
             const float wh = thi / (a2 * (1.0f - 2.6f * f));
             above_thr = !(wh < 1.2f) ? 1e30f : 2.0f * sinf(wh) * (1.0f + 1e-5f);
         } else {
@@ -273,10 +274,17 @@ __device__ bool select_row(typename C::Shared& sh, const SelectArgs& a, const Ro
                     // with the near-angle form when the whole warp is within 60 degrees
                     float d32;
                     if (GEO) {
-                        const GeoChord g = geo_chord32(c.fa, c.fb, c.fa.z + c.fb.z, a.pts[2 * (size_t)j],
-                                                       a.pts[2 * (size_t)j + 1]);
-                        const float d2 = __all_sync(0xffffffffu, g.S <= 0.25f) ? geo_d2_near(g) : geo_d2_from_chord(g);
-                        d32 = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
+                        float d2;
+                        if (d2r) {
+                            // the same value from the distance cache: point `lane` of the
+                            // tile sits at [quarter lane / 8][half (lane / 4) % 2][row][lane % 4]
+                            d2 = __ldg(d2r + (size_t)tile * 4096 + (lane >> 2) * 512 + (lane & 3));
+                        } else {
+                            const float4 pa = a.pts[2 * (size_t)j], pb = a.pts[2 * (size_t)j + 1];
+                            const GeoChord g = geo_chord32(c.fa, c.fb, c.fa.z + c.fb.z, pa, pb);
+                            d2 = __all_sync(0xffffffffu, g.S <= 0.25f) ? geo_d2_near(g) : geo_d2_far(g, c.fa, c.fb, pa, pb);
+                        }
+                        d32 = d2 > 0.0f ? d2 * rsqrt_ftz(d2) : 0.0f;
                     } else {
                         d32 = sqrtf(planar_d2_32(c.fa, a.pts[j]));
                     }
@@ -456,14 +464,17 @@ __device__ void select_one(typename C::Shared& sh, const SelectArgs& a, int row,
         w = linear_window<C>(lo, hi);
         cache_row = nullptr;
     }
+    // the row's slice of the distance cache: block row / 128, row row % 128
+    const float* d2r =
+        GEO && a.d2c && !a.F.u ? a.d2c + (size_t)(row >> 7) * a.ntiles * 4096 + (size_t)(row & 127) * 4 : nullptr;
     double q = __longlong_as_double(0x7ff8000000000000ll);
-    if (ok) ok = select_row<GEO, false, C>(sh, a, c, T_lo, T_hi, w, a.cache_valid ? nullptr : cache_row, q);
+    if (ok) ok = select_row<GEO, false, C>(sh, a, c, T_lo, T_hi, w, a.cache_valid ? nullptr : cache_row, d2r, q);
     double result = q;
     // stage B: the reference's FP64 value, inside the proxy band around q
     if (EXACT && ok) {
         const double lo = q * (1.0 - a.eps) - a.delta, hi = q * (1.0 + a.eps) + a.delta;
         const double blo = lo > 0.0 ? lo : 0.0;
-        ok = select_row<GEO, true, C>(sh, a, c, blo, hi, linear_window<C>(dkey(blo), dkey(hi)), nullptr, result);
+        ok = select_row<GEO, true, C>(sh, a, c, blo, hi, linear_window<C>(dkey(blo), dkey(hi)), nullptr, d2r, result);
     }
     if (t == 0) {
         if (!ok) {
@@ -586,8 +597,8 @@ __device__ void hist_rows(unsigned* hs, float4 (*rf)[2], const SelectArgs& a, in
                     const float4 rb = rf[r][1];
                     const GeoChord gc = geo_chord32(ra, rb, ra.z + rb.z, pa, pb);
                     const bool near = __all_sync(0xffffffffu, gc.S <= 0.25f);
-                    const float d2 = near ? geo_d2_near(gc) : geo_d2_from_chord(gc);
-                    d32 = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
+                    const float d2 = near ? geo_d2_near(gc) : geo_d2_far(gc, ra, rb, pa, pb);
+                    d32 = d2 > 0.0f ? d2 * rsqrt_ftz(d2) : 0.0f;
                 } else {
                     d32 = sqrtf(planar_d2_32(ra, pa));
                 }
@@ -694,16 +705,20 @@ __device__ void hist_rows_fill(unsigned* hs, float4 (*rf)[2], const SelectArgs& 
             for (int e = 0; e < 4; e++) g[e] = geo_chord32(ra, rb, fz, tp[2 * (q4 * 4 + e)], tp[2 * (q4 * 4 + e) + 1]);
             const bool near = __all_sync(0xffffffffu, fmaxf(fmaxf(g[0].S, g[1].S), fmaxf(g[2].S, g[3].S)) <= 0.25f);
             float d[4];
+            if (near) {  // warp-uniform: the far form's extra work only where a pair needs it
 #pragma unroll
-            for (int e = 0; e < 4; e++) {
-                const float d2 = near ? geo_d2_near(g[e]) : geo_d2_from_chord(g[e]);
-                d[e] = q4 * 4 + e < nv ? d2 : 3.402823466e38f;
+                for (int e = 0; e < 4; e++) d[e] = geo_d2_near(g[e]);
+            } else {
+#pragma unroll
+                for (int e = 0; e < 4; e++) d[e] = geo_d2_far(g[e], ra, rb, tp[2 * (q4 * 4 + e)], tp[2 * (q4 * 4 + e) + 1]);
             }
+#pragma unroll
+            for (int e = 0; e < 4; e++) d[e] = q4 * 4 + e < nv ? d[e] : 3.402823466e38f;
             if (row_ok) __stcs(out + (size_t)tile * 1024 + q4 * 128, make_float4(d[0], d[1], d[2], d[3]));
 #pragma unroll
             for (int e = 0; e < 4; e++) {
                 if (q4 * 4 + e >= nv) continue;
-                const float d32 = d[e] > 0.0f ? d[e] * rsqrtf(d[e]) : 0.0f;
+                const float d32 = d[e] > 0.0f ? d[e] * rsqrt_ftz(d[e]) : 0.0f;
                 if (d32 == d32) {
                     const uint32_t fb = __float_as_uint(d32);
                     unsigned bin;

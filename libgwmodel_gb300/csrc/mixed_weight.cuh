@@ -12,6 +12,25 @@ namespace gwgpu {
 // z_lo, 0), so z = sin(lat).  Planar: one float4 (u_hi, u_lo, v_hi, v_lo)
 // relative to the centroid.
 
+// The hardware approximations of 1/sqrt(x) and 1/x with subnormal inputs and
+// results flushed to zero.  The proxy arithmetic never meets a subnormal (its
+// smallest nonzero intermediate values are near 1e-31), so the flush costs no
+// precision and saves the subnormal handling; every proxy value of every
+// kernel is computed with these, so all kernels see the same values.
+__device__ __forceinline__ float rsqrt_ftz(float x)
+{
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ float rcp_ftz(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // asin(x) / x as a polynomial in S = x^2 on [0, 0.25]: the degree-5 Chebyshev
 // interpolant at the Chebyshev nodes of that interval, converted to monomials
 // (largest relative deviation 4.8e-9, below FP32 rounding).
@@ -59,40 +78,57 @@ __device__ __forceinline__ GeoChord geo_chord32(const float4& fa, const float4& 
 //   c = (f / 8) [(3 sqrt C - A) zs^2 S - (3 sqrt C + A) dz^2 C] / (A S C),
 // so Q = A + (f / 8) num / (S C): A cancels from the correction.  num is
 // O(S) (|dz| <= 2 sqrt S), so clamping S C below at 1e-30 only keeps the
-// reciprocal finite: S = 0 gives Q = A and D = 0.
-__device__ __forceinline__ float geo_lambert_d2(const GeoChord& g, float A)
+// reciprocal finite: S = 0 gives Q = A and D = 0.  Towards the antipode num is
+// O(C) (zs^2 <= 4 C), so the correction stays bounded given accurate C and zs.
+// Here cq = sqrt(C).
+__device__ __forceinline__ float geo_lambert_d2(const GeoChord& g, float A, float C, float cq)
 {
     const float S = g.S;
-    const float C = fmaxf(1.0f - S, 0.0f);
-    const float cq = C * rsqrtf(C);
     const float t1 = fmaf(3.0f, cq, -A), t2 = fmaf(3.0f, cq, A);
     const float num = fmaf(t1 * (g.zs * g.zs), S, -(t2 * (g.dz * g.dz)) * C);
-    const float Q = fmaf((0.125f * kGeoF) * num, __fdividef(1.0f, fmaxf(S * C, 1e-30f)), A);
+    const float Q = fmaf((0.125f * kGeoF) * num, rcp_ftz(fmaxf(S * C, 1e-30f)), A);
     return kGeoK * S * (Q * Q);
 }
 
-// Half angles up to 60 degrees (S <= 0.25): A from the polynomial directly.
-// The caller makes sure S <= 0.25.
-__device__ __forceinline__ float geo_d2_near(const GeoChord& g) { return geo_lambert_d2(g, asin_over_x(g.S)); }
+// Half angles up to 60 degrees (S <= 0.25): A from the polynomial directly and
+// C = 1 - S (at least 0.75: no precision lost).  The caller makes sure S <= 0.25.
+__device__ __forceinline__ float geo_d2_near(const GeoChord& g)
+{
+    const float C = fmaxf(1.0f - g.S, 0.0f);
+    return geo_lambert_d2(g, asin_over_x(g.S), C, C * rsqrt_ftz(C));
+}
 
-// Any S: beyond 0.25, asin x = pi/2 - 2 asin(sqrt y) with y = (1 - x) / 2
+// Any S, from the chord terms g of the focus record (fa, fb) and the point
+// record (pa, pb).  Beyond S = 0.25 C = cos^2 w = |f + p|^2 / 4 and zs come
+// from the sums of the two unit vectors (hi + lo), which keep their relative
+// precision towards the antipode where 1 - S and 2 fz + dz lose it, and
+// asin x = pi/2 - 2 asin(sqrt y) with y = (1 - sqrt S) / 2 = C / (2 (1 + sqrt S))
 // <= 0.25 reuses the polynomial.  Branch-free (the cases are selects), and
 // equal to geo_d2_near wherever S <= 0.25.
-__device__ __forceinline__ float geo_d2_from_chord(const GeoChord& g)
+__device__ __forceinline__ float geo_d2_far(const GeoChord& g, const float4& fa, const float4& fb, const float4& pa,
+                                            const float4& pb)
 {
     const float S = g.S;
     const bool near = S <= 0.25f;
-    const float rs = rsqrtf(S);
-    const float y = 0.5f - 0.5f * (S * rs);  // (1 - sqrt S) / 2
+    const float sx = (pa.x + fa.x) + (pb.x + fb.x);
+    const float sy = (pa.y + fa.y) + (pb.y + fb.y);
+    const float sz = (pa.z + fa.z) + (pb.z + fb.z);  // sin phi_p + sin phi_f
+    const float C = near ? fmaxf(1.0f - S, 0.0f) : 0.25f * fmaf(sx, sx, fmaf(sy, sy, sz * sz));
+    const float cq = C > 0.0f ? C * rsqrt_ftz(C) : 0.0f;
+    const float rs = rsqrt_ftz(S);
+    const float y = C * rcp_ftz(fmaf(2.0f, S * rs, 2.0f));  // (1 - sqrt S) / 2
     const float z = near ? S : y;
     const float Pz = asin_over_x(z);
-    const float far_w = fmaf(-2.0f * (z * rsqrtf(z)), Pz, 1.5707963267948966f);  // asin(sqrt S)
-    return geo_lambert_d2(g, near ? Pz : far_w * rs);
+    const float zr = z > 0.0f ? z * rsqrt_ftz(z) : 0.0f;
+    const float far_w = fmaf(-2.0f * zr, Pz, 1.5707963267948966f);  // asin(sqrt S)
+    GeoChord h = g;
+    h.zs = near ? g.zs : sz;
+    return geo_lambert_d2(h, near ? Pz : far_w * rs, C, cq);
 }
 
 __device__ __forceinline__ float geo_d2_32(const float4& fa, const float4& fb, const float4& pa, const float4& pb)
 {
-    return geo_d2_from_chord(geo_chord32(fa, fb, fa.z + fb.z, pa, pb));
+    return geo_d2_far(geo_chord32(fa, fb, fa.z + fb.z, pa, pb), fa, fb, pa, pb);
 }
 
 // True when a pair with haversine term S lies beyond a compact kernel's
@@ -103,7 +139,7 @@ __device__ __forceinline__ bool geo_beyond(float S, float s_cut) { return S >= s
 __device__ __forceinline__ float geo_dist32(const float4& fa, const float4& fb, const float4& pa, const float4& pb)
 {
     const float d2 = geo_d2_32(fa, fb, pa, pb);
-    return d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
+    return d2 > 0.0f ? d2 * rsqrt_ftz(d2) : 0.0f;
 }
 
 // Haversine cut-off of a focus row for a compactly supported kernel with

@@ -50,6 +50,17 @@ def test_cached_criterion_bit_identical(kernel, adaptive, bws, crit):
     assert not plain.distance_cache_active()
 
 
+@pytest.mark.parametrize("n,bws", [(2345, [2, 25, 300, 1000, 2344]), (25003, [21000, 4000, 60])])
+def test_cached_thresholds_bit_identical(n, bws):
+    """The selects of the cached engine read the proxy distances from the
+    cache (both select widths: ranks above 20,000 take the four-warp form)."""
+    x, y, coords = sphere_problem(n, 3, 15)
+    cached, plain = engines(x, y, coords)
+    for bw in bws:
+        np.testing.assert_array_equal(cached.thresholds(bw), plain.thresholds(bw), err_msg=str(bw))
+    assert cached.distance_cache_active()
+
+
 def test_cached_fit_bit_identical():
     x, y, coords = sphere_problem(3001, 6, 12)
     cached, plain = engines(x, y, coords)

@@ -73,6 +73,35 @@ def test_antimeridian_and_high_latitude(bw, gc_host):
     assert abs(got - ref) <= 1e-5 * abs(ref)
 
 
+def test_whole_sphere_smallest_and_largest_ranks(gc_host):
+    """25,003 points over the whole sphere, so dozens of pairs lie within
+    4e-4 rad of each other's antipode: the FP32 proxy of such a pair keeps its
+    precision (the exact select's band around it holds), and a window that
+    reaches past 19,200 km still classifies tiles below it correctly.  Rows:
+    the 24 whose nearest antipodal neighbour is closest, and 24 at random."""
+    rng = np.random.default_rng(44)
+    n = 25003
+    lon = rng.uniform(-180.0, 180.0, n)
+    lat = np.degrees(np.arcsin(rng.uniform(-0.999, 0.999, n)))
+    x, y, c = problem(n, 3, np.column_stack([lon, lat]), 45)
+    lo, la = np.radians(c[:, 0]), np.radians(c[:, 1])
+    u = np.column_stack([np.cos(la) * np.cos(lo), np.cos(la) * np.sin(lo), np.sin(la)])
+    anti = np.concatenate([np.max(-(u[s:s + 2048] @ u.T), axis=1) for s in range(0, n, 2048)])
+    rows = sorted(set(np.argsort(-anti)[:24].tolist()) | set(rng.choice(n, 24, replace=False).tolist()))
+    assert anti[rows].max() > 1.0 - 2e-8  # a pair within 2e-4 rad of the antipode
+    libm, cr = geo_rows(c, rows, gc_host)
+    e = Engine(0)
+    e.set_data(x, y, c, True)
+    m = Engine(0)
+    m.set_data(x, y, c, True)
+    m.set_precision(Precision.Mixed)
+    for bw in (2, 25, 4000, n - 1):
+        got = e.thresholds(bw)
+        check_geo_thresholds(got[rows], libm, cr, bw)
+        mixed = m.thresholds(bw)
+        assert np.max(np.abs(mixed - got) / got) <= 1e-5, bw
+
+
 @pytest.mark.parametrize("n", [3, 4, 5])
 def test_smallest_problems(n):
     """At n = 3 a boxcar of 3 neighbours leaves 2 points for 2 coefficients: an
