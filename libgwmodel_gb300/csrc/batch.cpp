@@ -303,7 +303,8 @@ private:
             const Engine& e = *eng_[segs_[s].q];
             off_row[s + 1] = off_row[s] + e.n_;
             off_g[s + 1] = off_g[s] + (size_t)e.n_ * e.m_;
-            off_acc[s + 1] = off_acc[s] + (precision_ == kMixed ? (size_t)e.n_ * e.npad_ : 0);
+            // rows in groups of 128 (the contraction's layout)
+            off_acc[s + 1] = off_acc[s] + (precision_ == kMixed ? (size_t)(e.n_ + 127) / 128 * 128 * e.npad_ : 0);
         }
         rows_total_ = off_row[S];
         seg_g_.resize(S);

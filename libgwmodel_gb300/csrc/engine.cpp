@@ -724,7 +724,8 @@ void Engine::ensureMixed()
     ys_.alloc(n);
     zs_.alloc((size_t)n * m_);
     zimg_.alloc((size_t)ntiles32_ * 2 * npad_ * 128);
-    acc_.alloc((size_t)n * npad_);
+    acc_.alloc((size_t)(n + 127) / 128 * 128 * npad_);  // rows in groups of 128 (the contraction's layout)
+    stage_.alloc((size_t)(n + 127) / 128 * 128 * npad_);
     thr32_.alloc(n);
     err_.alloc(1);
     tinv_.alloc(p);
@@ -817,6 +818,7 @@ void Engine::contractMixed(double* G, int ldg, int mcols, double bw, bool adapti
     a.wait_limit = tc_wait_limit_;
     a.wpow = wpow;
     a.acc = acc_.get();
+    a.stage = stage_.get();
     a.G = G;
     a.ldg = ldg;
     a.err = err_.get();
@@ -1263,7 +1265,8 @@ size_t Engine::estimateBytes(int n, int p, bool geographic, bool mixed, bool ada
     b += 32 * t16 * (1 + g) + 32 * t32 * (1 + g);                     // tile boxes and caps (16 and 32 points)
     b += 16 * t32 * 32 * (1 + g) + 16 * t32 + 20 * t16;               // point records, tile bounds, tile thresholds
     b += 8 * N * kMaxP + 8 * (kMaxP * (kMaxP + 3) / 2 + kMaxP);       // variable-selection scratch
-    if (mixed) b += 8 * N * (P + 1 + m) + t32 * 2 * npad * 128 + 8 * N * npad + 4 * N;
+    const double n128 = std::ceil(N / 128) * 128;                    // rows of the contraction's sums
+    if (mixed) b += 8 * N * (P + 1 + m) + t32 * 2 * npad * 128 + 12 * n128 * npad + 4 * N;
     b += 8 * N * (mm + 2 * P + 2);                                    // fit: G2, v, betasSE, qDiag, S row
     if (adaptive) {
         const double h = 4.0 * (4096 + 64) * N;  // histograms and their segment counts
@@ -1282,7 +1285,7 @@ size_t Engine::bytesHeld() const
                tiles_.capacityBytes() + caps_.capacityBytes() + boxes32_.capacityBytes() + caps32_.capacityBytes() +
                rvec_.capacityBytes() + pts32_.capacityBytes() + tbsel_.capacityBytes() + tb16_.capacityBytes() +
                tile_thr16_.capacityBytes() + xs_.capacityBytes() + ys_.capacityBytes() + zs_.capacityBytes() +
-               zimg_.capacityBytes() + acc_.capacityBytes() + thr32_.capacityBytes() + g2_.capacityBytes() +
+               zimg_.capacityBytes() + acc_.capacityBytes() + stage_.capacityBytes() + thr32_.capacityBytes() + g2_.capacityBytes() +
                vvec_.capacityBytes() + bse_.capacityBytes() + qdiag_.capacityBytes() + S_.capacityBytes() +
                hist_.capacityBytes() + hcoarse_.capacityBytes() + xsub_.capacityBytes() + gsub_.capacityBytes() + stb_.capacityBytes();
     for (auto& r : ranks_) b += r->v.capacityBytes();

@@ -285,6 +285,7 @@ private:
     DevBuf<TileCap> caps32_;
     DevBuf<double> rvec_;
     DevBuf<float2> acc_;
+    DevBuf<float> stage_;
     DevBuf<float> thr32_;
     DevBuf<int> err_;
     long long d2c_limit_bytes_ = -1;

@@ -166,7 +166,8 @@ struct TcArgs {
     const float* thr;             // per-row threshold, or null for the fixed bandwidth bw
     float bw;
     int kernel, exclude_self, skip, flush_tiles, wpow;
-    float2* acc;                  // n x npad double-float accumulators
+    float2* acc;                  // double-float sums: ceil(n / 128) x npad x 128 (rows in groups of 128)
+    float* stage;                 // FP32 staging of one chunk, same layout (single-accumulator form), or null
     double* G;                    // n x ldg FP64 output (first mcols columns)
     int ldg;
     int* err;                     // set to 1 if a bounded wait timed out

@@ -6,8 +6,8 @@
 //    data tile in FP32 from the point records (planar or WGS-84 great-circle,
 //    prefetched into shared memory by a bulk copy two tiles ahead) or from
 //    the distance cache, split every weight into TF32 hi + lo and write both
-//    into tensor memory (tcgen05.st; two weight stages) or, for npad > 192,
-//    into shared memory in the 128-byte-swizzled K-major layout;
+//    into tensor memory (tcgen05.st; five weight stages) or, for npad > 192,
+//    into shared memory in the 128-byte-swizzled K-major layout (two stages);
 //  * the matching Z~ tile (scaled/centred products, split hi + lo, stored in
 //    global memory already in the swizzled image) arrives by 1-D bulk copies
 //    issued by one thread of a copy warp, up to four stages ahead (three with
@@ -21,11 +21,13 @@
 //    two thirds of the time.  Both single-thread loops keep their stage and
 //    chunk positions as counters: a division by a run-time value there costs
 //    a dependent chain on the thread that gates the whole CTA;
-//  * chunks of flush_tiles tiles alternate between two TMEM accumulators; four
-//    drain warps (one per TMEM lane quadrant) read a finished chunk back with
-//    tcgen05.ld and add it into double-float (hi, lo) sums in global memory,
-//    so FP32 rounding never sums more than a chunk of points, the tensor core
-//    never waits for a drain and the producers never drain.
+//  * chunks of flush_tiles tiles accumulate in TMEM; four drain warps (one per
+//    TMEM lane quadrant) read a finished chunk back with tcgen05.ld and add it
+//    into double-float (hi, lo) sums in global memory, so FP32 rounding never
+//    sums more than a chunk of points.  With weights in tensor memory there is
+//    one accumulator: the drain first copies it out to a staging buffer
+//    (coalesced, a few microseconds) and releases it, and adds the staged
+//    values while the next chunk runs; otherwise two accumulators alternate.
 // Compactly supported kernels skip data tiles farther than the block's
 // largest threshold (FP32 tile bounds) and, for great-circle distances, pairs
 // beyond the row's haversine cut-off.  Every wait is bounded and reports
@@ -53,28 +55,32 @@ constexpr int TC_PROD_WARPS = 16;
 constexpr int TC_PROD = TC_PROD_WARPS * 32;   // producer threads
 constexpr int TC_DRAIN_WARPS = 4;             // one per TMEM lane quadrant
 constexpr int TC_CTRL_WARP = TC_PROD_WARPS + TC_DRAIN_WARPS;  // issues the MMAs
-constexpr int TC_COPY_WARP = TC_CTRL_WARP + 1;                 // issues the bulk copies
-constexpr int TC_THREADS = TC_PROD + TC_DRAIN_WARPS * 32 + 64;
+constexpr int TC_COPY_WARP = TC_CTRL_WARP + 1;                 // issues the Z copies
+constexpr int TC_PCOPY_WARP = TC_COPY_WARP + 1;                // issues the point / distance-block copies
+constexpr int TC_THREADS = TC_PROD + TC_DRAIN_WARPS * 32 + 96;
+constexpr int TC_MAX_NP = 3;  // point / distance-block buffers at most
 constexpr int TC_M = 128;
 constexpr int TC_BK = 32;  // points per stage (128 bytes of TF32 per row)
 constexpr uint32_t TC_A_BYTES = TC_M * 128;  // one split part of the weight tile
 constexpr uint32_t TC_WAIT = 1u << 22;
 constexpr uint32_t TC_ACC_COLS = 256;  // TMEM column of the second accumulator
-// Weights in tensor memory (npad <= 192): accumulators at columns 0 and 192,
-// weight stage s at 384 + 64 s (hi: 32 columns, then lo: 32 columns)
+// Weights in tensor memory (npad <= 192): one accumulator at column 0 and
+// TC_ATM_STAGES weight stages at 192 + 64 s (hi: 32 columns, then lo: 32 columns)
 constexpr uint32_t TC_ATM_ACC_COLS = 192;
-constexpr uint32_t TC_ATM_A_COL = 384;
+constexpr uint32_t TC_ATM_A_COL = 192;
+constexpr int TC_ATM_STAGES = 5;
+constexpr int TC_DONE_SLOTS = 8;  // tile_done slots: tile k commits to slot k % 8
 constexpr int TC_MAX_NB = 4;           // Z stages at most
 constexpr uint32_t TC_P_MAX = 2u * 16u * TC_BK;  // point records of one tile, geographic
 constexpr uint32_t TC_D_BYTES = TC_M * TC_BK * 4;  // one cached 128 x 32 distance block
 
 struct Smem {
-    uint64_t full_a[2];          // weight tile k written: one arrival per producer warp
-    uint64_t tile_done[4];       // tcgen05.commit after the MMAs of tile k (slot k % 4; every earlier MMA too)
+    uint64_t full_a[TC_ATM_STAGES];       // weight tile k written: one arrival per producer warp
+    uint64_t tile_done[TC_DONE_SLOTS];    // tcgen05.commit after the MMAs of tile k (every earlier MMA too)
     uint64_t full_b[TC_MAX_NB];  // Z tile landed (bulk copy)
-    uint64_t full_p[2];          // point records or cached distances of a tile landed (bulk copy)
-    uint64_t tmem_free[2];       // accumulator drained: one arrival per drain warp
-    uint64_t acc_full[2];        // tcgen05.commit after the last MMA of a chunk into accumulator c % 2
+    uint64_t full_p[TC_MAX_NP];  // point records or cached distances of a tile landed (bulk copy)
+    uint64_t tmem_free[2];       // accumulator drained (read out): one arrival per drain warp
+    uint64_t acc_full[2];        // tcgen05.commit after the last MMA of a chunk
     uint32_t tmem_base;
     int abort;
     int ktotal;                  // tiles this CTA visits
@@ -104,6 +110,14 @@ struct TileWalker {
     }
 };
 
+// Element (row, col) of the double-float sums and of the staging buffer: rows
+// in groups of 128, column-major inside a group, so the 32 lanes of a drain
+// warp (32 consecutive rows) touch 32 consecutive elements of one column.
+__device__ __forceinline__ size_t acc_at(int row, int col, int npad)
+{
+    return ((size_t)(row >> 7) * npad + col) * TC_M + (row & (TC_M - 1));
+}
+
 // Double-float accumulate: (hi, lo) += v.
 __device__ __forceinline__ float2 df_add(float2 a, float v)
 {
@@ -124,26 +138,39 @@ __device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity, uint32
 // points [8 quarter, 8 quarter + 8) of row r); warps 16-19 drain the
 // accumulators (warp 16 + q owns TMEM lanes 32 q .. 32 q + 31, all columns);
 // lane 0 of warp 20 issues the MMAs and lane 0 of warp 21 the bulk copies
-// (Z stage j % nb is refilled once tile_done[j % 4] reports the MMAs of tile j done;
-// the same commit frees weight stage j % 2 for the producers).  Tile k uses weight
-// stage k % 2, Z stage k % nb and point buffer k % 2; chunk c = k / F of F
-// tiles accumulates in TMEM accumulator c % 2, whose last MMA commits to
-// acc_full[c % 2]; the drain warps then add it into the double-float sums and
-// release it through tmem_free[c % 2].
+// (Z stage j % nb is refilled once tile_done[j % 8] reports the MMAs of tile j
+// done; the same commit frees weight stage j % NW for the producers).  Tile k
+// uses weight stage k % NW, Z stage k % nb and point buffer k % 2 (refilled
+// once full_a reports the producers done with tile k).  Chunk c = k / F of F
+// tiles accumulates in TMEM accumulator c % NACC, whose last MMA commits to
+// acc_full; the drain warps read it out and release it through tmem_free.
+// Every single-thread wait is for a barrier phase whose successor needs an
+// action of that thread still to come, so no waiter can fall two phases behind.
 // KERN: the weight kernel when fixed at compile time, -1 to read it from the arguments.
 // BATCH: CTA b works on segment work[b].x (arguments segs[work[b].x]) at row
 // block work[b].y, so one launch covers many datasets and bandwidths.
 // CACHED: weights from the distance cache a.d2c (geographic, single dataset only).
 // ATM: the weight tiles live in tensor memory (written with tcgen05.st, read by
 // the MMA as its A operand), which frees their 64 KB of shared memory for a
-// fourth Z stage and takes their traffic off shared memory; npad <= 192.
+// fourth Z stage and takes their traffic off shared memory; npad <= 192.  With
+// one accumulator beside them tensor memory holds five weight stages, so the
+// producers run up to five tiles ahead of the MMAs instead of two (the
+// producer -> MMA -> producer handshake of two stages left the tensor pipe
+// idle about half the time); a.stage must then hold the staging buffer.
 template <bool GEO, int KERN, bool BATCH, bool CACHED = false, bool ATM = false>
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    k_contract_tc(TcArgs a0, int nb, int nd, const TcArgs* __restrict__ segs, const int2* __restrict__ work)
+    k_contract_tc(TcArgs a0, int nb, int nd, int np, const TcArgs* __restrict__ segs, const int2* __restrict__ work)
 {
     static_assert(!CACHED || (GEO && !BATCH), "the distance cache serves single geographic datasets");
     static_assert(!ATM || !BATCH, "tensor-memory weights serve single datasets");
     constexpr uint32_t ACC_COLS = ATM ? TC_ATM_ACC_COLS : TC_ACC_COLS;
+    // Weight stages and accumulators.  Tensor memory holds one accumulator and
+    // five weight stages (ATM) or two accumulators (weights in shared memory,
+    // two stages there).  With one accumulator the MMAs of a chunk wait until
+    // the drain warps have copied the previous chunk out of it (a few
+    // microseconds per 64 tiles); five stages let the producers run ahead.
+    constexpr int NW = ATM ? TC_ATM_STAGES : 2;
+    constexpr int NACC = ATM ? 1 : 2;
     const TcArgs a = BATCH ? segs[work[blockIdx.x].x] : a0;
     const int kernel = KERN >= 0 ? KERN : a.kernel;
     // polls of a pipeline wait before it gives up; the waits of the clean-up after
@@ -159,9 +186,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     constexpr int NF = GEO ? 2 : 1;                    // float4 per point record
     // per tile: the point records, or with the cache the tile's 128 x 32 distance block
     constexpr uint32_t P_BYTES = CACHED ? TC_D_BYTES : NF * 16u * TC_BK;
-    constexpr uint32_t P_SLOT = CACHED ? TC_D_BYTES : TC_P_MAX;  // bytes per buffer (two buffers)
-    float4* ptsbuf = reinterpret_cast<float4*>(sB + (size_t)nb * 2 * b_bytes);  // 2 x P_SLOT
-    uint32_t* tmask = reinterpret_cast<uint32_t*>(sB + (size_t)nb * 2 * b_bytes + 2 * P_SLOT);
+    constexpr uint32_t P_SLOT = CACHED ? TC_D_BYTES : TC_P_MAX;  // bytes per buffer (np buffers, np <= NW)
+    float4* ptsbuf = reinterpret_cast<float4*>(sB + (size_t)nb * 2 * b_bytes);  // np x P_SLOT
+    uint32_t* tmask = reinterpret_cast<uint32_t*>(sB + (size_t)nb * 2 * b_bytes + (size_t)np * P_SLOT);
     const int nwords = (a.ntiles + 31) / 32;
 
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
@@ -178,10 +205,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         tmem_relinquish();
     }
     if (t == 0) {
-        for (int s = 0; s < 4; s++) mbar_init(&ctl.tile_done[s], 1);
+        for (int s = 0; s < TC_DONE_SLOTS; s++) mbar_init(&ctl.tile_done[s], 1);
+        for (int s = 0; s < NW; s++) mbar_init(&ctl.full_a[s], TC_PROD_WARPS);
+        for (int s = 0; s < TC_MAX_NP; s++) mbar_init(&ctl.full_p[s], 1);
         for (int s = 0; s < 2; s++) {
-            mbar_init(&ctl.full_a[s], TC_PROD_WARPS);
-            mbar_init(&ctl.full_p[s], 1);
             mbar_init(&ctl.tmem_free[s], TC_DRAIN_WARPS);
             mbar_init(&ctl.acc_full[s], 1);
         }
@@ -252,6 +279,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         unsigned long long p_stage = 0, p_points = 0, p_weights = 0;  // phase cycles (prof)
         long long c0 = prof ? clock64() : 0, c1 = 0;
         const long long loop0 = c0;
+        int ws = 0, pb = 0, ppar = 0;  // k % NW, k % np and (k / np) & 1, kept as counters
         for (int tnext = walk.next(); tnext >= 0; k++) {
             const int tile = tnext;
             tnext = walk.next();
@@ -260,20 +288,27 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 ok = false;
                 break;
             }
-            const int s = k & 1;
+            const int s = ws;
+            if (++ws == NW) ws = 0;
             // no self pair and no padding point in this tile: the per-pair checks drop out
             const bool plain = (tile + 1) * TC_BK <= a.n && (self_j < 0 || tile < self_t0 || tile > self_t1);
             if (prof) c0 = clock64();
-            // weight stage s is free once the MMAs of tile k - 2 are done
-            const bool stage_ok =
-                k < 2 || warp_wait(&ctl.tile_done[(k - 2) & 3], (uint32_t)(((k - 2) >> 2) & 1), lim);
+            // weight stage s is free once the MMAs of tile k - NW are done
+            const bool stage_ok = k < NW || warp_wait(&ctl.tile_done[(k - NW) & (TC_DONE_SLOTS - 1)],
+                                                      (uint32_t)(((k - NW) >> 3) & 1), lim);
             if (prof) {
                 c1 = clock64();
                 p_stage += c1 - c0;
                 c0 = c1;
             }
-            // the tile's point records (or, cached, its distance block) in buffer s
-            if (!stage_ok || !warp_wait(&ctl.full_p[s], (uint32_t)((k >> 1) & 1), lim)) {
+            // the tile's point records (or, cached, its distance block) in buffer k % np
+            const int pbuf = pb;
+            const bool pts_ok = stage_ok && warp_wait(&ctl.full_p[pbuf], (uint32_t)ppar, lim);
+            if (++pb == np) {
+                pb = 0;
+                ppar ^= 1;
+            }
+            if (!pts_ok) {
                 if (lane == 0) atomicExch(&ctl.abort, 1);
                 ok = false;
                 break;
@@ -284,7 +319,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 c0 = c1;
             }
             if constexpr (ATM) fence_after_sync();  // the MMAs that read stage s are done
-            const float4* tp = ptsbuf + (size_t)s * (P_SLOT / 16);
+            const float4* tp = ptsbuf + (size_t)pbuf * (P_SLOT / 16);
             unsigned char* A_hi = sA + (size_t)s * 2 * TC_A_BYTES;
             unsigned char* A_lo = A_hi + TC_A_BYTES;
             const int kbase = quarter * 8;
@@ -389,42 +424,86 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             atomicMax(a.prof + kTcProfTilesMax, (unsigned long long)k);
         }
     } else if (drainer) {
-        // chunk c: wait for its last MMA, add accumulator c % 2 (this warp's TMEM
-        // lane quadrant, every column) into the double-float sums, release it
+        // chunk c: wait for its last MMA and add the accumulator (this warp's TMEM
+        // lane quadrant, every column) into the double-float sums.  Two
+        // accumulators: add straight from tensor memory, then release it (the MMAs
+        // run on in the other one).  One accumulator: copy it out to the staging
+        // buffer first and release it, so the MMAs of the next chunk wait only for
+        // that copy, then add the staged values.
         const int quad = warp - TC_PROD_WARPS;
         const int grow = row0 + quad * 32 + lane;
         const int nchunks = (ktotal + F - 1) / F;
         const bool prof = a.prof && lane == 0 && quad == 0;
         unsigned long long pflush = 0;
+        const int np = a.npad;
         for (int c = 0; c < nchunks; c++) {
             if (__any_sync(0xffffffffu, *(volatile int*)&ctl.abort != 0)) break;
-            if (!warp_wait(&ctl.acc_full[c & 1], (uint32_t)((c >> 1) & 1), lim)) {
+            const int ab = NACC == 2 ? (c & 1) : 0;
+            const uint32_t apar = NACC == 2 ? (uint32_t)((c >> 1) & 1) : (uint32_t)(c & 1);
+            if (!warp_wait(&ctl.acc_full[ab], apar, lim)) {
                 if (lane == 0) atomicExch(&ctl.abort, 1);
                 break;
             }
             const long long c0 = prof ? clock64() : 0;
             fence_after_sync();
-            const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(c & 1) * ACC_COLS;
-            for (int col0 = 0; col0 < a.npad; col0 += 16) {
-                uint32_t v[16];
-                tmem_ld16(tbase + (uint32_t)col0, v);
-                tmem_wait_ld();
+            const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)ab * ACC_COLS;
+            if constexpr (NACC == 2) {
+                for (int col0 = 0; col0 < np; col0 += 16) {
+                    uint32_t v[16];
+                    tmem_ld16(tbase + (uint32_t)col0, v);
+                    tmem_wait_ld();
+                    if (grow < a.n) {
+                        // the 16 loads first, then the sums: one memory latency per 16 columns
+                        float2* __restrict__ e = a.acc + acc_at(grow, col0, np);
+                        float2 o[16];
+#pragma unroll
+                        for (int q = 0; q < 16; q++) o[q] = c == 0 ? make_float2(0.f, 0.f) : e[(size_t)q * TC_M];
+#pragma unroll
+                        for (int q = 0; q < 16; q++) e[(size_t)q * TC_M] = df_add(o[q], __uint_as_float(v[q]));
+                    }
+                }
+                fence_before_sync();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&ctl.tmem_free[ab]);
+            } else {
+                for (int col0 = 0; col0 < np; col0 += 32) {
+                    uint32_t v0[16], v1[16];
+                    const bool two = col0 + 16 < np;  // npad is a multiple of 16
+                    tmem_ld16(tbase + (uint32_t)col0, v0);
+                    if (two) tmem_ld16(tbase + (uint32_t)col0 + 16u, v1);
+                    tmem_wait_ld();
+                    if (grow < a.n) {
+                        float* st = a.stage + acc_at(grow, col0, np);
+#pragma unroll
+                        for (int q = 0; q < 16; q++) st[(size_t)q * TC_M] = __uint_as_float(v0[q]);
+                        if (two) {
+#pragma unroll
+                            for (int q = 0; q < 16; q++) st[(size_t)(16 + q) * TC_M] = __uint_as_float(v1[q]);
+                        }
+                    }
+                }
+                fence_before_sync();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&ctl.tmem_free[0]);
                 if (grow < a.n) {
-                    float4* acc = reinterpret_cast<float4*>(a.acc + (size_t)grow * a.npad + col0);
-                    float4 o[8];
+                    // 16 columns at a time, every load before the sums: one memory
+                    // latency per 16 columns
+                    for (int col0 = 0; col0 < np; col0 += 16) {
+                        const size_t x = acc_at(grow, col0, np);
+                        float2* __restrict__ e = a.acc + x;
+                        const float* __restrict__ sv = a.stage + x;
+                        float2 o[16];
+                        float v[16];
 #pragma unroll
-                    for (int q = 0; q < 8; q++) o[q] = c == 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : acc[q];
+                        for (int q = 0; q < 16; q++) {
+                            v[q] = sv[(size_t)q * TC_M];
+                            o[q] = c == 0 ? make_float2(0.f, 0.f) : e[(size_t)q * TC_M];
+                        }
 #pragma unroll
-                    for (int q = 0; q < 8; q++) {
-                        const float2 h0 = df_add(make_float2(o[q].x, o[q].y), __uint_as_float(v[2 * q]));
-                        const float2 h1 = df_add(make_float2(o[q].z, o[q].w), __uint_as_float(v[2 * q + 1]));
-                        acc[q] = make_float4(h0.x, h0.y, h1.x, h1.y);
+                        for (int q = 0; q < 16; q++) e[(size_t)q * TC_M] = df_add(o[q], v[q]);
                     }
                 }
             }
-            fence_before_sync();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&ctl.tmem_free[c & 1]);
             if (prof) pflush += clock64() - c0;
         }
         if (prof) atomicAdd(a.prof + kTcProfFlush, pflush);
@@ -433,21 +512,45 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         // it, so this thread does nothing but wait for a tile's weights, its Z tile
         // and a free accumulator and issue: every copy is the copy warp's.
         if (lane == 0) {
-            TileWalker wm;
-            wm.init(tmask, nwords);
             int last_mma = -1;
             const uint32_t idesc = idesc_tf32(TC_M, a.npad);
             const bool prof = a.prof != nullptr;
             unsigned long long p_a = 0, p_z = 0, p_i = 0;
             long long c0 = 0, c1 = 0;
-            // k % nb, (k / nb) & 1, k % F and k / F kept as counters: divisions by
-            // run-time values are long dependent chains on this critical thread
-            int sb = 0, zpar = 0, kf = 0, c = 0;
-            for (int tile = wm.next(); tile >= 0; tile = wm.next(), k++) {
-                if ((k & 15) == 0 && *(volatile int*)&ctl.abort) break;
-                const int s = k & 1;
+            // k % NW, (k / NW) & 1, k % nb, (k / nb) & 1, k % F and k / F kept as
+            // counters: divisions by run-time values are long dependent chains on
+            // this critical thread
+            int ws = 0, wpar = 0, sb = 0, zpar = 0, kf = 0, c = 0;
+            // Up to two tiles per pass: the waits for both come first, then their
+            // 24 MMAs back to back, so the tensor pipe does not idle through this
+            // thread's waits and bookkeeping between the two tiles.  A pass never
+            // straddles a chunk.
+            bool failed = false;
+            while (k < ktotal && !failed) {
+                if ((k & 15) < 2 && *(volatile int*)&ctl.abort) break;
+                const int nt = (k + 1 < ktotal && kf + 1 < F) ? 2 : 1;
                 if (prof) c0 = clock64();
-                if (!mbar_wait(&ctl.full_a[s], (uint32_t)((k >> 1) & 1), lim)) {
+                int s2 = ws, wp2 = wpar, sb2 = sb, zp2 = zpar;
+                for (int u = 0; u < nt && !failed; u++) {
+                    if (!mbar_wait(&ctl.full_a[s2], (uint32_t)wp2, lim) || !mbar_wait(&ctl.full_b[sb2], (uint32_t)zp2, lim))
+                        failed = true;
+                    if (++s2 == NW) {
+                        s2 = 0;
+                        wp2 ^= 1;
+                    }
+                    if (++sb2 == nb) {
+                        sb2 = 0;
+                        zp2 ^= 1;
+                    }
+                }
+                // a chunk starts once its accumulator is drained (chunk c - NACC)
+                if (!failed && kf == 0 && c >= NACC) {
+                    bool ok;
+                    if constexpr (NACC == 2) ok = mbar_wait(&ctl.tmem_free[c & 1], (uint32_t)(((c >> 1) - 1) & 1), lim);
+                    else ok = mbar_wait(&ctl.tmem_free[0], (uint32_t)((c - 1) & 1), lim);
+                    failed = !ok;
+                }
+                if (failed) {
                     atomicExch(&ctl.abort, 1);
                     break;
                 }
@@ -456,56 +559,52 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     p_a += c1 - c0;
                     c0 = c1;
                 }
-                bool ok = mbar_wait(&ctl.full_b[sb], (uint32_t)zpar, lim);
-                if (ok && kf == 0 && c >= 2)
-                    ok = mbar_wait(&ctl.tmem_free[c & 1], (uint32_t)(((c >> 1) - 1) & 1), lim);
-                if (!ok) {
-                    atomicExch(&ctl.abort, 1);
-                    break;
-                }
-                if (prof) {
-                    c1 = clock64();
-                    p_z += c1 - c0;
-                    c0 = c1;
-                }
                 fence_after_sync();
-                unsigned char* A_hi = sA + (size_t)s * 2 * TC_A_BYTES;
-                unsigned char* B_hi = sB + (size_t)sb * 2 * b_bytes;
-                const uint64_t ahi = sw128_kmajor_desc(smem_u32(A_hi));
-                const uint64_t alo = sw128_kmajor_desc(smem_u32(A_hi + TC_A_BYTES));
-                const uint64_t bhi = sw128_kmajor_desc(smem_u32(B_hi));
-                const uint64_t blo = sw128_kmajor_desc(smem_u32(B_hi + b_bytes));
-                const uint32_t d = tmem + (uint32_t)(c & 1) * ACC_COLS;
-                if constexpr (ATM) {
-                    const uint32_t ta = tmem + TC_ATM_A_COL + (uint32_t)s * 64u;  // hi; lo 32 columns on
+                for (int u = 0; u < nt; u++) {
+                    const int s = ws;
+                    unsigned char* A_hi = sA + (size_t)s * 2 * TC_A_BYTES;
+                    unsigned char* B_hi = sB + (size_t)sb * 2 * b_bytes;
+                    const uint64_t ahi = sw128_kmajor_desc(smem_u32(A_hi));
+                    const uint64_t alo = sw128_kmajor_desc(smem_u32(A_hi + TC_A_BYTES));
+                    const uint64_t bhi = sw128_kmajor_desc(smem_u32(B_hi));
+                    const uint64_t blo = sw128_kmajor_desc(smem_u32(B_hi + b_bytes));
+                    const uint32_t d = tmem + (NACC == 2 ? (uint32_t)(c & 1) * ACC_COLS : 0u);
+                    if constexpr (ATM) {
+                        const uint32_t ta = tmem + TC_ATM_A_COL + (uint32_t)s * 64u;  // hi; lo 32 columns on
 #pragma unroll
-                    for (int kk = 0; kk < 4; kk++) {
-                        const uint64_t dk = (uint64_t)(kk * 2);  // 32 bytes = 8 TF32 along K
-                        const uint32_t tk = ta + (uint32_t)(kk * 8);
-                        mma_tf32_ts(d, tk, bhi + dk, idesc, (kf != 0 || kk > 0) ? 1u : 0u);
-                        mma_tf32_ts(d, tk, blo + dk, idesc, 1u);
-                        mma_tf32_ts(d, tk + 32u, bhi + dk, idesc, 1u);
-                    }
-                } else {
+                        for (int kk = 0; kk < 4; kk++) {
+                            const uint64_t dk = (uint64_t)(kk * 2);  // 32 bytes = 8 TF32 along K
+                            const uint32_t tk = ta + (uint32_t)(kk * 8);
+                            mma_tf32_ts(d, tk, bhi + dk, idesc, (kf != 0 || kk > 0) ? 1u : 0u);
+                            mma_tf32_ts(d, tk, blo + dk, idesc, 1u);
+                            mma_tf32_ts(d, tk + 32u, bhi + dk, idesc, 1u);
+                        }
+                    } else {
 #pragma unroll
-                    for (int kk = 0; kk < 4; kk++) {
-                        const uint64_t dk = (uint64_t)(kk * 2);  // 32 bytes = 8 TF32 along K
-                        mma_tf32(d, ahi + dk, bhi + dk, idesc, (kf != 0 || kk > 0) ? 1u : 0u);
-                        mma_tf32(d, ahi + dk, blo + dk, idesc, 1u);
-                        mma_tf32(d, alo + dk, bhi + dk, idesc, 1u);
+                        for (int kk = 0; kk < 4; kk++) {
+                            const uint64_t dk = (uint64_t)(kk * 2);  // 32 bytes = 8 TF32 along K
+                            mma_tf32(d, ahi + dk, bhi + dk, idesc, (kf != 0 || kk > 0) ? 1u : 0u);
+                            mma_tf32(d, ahi + dk, blo + dk, idesc, 1u);
+                            mma_tf32(d, alo + dk, bhi + dk, idesc, 1u);
+                        }
                     }
-                }
-                // one commit frees weight stage s (producers) and Z stage sb (copy warp)
-                mma_commit(&ctl.tile_done[k & 3]);
-                if (kf == F - 1 || k == ktotal - 1) mma_commit(&ctl.acc_full[c & 1]);  // chunk c complete
-                last_mma = k;
-                if (++sb == nb) {
-                    sb = 0;
-                    zpar ^= 1;
-                }
-                if (++kf == F) {
-                    kf = 0;
-                    c++;
+                    // one commit frees weight stage s (producers) and Z stage sb (copy warp)
+                    mma_commit(&ctl.tile_done[k & (TC_DONE_SLOTS - 1)]);
+                    if (kf == F - 1 || k == ktotal - 1) mma_commit(&ctl.acc_full[NACC == 2 ? (c & 1) : 0]);  // chunk c complete
+                    last_mma = k;
+                    if (++ws == NW) {
+                        ws = 0;
+                        wpar ^= 1;
+                    }
+                    if (++sb == nb) {
+                        sb = 0;
+                        zpar ^= 1;
+                    }
+                    if (++kf == F) {
+                        kf = 0;
+                        c++;
+                    }
+                    k++;
                 }
                 if (prof) p_i += clock64() - c0;
             }
@@ -516,27 +615,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             // leave no MMA in flight before TMEM and the CTA go away
             if (*(volatile int*)&ctl.abort && last_mma >= 0)
-                mbar_wait(&ctl.tile_done[last_mma & 3], (uint32_t)((last_mma >> 2) & 1), TC_WAIT);
+                mbar_wait(&ctl.tile_done[last_mma & (TC_DONE_SLOTS - 1)], (uint32_t)((last_mma >> 3) & 1), TC_WAIT);
         }
     } else if (warp == TC_COPY_WARP) {
-        // Copies (lane 0): the Z tiles nb ahead (a stage is refilled once the MMAs
-        // of the tile that read it are done), the point records or, with the
-        // cache, the 16 KB distance block of a tile two ahead (once the producers
-        // are done with a buffer), and with the cache an L2 prefetch of the
-        // distance blocks nd ahead.  Each wait is for a phase whose successor
-        // needs a copy this thread has not issued yet, so it can never be two
-        // phases behind.
+        // Z copies (lane 0): the Z tiles nb ahead; stage j % nb is refilled once
+        // tile_done reports the MMAs of tile j done.  The next phase of that
+        // barrier slot (tile j + 8) needs Z tile j + 8, issued only after this
+        // wait, so the wait can never be two phases behind.
         if (lane == 0) {
-            TileWalker wz, wp, wl;
+            TileWalker wz;
             wz.init(tmask, nwords);
-            wp.init(tmask, nwords);
-            wl.init(tmask, nwords);
-            int kz = 0, kp = 0, kl = 0;  // copies and prefetches issued
-            const float* d2blk = CACHED ? a.d2c + (size_t)blockIdx.x * a.ntiles * (TC_D_BYTES / 4) : nullptr;
-            auto issue_l = [&](int tl) {
-                bulk_prefetch_l2(d2blk + (size_t)tl * (TC_D_BYTES / 4), TC_D_BYTES);
-                kl++;
-            };
+            int kz = 0;
             int zsb = 0;  // kz % nb, kept as a counter (no run-time divisions on this thread)
             auto issue_z = [&](int tl) {
                 const int sb = zsb;
@@ -549,60 +638,90 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 for (int q = 0; q < 4; q++) bulk_g2s(B + q * piece, src + q * piece, piece, &ctl.full_b[sb]);
                 kz++;
             };
-            auto issue_p = [&](int tl) {
-                const int sp = kp & 1;
-                const void* src = CACHED ? static_cast<const void*>(d2blk + (size_t)tl * (TC_D_BYTES / 4))
-                                         : static_cast<const void*>(a.pts + (size_t)NF * TC_BK * tl);
-                mbar_arrive_expect_tx(&ctl.full_p[sp], P_BYTES);
-                bulk_g2s(ptsbuf + (size_t)sp * (P_SLOT / 16), src, P_BYTES, &ctl.full_p[sp]);
-                kp++;
-            };
             for (int q = 0; q < nb; q++) {
                 const int tl = wz.next();
                 if (tl < 0) break;
                 issue_z(tl);
             }
+            for (int j = 0; j < ktotal && kz < ktotal; j++) {
+                if ((j & 15) == 0 && *(volatile int*)&ctl.abort) break;
+                if (!mbar_wait(&ctl.tile_done[j & (TC_DONE_SLOTS - 1)], (uint32_t)((j >> 3) & 1), lim)) {
+                    atomicExch(&ctl.abort, 1);
+                    break;
+                }
+                const int tl = wz.next();
+                if (tl >= 0) issue_z(tl);
+            }
+            if (*(volatile int*)&ctl.abort) {
+                // leave no bulk copy in flight before the CTA goes away
+                for (int j = kz - nb > 0 ? kz - nb : 0; j < kz; j++)
+                    mbar_wait(&ctl.full_b[j % nb], (uint32_t)((j / nb) & 1), TC_WAIT);
+            }
+        }
+    } else if (warp == TC_PCOPY_WARP) {
+        // Point-record copies (lane 0): the records or, with the cache, the 16 KB
+        // distance block of a tile np ahead into buffer j % np, once full_a
+        // reports the producers done with tile j; with the cache also an L2
+        // prefetch of the distance blocks nd ahead.  The next phase of full_a[j %
+        // NW] (tile j + NW) needs the copy for tile j + NW, issued after this
+        // wait as np <= NW, so the wait can never be two phases behind.
+        if (lane == 0) {
+            TileWalker wp, wl;
+            wp.init(tmask, nwords);
+            wl.init(tmask, nwords);
+            int kp = 0, kl = 0;  // copies and prefetches issued
+            const float* d2blk = CACHED ? a.d2c + (size_t)blockIdx.x * a.ntiles * (TC_D_BYTES / 4) : nullptr;
+            // a distance block is read once per launch: first out of L2, so the Z
+            // images that every CTA reads stay in it
+            const uint64_t stream_pol = l2_policy_evict_first();
+            auto issue_l = [&](int tl) {
+                bulk_prefetch_l2_hint(d2blk + (size_t)tl * (TC_D_BYTES / 4), TC_D_BYTES, stream_pol);
+                kl++;
+            };
+            int psb = 0;  // kp % np
+            auto issue_p = [&](int tl) {
+                const int sp = psb;
+                if (++psb == np) psb = 0;
+                const void* src = CACHED ? static_cast<const void*>(d2blk + (size_t)tl * (TC_D_BYTES / 4))
+                                         : static_cast<const void*>(a.pts + (size_t)NF * TC_BK * tl);
+                mbar_arrive_expect_tx(&ctl.full_p[sp], P_BYTES);
+                if (CACHED) bulk_g2s_hint(ptsbuf + (size_t)sp * (P_SLOT / 16), src, P_BYTES, &ctl.full_p[sp], stream_pol);
+                else bulk_g2s(ptsbuf + (size_t)sp * (P_SLOT / 16), src, P_BYTES, &ctl.full_p[sp]);
+                kp++;
+            };
             for (int q = 0; CACHED && q < nd; q++) {
                 const int tl = wl.next();
                 if (tl < 0) break;
                 issue_l(tl);
             }
-            for (int q = 0; q < 2; q++) {
+            for (int q = 0; q < np; q++) {
                 const int tl = wp.next();
                 if (tl < 0) break;
                 issue_p(tl);
             }
-            for (int j = 0; j < ktotal && (kz < ktotal || kp < ktotal || (CACHED && kl < ktotal)); j++) {
-                if (*(volatile int*)&ctl.abort) break;
+            int pw = 0, wpar = 0;  // j % NW, (j / NW) & 1
+            for (int j = 0; j < ktotal && (kp < ktotal || (CACHED && kl < ktotal)); j++) {
+                if ((j & 15) == 0 && *(volatile int*)&ctl.abort) break;
                 if (CACHED && kl < ktotal) {
                     const int tl = wl.next();
                     if (tl >= 0) issue_l(tl);
                 }
                 if (kp < ktotal) {
-                    // buffer j % 2 is free once the producers are done with tile j
-                    if (!mbar_wait(&ctl.full_a[j & 1], (uint32_t)((j >> 1) & 1), lim)) {
+                    if (!mbar_wait(&ctl.full_a[pw], (uint32_t)wpar, lim)) {
                         atomicExch(&ctl.abort, 1);
                         break;
                     }
                     const int tl = wp.next();
                     if (tl >= 0) issue_p(tl);
                 }
-                if (kz < ktotal) {
-                    // Z stage j % nb is free once the MMAs of tile j are done
-                    if (!mbar_wait(&ctl.tile_done[j & 3], (uint32_t)((j >> 2) & 1), lim)) {
-                        atomicExch(&ctl.abort, 1);
-                        break;
-                    }
-                    const int tl = wz.next();
-                    if (tl >= 0) issue_z(tl);
+                if (++pw == NW) {
+                    pw = 0;
+                    wpar ^= 1;
                 }
             }
             if (*(volatile int*)&ctl.abort) {
-                // leave no bulk copy in flight before the CTA goes away
-                for (int j = kz - nb > 0 ? kz - nb : 0; j < kz; j++)
-                    mbar_wait(&ctl.full_b[j % nb], (uint32_t)((j / nb) & 1), TC_WAIT);
-                for (int j = kp - 2 > 0 ? kp - 2 : 0; j < kp; j++)
-                    mbar_wait(&ctl.full_p[j & 1], (uint32_t)((j >> 1) & 1), TC_WAIT);
+                for (int j = kp - np > 0 ? kp - np : 0; j < kp; j++)
+                    mbar_wait(&ctl.full_p[j % np], (uint32_t)((j / np) & 1), TC_WAIT);
             }
         }
     }
@@ -622,7 +741,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (grow >= a.n) continue;
             double v = 0.0;
             if (k > 0) {
-                const float2 x = acc[(size_t)grow * a.npad + c];
+                const float2 x = acc[acc_at(grow, c, a.npad)];
                 v = (double)x.x + (double)x.y;
             }
             G[(size_t)grow * a.ldg + c] = v;
@@ -786,17 +905,22 @@ cudaError_t launch_contract_tc(const TcArgs& a, bool geographic, cudaStream_t st
     const int nd = 4;
     const size_t mask = (size_t)((a.ntiles + 31) / 32) * 4;
     if ((uint32_t)a.npad <= TC_ATM_ACC_COLS) {
-        // weights in tensor memory: the shared memory holds only the Z stages
-        // (two buffers of point records, or of 16 KB distance blocks with the cache)
+        if (!a.stage) return cudaErrorInvalidValue;  // the single accumulator drains through it
+        // weights in tensor memory: the shared memory holds only the Z stages and
+        // np buffers of point records (or of 16 KB distance blocks with the cache):
+        // three when they fit beside four Z stages, else two and fewer Z stages.
+        // The barriers' static shared memory comes out of the same 227 KB.
         const size_t pbuf = a.d2c && geographic ? TC_D_BYTES : TC_P_MAX;
-        auto bytes = [&](int b) { return 1024 + (size_t)b * 2 * a.npad * 128 + 2 * pbuf + mask; };
-        int nb = TC_MAX_NB;
-        while (nb > 2 && bytes(nb) > 227 * 1024) nb--;
-        const size_t smem = bytes(nb);
-        if (smem > 227 * 1024) return cudaErrorInvalidValue;
+        const size_t lim = 227 * 1024 - 1024;
+        auto bytes = [&](int b, int p) { return 1024 + (size_t)b * 2 * a.npad * 128 + (size_t)p * pbuf + mask; };
+        int nb = TC_MAX_NB, np = TC_MAX_NP;
+        if (bytes(nb, np) > lim) np = 2;
+        while (nb > 2 && bytes(nb, np) > lim) nb--;
+        const size_t smem = bytes(nb, np);
+        if (smem > lim) return cudaErrorInvalidValue;
         auto go = [&](auto kfn) {
             raise_smem_limit((const void*)kfn, smem);
-            kfn<<<grid, TC_THREADS, smem, stream>>>(a, nb, nd, nullptr, nullptr);
+            kfn<<<grid, TC_THREADS, smem, stream>>>(a, nb, nd, np, nullptr, nullptr);
         };
         if (geographic && a.d2c) {
             if (a.kernel == GW_KERNEL_BISQUARE) go(k_contract_tc<true, GW_KERNEL_BISQUARE, false, true, true>);
@@ -821,7 +945,7 @@ cudaError_t launch_contract_tc(const TcArgs& a, bool geographic, cudaStream_t st
     if (smem > 227 * 1024) return cudaErrorInvalidValue;
     auto go = [&](auto kfn) {
         raise_smem_limit((const void*)kfn, smem);
-        kfn<<<grid, TC_THREADS, smem, stream>>>(a, nb, nd, nullptr, nullptr);
+        kfn<<<grid, TC_THREADS, smem, stream>>>(a, nb, nd, 2, nullptr, nullptr);
     };
     if (geographic && a.d2c) go(k_contract_tc<true, -1, false, true>);
     else if (geographic) go(k_contract_tc<true, -1, false>);
@@ -841,7 +965,7 @@ cudaError_t launch_contract_tc_batch(const TcArgs* segs, const int2* work, int n
     TcArgs none{};
     auto go = [&](auto kfn) {
         raise_smem_limit((const void*)kfn, smem);
-        kfn<<<nwork, TC_THREADS, smem, stream>>>(none, nb, 2, segs, work);
+        kfn<<<nwork, TC_THREADS, smem, stream>>>(none, nb, 2, 2, segs, work);
     };
     if (geographic) {
         if (kernel == GW_KERNEL_BISQUARE) go(k_contract_tc<true, GW_KERNEL_BISQUARE, true>);
