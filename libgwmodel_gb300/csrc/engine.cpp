@@ -934,25 +934,26 @@ const double* Engine::orderStatistic(unsigned rank)
     a.out = r->v.get();
     a.err = sel_err_.get();
     if (hist_.get() && !hist_valid_) {
-        // geographic mixed data: the histogram pass fills the distance cache on the way
+        // geographic mixed data: the distance cache is filled first (each pair once,
+        // the distance being symmetric) and the histograms are read back from it
         DeviceD2Cache& dc = device_d2c(device_);
         std::unique_lock<std::mutex> lk(dc.mu, std::defer_lock);
-        float* fill = nullptr;
+        const float* cache = nullptr;
         if (geographic_ && precision_ == kMixed && d2c_limit_bytes_ != 0) {
             lk.lock();
-            if (!(dc.owner == this && d2c_valid_)) fill = acquireDistanceCache();
-            if (!fill) lk.unlock();
+            cache = ensureDistanceCache();
+            if (!cache) lk.unlock();
         }
-        a.d2c_out = fill;
-        check(launch_select_hist(a, geographic_, num_sms_, stream_), "select histograms");
-        a.d2c_out = nullptr;
-        stats_.kernel_launches += 1;
-        if (fill) {
-            d2c_valid_ = true;
-            stats_.d2c_fills += 1;
+        if (cache) {
+            a.d2c = cache;
+            check(launch_select_hist_cached(a, num_sms_, stream_), "select histograms");
+            a.d2c = nullptr;
             check(cudaEventRecord(dc.used, stream_), "cudaEventRecord");
             lk.unlock();
+        } else {
+            check(launch_select_hist(a, geographic_, num_sms_, stream_), "select histograms");
         }
+        stats_.kernel_launches += 1;
         hist_valid_ = true;
         a.cache_valid = 1;
     }
@@ -1488,8 +1489,9 @@ const float* Engine::ensureDistanceCache()
     float* d2c = acquireDistanceCache();
     if (!d2c) return nullptr;
     cudaEvent_t e0 = stats_on_ ? timerBegin() : nullptr;
-    check(launch_fill_d2(n_, pts32_.get(), d2c, stream_), "fill distance cache");
-    stats_.kernel_launches += 1;
+    fill_scratch_.alloc((size_t)(n_ + 127) / 128 + 2);
+    check(launch_fill_d2_sym(n_, pts32_.get(), d2c, fill_scratch_.get(), num_sms_, stream_), "fill distance cache");
+    stats_.kernel_launches += 2;
     if (stats_on_) {
         timerEnd(e0, 2);
         stats_.d2c_fills += 1;

@@ -286,6 +286,7 @@ private:
     DevBuf<double> rvec_;
     DevBuf<float2> acc_;
     DevBuf<float> stage_;
+    DevBuf<int> fill_scratch_;  // work items of the symmetric distance-cache fill
     DevBuf<float> thr32_;
     DevBuf<int> err_;
     long long d2c_limit_bytes_ = -1;

@@ -49,6 +49,9 @@ size_t select_smem_bytes();
 // Fills hist_cache with every row's whole-row proxy histogram (the cache a
 // first select pass would store); the selects after it run with cache_valid.
 cudaError_t launch_select_hist(const SelectArgs& a, bool geographic, int num_sms, cudaStream_t stream);
+// The same histograms of geographic data rows read back from the filled
+// distance cache a.d2c instead of recomputing the distances.
+cudaError_t launch_select_hist_cached(const SelectArgs& a, int num_sms, cudaStream_t stream);
 // Batched forms over many datasets and ranks in one launch each (device
 // arrays of per-segment arguments; segment s owns the flattened items
 // [start[s], start[s + 1])): whole-row histograms (items are groups of 8
@@ -212,6 +215,9 @@ cudaError_t launch_build_zimg(int n, int mcols, int npad, const double* Z, int l
 // FLT_MAX.  pts: the 2 float4 records per point, padded to whole tiles.
 size_t d2_cache_bytes(int n);
 cudaError_t launch_fill_d2(int n, const float4* pts, float* d2c, cudaStream_t stream);
+// The same cache, each pair computed once (the FP32 distance is symmetric) and
+// written to both rows.  scratch: ceil(n / 128) + 2 ints of device memory.
+cudaError_t launch_fill_d2_sym(int n, const float4* pts, float* d2c, int* scratch, int num_sms, cudaStream_t stream);
 // D[128 x N] = A[128 x 32] B[N x 32]^T through tcgen05 (device pointers).
 cudaError_t launch_tc_selftest(const float* A, const float* B, float* D, int N, int* err, cudaStream_t stream);
 

@@ -228,7 +228,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const float inv_r2 = 1.0f / (rr * rr);
     // pairs with a haversine term in [s_cut, 0.86] have weight 0 under a compact kernel
     const float s_cut = (GEO && kernel >= GW_KERNEL_BISQUARE) ? geo_s_cut(rr) : __int_as_float(0x7f800000);
-    const float fz = fa.z + fb.z;  // sin(lat) of the focus
     const int self_j = a.exclude_self ? i : -1;
     // tiles that may hold a self pair of this block's rows (none without exclude_self)
     const int self_t0 = a.exclude_self ? row0 / TC_BK : a.ntiles, self_t1 = (row0 + TC_M - 1) / TC_BK;
@@ -356,7 +355,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     const int kk = kbase + q4 * 4 + e;
                     in[e] = row_ok && tile * TC_BK + kk < a.n;
                     if (GEO) {
-                        g[e] = geo_chord32(fa, fb, fz, tp[2 * kk], tp[2 * kk + 1]);
+                        g[e] = geo_chord32(fa, fb, tp[2 * kk], tp[2 * kk + 1]);
                         in[e] = in[e] && !geo_beyond(g[e].S, s_cut);
                     }
                     w[e] = 0.0f;
@@ -845,7 +844,6 @@ __global__ void __launch_bounds__(512) k_fill_d2(int n, int ntiles, const float4
         fa = pts[2 * (size_t)i];
         fb = pts[2 * (size_t)i + 1];
     }
-    const float fz = fa.z + fb.z;
     const int t0 = blockIdx.y * FD_TILES, t1 = min(ntiles, t0 + FD_TILES);
     float4* out = reinterpret_cast<float4*>(d2c) + (size_t)rb * ntiles * 1024 + quarter * 256 + r;
     for (int tile = t0; tile < t1; tile++) {
@@ -855,7 +853,7 @@ __global__ void __launch_bounds__(512) k_fill_d2(int n, int ntiles, const float4
 #pragma unroll
             for (int e = 0; e < 4; e++) {
                 const size_t j = (size_t)tile * TC_BK + quarter * 8 + q4 * 4 + e;  // records padded to whole tiles
-                g[e] = geo_chord32(fa, fb, fz, pts[2 * j], pts[2 * j + 1]);
+                g[e] = geo_chord32(fa, fb, pts[2 * j], pts[2 * j + 1]);
             }
             const bool near = __all_sync(0xffffffffu, fmaxf(fmaxf(g[0].S, g[1].S), fmaxf(g[2].S, g[3].S)) <= 0.25f);
             float d[4];
@@ -871,7 +869,125 @@ __global__ void __launch_bounds__(512) k_fill_d2(int n, int ntiles, const float4
     }
 }
 
+// Symmetric fill of the distance cache.  The FP32 distance is symmetric bit
+// for bit (geo_chord32), so each pair of row blocks (A, B), B >= A, is
+// computed once: thread (r, q) computes row A * 128 + r against the 32 points
+// of tile 4 B + q, writes them as its part of the cache tiles of rows A, and
+// keeps them in shared memory, from which the block's transpose becomes the
+// cache tiles 4 A .. 4 A + 3 of rows B.  Work items (row block A, chunk of
+// FS_CHUNK row blocks B) come from an atomic counter; item_start[A] is the
+// first item of row block A.
+constexpr int FS_CHUNK = 8;
+constexpr int FS_LD = TC_M + 1;  // padded row of the transpose buffer: no bank conflicts either way
+
+__global__ void k_fill_items(int nrb, int* __restrict__ item_start, int* __restrict__ counter)
+{
+    int acc = 0;
+    for (int A = 0; A < nrb; A++) {
+        item_start[A] = acc;
+        acc += (nrb - A + FS_CHUNK - 1) / FS_CHUNK;
+    }
+    item_start[nrb] = acc;
+    *counter = 0;
+}
+
+__global__ void __launch_bounds__(512, 2) k_fill_d2_sym(int n, int ntiles, int nrb, const float4* __restrict__ pts,
+                                                         float* __restrict__ d2c,
+                                                         const int* __restrict__ item_start, int* __restrict__ counter)
+{
+    extern __shared__ float sT[];  // 128 x FS_LD: sT[row of A][point of B]
+    __shared__ int s_item;
+    const int t = threadIdx.x, r = t & (TC_M - 1), q = t >> 7;
+    const int nitems = item_start[nrb];
+    for (;;) {
+        if (t == 0) s_item = atomicAdd(counter, 1);
+        __syncthreads();
+        const int item = s_item;
+        __syncthreads();
+        if (item >= nitems) break;
+        int lo = 0, hi = nrb;  // item_start[lo] <= item < item_start[hi]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (item_start[mid] <= item) lo = mid;
+            else hi = mid;
+        }
+        const int A = lo;
+        const int B0 = A + (item - item_start[A]) * FS_CHUNK, B1 = min(nrb, B0 + FS_CHUNK);
+        const int i = A * TC_M + r;
+        float4 fa = make_float4(0.f, 0.f, 0.f, 0.f), fb = fa;
+        if (i < n) {
+            fa = pts[2 * (size_t)i];
+            fb = pts[2 * (size_t)i + 1];
+        }
+        for (int B = B0; B < B1; B++) {
+            const int tile = 4 * B + q;  // warp-uniform
+            float4* outA = reinterpret_cast<float4*>(d2c) + ((size_t)A * ntiles + tile) * 1024 + r;
+#pragma unroll 2
+            for (int g8 = 0; g8 < 8; g8++) {  // points 4 g8 .. 4 g8 + 3 of the tile: [quarter g8 / 2][half g8 % 2]
+                float d[4];
+                if (tile < ntiles) {
+                    GeoChord g[4];
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        const size_t j = (size_t)tile * TC_BK + g8 * 4 + e;  // records padded to whole tiles
+                        g[e] = geo_chord32(fa, fb, pts[2 * j], pts[2 * j + 1]);
+                    }
+                    const bool near =
+                        __all_sync(0xffffffffu, fmaxf(fmaxf(g[0].S, g[1].S), fmaxf(g[2].S, g[3].S)) <= 0.25f);
+                    if (near) {
+#pragma unroll
+                        for (int e = 0; e < 4; e++) d[e] = geo_d2_near(g[e]);
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < 4; e++) {
+                            const size_t j = (size_t)tile * TC_BK + g8 * 4 + e;
+                            d[e] = geo_d2_far(g[e], fa, fb, pts[2 * j], pts[2 * j + 1]);
+                        }
+                    }
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        const int j = tile * TC_BK + g8 * 4 + e;
+                        d[e] = (i < n && j < n) ? d[e] : 3.402823466e38f;
+                    }
+                    __stcs(outA + g8 * 128, make_float4(d[0], d[1], d[2], d[3]));
+                } else {
+                    d[0] = d[1] = d[2] = d[3] = 3.402823466e38f;
+                }
+                if (B != A) {
+#pragma unroll
+                    for (int e = 0; e < 4; e++) sT[r * FS_LD + q * TC_BK + g8 * 4 + e] = d[e];
+                }
+            }
+            if (B != A) {
+                __syncthreads();
+                // rows B * 128 + r against the 32 points of tile 4 A + q: column r of sT
+                const int tileA = 4 * A + q;
+                if (tileA < ntiles) {
+                    float4* outB = reinterpret_cast<float4*>(d2c) + ((size_t)B * ntiles + tileA) * 1024 + r;
+#pragma unroll 2
+                    for (int g8 = 0; g8 < 8; g8++) {
+                        const float* c = sT + (q * TC_BK + g8 * 4) * FS_LD + r;
+                        __stcs(outB + g8 * 128, make_float4(c[0], c[FS_LD], c[2 * FS_LD], c[3 * FS_LD]));
+                    }
+                }
+                __syncthreads();
+            }
+        }
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_fill_d2_sym(int n, const float4* pts, float* d2c, int* scratch, int num_sms, cudaStream_t stream)
+{
+    if (n < 1) return cudaErrorInvalidValue;
+    const int nrb = (n + TC_M - 1) / TC_M, ntiles = (n + TC_BK - 1) / TC_BK;
+    k_fill_items<<<1, 1, 0, stream>>>(nrb, scratch, scratch + nrb + 1);
+    const size_t smem = (size_t)TC_M * FS_LD * sizeof(float);
+    raise_smem_limit((const void*)k_fill_d2_sym, smem);
+    k_fill_d2_sym<<<2 * num_sms, 512, smem, stream>>>(n, ntiles, nrb, pts, d2c, scratch, scratch + nrb + 1);
+    return cudaGetLastError();
+}
 
 size_t d2_cache_bytes(int n)
 {

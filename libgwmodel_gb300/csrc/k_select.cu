@@ -281,7 +281,7 @@ __device__ bool select_row(typename C::Shared& sh, const SelectArgs& a, const Ro
                             d2 = __ldg(d2r + (size_t)tile * 4096 + (lane >> 2) * 512 + (lane & 3));
                         } else {
                             const float4 pa = a.pts[2 * (size_t)j], pb = a.pts[2 * (size_t)j + 1];
-                            const GeoChord g = geo_chord32(c.fa, c.fb, c.fa.z + c.fb.z, pa, pb);
+                            const GeoChord g = geo_chord32(c.fa, c.fb, pa, pb);
                             d2 = __all_sync(0xffffffffu, g.S <= 0.25f) ? geo_d2_near(g) : geo_d2_far(g, c.fa, c.fb, pa, pb);
                         }
                         d32 = d2 > 0.0f ? d2 * rsqrt_ftz(d2) : 0.0f;
@@ -595,7 +595,7 @@ __device__ void hist_rows(unsigned* hs, float4 (*rf)[2], const SelectArgs& a, in
                 float d32;
                 if (GEO) {
                     const float4 rb = rf[r][1];
-                    const GeoChord gc = geo_chord32(ra, rb, ra.z + rb.z, pa, pb);
+                    const GeoChord gc = geo_chord32(ra, rb, pa, pb);
                     const bool near = __all_sync(0xffffffffu, gc.S <= 0.25f);
                     const float d2 = near ? geo_d2_near(gc) : geo_d2_far(gc, ra, rb, pa, pb);
                     d32 = d2 > 0.0f ? d2 * rsqrt_ftz(d2) : 0.0f;
@@ -690,7 +690,6 @@ __device__ void hist_rows_fill(unsigned* hs, float4 (*rf)[2], const SelectArgs& 
     const int row = row0 + r;
     const bool row_ok = r < nrows;
     const float4 ra = rf[r][0], rb = rf[r][1];
-    const float fz = ra.z + rb.z;
     unsigned* hrow = hs + r * HS_STRIDE;
     float4* out = reinterpret_cast<float4*>(a.d2c_out) + (size_t)(row / 128) * a.ntiles * 1024 + quarter * 256 +
                   (row & 127);
@@ -702,7 +701,7 @@ __device__ void hist_rows_fill(unsigned* hs, float4 (*rf)[2], const SelectArgs& 
         for (int q4 = 0; q4 < 2; q4++) {
             GeoChord g[4];
 #pragma unroll
-            for (int e = 0; e < 4; e++) g[e] = geo_chord32(ra, rb, fz, tp[2 * (q4 * 4 + e)], tp[2 * (q4 * 4 + e) + 1]);
+            for (int e = 0; e < 4; e++) g[e] = geo_chord32(ra, rb, tp[2 * (q4 * 4 + e)], tp[2 * (q4 * 4 + e) + 1]);
             const bool near = __all_sync(0xffffffffu, fmaxf(fmaxf(g[0].S, g[1].S), fmaxf(g[2].S, g[3].S)) <= 0.25f);
             float d[4];
             if (near) {  // warp-uniform: the far form's extra work only where a pair needs it
@@ -738,6 +737,76 @@ __device__ void hist_rows_fill(unsigned* hs, float4 (*rf)[2], const SelectArgs& 
     }
     __syncthreads();
     hist_store(hs, a, row0, nrows);
+}
+
+// Whole-row histograms read back from a filled distance cache a.d2c (layout
+// of launch_fill_d2): the same proxy values, so the same counts as
+// hist_rows_fill.  Lane (r = lane % 8, u = lane / 8) of warp w reads all 32
+// values of row row0 + r in tile w + 32 (4 s + u), s = 0, 1, ...: each warp
+// load is four whole 128-byte lines, all 32 values are loaded before the
+// first is used (the pass streams the whole cache), and the 32 lanes of one
+// shared-memory atomic are 8 rows x 4 tiles far apart along the curve, which
+// rarely hit the same bin.
+__device__ void hist_rows_cached(unsigned* hs, const SelectArgs& a, int row0)
+{
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int n = a.n;
+    const Window wlog = coarse_window(a);
+    const bool fastbin = wlog.shift >= 29 && wlog.shift <= 52;
+    const int s2 = fastbin ? wlog.shift - 29 : 0;
+    const long long kbin = fastbin ? (long long)((896ull << 23) >> s2) + (long long)((1ull << 63) >> wlog.shift) -
+                                         (long long)(wlog.base >> wlog.shift)
+                                   : 0;
+    const bool bin32 = fastbin && kbin > -(1ll << 30) && kbin + (long long)(0x7f800000u >> s2) < (1ll << 30);
+    const int kbin32 = bin32 ? (int)kbin : 0;
+    const int nrows = min(HS_ROWS, n - row0);
+    for (int b = t; b < HS_ROWS * HS_STRIDE; b += HS_THREADS) hs[b] = 0;
+    __syncthreads();
+    const int r = lane & 7, u = lane >> 3;
+    const int row = row0 + r;
+    const bool row_ok = r < nrows;
+    unsigned* hrow = hs + r * HS_STRIDE;
+    const float4* in = reinterpret_cast<const float4*>(a.d2c) + (size_t)(row / 128) * a.ntiles * 1024 + (row & 127);
+    constexpr int WARPS = HS_THREADS / 32;
+    for (int base = 0; base < a.ntiles; base += 4 * WARPS) {
+        const int tile = base + 4 * warp + u;
+        const bool tile_ok = tile < a.ntiles;
+        float4 dv[8];  // [quarter][half]: points 4 k .. 4 k + 3 of the tile
+#pragma unroll
+        for (int k = 0; k < 8; k++) dv[k] = tile_ok ? __ldcs(in + (size_t)tile * 1024 + k * 128) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const int nv = (row_ok && tile_ok) ? min(SEL_TILE, n - tile * SEL_TILE) : 0;  // points of the 32
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const float d[4] = {dv[k].x, dv[k].y, dv[k].z, dv[k].w};
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                if (k * 4 + e >= nv) continue;
+                const float d32 = d[e] > 0.0f ? d[e] * rsqrt_ftz(d[e]) : 0.0f;
+                if (d32 == d32) {
+                    const uint32_t fb = __float_as_uint(d32);
+                    unsigned bin;
+                    if (bin32) {
+                        const int qb = (int)(fb >> s2) + kbin32;
+                        bin = fb < 0x00800000u ? 0u : (unsigned)min(max(qb, 0), SEL_BINS - 1);
+                    } else if (fastbin) {
+                        const long long qb = (long long)(fb >> s2) + kbin;
+                        bin = fb < 0x00800000u ? 0u : (unsigned)min(max(qb, 0ll), (long long)(SEL_BINS - 1));
+                    } else {
+                        bin = bucket_of(wlog, dkey_f(d32));
+                    }
+                    atomicAdd(&hrow[bin], 1u);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    hist_store(hs, a, row0, nrows);
+}
+
+__global__ void __launch_bounds__(HS_THREADS, 1) k_select_hist_cached(SelectArgs a)
+{
+    extern __shared__ __align__(16) unsigned hs[];  // HS_ROWS x HS_STRIDE
+    for (int row0 = blockIdx.x * HS_ROWS; row0 < a.n; row0 += gridDim.x * HS_ROWS) hist_rows_cached(hs, a, row0);
 }
 
 template <bool GEO>
@@ -859,6 +928,17 @@ cudaError_t launch_select(const SelectArgs& a, bool geographic, bool exact, int 
     if (!narrow) return launch_select_cfg<SelWide>(a, geographic, exact, grid, stream);
     return wide_rows ? launch_select_cfg<SelNarrow4>(a, geographic, exact, grid, stream)
                      : launch_select_cfg<SelNarrow>(a, geographic, exact, grid, stream);
+}
+
+cudaError_t launch_select_hist_cached(const SelectArgs& a, int num_sms, cudaStream_t stream)
+{
+    if (!a.hist_cache || !a.d2c || a.F.u || a.n < 1) return cudaErrorInvalidValue;
+    const size_t smem = (size_t)HS_ROWS * HS_STRIDE * sizeof(unsigned);
+    int grid = (a.n + HS_ROWS - 1) / HS_ROWS;
+    if (grid > num_sms) grid = num_sms;
+    raise_smem_limit((const void*)k_select_hist_cached, smem);
+    k_select_hist_cached<<<grid, HS_THREADS, smem, stream>>>(a);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_select_hist(const SelectArgs& a, bool geographic, int num_sms, cudaStream_t stream)

@@ -50,13 +50,15 @@ constexpr float kGeoK = 4.0f * kGeoA * kGeoA;       // (2a)^2
 
 // Chord terms of a pair of geographic records: S = sin^2 w = |chord|^2 / 4
 // (w = half the central angle), dz = sin phi_p - sin phi_f and
-// zs = sin phi_p + sin phi_f, from the focus's fz = sin phi_f (hi + lo).
+// zs = sin phi_p + sin phi_f, each from the hi and lo parts separately.
+// Swapping the focus and the point negates every difference exactly and
+// leaves every sum unchanged, so every value below is the same for (f, p)
+// and (p, f): the distance of a pair is symmetric bit for bit.
 struct GeoChord {
     float S, dz, zs;
 };
 
-__device__ __forceinline__ GeoChord geo_chord32(const float4& fa, const float4& fb, float fz, const float4& pa,
-                                                const float4& pb)
+__device__ __forceinline__ GeoChord geo_chord32(const float4& fa, const float4& fb, const float4& pa, const float4& pb)
 {
     const float dx = (pa.x - fa.x) + (pb.x - fb.x);
     const float dy = (pa.y - fa.y) + (pb.y - fb.y);
@@ -64,7 +66,7 @@ __device__ __forceinline__ GeoChord geo_chord32(const float4& fa, const float4& 
     GeoChord g;
     g.S = 0.25f * fmaf(dx, dx, fmaf(dy, dy, dz * dz));
     g.dz = dz;
-    g.zs = fmaf(2.0f, fz, dz);
+    g.zs = (pa.z + fa.z) + (pb.z + fb.z);
     return g;
 }
 
@@ -99,9 +101,9 @@ __device__ __forceinline__ float geo_d2_near(const GeoChord& g)
 }
 
 // Any S, from the chord terms g of the focus record (fa, fb) and the point
-// record (pa, pb).  Beyond S = 0.25 C = cos^2 w = |f + p|^2 / 4 and zs come
-// from the sums of the two unit vectors (hi + lo), which keep their relative
-// precision towards the antipode where 1 - S and 2 fz + dz lose it, and
+// record (pa, pb).  Beyond S = 0.25 C = cos^2 w = |f + p|^2 / 4 comes from the
+// sum of the two unit vectors (hi + lo), which keeps its relative precision
+// towards the antipode where 1 - S loses it, and
 // asin x = pi/2 - 2 asin(sqrt y) with y = (1 - sqrt S) / 2 = C / (2 (1 + sqrt S))
 // <= 0.25 reuses the polynomial.  Branch-free (the cases are selects), and
 // equal to geo_d2_near wherever S <= 0.25.
@@ -112,7 +114,7 @@ __device__ __forceinline__ float geo_d2_far(const GeoChord& g, const float4& fa,
     const bool near = S <= 0.25f;
     const float sx = (pa.x + fa.x) + (pb.x + fb.x);
     const float sy = (pa.y + fa.y) + (pb.y + fb.y);
-    const float sz = (pa.z + fa.z) + (pb.z + fb.z);  // sin phi_p + sin phi_f
+    const float sz = g.zs;  // sin phi_p + sin phi_f
     const float C = near ? fmaxf(1.0f - S, 0.0f) : 0.25f * fmaf(sx, sx, fmaf(sy, sy, sz * sz));
     const float cq = C > 0.0f ? C * rsqrt_ftz(C) : 0.0f;
     const float rs = rsqrt_ftz(S);
@@ -121,14 +123,12 @@ __device__ __forceinline__ float geo_d2_far(const GeoChord& g, const float4& fa,
     const float Pz = asin_over_x(z);
     const float zr = z > 0.0f ? z * rsqrt_ftz(z) : 0.0f;
     const float far_w = fmaf(-2.0f * zr, Pz, 1.5707963267948966f);  // asin(sqrt S)
-    GeoChord h = g;
-    h.zs = near ? g.zs : sz;
-    return geo_lambert_d2(h, near ? Pz : far_w * rs, C, cq);
+    return geo_lambert_d2(g, near ? Pz : far_w * rs, C, cq);
 }
 
 __device__ __forceinline__ float geo_d2_32(const float4& fa, const float4& fb, const float4& pa, const float4& pb)
 {
-    return geo_d2_far(geo_chord32(fa, fb, fa.z + fb.z, pa, pb), fa, fb, pa, pb);
+    return geo_d2_far(geo_chord32(fa, fb, pa, pb), fa, fb, pa, pb);
 }
 
 // True when a pair with haversine term S lies beyond a compact kernel's
