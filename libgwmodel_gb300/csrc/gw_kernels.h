@@ -36,9 +36,6 @@ struct SelectArgs {
     // coordinates and FP32 records of F.n focus points.  Null F.u: the data.
     DevPoints F;
     const float4* fpts;
-    // Geographic data rows only (F.u null), or null: the histogram pass also
-    // fills this distance cache (layout of launch_fill_d2) from the same values.
-    float* d2c_out;
     // Geographic data rows only, or null: the distance cache that histogram pass
     // filled; the selects read their proxy values from it instead of recomputing them.
     const float* d2c;
@@ -176,7 +173,7 @@ struct TcArgs {
     int* err;                     // set to 1 if a bounded wait timed out
     unsigned long long* tiles;    // if not null: += 128 x 32 weight tiles processed
     unsigned long long* prof;     // if not null: += clock64 cycles per phase (kTcProfSlots slots)
-    const float* d2c;             // geographic only, optional: the distance cache of launch_fill_d2
+    const float* d2c;             // geographic only, optional: the distance cache of launch_fill_d2_sym
     unsigned wait_limit;          // polls of a pipeline wait before it times out (0: the default)
 };
 // Phase slots of TcArgs::prof, summed over CTAs (producer: warp 0 lane 0;
@@ -214,9 +211,11 @@ cudaError_t launch_build_zimg(int n, int mcols, int npad, const double* Z, int l
 // points as two float4 and a warp's loads are contiguous; padded pairs hold
 // FLT_MAX.  pts: the 2 float4 records per point, padded to whole tiles.
 size_t d2_cache_bytes(int n);
-cudaError_t launch_fill_d2(int n, const float4* pts, float* d2c, cudaStream_t stream);
-// The same cache, each pair computed once (the FP32 distance is symmetric) and
-// written to both rows.  scratch: ceil(n / 128) + 2 ints of device memory.
+// The distance cache of geographic mixed data: every pair's FP32 squared
+// distance, block (row block rb of 128 rows, 32-point tile t) of 4096 floats at
+// (rb * ntiles + t) * 4096, ordered [quarter 4][half 2][row 128][4 points].
+// Each pair is computed once (the FP32 distance is symmetric) and written to
+// both rows.  scratch: ceil(n / 128) + 2 ints of device memory.
 cudaError_t launch_fill_d2_sym(int n, const float4* pts, float* d2c, int* scratch, int num_sms, cudaStream_t stream);
 // D[128 x N] = A[128 x 32] B[N x 32]^T through tcgen05 (device pointers).
 cudaError_t launch_tc_selftest(const float* A, const float* B, float* D, int N, int* err, cudaStream_t stream);

@@ -33,13 +33,12 @@
 // beyond the row's haversine cut-off.  Every wait is bounded and reports
 // through err.
 // With a distance cache (CACHED, geographic) the producers read each pair's
-// FP32 squared distance -- filled once per dataset, by the histogram pass of
-// the select or by k_fill_d2, with the same arithmetic -- instead of computing
-// it: about 14 instead of 58 instructions per weight, bit-identical weights.
-// The tile's 16 KB distance block takes the place of its point records: a
-// bulk copy two tiles ahead into shared memory (after an L2 prefetch nd tiles
-// ahead), so the producers never wait on global loads (reading the block with
-// per-thread global loads one tile ahead cost 3.6% more time per launch).
+// FP32 squared distance -- filled once per dataset by k_fill_d2_sym with the
+// same arithmetic -- instead of computing it: about 14 instead of 58
+// instructions per weight, bit-identical weights.  The tile's 16 KB distance
+// block takes the place of its point records: a bulk copy np tiles ahead into
+// shared memory (after an L2 prefetch nd tiles ahead, both marked evict-first
+// in L2), so the producers never wait on global loads.
 #include "gw_common.cuh"
 #include "gw_kernels.h"
 #include "mixed_weight.cuh"
@@ -826,49 +825,6 @@ __global__ void k_build_zimg(int n, int mcols, int npad, const double* __restric
     }
 }
 
-// Distance cache: CTA (row block rb, group of FD_TILES tiles); thread (r,
-// quarter) computes points [8 quarter, 8 quarter + 8) of row rb * 128 + r for
-// every tile of the group with the producer's arithmetic (geo_chord32, the
-// warp-voted near-angle form) and streams them out as two float4, so each
-// warp store covers 512 contiguous bytes.
-constexpr int FD_TILES = 32;
-
-__global__ void __launch_bounds__(512) k_fill_d2(int n, int ntiles, const float4* __restrict__ pts,
-                                                  float* __restrict__ d2c)
-{
-    const int t = threadIdx.x, r = t & (TC_M - 1), quarter = t >> 7;
-    const int rb = blockIdx.x;
-    const int i = rb * TC_M + r;
-    float4 fa = make_float4(0.f, 0.f, 0.f, 0.f), fb = fa;
-    if (i < n) {
-        fa = pts[2 * (size_t)i];
-        fb = pts[2 * (size_t)i + 1];
-    }
-    const int t0 = blockIdx.y * FD_TILES, t1 = min(ntiles, t0 + FD_TILES);
-    float4* out = reinterpret_cast<float4*>(d2c) + (size_t)rb * ntiles * 1024 + quarter * 256 + r;
-    for (int tile = t0; tile < t1; tile++) {
-#pragma unroll
-        for (int q4 = 0; q4 < 2; q4++) {
-            GeoChord g[4];
-#pragma unroll
-            for (int e = 0; e < 4; e++) {
-                const size_t j = (size_t)tile * TC_BK + quarter * 8 + q4 * 4 + e;  // records padded to whole tiles
-                g[e] = geo_chord32(fa, fb, pts[2 * j], pts[2 * j + 1]);
-            }
-            const bool near = __all_sync(0xffffffffu, fmaxf(fmaxf(g[0].S, g[1].S), fmaxf(g[2].S, g[3].S)) <= 0.25f);
-            float d[4];
-#pragma unroll
-            for (int e = 0; e < 4; e++) {
-                const int j = tile * TC_BK + quarter * 8 + q4 * 4 + e;
-                const size_t jr = (size_t)j;
-                const float d2 = near ? geo_d2_near(g[e]) : geo_d2_far(g[e], fa, fb, pts[2 * jr], pts[2 * jr + 1]);
-                d[e] = (i < n && j < n) ? d2 : 3.402823466e38f;
-            }
-            __stcs(out + (size_t)tile * 1024 + q4 * 128, make_float4(d[0], d[1], d[2], d[3]));
-        }
-    }
-}
-
 // Symmetric fill of the distance cache.  The FP32 distance is symmetric bit
 // for bit (geo_chord32), so each pair of row blocks (A, B), B >= A, is
 // computed once: thread (r, q) computes row A * 128 + r against the 32 points
@@ -995,15 +951,6 @@ size_t d2_cache_bytes(int n)
     return nrb * ntiles * (size_t)TC_M * TC_BK * sizeof(float);
 }
 
-cudaError_t launch_fill_d2(int n, const float4* pts, float* d2c, cudaStream_t stream)
-{
-    if (n < 1 || !pts || !d2c) return cudaErrorInvalidValue;
-    const int nrb = (n + TC_M - 1) / TC_M, ntiles = (n + TC_BK - 1) / TC_BK;
-    const int groups = (ntiles + FD_TILES - 1) / FD_TILES;
-    if (groups > 65535) return cudaErrorInvalidValue;
-    k_fill_d2<<<dim3(nrb, groups), 512, 0, stream>>>(n, ntiles, pts, d2c);
-    return cudaGetLastError();
-}
 
 size_t contract_tc_smem_bytes(int npad, int ntiles, int nb, bool cached)
 {

@@ -656,92 +656,9 @@ __device__ void hist_store(const unsigned* hs, const SelectArgs& a, int row0, in
     __syncthreads();
 }
 
-// The histogram pass of geographic data rows that also fills the distance
-// cache a.d2c_out (block (rb, tile) of 4096 floats at (rb * ntiles + tile) *
-// 4096, ordered [quarter 4][half 2][row 128][4 points]).  Lane (r = lane % 8,
-// quarter = lane / 8) of warp w computes row row0 + r's distances to points
-// [8 quarter, 8 quarter + 8) of tiles w, w + 32, ...; the 8 rows of a group
-// are consecutive within one 128-row block, so every (quarter, half) store of
-// a warp is one whole 128-byte line.  The distances and bins are those of
-// hist_rows (the same chord, the same near/far forms, which agree wherever
-// both apply), so the counts are identical.
-__device__ void hist_rows_fill(unsigned* hs, float4 (*rf)[2], const SelectArgs& a, int row0)
-{
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const int n = a.n;
-    const Window wlog = coarse_window(a);
-    const bool fastbin = wlog.shift >= 29 && wlog.shift <= 52;
-    const int s2 = fastbin ? wlog.shift - 29 : 0;
-    const long long kbin = fastbin ? (long long)((896ull << 23) >> s2) + (long long)((1ull << 63) >> wlog.shift) -
-                                         (long long)(wlog.base >> wlog.shift)
-                                   : 0;
-    // the same bins in 32-bit integer steps when the window's constants allow it (they do
-    // for distances in km): (bits >> s2) + kbin then stays inside int32 for every positive float
-    const bool bin32 = fastbin && kbin > -(1ll << 30) && kbin + (long long)(0x7f800000u >> s2) < (1ll << 30);
-    const int kbin32 = bin32 ? (int)kbin : 0;
-    const int nrows = min(HS_ROWS, n - row0);
-    for (int b = t; b < HS_ROWS * HS_STRIDE; b += HS_THREADS) hs[b] = 0;
-    if (t < HS_ROWS * 2) {
-        const int r = t / 2, q = t % 2;
-        rf[r][q] = r < nrows ? a.pts[2 * (size_t)(row0 + r) + q] : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-    __syncthreads();
-    const int r = lane & 7, quarter = lane >> 3;
-    const int row = row0 + r;
-    const bool row_ok = r < nrows;
-    const float4 ra = rf[r][0], rb = rf[r][1];
-    unsigned* hrow = hs + r * HS_STRIDE;
-    float4* out = reinterpret_cast<float4*>(a.d2c_out) + (size_t)(row / 128) * a.ntiles * 1024 + quarter * 256 +
-                  (row & 127);
-    for (int tile = warp; tile < a.ntiles; tile += HS_THREADS / 32) {
-        const int jl = tile * SEL_TILE + quarter * 8;                 // this lane's first point
-        const float4* tp = a.pts + 2 * (size_t)jl;                    // its 8 records (padded to whole tiles)
-        const int nv = row_ok ? min(8, n - jl) : 0;                   // how many of them are points
-#pragma unroll
-        for (int q4 = 0; q4 < 2; q4++) {
-            GeoChord g[4];
-#pragma unroll
-            for (int e = 0; e < 4; e++) g[e] = geo_chord32(ra, rb, tp[2 * (q4 * 4 + e)], tp[2 * (q4 * 4 + e) + 1]);
-            const bool near = __all_sync(0xffffffffu, fmaxf(fmaxf(g[0].S, g[1].S), fmaxf(g[2].S, g[3].S)) <= 0.25f);
-            float d[4];
-            if (near) {  // warp-uniform: the far form's extra work only where a pair needs it
-#pragma unroll
-                for (int e = 0; e < 4; e++) d[e] = geo_d2_near(g[e]);
-            } else {
-#pragma unroll
-                for (int e = 0; e < 4; e++) d[e] = geo_d2_far(g[e], ra, rb, tp[2 * (q4 * 4 + e)], tp[2 * (q4 * 4 + e) + 1]);
-            }
-#pragma unroll
-            for (int e = 0; e < 4; e++) d[e] = q4 * 4 + e < nv ? d[e] : 3.402823466e38f;
-            if (row_ok) __stcs(out + (size_t)tile * 1024 + q4 * 128, make_float4(d[0], d[1], d[2], d[3]));
-#pragma unroll
-            for (int e = 0; e < 4; e++) {
-                if (q4 * 4 + e >= nv) continue;
-                const float d32 = d[e] > 0.0f ? d[e] * rsqrt_ftz(d[e]) : 0.0f;
-                if (d32 == d32) {
-                    const uint32_t fb = __float_as_uint(d32);
-                    unsigned bin;
-                    if (bin32) {
-                        const int q = (int)(fb >> s2) + kbin32;
-                        bin = fb < 0x00800000u ? 0u : (unsigned)min(max(q, 0), SEL_BINS - 1);
-                    } else if (fastbin) {
-                        const long long q = (long long)(fb >> s2) + kbin;
-                        bin = fb < 0x00800000u ? 0u : (unsigned)min(max(q, 0ll), (long long)(SEL_BINS - 1));
-                    } else {
-                        bin = bucket_of(wlog, dkey_f(d32));
-                    }
-                    atomicAdd(&hrow[bin], 1u);
-                }
-            }
-        }
-    }
-    __syncthreads();
-    hist_store(hs, a, row0, nrows);
-}
-
 // Whole-row histograms read back from a filled distance cache a.d2c (layout
-// of launch_fill_d2): the same proxy values, so the same counts as
-// hist_rows_fill.  Lane (r = lane % 8, u = lane / 8) of warp w reads all 32
+// of launch_fill_d2_sym): the same proxy values, so the same counts as
+// hist_rows.  Lane (r = lane % 8, u = lane / 8) of warp w reads all 32
 // values of row row0 + r in tile w + 32 (4 s + u), s = 0, 1, ...: each warp
 // load is four whole 128-byte lines, all 32 values are loaded before the
 // first is used (the pass streams the whole cache), and the 32 lanes of one
@@ -815,11 +732,7 @@ __global__ void __launch_bounds__(HS_THREADS, 1) k_select_hist(SelectArgs a)
     extern __shared__ __align__(16) unsigned hs[];  // HS_ROWS x HS_STRIDE
     __shared__ float4 rf[HS_ROWS][2];
     const int nfocus = a.F.u ? a.F.n : a.n;
-    const bool fill = GEO && a.d2c_out && !a.F.u;
-    for (int row0 = blockIdx.x * HS_ROWS; row0 < nfocus; row0 += gridDim.x * HS_ROWS) {
-        if (fill) hist_rows_fill(hs, rf, a, row0);
-        else hist_rows<GEO>(hs, rf, a, row0);
-    }
+    for (int row0 = blockIdx.x * HS_ROWS; row0 < nfocus; row0 += gridDim.x * HS_ROWS) hist_rows<GEO>(hs, rf, a, row0);
 }
 
 // Histogram caches of many datasets in one launch: segment s owns the row
