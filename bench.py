@@ -136,7 +136,8 @@ def peaks():
 
 def ncu_traffic_per_tile(name):
     """DRAM bytes per processed 32-point tile of the contraction, from the committed
-    ncu summary (a small-case capture; the traffic grows with the tiles processed)."""
+    ncu summary (a one-launch capture of the config-2 workload; the traffic grows
+    with the tiles processed: every visited tile streams its distance block)."""
     path = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(path):
         return None
@@ -683,12 +684,15 @@ def run_ours(args):
     per_tile = ncu_traffic_per_tile("contract_tc_config2.md") if prec == Precision.Mixed else None
     tiles_per_launch = stats["contract_tiles"] / max(stats["contract_launches"], 1)
     traffic = per_tile * tiles_per_launch if per_tile else None
+    launch_s = stats["contract_ms"] / 1e3 / max(stats["contract_launches"], 1)
     if prec == Precision.Mixed:
         roof = {"bound": "tensor", "achieved": achieved, "peak": tf32_peak, "unit": "TFLOP/s",
                 "frac": achieved / tf32_peak, "traffic": traffic,
-                "traffic_note": "DRAM bytes per processed tile from the small-case ncu capture "
+                "traffic_note": "DRAM bytes per processed tile from the ncu capture of the first config-2 launch "
                                 "(profiles/contract_tc_config2.md) x mean tiles per launch of this step",
                 "tiles_per_launch": tiles_per_launch,
+                "dram_gbs": traffic / launch_s / 1e9 if traffic and launch_s > 0 else None,
+                "dram_frac_of_measured_hbm": traffic / launch_s / 1e9 / hbm if traffic and launch_s > 0 else None,
                 "kernel": "k_contract_tc (tcgen05 TF32x3 W.Z)",
                 "note": f"useful 2*m*P FLOPs (m=170, P=nonzero-weight pairs) / event-timed launch; peak = {src} "
                         f"bf16 burst {bf16:.0f} TF/s halved for dense TF32"}
