@@ -263,10 +263,19 @@ __device__ bool select_row(typename C::Shared& sh, const SelectArgs& a, const Ro
                 if (mytile < a.ntiles) cls = classify_tile<GEO>(a.tb[mytile], c, below_thr, above_thr);
                 if (cls < 0) below += (unsigned)min(SEL_TILE, n - mytile * SEL_TILE);
                 unsigned straddle = __ballot_sync(0xffffffffu, cls == 0);
+                // with the distance cache, the next straddling tile's value is loaded
+                // before this one is used: point `lane` of a tile sits at
+                // [quarter lane / 8][half (lane / 4) % 2][row][lane % 4] of its block
+                const size_t lane_off = (size_t)(lane >> 2) * 512 + (lane & 3);
+                float d2next = 0.0f;
+                if (GEO && d2r && straddle) d2next = __ldg(d2r + (size_t)(tbase + __ffs(straddle) - 1) * 4096 + lane_off);
                 while (straddle) {
                     const int k = __ffs(straddle) - 1;
                     straddle &= straddle - 1;
                     const int tile = tbase + k;
+                    const float d2cached = d2next;
+                    if (GEO && d2r && straddle)
+                        d2next = __ldg(d2r + (size_t)(tbase + __ffs(straddle) - 1) * 4096 + lane_off);
                     const int j = tile * SEL_TILE + lane;
                     bool in = false;
                     uint64_t key = 0;
@@ -276,9 +285,7 @@ __device__ bool select_row(typename C::Shared& sh, const SelectArgs& a, const Ro
                     if (GEO) {
                         float d2;
                         if (d2r) {
-                            // the same value from the distance cache: point `lane` of the
-                            // tile sits at [quarter lane / 8][half (lane / 4) % 2][row][lane % 4]
-                            d2 = __ldg(d2r + (size_t)tile * 4096 + (lane >> 2) * 512 + (lane & 3));
+                            d2 = d2cached;  // the same value from the distance cache
                         } else {
                             const float4 pa = a.pts[2 * (size_t)j], pb = a.pts[2 * (size_t)j + 1];
                             const GeoChord g = geo_chord32(c.fa, c.fb, pa, pb);
@@ -685,36 +692,44 @@ __device__ void hist_rows_cached(unsigned* hs, const SelectArgs& a, int row0)
     unsigned* hrow = hs + r * HS_STRIDE;
     const float4* in = reinterpret_cast<const float4*>(a.d2c) + (size_t)(row / 128) * a.ntiles * 1024 + (row & 127);
     constexpr int WARPS = HS_THREADS / 32;
-    for (int base = 0; base < a.ntiles; base += 4 * WARPS) {
-        const int tile = base + 4 * warp + u;
-        const bool tile_ok = tile < a.ntiles;
-        float4 dv[8];  // [quarter][half]: points 4 k .. 4 k + 3 of the tile
+    // the bin of one value; values that are not points (padding, rows past n) and
+    // NaN go to word SEL_BINS of the row, the padding word that is never stored.
+    // The window's form is fixed for the pass, so each form has its own loop.
+    auto pass = [&](auto bin_of) {
+        for (int base = 0; base < a.ntiles; base += 4 * WARPS) {
+            const int tile = base + 4 * warp + u;
+            const bool tile_ok = tile < a.ntiles;
+            float4 dv[8];  // [quarter][half]: points 4 k .. 4 k + 3 of the tile
 #pragma unroll
-        for (int k = 0; k < 8; k++) dv[k] = tile_ok ? __ldcs(in + (size_t)tile * 1024 + k * 128) : make_float4(0.f, 0.f, 0.f, 0.f);
-        const int nv = (row_ok && tile_ok) ? min(SEL_TILE, n - tile * SEL_TILE) : 0;  // points of the 32
+            for (int k = 0; k < 8; k++)
+                dv[k] = tile_ok ? __ldcs(in + (size_t)tile * 1024 + k * 128) : make_float4(0.f, 0.f, 0.f, 0.f);
+            const int nv = (row_ok && tile_ok) ? min(SEL_TILE, n - tile * SEL_TILE) : 0;  // points of the 32
 #pragma unroll
-        for (int k = 0; k < 8; k++) {
-            const float d[4] = {dv[k].x, dv[k].y, dv[k].z, dv[k].w};
+            for (int k = 0; k < 8; k++) {
+                const float d[4] = {dv[k].x, dv[k].y, dv[k].z, dv[k].w};
 #pragma unroll
-            for (int e = 0; e < 4; e++) {
-                if (k * 4 + e >= nv) continue;
-                const float d32 = d[e] > 0.0f ? d[e] * rsqrt_ftz(d[e]) : 0.0f;
-                if (d32 == d32) {
-                    const uint32_t fb = __float_as_uint(d32);
-                    unsigned bin;
-                    if (bin32) {
-                        const int qb = (int)(fb >> s2) + kbin32;
-                        bin = fb < 0x00800000u ? 0u : (unsigned)min(max(qb, 0), SEL_BINS - 1);
-                    } else if (fastbin) {
-                        const long long qb = (long long)(fb >> s2) + kbin;
-                        bin = fb < 0x00800000u ? 0u : (unsigned)min(max(qb, 0ll), (long long)(SEL_BINS - 1));
-                    } else {
-                        bin = bucket_of(wlog, dkey_f(d32));
-                    }
+                for (int e = 0; e < 4; e++) {
+                    const float d32 = d[e] > 0.0f ? d[e] * rsqrt_ftz(d[e]) : 0.0f;
+                    const unsigned bin = (k * 4 + e < nv && d32 == d32) ? bin_of(d32) : (unsigned)SEL_BINS;
                     atomicAdd(&hrow[bin], 1u);
                 }
             }
         }
+    };
+    if (bin32) {
+        pass([&](float d32) {
+            const uint32_t fb = __float_as_uint(d32);
+            const int qb = (int)(fb >> s2) + kbin32;
+            return fb < 0x00800000u ? 0u : (unsigned)min(max(qb, 0), SEL_BINS - 1);
+        });
+    } else if (fastbin) {
+        pass([&](float d32) {
+            const uint32_t fb = __float_as_uint(d32);
+            const long long qb = (long long)(fb >> s2) + kbin;
+            return fb < 0x00800000u ? 0u : (unsigned)min(max(qb, 0ll), (long long)(SEL_BINS - 1));
+        });
+    } else {
+        pass([&](float d32) { return bucket_of(wlog, dkey_f(d32)); });
     }
     __syncthreads();
     hist_store(hs, a, row0, nrows);
