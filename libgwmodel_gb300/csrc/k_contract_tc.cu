@@ -877,6 +877,7 @@ __global__ void __launch_bounds__(512, 2) k_fill_d2_sym(int n, int ntiles, int n
         }
         for (int B = B0; B < B1; B++) {
             const int tile = 4 * B + q;  // warp-uniform
+            const bool full = (A + 1) * TC_M <= n && (B + 1) * TC_M <= n;  // no padding row or point
             float4* outA = reinterpret_cast<float4*>(d2c) + ((size_t)A * ntiles + tile) * 1024 + r;
 #pragma unroll 2
             for (int g8 = 0; g8 < 8; g8++) {  // points 4 g8 .. 4 g8 + 3 of the tile: [quarter g8 / 2][half g8 % 2]
@@ -900,10 +901,12 @@ __global__ void __launch_bounds__(512, 2) k_fill_d2_sym(int n, int ntiles, int n
                             d[e] = geo_d2_far(g[e], fa, fb, pts[2 * j], pts[2 * j + 1]);
                         }
                     }
+                    if (!full) {
 #pragma unroll
-                    for (int e = 0; e < 4; e++) {
-                        const int j = tile * TC_BK + g8 * 4 + e;
-                        d[e] = (i < n && j < n) ? d[e] : 3.402823466e38f;
+                        for (int e = 0; e < 4; e++) {
+                            const int j = tile * TC_BK + g8 * 4 + e;
+                            d[e] = (i < n && j < n) ? d[e] : 3.402823466e38f;
+                        }
                     }
                     __stcs(outA + g8 * 128, make_float4(d[0], d[1], d[2], d[3]));
                 } else {
