@@ -13,15 +13,14 @@
 //    issued by one thread of a copy warp, up to four stages ahead (three with
 //    weights in shared memory);
 //  * one thread of the MMA warp issues 3 x 4 tcgen05.mma.kind::tf32
-//    (hi.hi + hi.lo + lo.hi, K = 8 each) per tile, up to four tiles per pass,
-//    into a 128 x N FP32 accumulator in TMEM and commits once per tile
-//    (tile_done frees both the weight stage and the Z stage of that tile).
-//    An MMA issue returns only when the tensor pipe accepts it (about as long
-//    as the MMA runs), so that thread issues nothing else: with the copies on
-//    the same thread the pipe idled about two thirds of the time.  The
-//    single-thread loops keep their stage and chunk positions as counters: a
-//    division by a run-time value there costs a dependent chain on the thread
-//    that gates the whole CTA;
+//    (hi.hi + hi.lo + lo.hi, K = 8 each) per tile, two tiles per pass, into a
+//    128 x N FP32 accumulator in TMEM and commits once per tile (tile_done
+//    frees both the weight stage and the Z stage of that tile).  An MMA issue returns only when the tensor
+//    pipe accepts it (about as long as the MMA runs), so that thread issues
+//    nothing else: with the copies on the same thread the pipe idled about
+//    two thirds of the time.  Both single-thread loops keep their stage and
+//    chunk positions as counters: a division by a run-time value there costs
+//    a dependent chain on the thread that gates the whole CTA;
 //  * chunks of flush_tiles tiles accumulate in TMEM; four drain warps (one per
 //    TMEM lane quadrant) read a finished chunk back with tcgen05.ld and add it
 //    into double-float (hi, lo) sums in global memory, so FP32 rounding never
@@ -520,17 +519,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             // counters: divisions by run-time values are long dependent chains on
             // this critical thread
             int ws = 0, wpar = 0, sb = 0, zpar = 0, kf = 0, c = 0;
-            // Up to four tiles per pass: the waits for all of them come first, then
-            // their MMAs back to back, so the tensor pipe does not idle through this
-            // thread's waits and bookkeeping between the tiles (2,125 -> 1,843
-            // cycles per tile with two; four took 3.4% less time again).  Waiting
-            // for tile k + 3 before issuing tile k cannot deadlock: its weights
-            // need the MMAs of tile k - 2 done, its Z tile those of tile k - 1.
-            // A pass never straddles a chunk.
+            // Up to two tiles per pass: the waits for both come first, then their
+            // 24 MMAs back to back, so the tensor pipe does not idle through this
+            // thread's waits and bookkeeping between the two tiles (2,125 -> 1,843
+            // cycles per tile).  Waiting for tile k + 1 before issuing tile k needs
+            // its weights (the MMAs of tile k + 1 - NW done) and its Z tile (those
+            // of tile k + 1 - nb), both issued already as NW, nb >= 2.  A pass of
+            // j tiles needs NW, nb >= j: with two weight stages (weights in shared
+            // memory) a longer pass would wait on MMAs it has not issued yet.  A
+            // pass never straddles a chunk.
             bool failed = false;
             while (k < ktotal && !failed) {
-                if ((k & 15) < 4 && *(volatile int*)&ctl.abort) break;
-                const int nt = min(4, min(ktotal - k, F - kf));
+                if ((k & 15) < 2 && *(volatile int*)&ctl.abort) break;
+                const int nt = (k + 1 < ktotal && kf + 1 < F) ? 2 : 1;
                 if (prof) c0 = clock64();
                 int s2 = ws, wp2 = wpar, sb2 = sb, zp2 = zpar;
                 for (int u = 0; u < nt && !failed; u++) {
