@@ -128,6 +128,30 @@ def test_great_circle_against_libm(gc_host):
     assert worst <= 8, worst
 
 
+@pytest.mark.parametrize("delta", [1e-1, 1e-3, 1e-5])
+def test_great_circle_near_the_antipode(gc_host, delta):
+    """Pairs within delta rad of each other's antipode, where the Lambert
+    correction's 1/cos^2 terms grow: the correctly rounded form and libm stay
+    within the bar of test_great_circle_against_libm, and the distances stay
+    finite and near half the meridian circumference (the whole-sphere GPU test
+    selects on such pairs)."""
+    rng = np.random.default_rng(11)
+    n = 600
+    lon1 = rng.uniform(-180.0, 180.0, n)
+    lat1 = np.degrees(np.arcsin(rng.uniform(-0.99, 0.99, n)))
+    ang = rng.uniform(0.0, 2.0 * np.pi, n)
+    lon2 = lon1 + 180.0 + np.degrees(delta * np.cos(ang) / np.cos(np.radians(lat1)))
+    lon2 = (lon2 + 180.0) % 360.0 - 180.0
+    lat2 = -lat1 + np.degrees(delta * np.sin(ang))
+    row = gc_host.rows(np.column_stack([np.concatenate([lon1, lon2]), np.concatenate([lat1, lat2])]))
+    cr = np.array([row(n + k)[k] for k in range(n)])
+    libm = np.array([O.gcdist(lon1[k], lon2[k], lat1[k], lat2[k]) for k in range(n)])
+    assert np.all(np.isfinite(cr)) and np.all(np.isfinite(libm))
+    assert np.all((cr > 19000.0) & (cr < 20100.0)), (cr.min(), cr.max())
+    ulp = np.abs(cr.view(np.int64) - libm.view(np.int64))
+    assert (ulp > 0).sum() <= 0.02 * n and ulp.max() <= 8, (int((ulp > 0).sum()), int(ulp.max()))
+
+
 def test_great_circle_edge_cases():
     assert O.gcdist(10, 10, 45, 45) == 0.0
     assert O.gcdist(180, -180, 10, 10) == 0.0      # |lon1|+|lon2| == 360 branch
